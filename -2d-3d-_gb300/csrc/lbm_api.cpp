@@ -1,0 +1,944 @@
+// lbm_api.cpp - host side of the C ABI declared in include/lbm_gpu.h.
+//
+// A handle owns one lattice resident in HBM, a CUDA stream and (after the first
+// lbm_step) a captured CUDA graph that replays a chunk of fused steps.  State lives in
+// one of two forms:
+//   * "module" form: the reference's arrays after a full iteration (f, g, rho, u, v, w,
+//     T, B_prev, F), used by the stage entry points, the diagnostics and state transfer;
+//   * "fused" form: post-collision buffers f_post_N / g_post_N plus the lag fields,
+//     advanced by the fused kernels.
+// lbm_step leaves the handle in fused form; any call that needs the module arrays first
+// rebuilds them with one materialisation pass (bit-identical to what the reference
+// holds after iteration N, so stepping resumes on the same trajectory).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm_gpu.h"
+#include "lbm_fast.h"
+#include "lbm_internal.h"
+
+using namespace lbm;
+
+namespace {
+
+const double kPi = 3.141592653589793115997963468544185161590576171875;  // acos(-1.0d0)
+constexpr int kChunkSteps = 32;  // fused steps per captured graph (even: ends on buffer 0)
+
+}  // namespace
+
+struct lbm_handle {
+    lbm_params p;
+    lbm_constants c;
+    int dim = 3, q = 19, qt = 7;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    Geo geo{};
+    PhysC phys{};
+    DiagScalars dsc{};
+    std::string err;
+    int64_t itc = 0;
+    bool initialised = false;
+
+    // FP64 plain method
+    ExactArrays A{};
+    double* fbuf[2] = {nullptr, nullptr};
+    double* gbuf[2] = {nullptr, nullptr};
+    bool fused_valid = false;  // true: current state is in the fused buffers
+    int cur = 0;               // fused buffer index holding f_post_N / g_post_N
+
+    // FP32 / FP16 storage forms
+    FastState F{};
+
+    // captured chunk of fused steps
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+
+    // scratch
+    double* d_part = nullptr;
+    std::vector<double> h_part;
+    double* d_tb = nullptr;
+    double* d_nub = nullptr;
+    double* d_stage = nullptr;  // AoS staging for state transfer
+    size_t stage_cap = 0;
+    double* d_sx = nullptr;
+    double* d_sy = nullptr;
+    std::vector<void*> allocs;
+};
+
+// ------------------------------------------------------------------------------------
+// helpers
+// ------------------------------------------------------------------------------------
+static int fail(lbm_handle* h, int status, const std::string& msg) {
+    if (h) h->err = msg;
+    return status;
+}
+
+static int cuda_fail(lbm_handle* h, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return fail(h, e == cudaErrorMemoryAllocation ? LBM_ERR_OOM : LBM_ERR_CUDA, m);
+}
+
+#define CK(h, call)                                              \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, #call); \
+    } while (0)
+
+#define CK_LAUNCH(h, what)                                     \
+    do {                                                       \
+        cudaError_t e_ = cudaGetLastError();                   \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, what); \
+    } while (0)
+
+template <class T>
+static int dalloc(lbm_handle* h, T** ptr, size_t count) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 1);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return cuda_fail(h, e, "cudaMalloc");
+    }
+    h->allocs.push_back(p);
+    *ptr = (T*)p;
+    return LBM_OK;
+}
+
+static int validate(const lbm_params* p) {
+    if (!p) return LBM_ERR_PARAM;
+    if (p->dim != 2 && p->dim != 3) return LBM_ERR_PARAM;
+    if (p->nx < 5 || p->ny < 5) return LBM_ERR_PARAM;
+    if (p->dim == 2 && p->nz != 1) return LBM_ERR_PARAM;
+    if (p->dim == 3 && p->nz < 2) return LBM_ERR_PARAM;
+    if ((long long)p->nx * p->ny * (long long)p->nz > (1LL << 31)) return LBM_ERR_PARAM;
+    if (!(p->Ra > 0) || !(p->Pr > 0) || !(p->Mach > 0)) return LBM_ERR_PARAM;
+    if (!(p->Thot > p->Tcold)) return LBM_ERR_PARAM;
+    if (p->cell != LBM_CELL_RB && p->cell != LBM_CELL_SIDE) return LBM_ERR_PARAM;
+    // only the boundary switches the reference defines (3DRB.F90:14-37, 2DRB.F90:15-32)
+    if (p->bc_flow[0] != LBM_BC_NOSLIP && p->bc_flow[0] != LBM_BC_PERIODIC) return LBM_ERR_PARAM;
+    if (p->bc_flow[1] != LBM_BC_NOSLIP) return LBM_ERR_PARAM;
+    if (p->bc_thermal[0] < LBM_BCT_CONST || p->bc_thermal[0] > LBM_BCT_PERIODIC) return LBM_ERR_PARAM;
+    if (p->bc_thermal[1] != LBM_BCT_CONST && p->bc_thermal[1] != LBM_BCT_ADIABATIC) return LBM_ERR_PARAM;
+    if (p->dim == 3) {
+        if (p->bc_flow[2] != LBM_BC_NOSLIP && p->bc_flow[2] != LBM_BC_PERIODIC) return LBM_ERR_PARAM;
+        if (p->bc_thermal[2] != LBM_BCT_ADIABATIC && p->bc_thermal[2] != LBM_BCT_PERIODIC) return LBM_ERR_PARAM;
+    }
+    if (p->precision < LBM_FP64 || p->precision > LBM_FP16) return LBM_ERR_PARAM;
+    if (p->pattern != LBM_PATTERN_AB && p->pattern != LBM_PATTERN_AA) return LBM_ERR_PARAM;
+    return LBM_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// parameters
+// ------------------------------------------------------------------------------------
+extern "C" int lbm_params_default(int dim, lbm_params* out) {
+    if (!out || (dim != 2 && dim != 3)) return LBM_ERR_PARAM;
+    std::memset(out, 0, sizeof(*out));
+    out->dim = dim;
+    if (dim == 2) {  // 2DRB.F90:11-38, 61-71
+        out->nx = 320; out->ny = 160; out->nz = 1;
+        out->Ra = 5.0e4;
+        out->bc_flow[0] = LBM_BC_PERIODIC;
+        out->bc_thermal[0] = LBM_BCT_PERIODIC;
+    } else {  // RayleighBenardCell variant of 3DRB.F90:9-47, 73-83
+        out->nx = 120; out->ny = 120; out->nz = 120;
+        out->Ra = 1.0e7;
+        out->bc_flow[0] = LBM_BC_NOSLIP;
+        out->bc_thermal[0] = LBM_BCT_ADIABATIC;
+    }
+    out->Pr = 0.71;
+    out->Mach = 0.1;
+    out->Thot = 0.5;
+    out->Tcold = -0.5;
+    out->cell = LBM_CELL_RB;
+    out->bc_flow[1] = LBM_BC_NOSLIP;
+    out->bc_flow[2] = LBM_BC_NOSLIP;
+    out->bc_thermal[1] = LBM_BCT_CONST;
+    out->bc_thermal[2] = LBM_BCT_ADIABATIC;
+    out->use_g = 1;
+    out->legacy_thermal = 0;
+    out->precision = LBM_FP64;
+    out->pattern = LBM_PATTERN_AB;
+    out->seed = 20261203ULL;
+    out->noise_amp = 0.0;
+    return LBM_OK;
+}
+
+// commondata (2DRB.F90:61-115) / commondata3d (3DRB.F90:73-123), same operation order.
+extern "C" int lbm_derive_constants(const lbm_params* p, lbm_constants* c) {
+    if (!c || validate(p) != LBM_OK) return LBM_ERR_PARAM;
+    std::memset(c, 0, sizeof(*c));
+    const double L = (p->cell == LBM_CELL_SIDE) ? (double)p->nx : (double)p->ny;
+    c->lengthUnit = L;
+    c->Tref = 0.5 * (p->Thot + p->Tcold);
+    c->tauf = 0.5 + p->Mach * L * std::sqrt(3.0 * p->Pr / p->Ra);
+    c->viscosity = (c->tauf - 0.5) / 3.0;
+    c->diffusivity = c->viscosity / p->Pr;
+    c->heatFluxScale = L / c->diffusivity;
+    c->velocityScaleCompare = L / c->diffusivity;
+    const double gBeta1 = p->Ra * c->viscosity * c->diffusivity / L;
+    c->gBeta = gBeta1 / L / L;
+    c->timeUnit = std::sqrt(L / c->gBeta);
+    c->velocityUnit = std::sqrt(c->gBeta * L);
+    c->Snu = 1.0 / c->tauf;
+    c->Sq = 8.0 * (2.0 * c->tauf - 1.0) / (8.0 * c->tauf - 1.0);
+    if (p->dim == 2) {
+        c->paraA = 20.0 * std::sqrt(3.0) * c->diffusivity - 4.0;
+        if (p->legacy_thermal) {
+            if ((c->paraA >= 1.0) || (c->paraA <= -4.0)) return LBM_ERR_PARAM;  // 2DRB.F90:404-414
+            c->Qk = 3.0 - std::sqrt(3.0);
+            c->Qnu = 4.0 * std::sqrt(3.0) - 6.0;
+            c->thermalGeqCoeff = 10.0 / (4.0 + c->paraA);
+            c->omegaT0 = (1.0 - c->paraA) / 5.0;
+            c->omegaT1 = (c->paraA + 4.0) / 20.0;
+        } else {
+            c->taug = 0.5 + (c->tauf - 0.5) / p->Pr;
+            c->Qnu = 1.0;
+            c->Qk = 1.0 / c->taug;
+            c->thermalGeqCoeff = 3.0;
+            c->omegaT0 = 1.0 / 3.0;
+            c->omegaT1 = 1.0 / 6.0;
+        }
+    } else {
+        c->cs2T = 0.25;
+        c->paraA = 42.0 * std::sqrt(3.0) * c->diffusivity - 6.0;
+        c->Se = 1.0 / c->tauf;
+        c->Seps = 1.0 / c->tauf;
+        c->Spi = 1.0 / c->tauf;
+        c->Sm = 8.0 * (2.0 * c->tauf - 1.0) / (8.0 * c->tauf - 1.0);
+        if (p->legacy_thermal) {
+            if ((c->paraA >= 1.0) || (c->paraA <= -6.0)) return LBM_ERR_PARAM;  // 3DRB.F90:379-388
+            c->Qk = 3.0 - std::sqrt(3.0);
+            c->Qnu = 4.0 * std::sqrt(3.0) - 6.0;
+            c->thermalGeqCoeff = 7.0 / ((6.0 + c->paraA) * c->cs2T);
+            c->omegaT0 = (1.0 - c->paraA) / 7.0;
+            c->omegaT1 = (6.0 + c->paraA) / 42.0;
+        } else {
+            c->taug = 0.5 + c->diffusivity / c->cs2T;
+            c->Qnu = 1.0;
+            c->Qk = 1.0 / c->taug;
+            c->thermalGeqCoeff = 1.0 / c->cs2T;
+            c->omegaT0 = 1.0 / 4.0;
+            c->omegaT1 = 1.0 / 8.0;
+        }
+    }
+    c->SG = 1.0 - 0.5 * c->Qk;
+    if (!(c->tauf > 0.5)) return LBM_ERR_PARAM;
+    return LBM_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// lifecycle
+// ------------------------------------------------------------------------------------
+static void release(lbm_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    for (void* p : h->allocs) cudaFree(p);
+    h->allocs.clear();
+    if (h->stream) cudaStreamDestroy(h->stream);
+    h->stream = nullptr;
+}
+
+static int allocate(lbm_handle* h) {
+    const long long n = h->geo.ncell;
+    const bool d3 = h->dim == 3;
+    int st;
+#define AL(ptr, cnt)                                      \
+    do {                                                  \
+        if ((st = dalloc(h, &(ptr), (size_t)(cnt))) != LBM_OK) return st; \
+    } while (0)
+    if (h->p.precision == LBM_FP64) {
+        AL(h->fbuf[0], h->q * n);
+        AL(h->fbuf[1], h->q * n);
+        AL(h->gbuf[0], h->qt * n);
+        AL(h->gbuf[1], h->qt * n);
+        AL(h->A.f, h->q * n);
+        AL(h->A.g, h->qt * n);
+        h->A.fpost = h->fbuf[0];
+        h->A.gpost = h->gbuf[0];
+        AL(h->A.rho, n);
+        AL(h->A.u, n);
+        AL(h->A.v, n);
+        AL(h->A.T, n);
+        AL(h->A.Bx, n);
+        AL(h->A.By, n);
+        AL(h->A.up, n);
+        AL(h->A.vp, n);
+        AL(h->A.Tp, n);
+        if (d3) {
+            AL(h->A.w, n);
+            AL(h->A.Bz, n);
+            AL(h->A.wp, n);
+            AL(h->A.Tlag, n);
+        } else {
+            AL(h->A.Fx, n);
+            AL(h->A.Fy, n);
+        }
+    } else {
+        st = fast_allocate(h->F, h->p, h->geo, [h](void** p, size_t bytes) {
+            cudaError_t e = cudaMalloc(p, bytes > 0 ? bytes : 1);
+            if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc");
+            h->allocs.push_back(*p);
+            return LBM_OK;
+        });
+        if (st != LBM_OK) return st;
+    }
+    AL(h->d_part, (size_t)diag_blocks(n) * DIAG_NSUM);
+    AL(h->d_tb, h->geo.nx);
+    AL(h->d_nub, h->geo.nx);
+    AL(h->d_sx, h->geo.nx);
+    AL(h->d_sy, h->geo.ny);
+#undef AL
+    h->h_part.assign((size_t)diag_blocks(n) * DIAG_NSUM, 0.0);
+    return LBM_OK;
+}
+
+extern "C" int lbm_create(const lbm_params* p, int device, lbm_handle** out) {
+    if (!out) return LBM_ERR_PARAM;
+    *out = nullptr;
+    if (validate(p) != LBM_OK) return LBM_ERR_PARAM;
+    lbm_handle* h = new (std::nothrow) lbm_handle();
+    if (!h) return LBM_ERR_OOM;
+    h->p = *p;
+    if (lbm_derive_constants(p, &h->c) != LBM_OK) {
+        delete h;
+        return LBM_ERR_PARAM;
+    }
+    h->dim = p->dim;
+    h->q = p->dim == 3 ? 19 : 9;
+    h->qt = p->dim == 3 ? 7 : 5;
+    h->device = device;
+    const lbm_constants& c = h->c;
+
+    Geo& g = h->geo;
+    g.nx = p->nx;
+    g.ny = p->ny;
+    g.nz = p->dim == 3 ? p->nz : 1;
+    g.ncell = (long long)g.nx * g.ny * g.nz;
+    for (int a = 0; a < 3; ++a) {
+        g.bcf[a] = p->bc_flow[a];
+        g.bct[a] = p->bc_thermal[a];
+        if (p->dim == 2 && a == 2) {
+            g.bcf[a] = LBM_BC_NOSLIP;
+            g.bct[a] = LBM_BCT_ADIABATIC;
+        }
+        // anti-bounce-back source (2DRB.F90:1052-1059, 1094-1101; 3DRB.F90:1265-1271, 1309-1315)
+        if (p->legacy_thermal) {
+            const double cc = p->dim == 2 ? (4.0 + c.paraA) / 10.0 : (6.0 + c.paraA) / 21.0;
+            g.bcT_lo[a] = cc * p->Thot;
+            g.bcT_hi[a] = cc * p->Tcold;
+        } else {
+            g.bcT_lo[a] = 2.0 * c.omegaT1 * p->Thot;
+            g.bcT_hi[a] = 2.0 * c.omegaT1 * p->Tcold;
+        }
+    }
+    PhysC& P = h->phys;
+    P.gBeta = c.gBeta;
+    P.Tref = c.Tref;
+    P.Snu = c.Snu;
+    P.Sq = c.Sq;
+    P.Se = c.Se;
+    P.Seps = c.Seps;
+    P.Spi = c.Spi;
+    P.Sm = c.Sm;
+    P.Qk = c.Qk;
+    P.Qnu = c.Qnu;
+    P.SG = c.SG;
+    P.paraA = c.paraA;
+    P.omegaT0 = c.omegaT0;
+    P.omegaT1 = c.omegaT1;
+    P.geqc = c.thermalGeqCoeff;
+    P.use_g = p->use_g ? 1 : 0;
+    P.legacy = p->legacy_thermal ? 1 : 0;
+    DiagScalars& D = h->dsc;
+    D.Thot = p->Thot;
+    D.Tcold = p->Tcold;
+    D.Tref = c.Tref;
+    D.dy = 1.0 / c.lengthUnit;
+    D.deltaT = p->Thot - p->Tcold;
+    D.coef = c.velocityScaleCompare;
+    D.side = p->cell == LBM_CELL_SIDE;
+    D.d3 = p->dim == 3;
+
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        delete h;
+        return LBM_ERR_CUDA;
+    }
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete h;
+        return LBM_ERR_CUDA;
+    }
+    int st = allocate(h);
+    if (st != LBM_OK) {
+        release(h);
+        delete h;
+        return st;
+    }
+    *out = h;
+    return LBM_OK;
+}
+
+extern "C" int lbm_destroy(lbm_handle* h) {
+    if (!h) return LBM_ERR_PARAM;
+    release(h);
+    delete h;
+    return LBM_OK;
+}
+
+extern "C" const char* lbm_last_error(const lbm_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+extern "C" const char* lbm_status_string(int s) {
+    switch (s) {
+        case LBM_OK: return "LBM_OK";
+        case LBM_ERR_PARAM: return "LBM_ERR_PARAM";
+        case LBM_ERR_CUDA: return "LBM_ERR_CUDA";
+        case LBM_ERR_OOM: return "LBM_ERR_OOM";
+        case LBM_ERR_DIVERGED: return "LBM_ERR_DIVERGED";
+        case LBM_ERR_TIMEOUT: return "LBM_ERR_TIMEOUT";
+        case LBM_ERR_STATE: return "LBM_ERR_STATE";
+        default: return "unknown status";
+    }
+}
+
+extern "C" int lbm_get_constants(const lbm_handle* h, lbm_constants* out) {
+    if (!h || !out) return LBM_ERR_PARAM;
+    *out = h->c;
+    return LBM_OK;
+}
+
+extern "C" int64_t lbm_itc(const lbm_handle* h) { return h ? h->itc : -1; }
+
+extern "C" int lbm_sync(lbm_handle* h) {
+    if (!h) return LBM_ERR_PARAM;
+    CK(h, cudaSetDevice(h->device));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return LBM_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// initial (2DRB.F90:371-663, 3DRB.F90:342-643)
+// ------------------------------------------------------------------------------------
+extern "C" int lbm_initial(lbm_handle* h) {
+    if (!h) return LBM_ERR_PARAM;
+    CK(h, cudaSetDevice(h->device));
+    const lbm_params& p = h->p;
+    const double L = h->c.lengthUnit;
+    InitC I{};
+    I.L = L;
+    I.Thot = p.Thot;
+    I.Tcold = p.Tcold;
+    I.noise_amp = p.noise_amp;
+    I.seed = p.seed;
+    I.sx = h->d_sx;
+    I.sy = h->d_sy;
+    // RB sinusoidal perturbation, only for small Ra (2DRB.F90:567-581: Ra < 1e4;
+    // 3DRB.F90:545-556: Ra <= 1e4).  sin/cos come from the host libm.
+    const bool small_ra = h->dim == 2 ? (p.Ra < 1.0e4) : (p.Ra <= 1.0e4);
+    I.perturb = (p.cell == LBM_CELL_RB && p.bc_thermal[1] == LBM_BCT_CONST && small_ra) ? 1 : 0;
+    I.pert_amp = 1.0e-3 * (p.Thot - p.Tcold);
+    if (I.perturb) {
+        const int nx = h->geo.nx, ny = h->geo.ny;
+        std::vector<double> sx(nx), sy(ny);
+        const double xLen = (double)nx / L, yLen = (double)ny / L;
+        for (int i = 1; i <= nx; ++i) {
+            const double xp = ((double)i - 0.5) / L;
+            sx[i - 1] = h->dim == 3 ? std::cos(2.0 * kPi * xp / xLen) : std::sin(2.0 * kPi * xp / xLen);
+        }
+        for (int j = 1; j <= ny; ++j) {
+            const double yp = ((double)j - 0.5) / L;
+            sy[j - 1] = std::sin(kPi * yp / yLen);
+        }
+        CK(h, cudaMemcpyAsync(h->d_sx, sx.data(), nx * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        CK(h, cudaMemcpyAsync(h->d_sy, sy.data(), ny * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
+    if (h->p.precision == LBM_FP64) {
+        h->A.fpost = h->fbuf[0];
+        h->A.gpost = h->gbuf[0];
+        h->cur = 0;
+        h->fused_valid = false;
+        exact_initial(h->geo, h->phys, I, h->A, h->dim, h->stream);
+    } else {
+        fast_initial(h->F, h->geo, h->phys, I, h->dim, h->stream);
+    }
+    CK_LAUNCH(h, "initial");
+    h->itc = 0;
+    h->initialised = true;
+    return LBM_OK;
+}
+
+// Rebuild the module arrays from the fused buffers (no-op when already there).
+static int materialize(lbm_handle* h) {
+    if (h->p.precision != LBM_FP64) {
+        fast_materialize(h->F, h->geo, h->phys, h->dim, h->stream);
+        CK_LAUNCH(h, "materialize");
+        return LBM_OK;
+    }
+    if (!h->fused_valid) return LBM_OK;
+    exact_materialize(h->geo, h->phys, h->A, h->dim, h->fbuf[h->cur], h->gbuf[h->cur], h->stream);
+    CK_LAUNCH(h, "materialize");
+    h->A.fpost = h->fbuf[h->cur];
+    h->A.gpost = h->gbuf[h->cur];
+    h->fused_valid = false;
+    return LBM_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// stage entry points
+// ------------------------------------------------------------------------------------
+static int stage(lbm_handle* h, int which) {
+    if (!h) return LBM_ERR_PARAM;
+    if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
+    if (h->p.precision != LBM_FP64)
+        return fail(h, LBM_ERR_STATE, "stage entry points exist for the FP64 plain method only");
+    CK(h, cudaSetDevice(h->device));
+    int st = materialize(h);
+    if (st != LBM_OK) return st;
+    if (which == STAGE_COLLISION) h->itc += 1;
+    exact_stage(which, h->geo, h->phys, h->A, h->dim, h->stream);
+    CK_LAUNCH(h, "stage kernel");
+    return LBM_OK;
+}
+
+extern "C" int lbm_collision(lbm_handle* h) { return stage(h, STAGE_COLLISION); }
+extern "C" int lbm_streaming(lbm_handle* h) { return stage(h, STAGE_STREAMING); }
+extern "C" int lbm_bounceback(lbm_handle* h) { return stage(h, STAGE_BOUNCEBACK); }
+extern "C" int lbm_macro(lbm_handle* h) { return stage(h, STAGE_MACRO); }
+extern "C" int lbm_collisionT(lbm_handle* h) { return stage(h, STAGE_COLLISIONT); }
+extern "C" int lbm_streamingT(lbm_handle* h) { return stage(h, STAGE_STREAMINGT); }
+extern "C" int lbm_bouncebackT(lbm_handle* h) { return stage(h, STAGE_BOUNCEBACKT); }
+extern "C" int lbm_macroT(lbm_handle* h) { return stage(h, STAGE_MACROT); }
+
+// ------------------------------------------------------------------------------------
+// fused stepping
+// ------------------------------------------------------------------------------------
+static void enqueue_one(lbm_handle* h, bool first) {
+    const int nxt = h->cur ^ 1;
+    if (h->p.precision == LBM_FP64) {
+        exact_fused_step(h->geo, h->phys, h->A, h->dim, first, h->fbuf[h->cur], h->gbuf[h->cur], h->fbuf[nxt],
+                         h->gbuf[nxt], h->stream);
+        h->cur = nxt;
+    } else {
+        fast_step(h->F, h->geo, h->phys, h->dim, first, h->stream);
+    }
+}
+
+static bool at_graph_origin(const lbm_handle* h) {
+    return h->p.precision == LBM_FP64 ? h->cur == 0 : fast_at_origin(h->F);
+}
+
+static int capture_chunk(lbm_handle* h) {
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < kChunkSteps; ++s) enqueue_one(h, false);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+    h->graph = g;
+    CK(h, cudaGraphInstantiate(&h->graph_exec, g, 0));
+    return LBM_OK;
+}
+
+extern "C" int lbm_step(lbm_handle* h, int64_t nsteps) {
+    if (!h) return LBM_ERR_PARAM;
+    if (nsteps < 0) return fail(h, LBM_ERR_PARAM, "nsteps < 0");
+    if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
+    if (nsteps == 0) return LBM_OK;
+    CK(h, cudaSetDevice(h->device));
+    int64_t done = 0;
+    const bool fused = h->p.precision == LBM_FP64 ? h->fused_valid : fast_fused_valid(h->F);
+    if (!fused) {
+        enqueue_one(h, true);
+        if (h->p.precision == LBM_FP64) h->fused_valid = true;
+        done = 1;
+    }
+    while (done < nsteps) {
+        if (at_graph_origin(h) && nsteps - done >= kChunkSteps) {
+            if (!h->graph_exec) {
+                int st = capture_chunk(h);
+                if (st != LBM_OK) return st;
+            }
+            CK(h, cudaGraphLaunch(h->graph_exec, h->stream));
+            done += kChunkSteps;
+        } else {
+            enqueue_one(h, false);
+            done += 1;
+        }
+    }
+    CK_LAUNCH(h, "fused step");
+    h->itc += nsteps;
+    return LBM_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// diagnostics
+// ------------------------------------------------------------------------------------
+static int run_reduce(lbm_handle* h, DiagOp op, double sums[DIAG_NSUM]) {
+    const int nb = diag_blocks(op == DIAG_NU_COLD_MID ? (long long)h->geo.nx * h->geo.nz : h->geo.ncell);
+    if (h->p.precision == LBM_FP64) {
+        DiagFields<double> F{h->A.u, h->A.v, h->A.w, h->A.T, h->A.rho, h->A.up, h->A.vp, h->A.wp, h->A.Tp};
+        diag_reduce<double>(op, h->geo, h->dsc, F, h->d_part, nb, h->stream);
+    } else {
+        DiagFields<float> F = fast_diag_fields(h->F);
+        diag_reduce<float>(op, h->geo, h->dsc, F, h->d_part, nb, h->stream);
+    }
+    CK_LAUNCH(h, "reduction");
+    CK(h, cudaMemcpyAsync(h->h_part.data(), h->d_part, (size_t)nb * DIAG_NSUM * sizeof(double), cudaMemcpyDeviceToHost,
+                          h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int s = 0; s < DIAG_NSUM; ++s) sums[s] = 0.0;
+    for (int b = 0; b < nb; ++b)
+        for (int s = 0; s < DIAG_NSUM; ++s) sums[s] += h->h_part[(size_t)b * DIAG_NSUM + s];
+    return LBM_OK;
+}
+
+static int diag_prologue(lbm_handle* h) {
+    if (!h) return LBM_ERR_PARAM;
+    if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
+    CK(h, cudaSetDevice(h->device));
+    return materialize(h);
+}
+
+extern "C" int lbm_check(lbm_handle* h, double* errU, double* errT) {
+    int st = diag_prologue(h);
+    if (st != LBM_OK) return st;
+    if (!errU || !errT) return fail(h, LBM_ERR_PARAM, "null output");
+    double s[DIAG_NSUM];
+    if ((st = run_reduce(h, DIAG_CHECK, s)) != LBM_OK) return st;
+    if (h->dim == 3) {  // 3DRB.F90:1511-1520
+        *errU = (s[1] > 1.0e-30) ? std::sqrt(s[0]) / std::sqrt(s[1]) : std::sqrt(s[0]);
+        *errT = (s[3] > 1.0e-30) ? s[2] / s[3] : s[2];
+    } else {  // 2DRB.F90:1244-1245
+        *errU = std::sqrt(s[0]) / std::sqrt(s[1]);
+        *errT = s[2] / s[3];
+    }
+    if (s[4] != 0.0 || !std::isfinite(s[0]) || !std::isfinite(s[2]))
+        return fail(h, LBM_ERR_DIVERGED, "non-finite field or rho <= 0 in " + std::to_string((long long)s[4]) + " cells");
+    return LBM_OK;
+}
+
+extern "C" int lbm_calNuRe(lbm_handle* h, double* Nu, double* Re) {
+    int st = diag_prologue(h);
+    if (st != LBM_OK) return st;
+    if (!Nu || !Re) return fail(h, LBM_ERR_PARAM, "null output");
+    double s[DIAG_NSUM];
+    if ((st = run_reduce(h, DIAG_NURE, s)) != LBM_OK) return st;
+    const double N = (double)h->geo.ncell;
+    *Nu = s[0] / N * h->c.lengthUnit / h->c.diffusivity + 1.0;
+    *Re = std::sqrt(s[1] / N) * h->c.lengthUnit / h->c.viscosity;
+    if (s[4] != 0.0 || !std::isfinite(*Nu) || !std::isfinite(*Re))
+        return fail(h, LBM_ERR_DIVERGED, "non-finite field or rho <= 0 in " + std::to_string((long long)s[4]) + " cells");
+    return LBM_OK;
+}
+
+extern "C" int lbm_RBcalc_Nu_global(lbm_handle* h, double* Nu) {
+    int st = diag_prologue(h);
+    if (st != LBM_OK) return st;
+    if (!Nu) return fail(h, LBM_ERR_PARAM, "null output");
+    double s[DIAG_NSUM];
+    if ((st = run_reduce(h, DIAG_NU_GLOBAL, s)) != LBM_OK) return st;
+    *Nu = (s[0] / (double)h->geo.ncell) / h->dsc.deltaT;
+    return std::isfinite(*Nu) ? LBM_OK : fail(h, LBM_ERR_DIVERGED, "non-finite Nu_global");
+}
+
+// fit_adiabatic_wall_T4 (2DRB.F90:1953-1991)
+static double fit_adiabatic_wall_T4(double y0, const double y[4], const double tt[4]) {
+    double s[4];
+    for (int k = 0; k < 4; ++k) s[k] = (y[k] - y0) * (y[k] - y0);
+    double S0 = 4.0, S1 = 0.0, S2 = 0.0, B0 = 0.0, B1 = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        S1 = S1 + s[k];
+        S2 = S2 + s[k] * s[k];
+        B0 = B0 + tt[k];
+        B1 = B1 + tt[k] * s[k];
+    }
+    const double D = S0 * S2 - S1 * S1;
+    return (B0 * S2 - B1 * S1) / D;
+}
+
+// fit_parabola_ls5: 2D form (2DRB.F90:1999-2080) solves for (quadratic, linear,
+// constant); 3D form (3DRB.F90:2257-2334) for (constant, linear, quadratic) and also
+// rejects a parabola of the wrong curvature.
+static void fit_parabola_ls5(bool d3, const double y[5], const double f[5], int mode, double* fstar, double* ystar) {
+    const double epsD = 1.0e-20, epsA = 1.0e-14;
+    int kb = 0;
+    for (int k = 1; k < 5; ++k) {
+        if (mode == 1 ? (f[k] > f[kb]) : (f[k] < f[kb])) kb = k;
+    }
+    double S0 = 0, S1 = 0, S2 = 0, S3 = 0, S4 = 0, F0 = 0, F1 = 0, F2 = 0;
+    for (int k = 0; k < 5; ++k) {
+        S0 = S0 + 1.0;
+        S1 = S1 + y[k];
+        S2 = S2 + y[k] * y[k];
+        S3 = S3 + y[k] * y[k] * y[k];
+        S4 = S4 + y[k] * y[k] * y[k] * y[k];
+        F0 = F0 + f[k];
+        if (d3) {
+            F1 = F1 + f[k] * y[k];
+            F2 = F2 + f[k] * y[k] * y[k];
+        } else {
+            F1 = F1 + y[k] * f[k];
+            F2 = F2 + y[k] * y[k] * f[k];
+        }
+    }
+    double ymin = y[0], ymax = y[0];
+    for (int k = 1; k < 5; ++k) {
+        ymin = y[k] < ymin ? y[k] : ymin;
+        ymax = y[k] > ymax ? y[k] : ymax;
+    }
+    *ystar = y[kb];
+    *fstar = f[kb];
+    if (!d3) {
+        const double D = S4 * (S2 * S0 - S1 * S1) - S3 * (S3 * S0 - S1 * S2) + S2 * (S3 * S1 - S2 * S2);
+        const double DA = F2 * (S2 * S0 - S1 * S1) - S3 * (F1 * S0 - S1 * F0) + S2 * (F1 * S1 - S2 * F0);
+        const double DB = S4 * (F1 * S0 - S1 * F0) - F2 * (S3 * S0 - S1 * S2) + S2 * (S3 * F0 - F1 * S2);
+        const double DC = S4 * (S2 * F0 - F1 * S1) - S3 * (S3 * F0 - F1 * S2) + F2 * (S3 * S1 - S2 * S2);
+        if (std::fabs(D) > epsD) {
+            const double A = DA / D, B = DB / D, C = DC / D;
+            if (std::fabs(A) > epsA) {
+                const double ys = -B / (2.0 * A);
+                if (ys >= ymin && ys <= ymax) {
+                    *ystar = ys;
+                    *fstar = C - B * B / (4.0 * A);
+                }
+            }
+        }
+        return;
+    }
+    const double D = S0 * (S2 * S4 - S3 * S3) - S1 * (S1 * S4 - S2 * S3) + S2 * (S1 * S3 - S2 * S2);
+    const double DA = F0 * (S2 * S4 - S3 * S3) - S1 * (F1 * S4 - S3 * F2) + S2 * (F1 * S3 - S2 * F2);
+    const double DB = S0 * (F1 * S4 - S3 * F2) - F0 * (S1 * S4 - S2 * S3) + S2 * (S1 * F2 - F1 * S2);
+    const double DC = S0 * (S2 * F2 - F1 * S3) - S1 * (S1 * F2 - F1 * S2) + F0 * (S1 * S3 - S2 * S2);
+    if (std::fabs(D) <= epsD) return;
+    const double A = DA / D, B = DB / D, C = DC / D;
+    if (std::fabs(C) <= epsA || (mode == 1 && C >= 0.0) || (mode == -1 && C <= 0.0)) return;
+    const double ys = -B / (2.0 * C);
+    if (ys < ymin || ys > ymax) return;
+    *ystar = ys;
+    *fstar = A + B * ys + C * ys * ys;
+}
+
+extern "C" int lbm_RBcalc_Nu_wall_avg(lbm_handle* h, lbm_nu_wall* out) {
+    int st = diag_prologue(h);
+    if (st != LBM_OK) return st;
+    if (!out) return fail(h, LBM_ERR_PARAM, "null output");
+    const int nx = h->geo.nx, nz = h->geo.nz;
+    const bool d3 = h->dim == 3;
+    if (h->p.precision == LBM_FP64) diag_wall_columns<double>(h->geo, h->dsc, h->A.T, h->d_tb, h->d_nub, h->stream);
+    else diag_wall_columns<float>(h->geo, h->dsc, fast_diag_fields(h->F).T, h->d_tb, h->d_nub, h->stream);
+    CK_LAUNCH(h, "wall columns");
+    std::vector<double> Tb(nx + 2, 0.0), Nub(nx + 2, 0.0);
+    CK(h, cudaMemcpyAsync(Tb.data() + 1, h->d_tb, nx * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(Nub.data() + 1, h->d_nub, nx * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    const double L = h->c.lengthUnit, dy = h->dsc.dy, deltaT = h->dsc.deltaT, Thot = h->p.Thot;
+    std::vector<double> xp(nx + 2);
+    xp[0] = 0.0 / L;
+    xp[nx + 1] = (double)nx / L;
+    for (int i = 1; i <= nx; ++i) xp[i] = ((double)i - 0.5) / L;
+    // (1) hot wall mean (2DRB.F90:2329-2337, 3DRB.F90:2067-2080)
+    double sum_hot = 0.0;
+    for (int i = 1; i <= nx; ++i) sum_hot = sum_hot + Nub[i];
+    out->Nu_hot = sum_hot / (double)nx;
+    // (1.1) corner extension by the 4-point adiabatic fit
+    double xf[4], Tf[4];
+    for (int m = 0; m < 4; ++m) { xf[m] = xp[1 + m]; Tf[m] = Tb[1 + m]; }
+    const double T_wl = fit_adiabatic_wall_T4(0.0, xf, Tf);
+    for (int m = 0; m < 4; ++m) { xf[m] = xp[nx - 3 + m]; Tf[m] = Tb[nx - 3 + m]; }
+    const double T_wr = fit_adiabatic_wall_T4(xp[nx + 1], xf, Tf);
+    std::vector<double> ext(Nub);
+    ext[0] = (2.0 * (Thot - T_wl) / dy) / deltaT;
+    ext[nx + 1] = (2.0 * (Thot - T_wr) / dy) / deltaT;
+    // (1.2) grid extremes, (1.3)/(1.4) 5-point least-squares parabola around them
+    int imax = 0, imin = 0;
+    double vmax = ext[0], vmin = ext[0];
+    for (int i = 1; i <= nx + 1; ++i) {
+        if (ext[i] > vmax) { vmax = ext[i]; imax = i; }
+        if (ext[i] < vmin) { vmin = ext[i]; imin = i; }
+    }
+    auto pick = [nx](int ic, int ii[5]) {
+        for (int m = 0; m < 5; ++m) ii[m] = (ic <= 2) ? m : (ic >= nx - 1 ? nx - 3 + m : ic - 2 + m);
+    };
+    int ii[5];
+    double xk[5], fk[5], fstar, xstar;
+    pick(imax, ii);
+    for (int m = 0; m < 5; ++m) { xk[m] = xp[ii[m]]; fk[m] = ext[ii[m]]; }
+    fit_parabola_ls5(d3, xk, fk, +1, &fstar, &xstar);
+    out->Nu_hot_max = fstar;
+    out->Nu_hot_max_position = xstar;
+    pick(imin, ii);
+    for (int m = 0; m < 5; ++m) { xk[m] = xp[ii[m]]; fk[m] = ext[ii[m]]; }
+    fit_parabola_ls5(d3, xk, fk, -1, &fstar, &xstar);
+    out->Nu_hot_min = fstar;
+    out->Nu_hot_min_position = xstar;
+    // (2) cold wall and mid-plane means
+    double s[DIAG_NSUM];
+    if ((st = run_reduce(h, DIAG_NU_COLD_MID, s)) != LBM_OK) return st;
+    out->Nu_cold = s[0] / (double)(nx * nz);
+    out->Nu_middle = s[1] / (double)(nx * nz);
+    return std::isfinite(out->Nu_hot) && std::isfinite(out->Nu_cold) ? LBM_OK
+                                                                      : fail(h, LBM_ERR_DIVERGED, "non-finite wall Nu");
+}
+
+// ------------------------------------------------------------------------------------
+// state transfer
+// ------------------------------------------------------------------------------------
+static int ensure_stage(lbm_handle* h, size_t count) {
+    if (h->stage_cap >= count) return LBM_OK;
+    if (h->d_stage) {
+        for (auto it = h->allocs.begin(); it != h->allocs.end(); ++it)
+            if (*it == h->d_stage) {
+                h->allocs.erase(it);
+                break;
+            }
+        cudaFree(h->d_stage);
+        h->d_stage = nullptr;
+        h->stage_cap = 0;
+    }
+    int st = dalloc(h, &h->d_stage, count);
+    if (st != LBM_OK) return st;
+    h->stage_cap = count;
+    return LBM_OK;
+}
+
+static double* scalar_ptr(lbm_handle* h, int field) {
+    ExactArrays& A = h->A;
+    const bool d3 = h->dim == 3;
+    switch (field) {
+        case LBM_FIELD_RHO: return A.rho;
+        case LBM_FIELD_U: return A.u;
+        case LBM_FIELD_V: return A.v;
+        case LBM_FIELD_W: return d3 ? A.w : nullptr;
+        case LBM_FIELD_T: return A.T;
+        case LBM_FIELD_BX_PREV: return A.Bx;
+        case LBM_FIELD_BY_PREV: return A.By;
+        case LBM_FIELD_BZ_PREV: return d3 ? A.Bz : nullptr;
+        case LBM_FIELD_FX: return d3 ? nullptr : A.Fx;
+        case LBM_FIELD_FY: return d3 ? nullptr : A.Fy;
+        default: return nullptr;
+    }
+}
+
+static int state_io(lbm_handle* h, int field, double* dst, const double* src, size_t count) {
+    if (!h || (!dst && !src)) return LBM_ERR_PARAM;
+    if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
+    CK(h, cudaSetDevice(h->device));
+    int st = materialize(h);
+    if (st != LBM_OK) return st;
+    const long long n = h->geo.ncell;
+    const bool pop = field == LBM_FIELD_F || field == LBM_FIELD_G || field == LBM_FIELD_F_POST || field == LBM_FIELD_G_POST;
+    const int qq = (field == LBM_FIELD_F || field == LBM_FIELD_F_POST) ? h->q : h->qt;
+    const size_t want = pop ? (size_t)qq * n : (size_t)n;
+    if (count != want) return fail(h, LBM_ERR_PARAM, "count does not match the field size");
+    if (h->p.precision != LBM_FP64) {
+        if ((st = ensure_stage(h, want)) != LBM_OK) return st;
+        if (dst) {
+            st = fast_export(h->F, h->geo, h->phys, h->dim, field, h->d_stage, h->stream);
+            if (st != LBM_OK) return fail(h, st, "field not available for this precision");
+            CK_LAUNCH(h, "export");
+            CK(h, cudaMemcpyAsync(dst, h->d_stage, want * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            CK(h, cudaStreamSynchronize(h->stream));
+        } else {
+            CK(h, cudaMemcpyAsync(h->d_stage, src, want * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+            st = fast_import(h->F, h->geo, h->phys, h->dim, field, h->d_stage, h->stream);
+            if (st != LBM_OK) return fail(h, st, "field not settable for this precision");
+            CK_LAUNCH(h, "import");
+            CK(h, cudaStreamSynchronize(h->stream));
+        }
+        return LBM_OK;
+    }
+    if (pop) {
+        double* soa = field == LBM_FIELD_F ? h->A.f : field == LBM_FIELD_G ? h->A.g : field == LBM_FIELD_F_POST ? h->A.fpost : h->A.gpost;
+        if ((st = ensure_stage(h, want)) != LBM_OK) return st;
+        if (dst) {
+            soa_to_aos(soa, h->d_stage, qq, n, h->stream);
+            CK_LAUNCH(h, "soa_to_aos");
+            CK(h, cudaMemcpyAsync(dst, h->d_stage, want * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        } else {
+            CK(h, cudaMemcpyAsync(h->d_stage, src, want * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+            aos_to_soa(h->d_stage, soa, qq, n, h->stream);
+            CK_LAUNCH(h, "aos_to_soa");
+        }
+        CK(h, cudaStreamSynchronize(h->stream));
+        return LBM_OK;
+    }
+    double* d = scalar_ptr(h, field);
+    if (!d) return fail(h, LBM_ERR_PARAM, "field not defined for this dimension");
+    if (dst) CK(h, cudaMemcpyAsync(dst, d, want * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    else CK(h, cudaMemcpyAsync(d, src, want * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return LBM_OK;
+}
+
+extern "C" int lbm_get_state(lbm_handle* h, int field, double* host, size_t count) {
+    if (!host) return LBM_ERR_PARAM;
+    return state_io(h, field, host, nullptr, count);
+}
+
+extern "C" int lbm_set_state(lbm_handle* h, int field, const double* host, size_t count) {
+    if (!host) return LBM_ERR_PARAM;
+    return state_io(h, field, nullptr, host, count);
+}
+
+// ------------------------------------------------------------------------------------
+// measurement hooks
+// ------------------------------------------------------------------------------------
+extern "C" int lbm_get_stream(lbm_handle* h, void** stream) {
+    if (!h || !stream) return LBM_ERR_PARAM;
+    *stream = (void*)h->stream;
+    return LBM_OK;
+}
+
+extern "C" int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, double* ms_thermal) {
+    if (!h || !ms_flow || !ms_thermal || nsteps <= 0) return LBM_ERR_PARAM;
+    if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
+    CK(h, cudaSetDevice(h->device));
+    const bool fused = h->p.precision == LBM_FP64 ? h->fused_valid : fast_fused_valid(h->F);
+    if (!fused) {
+        int st = lbm_step(h, 1);
+        if (st != LBM_OK) return st;
+    }
+    std::vector<cudaEvent_t> ev((size_t)(2 * nsteps + 1));
+    for (auto& e : ev) CK(h, cudaEventCreate(&e));
+    CK(h, cudaEventRecord(ev[0], h->stream));
+    for (int64_t k = 0; k < nsteps; ++k) {
+        if (h->p.precision == LBM_FP64) {
+            const int nxt = h->cur ^ 1;
+            exact_fused_step(h->geo, h->phys, h->A, h->dim, false, h->fbuf[h->cur], h->gbuf[h->cur], h->fbuf[nxt],
+                             h->gbuf[nxt], h->stream, 0);
+            CK(h, cudaEventRecord(ev[2 * k + 1], h->stream));
+            exact_fused_step(h->geo, h->phys, h->A, h->dim, false, h->fbuf[h->cur], h->gbuf[h->cur], h->fbuf[nxt],
+                             h->gbuf[nxt], h->stream, 1);
+            h->cur = nxt;
+        } else {
+            fast_step(h->F, h->geo, h->phys, h->dim, false, h->stream, 0);
+            CK(h, cudaEventRecord(ev[2 * k + 1], h->stream));
+            fast_step(h->F, h->geo, h->phys, h->dim, false, h->stream, 1);
+        }
+        CK(h, cudaEventRecord(ev[2 * k + 2], h->stream));
+    }
+    CK_LAUNCH(h, "timed steps");
+    CK(h, cudaEventSynchronize(ev.back()));
+    double tf = 0.0, tt = 0.0;
+    for (int64_t k = 0; k < nsteps; ++k) {
+        float a = 0.f, b = 0.f;
+        CK(h, cudaEventElapsedTime(&a, ev[2 * k], ev[2 * k + 1]));
+        CK(h, cudaEventElapsedTime(&b, ev[2 * k + 1], ev[2 * k + 2]));
+        tf += a;
+        tt += b;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    *ms_flow = tf / (double)nsteps;
+    *ms_thermal = tt / (double)nsteps;
+    h->itc += nsteps;
+    return LBM_OK;
+}

@@ -1,0 +1,156 @@
+// lbm_device.cuh - lattice tables, index arithmetic and the pull-with-boundary rule shared
+// by every kernel of the library (exact FP64, FP32/FP16 storage, reductions).
+//
+// Layout in HBM: structure of arrays, one plane of `ncell` values per direction,
+// cell index c = i + nx*(j + ny*k) with 0-based i,j,k (x fastest, so a warp reads 32
+// consecutive cells of one direction: fully coalesced).  No ghost layers are stored;
+// the reference's ghost-padded f_post (3DRB.F90:472) is replaced by the boundary rule
+// below, evaluated inside the streaming pull.
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/lbm_gpu.h"
+
+namespace lbm {
+
+// ------------------------------------------------------------------------------------
+// Lattice velocity sets.  D2Q9 order 0,E,N,W,S,NE,NW,SW,SE (2DRB.F90:189-190); D2Q5 is
+// its first five.  D3Q19 / D3Q7 order and opposites from 3DRB.F90:655-667.  The tables
+// are constexpr functions so that fully unrolled loops fold them into immediates.
+// ------------------------------------------------------------------------------------
+template <int Q> struct Lat;
+
+template <> struct Lat<9> {
+    static constexpr int D = 2;
+    __host__ __device__ static constexpr int ex(int a) { return (a == 1 || a == 5 || a == 8) ? 1 : (a == 3 || a == 6 || a == 7) ? -1 : 0; }
+    __host__ __device__ static constexpr int ey(int a) { return (a == 2 || a == 5 || a == 6) ? 1 : (a == 4 || a == 7 || a == 8) ? -1 : 0; }
+    __host__ __device__ static constexpr int ez(int) { return 0; }
+    __host__ __device__ static constexpr int opp(int a) { return a == 0 ? 0 : (a <= 4 ? ((a + 1) % 4) + 1 : ((a - 5 + 2) % 4) + 5); }
+};
+template <> struct Lat<5> {
+    static constexpr int D = 2;
+    __host__ __device__ static constexpr int ex(int a) { return Lat<9>::ex(a); }
+    __host__ __device__ static constexpr int ey(int a) { return Lat<9>::ey(a); }
+    __host__ __device__ static constexpr int ez(int) { return 0; }
+    __host__ __device__ static constexpr int opp(int a) { return Lat<9>::opp(a); }
+};
+template <> struct Lat<19> {
+    static constexpr int D = 3;
+    __host__ __device__ static constexpr int ex(int a) {
+        return (a == 1 || a == 7 || a == 9 || a == 11 || a == 13) ? 1 : (a == 2 || a == 8 || a == 10 || a == 12 || a == 14) ? -1 : 0;
+    }
+    __host__ __device__ static constexpr int ey(int a) {
+        return (a == 3 || a == 7 || a == 8 || a == 15 || a == 17) ? 1 : (a == 4 || a == 9 || a == 10 || a == 16 || a == 18) ? -1 : 0;
+    }
+    __host__ __device__ static constexpr int ez(int a) {
+        return (a == 5 || a == 11 || a == 12 || a == 15 || a == 16) ? 1 : (a == 6 || a == 13 || a == 14 || a == 17 || a == 18) ? -1 : 0;
+    }
+    __host__ __device__ static constexpr int opp(int a) {
+        return a == 0 ? 0 : (a <= 6 ? (a % 2 == 1 ? a + 1 : a - 1)
+                                    : (a <= 10 ? 17 - a : (a <= 14 ? 25 - a : 33 - a)));
+    }
+};
+template <> struct Lat<7> {
+    static constexpr int D = 3;
+    __host__ __device__ static constexpr int ex(int a) { return Lat<19>::ex(a); }
+    __host__ __device__ static constexpr int ey(int a) { return Lat<19>::ey(a); }
+    __host__ __device__ static constexpr int ez(int a) { return Lat<19>::ez(a); }
+    __host__ __device__ static constexpr int opp(int a) { return Lat<19>::opp(a); }
+};
+
+static_assert(Lat<9>::opp(1) == 3 && Lat<9>::opp(2) == 4 && Lat<9>::opp(3) == 1 && Lat<9>::opp(4) == 2, "d2q9 opp");
+static_assert(Lat<9>::opp(5) == 7 && Lat<9>::opp(6) == 8 && Lat<9>::opp(7) == 5 && Lat<9>::opp(8) == 6, "d2q9 opp");
+static_assert(Lat<19>::opp(7) == 10 && Lat<19>::opp(8) == 9 && Lat<19>::opp(11) == 14 && Lat<19>::opp(12) == 13, "d3q19 opp");
+static_assert(Lat<19>::opp(15) == 18 && Lat<19>::opp(16) == 17 && Lat<19>::opp(5) == 6 && Lat<19>::opp(2) == 1, "d3q19 opp");
+
+// ------------------------------------------------------------------------------------
+// Geometry and boundary switches of one lattice, passed by value to every kernel.
+// ------------------------------------------------------------------------------------
+struct Geo {
+    int nx, ny, nz;      // nz = 1 in 2D
+    long long ncell;
+    int bcf[3];          // LBM_BC_* per axis
+    int bct[3];          // LBM_BCT_* per axis
+    double bcT_lo[3];    // anti-bounce-back source term at the low face of each axis
+    double bcT_hi[3];    // ... and at the high face
+};
+
+__host__ __device__ inline long long cell_index(const Geo& g, int i, int j, int k) {
+    return (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
+}
+
+// Pull of direction `a` into cell (i,j,k) from a post-collision array, with the
+// reference's boundary handling folded in.
+//
+// The reference streams from a zero ghost layer and then overwrites the incoming
+// directions face by face in a fixed order: x faces, then y, then z
+// (3DRB.F90:987-1058, 2DRB.F90:811-866).  For a direction whose source lies outside
+// the lattice along one or more axes the last of those faces wins, so the value is
+// the boundary rule of the last out-of-range axis:
+//   no-slip  : f_post(opp(a)) of the same cell (half-way bounce-back);
+//   periodic : f_post(a) of the cell wrapped along that axis only, other indices
+//              unchanged (the reference's same-row copy, 2DRB.F90:821-828).
+// LOAD(dir, cell) returns the stored value converted to the arithmetic type.
+template <int Q, class T, class LOAD>
+__device__ __forceinline__ T pull_flow(const Geo& g, int a, int i, int j, int k, long long c, LOAD load) {
+    const int si = i - Lat<Q>::ex(a), sj = j - Lat<Q>::ey(a), sk = k - Lat<Q>::ez(a);
+    int axis = -1;
+    if (Lat<Q>::ex(a) != 0 && (si < 0 || si >= g.nx)) axis = 0;
+    if (Lat<Q>::ey(a) != 0 && (sj < 0 || sj >= g.ny)) axis = 1;
+    if (Lat<Q>::ez(a) != 0 && (sk < 0 || sk >= g.nz)) axis = 2;
+    if (axis < 0) {
+        const long long off = (long long)(-Lat<Q>::ex(a)) + (long long)g.nx * ((long long)(-Lat<Q>::ey(a)) + (long long)g.ny * (long long)(-Lat<Q>::ez(a)));
+        return load(a, c + off);
+    }
+    if (g.bcf[axis] == LBM_BC_NOSLIP) return load(Lat<Q>::opp(a), c);
+    if (axis == 0) return load(a, cell_index(g, si < 0 ? g.nx - 1 : 0, j, k));
+    if (axis == 1) return load(a, cell_index(g, i, sj < 0 ? g.ny - 1 : 0, k));
+    return load(a, cell_index(g, i, j, sk < 0 ? g.nz - 1 : 0));
+}
+
+// Thermal pull (D2Q5 / D3Q7, axis-aligned: at most one axis out of range), with the
+// bouncebackT rules (3DRB.F90:1243-1351, 2DRB.F90:1026-1107):
+//   constant T : -g_post(opp(a)) + bc term (2*omegaT*Tw, Tw = Thot low face / Tcold high);
+//   adiabatic  :  g_post(opp(a));
+//   periodic   :  g_post(a) of the wrapped cell.
+template <int QT, class T, class LOAD>
+__device__ __forceinline__ T pull_thermal(const Geo& g, int a, int i, int j, int k, long long c, LOAD load) {
+    if (a == 0) return load(0, c);
+    const int si = i - Lat<QT>::ex(a), sj = j - Lat<QT>::ey(a), sk = k - Lat<QT>::ez(a);
+    int axis = -1;
+    bool low = false;
+    if (Lat<QT>::ex(a) != 0 && (si < 0 || si >= g.nx)) { axis = 0; low = si < 0; }
+    if (Lat<QT>::ey(a) != 0 && (sj < 0 || sj >= g.ny)) { axis = 1; low = sj < 0; }
+    if (Lat<QT>::ez(a) != 0 && (sk < 0 || sk >= g.nz)) { axis = 2; low = sk < 0; }
+    if (axis < 0) {
+        const long long off = (long long)(-Lat<QT>::ex(a)) + (long long)g.nx * ((long long)(-Lat<QT>::ey(a)) + (long long)g.ny * (long long)(-Lat<QT>::ez(a)));
+        return load(a, c + off);
+    }
+    const int bt = g.bct[axis];
+    if (bt == LBM_BCT_CONST) return -load(Lat<QT>::opp(a), c) + (T)(low ? g.bcT_lo[axis] : g.bcT_hi[axis]);
+    if (bt == LBM_BCT_ADIABATIC) return load(Lat<QT>::opp(a), c);
+    if (axis == 0) return load(a, cell_index(g, si < 0 ? g.nx - 1 : 0, j, k));
+    if (axis == 1) return load(a, cell_index(g, i, sj < 0 ? g.ny - 1 : 0, k));
+    return load(a, cell_index(g, i, j, sk < 0 ? g.nz - 1 : 0));
+}
+
+// Decompose a linear thread index into (i,j,k).
+__device__ __forceinline__ void cell_coords(const Geo& g, long long c, int& i, int& j, int& k) {
+    const long long plane = (long long)g.nx * g.ny;
+    k = (int)(c / plane);
+    const long long r = c - (long long)k * plane;
+    j = (int)(r / g.nx);
+    i = (int)(r - (long long)j * g.nx);
+}
+
+// splitmix64 of (seed ^ cell) -> [0,1) with 53 random bits; integer-exact on host and device.
+__host__ __device__ inline double noise_xi(uint64_t seed, uint64_t idx) {
+    uint64_t z = (seed ^ idx) + 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z = z ^ (z >> 31);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+}  // namespace lbm

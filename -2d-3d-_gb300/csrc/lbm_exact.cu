@@ -1,0 +1,755 @@
+// lbm_exact.cu - the plain method: FP64 kernels that reproduce the reference's arithmetic.
+//
+// Compiled with -fmad=false (no multiply-add contraction) and IEEE division/sqrt, with
+// every expression in the reference's left-to-right order, so each kernel returns the
+// same bits as the reference's loop body on the same inputs.
+//
+//  * Stage kernels: one per reference subroutine (collision .. macroT), operating on the
+//    reference's module arrays (f, f_post, rho, u, v, w, T, ...), for stage-by-stage parity.
+//  * Fused step: two kernels per time step over SoA population buffers:
+//      k_flow    : pull f_post_{n-1} + boundary rule -> f_{n-1}; macro with the lagged
+//                  temperature; pull g_post_{n-1} -> T_{n-1}; MRT collision -> f_post_n.
+//      k_thermal : pull f_post_n -> f_n, rho_n, u_n; pull g_post_{n-1} -> g_{n-1}, T_{n-1};
+//                  thermal MRT collision with the M1G term -> g_post_n, B_prev, T lag.
+//    The reference's step order (collision, streaming, bounceback, macro, collisionT,
+//    streamingT, bouncebackT, macroT, 3DRB.F90:227-241) couples flow step n+1 to the
+//    thermal streaming of step n (a dependency cone of radius 2), so one pass per step
+//    cannot pull both; the split keeps each kernel a radius-1 pull.
+#include <cuda_runtime.h>
+
+#include "lbm_device.cuh"
+#include "lbm_internal.h"
+
+namespace lbm {
+
+// ------------------------------------------------------------------------------------
+// Per-cell arithmetic, verbatim from the reference.
+// ------------------------------------------------------------------------------------
+
+// collision (2DRB.F90:688-759).  Writes f_post and the stored body force (Fx, Fy).
+__device__ __forceinline__ void collide_2d(const double* F, double rho, double u, double v, double T,
+                                           const PhysC& P, double* FP, double& FxOut, double& FyOut) {
+    double m[9], meq[9], s[9], fSource[9], m_post[9];
+    m[0] = F[0] + F[1] + F[2] + F[3] + F[4] + F[5] + F[6] + F[7] + F[8];
+    m[1] = -4.0 * F[0] - F[1] - F[2] - F[3] - F[4] + 2.0 * (F[5] + F[6] + F[7] + F[8]);
+    m[2] = 4.0 * F[0] - 2.0 * (F[1] + F[2] + F[3] + F[4]) + F[5] + F[6] + F[7] + F[8];
+    m[3] = F[1] - F[3] + F[5] - F[6] - F[7] + F[8];
+    m[4] = -2.0 * F[1] + 2.0 * F[3] + F[5] - F[6] - F[7] + F[8];
+    m[5] = F[2] - F[4] + F[5] + F[6] - F[7] - F[8];
+    m[6] = -2.0 * F[2] + 2.0 * F[4] + F[5] + F[6] - F[7] - F[8];
+    m[7] = F[1] - F[2] + F[3] - F[4];
+    m[8] = F[5] - F[6] + F[7] - F[8];
+
+    meq[0] = rho;
+    meq[1] = rho * (-2.0 + 3.0 * (u * u + v * v));
+    meq[2] = rho * (1.0 - 3.0 * (u * u + v * v));
+    meq[3] = rho * u;
+    meq[4] = -(rho * u);
+    meq[5] = rho * v;
+    meq[6] = -(rho * v);
+    meq[7] = rho * (u * u - v * v);
+    meq[8] = rho * (u * v);
+
+    s[0] = 0.0; s[1] = P.Snu; s[2] = P.Snu; s[3] = 0.0; s[4] = P.Sq;
+    s[5] = 0.0; s[6] = P.Sq;  s[7] = P.Snu; s[8] = P.Snu;
+
+    const double Fx = 0.0;
+    const double Fy = rho * P.gBeta * (T - P.Tref);
+    FxOut = Fx;
+    FyOut = Fy;
+
+    fSource[0] = 0.0;
+    fSource[1] = (6.0 - 3.0 * s[1]) * (u * Fx + v * Fy);
+    fSource[2] = -((6.0 - 3.0 * s[2]) * (u * Fx + v * Fy));
+    fSource[3] = (1.0 - 0.5 * s[3]) * Fx;
+    fSource[4] = -((1.0 - 0.5 * s[4]) * Fx);
+    fSource[5] = (1.0 - 0.5 * s[5]) * Fy;
+    fSource[6] = -((1.0 - 0.5 * s[6]) * Fy);
+    fSource[7] = (2.0 - s[7]) * (u * Fx - v * Fy);
+    fSource[8] = (1.0 - 0.5 * s[8]) * (u * Fy + v * Fx);
+
+#pragma unroll
+    for (int a = 0; a < 9; ++a) m_post[a] = m[a] - s[a] * (m[a] - meq[a]) + fSource[a];
+
+    FP[0] = m_post[0] / 9.0 - m_post[1] / 9.0 + m_post[2] / 9.0;
+    FP[1] = m_post[0] / 9.0 - m_post[1] / 36.0 - m_post[2] / 18.0 + m_post[3] / 6.0 - m_post[4] / 6.0 + m_post[7] / 4.0;
+    FP[2] = m_post[0] / 9.0 - m_post[1] / 36.0 - m_post[2] / 18.0 + m_post[5] / 6.0 - m_post[6] / 6.0 - m_post[7] / 4.0;
+    FP[3] = m_post[0] / 9.0 - m_post[1] / 36.0 - m_post[2] / 18.0 - m_post[3] / 6.0 + m_post[4] / 6.0 + m_post[7] / 4.0;
+    FP[4] = m_post[0] / 9.0 - m_post[1] / 36.0 - m_post[2] / 18.0 - m_post[5] / 6.0 + m_post[6] / 6.0 - m_post[7] / 4.0;
+    FP[5] = m_post[0] / 9.0 + m_post[1] / 18.0 + m_post[2] / 36.0 + m_post[3] / 6.0 + m_post[4] / 12.0
+            + m_post[5] / 6.0 + m_post[6] / 12.0 + m_post[8] / 4.0;
+    FP[6] = m_post[0] / 9.0 + m_post[1] / 18.0 + m_post[2] / 36.0 - m_post[3] / 6.0 - m_post[4] / 12.0
+            + m_post[5] / 6.0 + m_post[6] / 12.0 - m_post[8] / 4.0;
+    FP[7] = m_post[0] / 9.0 + m_post[1] / 18.0 + m_post[2] / 36.0 - m_post[3] / 6.0 - m_post[4] / 12.0
+            - m_post[5] / 6.0 - m_post[6] / 12.0 + m_post[8] / 4.0;
+    FP[8] = m_post[0] / 9.0 + m_post[1] / 18.0 + m_post[2] / 36.0 + m_post[3] / 6.0 + m_post[4] / 12.0
+            - m_post[5] / 6.0 - m_post[6] / 12.0 - m_post[8] / 4.0;
+}
+
+// collision (3DRB.F90:704-943).
+__device__ __forceinline__ void collide_3d(const double* f, double rhoLoc, double uLoc, double vLoc, double wLoc,
+                                           double Tc, const PhysC& P, double* fp) {
+    double m[19], meq[19], s[19], fSource[19], mp[19];
+    const double u2 = uLoc * uLoc + vLoc * vLoc + wLoc * wLoc;
+    m[0] = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8] + f[9] + f[10] + f[11] + f[12]
+           + f[13] + f[14] + f[15] + f[16] + f[17] + f[18];
+    m[1] = -30.0 * f[0] - 11.0 * (f[1] + f[2] + f[3] + f[4] + f[5] + f[6])
+           + 8.0 * (f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14] + f[15] + f[16] + f[17] + f[18]);
+    m[2] = 12.0 * f[0] - 4.0 * (f[1] + f[2] + f[3] + f[4] + f[5] + f[6])
+           + (f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14] + f[15] + f[16] + f[17] + f[18]);
+    m[3] = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+    m[4] = -4.0 * f[1] + 4.0 * f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+    m[5] = f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
+    m[6] = -4.0 * f[3] + 4.0 * f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
+    m[7] = f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
+    m[8] = -4.0 * f[5] + 4.0 * f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
+    m[9] = 2.0 * (f[1] + f[2]) - (f[3] + f[4] + f[5] + f[6]) + (f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14])
+           - 2.0 * (f[15] + f[16] + f[17] + f[18]);
+    m[10] = -4.0 * (f[1] + f[2]) + 2.0 * (f[3] + f[4] + f[5] + f[6])
+            + (f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14]) - 2.0 * (f[15] + f[16] + f[17] + f[18]);
+    m[11] = (f[3] + f[4]) - (f[5] + f[6]) + (f[7] + f[8] + f[9] + f[10]) - (f[11] + f[12] + f[13] + f[14]);
+    m[12] = -2.0 * (f[3] + f[4]) + 2.0 * (f[5] + f[6]) + (f[7] + f[8] + f[9] + f[10]) - (f[11] + f[12] + f[13] + f[14]);
+    m[13] = f[7] - f[8] - f[9] + f[10];
+    m[14] = f[15] - f[16] - f[17] + f[18];
+    m[15] = f[11] - f[12] - f[13] + f[14];
+    m[16] = f[7] - f[8] + f[9] - f[10] - f[11] + f[12] - f[13] + f[14];
+    m[17] = -f[7] - f[8] + f[9] + f[10] + f[15] - f[16] + f[17] - f[18];
+    m[18] = f[11] + f[12] - f[13] - f[14] - f[15] - f[16] + f[17] + f[18];
+
+    meq[0] = rhoLoc;
+    meq[1] = rhoLoc * (-11.0 + 19.0 * u2);
+    meq[2] = rhoLoc * (3.0 - 11.0 * u2 / 2.0);
+    meq[3] = rhoLoc * uLoc;
+    meq[4] = -2.0 * rhoLoc * uLoc / 3.0;
+    meq[5] = rhoLoc * vLoc;
+    meq[6] = -2.0 * rhoLoc * vLoc / 3.0;
+    meq[7] = rhoLoc * wLoc;
+    meq[8] = -2.0 * rhoLoc * wLoc / 3.0;
+    meq[9] = rhoLoc * (2.0 * uLoc * uLoc - vLoc * vLoc - wLoc * wLoc);
+    meq[10] = -0.5 * meq[9];
+    meq[11] = rhoLoc * (vLoc * vLoc - wLoc * wLoc);
+    meq[12] = -0.5 * meq[11];
+    meq[13] = rhoLoc * uLoc * vLoc;
+    meq[14] = rhoLoc * vLoc * wLoc;
+    meq[15] = rhoLoc * uLoc * wLoc;
+    meq[16] = 0.0;
+    meq[17] = 0.0;
+    meq[18] = 0.0;
+
+    s[0] = 0.0;    s[1] = P.Se;   s[2] = P.Seps; s[3] = 0.0;    s[4] = P.Sq;
+    s[5] = 0.0;    s[6] = P.Sq;   s[7] = 0.0;    s[8] = P.Sq;   s[9] = P.Snu;
+    s[10] = P.Spi; s[11] = P.Snu; s[12] = P.Spi; s[13] = P.Snu; s[14] = P.Snu;
+    s[15] = P.Snu; s[16] = P.Sm;  s[17] = P.Sm;  s[18] = P.Sm;
+
+    const double FxLoc = 0.0;
+    const double FyLoc = rhoLoc * P.gBeta * (Tc - P.Tref);
+    const double FzLoc = 0.0;
+    const double uDotF = uLoc * FxLoc + vLoc * FyLoc + wLoc * FzLoc;
+
+    fSource[0] = 0.0;
+    fSource[1] = (1.0 - 0.5 * s[1]) * 38.0 * uDotF;
+    fSource[2] = (1.0 - 0.5 * s[2]) * (-11.0) * uDotF;
+    fSource[3] = (1.0 - 0.5 * s[3]) * FxLoc;
+    fSource[4] = (1.0 - 0.5 * s[4]) * (-2.0 / 3.0) * FxLoc;
+    fSource[5] = (1.0 - 0.5 * s[5]) * FyLoc;
+    fSource[6] = (1.0 - 0.5 * s[6]) * (-2.0 / 3.0) * FyLoc;
+    fSource[7] = (1.0 - 0.5 * s[7]) * FzLoc;
+    fSource[8] = (1.0 - 0.5 * s[8]) * (-2.0 / 3.0) * FzLoc;
+    fSource[9] = (1.0 - 0.5 * s[9]) * (4.0 * uLoc * FxLoc - 2.0 * vLoc * FyLoc - 2.0 * wLoc * FzLoc);
+    fSource[10] = (1.0 - 0.5 * s[10]) * (-2.0 * uLoc * FxLoc + vLoc * FyLoc + wLoc * FzLoc);
+    fSource[11] = (1.0 - 0.5 * s[11]) * (2.0 * vLoc * FyLoc - 2.0 * wLoc * FzLoc);
+    fSource[12] = (1.0 - 0.5 * s[12]) * (-(vLoc * FyLoc) + wLoc * FzLoc);
+    fSource[13] = (1.0 - 0.5 * s[13]) * (uLoc * FyLoc + vLoc * FxLoc);
+    fSource[14] = (1.0 - 0.5 * s[14]) * (vLoc * FzLoc + wLoc * FyLoc);
+    fSource[15] = (1.0 - 0.5 * s[15]) * (uLoc * FzLoc + wLoc * FxLoc);
+    fSource[16] = 0.0;
+    fSource[17] = 0.0;
+    fSource[18] = 0.0;
+
+#pragma unroll
+    for (int a = 0; a < 19; ++a) mp[a] = m[a] - s[a] * (m[a] - meq[a]) + fSource[a];
+
+    fp[0] = mp[0] / 19.0 - 5.0 * mp[1] / 399.0 + mp[2] / 21.0;
+    fp[1] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 + mp[3] / 10.0 - mp[4] / 10.0 + mp[9] / 18.0 - mp[10] / 18.0;
+    fp[2] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 - mp[3] / 10.0 + mp[4] / 10.0 + mp[9] / 18.0 - mp[10] / 18.0;
+    fp[3] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 + mp[5] / 10.0 - mp[6] / 10.0 - mp[9] / 36.0 + mp[10] / 36.0
+            + mp[11] / 12.0 - mp[12] / 12.0;
+    fp[4] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 - mp[5] / 10.0 + mp[6] / 10.0 - mp[9] / 36.0 + mp[10] / 36.0
+            + mp[11] / 12.0 - mp[12] / 12.0;
+    fp[5] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 + mp[7] / 10.0 - mp[8] / 10.0 - mp[9] / 36.0 + mp[10] / 36.0
+            - mp[11] / 12.0 + mp[12] / 12.0;
+    fp[6] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 - mp[7] / 10.0 + mp[8] / 10.0 - mp[9] / 36.0 + mp[10] / 36.0
+            - mp[11] / 12.0 + mp[12] / 12.0;
+    fp[7] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[3] / 10.0 + mp[4] / 40.0 + mp[5] / 10.0 + mp[6] / 40.0
+            + mp[9] / 36.0 + mp[10] / 72.0 + mp[11] / 12.0 + mp[12] / 24.0 + mp[13] / 4.0 + mp[16] / 8.0 - mp[17] / 8.0;
+    fp[8] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[3] / 10.0 - mp[4] / 40.0 + mp[5] / 10.0 + mp[6] / 40.0
+            + mp[9] / 36.0 + mp[10] / 72.0 + mp[11] / 12.0 + mp[12] / 24.0 - mp[13] / 4.0 - mp[16] / 8.0 - mp[17] / 8.0;
+    fp[9] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[3] / 10.0 + mp[4] / 40.0 - mp[5] / 10.0 - mp[6] / 40.0
+            + mp[9] / 36.0 + mp[10] / 72.0 + mp[11] / 12.0 + mp[12] / 24.0 - mp[13] / 4.0 + mp[16] / 8.0 + mp[17] / 8.0;
+    fp[10] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[3] / 10.0 - mp[4] / 40.0 - mp[5] / 10.0 - mp[6] / 40.0
+             + mp[9] / 36.0 + mp[10] / 72.0 + mp[11] / 12.0 + mp[12] / 24.0 + mp[13] / 4.0 - mp[16] / 8.0 + mp[17] / 8.0;
+    fp[11] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[3] / 10.0 + mp[4] / 40.0 + mp[7] / 10.0 + mp[8] / 40.0
+             + mp[9] / 36.0 + mp[10] / 72.0 - mp[11] / 12.0 - mp[12] / 24.0 + mp[15] / 4.0 - mp[16] / 8.0 + mp[18] / 8.0;
+    fp[12] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[3] / 10.0 - mp[4] / 40.0 + mp[7] / 10.0 + mp[8] / 40.0
+             + mp[9] / 36.0 + mp[10] / 72.0 - mp[11] / 12.0 - mp[12] / 24.0 - mp[15] / 4.0 + mp[16] / 8.0 + mp[18] / 8.0;
+    fp[13] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[3] / 10.0 + mp[4] / 40.0 - mp[7] / 10.0 - mp[8] / 40.0
+             + mp[9] / 36.0 + mp[10] / 72.0 - mp[11] / 12.0 - mp[12] / 24.0 - mp[15] / 4.0 - mp[16] / 8.0 - mp[18] / 8.0;
+    fp[14] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[3] / 10.0 - mp[4] / 40.0 - mp[7] / 10.0 - mp[8] / 40.0
+             + mp[9] / 36.0 + mp[10] / 72.0 - mp[11] / 12.0 - mp[12] / 24.0 + mp[15] / 4.0 + mp[16] / 8.0 - mp[18] / 8.0;
+    fp[15] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[5] / 10.0 + mp[6] / 40.0 + mp[7] / 10.0 + mp[8] / 40.0
+             - mp[9] / 18.0 - mp[10] / 36.0 + mp[14] / 4.0 + mp[17] / 8.0 - mp[18] / 8.0;
+    fp[16] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[5] / 10.0 - mp[6] / 40.0 + mp[7] / 10.0 + mp[8] / 40.0
+             - mp[9] / 18.0 - mp[10] / 36.0 - mp[14] / 4.0 - mp[17] / 8.0 - mp[18] / 8.0;
+    fp[17] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[5] / 10.0 + mp[6] / 40.0 - mp[7] / 10.0 - mp[8] / 40.0
+             - mp[9] / 18.0 - mp[10] / 36.0 - mp[14] / 4.0 + mp[17] / 8.0 + mp[18] / 8.0;
+    fp[18] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[5] / 10.0 - mp[6] / 40.0 - mp[7] / 10.0 - mp[8] / 40.0
+             - mp[9] / 18.0 - mp[10] / 36.0 + mp[14] / 4.0 - mp[17] / 8.0 + mp[18] / 8.0;
+}
+
+// collisionT (2DRB.F90:921-974).  B = (u T, v T); returns g_post and the new B.
+__device__ __forceinline__ void collideT_2d(const double* G, double u, double v, double T, double Bxp, double Byp,
+                                            const PhysC& P, double* GP, double& BxOut, double& ByOut) {
+    double n[5], neq[5], q[5], n_post[5];
+    const double Bx = u * T;
+    const double By = v * T;
+    double dBx, dBy;
+    if (P.use_g) {
+        dBx = Bx - Bxp;
+        dBy = By - Byp;
+    } else {
+        dBx = 0.0;
+        dBy = 0.0;
+    }
+    BxOut = Bx;
+    ByOut = By;
+    n[0] = G[0] + G[1] + G[2] + G[3] + G[4];
+    n[1] = G[1] - G[3];
+    n[2] = G[2] - G[4];
+    n[3] = -4.0 * G[0] + G[1] + G[2] + G[3] + G[4];
+    n[4] = G[1] - G[2] + G[3] - G[4];
+    neq[0] = T;
+    neq[1] = T * u;
+    neq[2] = T * v;
+    neq[3] = P.legacy ? T * P.paraA : T * (-2.0 / 3.0);
+    neq[4] = 0.0;
+    q[0] = 0.0; q[1] = P.Qk; q[2] = P.Qk; q[3] = P.Qnu; q[4] = P.Qnu;
+    n_post[0] = n[0] - q[0] * (n[0] - neq[0]);
+    n_post[1] = n[1] - q[1] * (n[1] - neq[1]) + P.SG * dBx;
+    n_post[2] = n[2] - q[2] * (n[2] - neq[2]) + P.SG * dBy;
+    n_post[3] = n[3] - q[3] * (n[3] - neq[3]);
+    n_post[4] = n[4] - q[4] * (n[4] - neq[4]);
+    GP[0] = 0.2 * n_post[0] - 0.2 * n_post[3];
+    GP[1] = 0.2 * n_post[0] + 0.5 * n_post[1] + 0.05 * n_post[3] + 0.25 * n_post[4];
+    GP[2] = 0.2 * n_post[0] + 0.5 * n_post[2] + 0.05 * n_post[3] - 0.25 * n_post[4];
+    GP[3] = 0.2 * n_post[0] - 0.5 * n_post[1] + 0.05 * n_post[3] + 0.25 * n_post[4];
+    GP[4] = 0.2 * n_post[0] - 0.5 * n_post[2] + 0.05 * n_post[3] - 0.25 * n_post[4];
+}
+
+// collisionT (3DRB.F90:1121-1191).
+__device__ __forceinline__ void collideT_3d(const double* g, double u, double v, double w, double T, double Bxp,
+                                            double Byp, double Bzp, const PhysC& P, double* gp, double& BxOut,
+                                            double& ByOut, double& BzOut) {
+    double n[7], neq[7], q[7], n_post[7];
+    const double Bx = u * T, By = v * T, Bz = w * T;
+    double dBx, dBy, dBz;
+    if (P.use_g) {
+        dBx = Bx - Bxp;
+        dBy = By - Byp;
+        dBz = Bz - Bzp;
+    } else {
+        dBx = 0.0;
+        dBy = 0.0;
+        dBz = 0.0;
+    }
+    BxOut = Bx;
+    ByOut = By;
+    BzOut = Bz;
+    n[0] = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6];
+    n[1] = g[1] - g[2];
+    n[2] = g[3] - g[4];
+    n[3] = g[5] - g[6];
+    n[4] = -6.0 * g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6];
+    n[5] = 2.0 * g[1] + 2.0 * g[2] - g[3] - g[4] - g[5] - g[6];
+    n[6] = g[3] + g[4] - g[5] - g[6];
+    neq[0] = T;
+    neq[1] = Bx;
+    neq[2] = By;
+    neq[3] = Bz;
+    neq[4] = P.legacy ? P.paraA * T : -0.75 * T;
+    neq[5] = 0.0;
+    neq[6] = 0.0;
+    q[0] = 0.0; q[1] = P.Qk; q[2] = P.Qk; q[3] = P.Qk; q[4] = P.Qnu; q[5] = P.Qnu; q[6] = P.Qnu;
+    n_post[0] = n[0] - q[0] * (n[0] - neq[0]);
+    n_post[1] = n[1] - q[1] * (n[1] - neq[1]) + P.SG * dBx;
+    n_post[2] = n[2] - q[2] * (n[2] - neq[2]) + P.SG * dBy;
+    n_post[3] = n[3] - q[3] * (n[3] - neq[3]) + P.SG * dBz;
+    n_post[4] = n[4] - q[4] * (n[4] - neq[4]);
+    n_post[5] = n[5] - q[5] * (n[5] - neq[5]);
+    n_post[6] = n[6] - q[6] * (n[6] - neq[6]);
+    gp[0] = n_post[0] / 7.0 - n_post[4] / 7.0;
+    gp[1] = n_post[0] / 7.0 + n_post[1] / 2.0 + n_post[4] / 42.0 + n_post[5] / 6.0;
+    gp[2] = n_post[0] / 7.0 - n_post[1] / 2.0 + n_post[4] / 42.0 + n_post[5] / 6.0;
+    gp[3] = n_post[0] / 7.0 + n_post[2] / 2.0 + n_post[4] / 42.0 - n_post[5] / 12.0 + n_post[6] / 4.0;
+    gp[4] = n_post[0] / 7.0 - n_post[2] / 2.0 + n_post[4] / 42.0 - n_post[5] / 12.0 + n_post[6] / 4.0;
+    gp[5] = n_post[0] / 7.0 + n_post[3] / 2.0 + n_post[4] / 42.0 - n_post[5] / 12.0 - n_post[6] / 4.0;
+    gp[6] = n_post[0] / 7.0 - n_post[3] / 2.0 + n_post[4] / 42.0 - n_post[5] / 12.0 - n_post[6] / 4.0;
+}
+
+// macro (2DRB.F90:884-889): u = (sum e f + Fx/2)/rho with the force stored by collision.
+__device__ __forceinline__ void macro_2d(const double* F, double Fx, double Fy, double& rho, double& u, double& v) {
+    rho = F[0] + F[1] + F[2] + F[3] + F[4] + F[5] + F[6] + F[7] + F[8];
+    u = (F[1] - F[3] + F[5] - F[6] - F[7] + F[8] + 0.5 * Fx) / rho;
+    v = (F[2] - F[4] + F[5] + F[6] - F[7] - F[8] + 0.5 * Fy) / rho;
+}
+
+// macro (3DRB.F90:1077-1092): F_y recomputed with the new rho and the lagged T.
+__device__ __forceinline__ void macro_3d(const double* f, double Tlag, const PhysC& P, double& rho, double& u,
+                                         double& v, double& w) {
+    rho = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14]
+          + f[15] + f[16] + f[17] + f[18];
+    const double FyLoc = rho * P.gBeta * (Tlag - P.Tref);
+    u = (f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14]) / rho;
+    v = (f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18] + 0.5 * FyLoc) / rho;
+    w = (f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18]) / rho;
+}
+
+template <int QT>
+__device__ __forceinline__ double sumT(const double* g) {
+    double T = g[0] + g[1] + g[2] + g[3] + g[4];
+    if (QT == 7) T = T + g[5] + g[6];
+    return T;
+}
+
+__device__ __forceinline__ bool thread_cell(const Geo& g, long long& c, int& i, int& j, int& k) {
+    c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncell) return false;
+    cell_coords(g, c, i, j, k);
+    return true;
+}
+
+// ------------------------------------------------------------------------------------
+// initial (2DRB.F90:460-617, 3DRB.F90:445-603), loadInitField = 0
+// ------------------------------------------------------------------------------------
+template <int D>
+__global__ void k_initial(Geo g, PhysC P, InitC I, ExactArrays A) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
+    // xp(i) = (i - 0.5)/lengthUnit, xp(0) = 0, xp(nx+1) = nx/lengthUnit (1-based Fortran i)
+    const double xpi = ((double)(i + 1) - 0.5) / I.L, yp_j = ((double)(j + 1) - 0.5) / I.L;
+    const double xp0 = 0.0 / I.L, xpe = (double)g.nx / I.L, yp0 = 0.0 / I.L, ype = (double)g.ny / I.L;
+    double T = 0.0;
+    if (g.bct[0] == LBM_BCT_CONST) T = I.Thot + (xpi - xp0) / (xpe - xp0) * (I.Tcold - I.Thot);
+    if (g.bct[1] == LBM_BCT_CONST) {
+        T = I.Thot + (yp_j - yp0) / (ype - yp0) * (I.Tcold - I.Thot);
+        if (I.perturb) T = T + I.pert_amp * I.sx[i] * I.sy[j];
+    }
+    if (I.noise_amp != 0.0) T = T + I.noise_amp * (2.0 * noise_xi(I.seed, (uint64_t)c) - 1.0);
+    const double rho = 1.0, u = 0.0, v = 0.0, w = 0.0;
+    A.rho[c] = rho;
+    A.u[c] = u;
+    A.v[c] = v;
+    A.T[c] = T;
+    if (D == 3) A.w[c] = w;
+    const long long n = g.ncell;
+    if (D == 2) {
+        const double us2 = u * u + v * v;
+#pragma unroll
+        for (int a = 0; a < 9; ++a) {
+            const double un = u * (double)Lat<9>::ex(a) + v * (double)Lat<9>::ey(a);
+            const double om = (a == 0) ? 4.0 / 9.0 : (a <= 4 ? 1.0 / 9.0 : 1.0 / 36.0);
+            A.f[a * n + c] = rho * om * (1.0 + 3.0 * un + 4.5 * un * un - 1.5 * us2);
+        }
+#pragma unroll
+        for (int a = 0; a < 5; ++a) {
+            const double un = u * (double)Lat<9>::ex(a) + v * (double)Lat<9>::ey(a);
+            const double omT = (a == 0) ? P.omegaT0 : P.omegaT1;
+            A.g[a * n + c] = omT * T * (1.0 + P.geqc * un);
+        }
+    } else {
+        const double u2Loc = u * u + v * v + w * w;
+#pragma unroll
+        for (int a = 0; a < 19; ++a) {
+            const double eu = (double)Lat<19>::ex(a) * u + (double)Lat<19>::ey(a) * v + (double)Lat<19>::ez(a) * w;
+            const double om = (a == 0) ? 1.0 / 3.0 : (a <= 6 ? 1.0 / 18.0 : 1.0 / 36.0);
+            A.f[a * n + c] = om * rho * (1.0 + 3.0 * eu + 4.5 * eu * eu - 1.5 * u2Loc);
+        }
+#pragma unroll
+        for (int a = 0; a < 7; ++a) {
+            const double eu = (double)Lat<7>::ex(a) * u + (double)Lat<7>::ey(a) * v + (double)Lat<7>::ez(a) * w;
+            const double omT = (a == 0) ? P.omegaT0 : P.omegaT1;
+            A.g[a * n + c] = omT * T * (1.0 + P.geqc * eu);
+        }
+    }
+    A.Bx[c] = P.use_g ? u * T : 0.0;
+    A.By[c] = P.use_g ? v * T : 0.0;
+    if (D == 3) A.Bz[c] = P.use_g ? w * T : 0.0;
+    if (D == 2) {
+        A.Fx[c] = 0.0;
+        A.Fy[c] = 0.0;
+    }
+    A.up[c] = 0.0;
+    A.vp[c] = 0.0;
+    A.Tp[c] = 0.0;
+    if (D == 3) A.wp[c] = 0.0;
+#pragma unroll
+    for (int a = 0; a < Q; ++a) A.fpost[a * n + c] = 0.0;
+#pragma unroll
+    for (int a = 0; a < QT; ++a) A.gpost[a * n + c] = 0.0;
+}
+
+// ------------------------------------------------------------------------------------
+// Stage kernels: one per reference subroutine
+// ------------------------------------------------------------------------------------
+template <int D>
+__global__ void k_collision(Geo g, PhysC P, ExactArrays A) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    const long long n = g.ncell;
+    if (D == 2) {
+        double F[9], FP[9], Fx, Fy;
+#pragma unroll
+        for (int a = 0; a < 9; ++a) F[a] = A.f[a * n + c];
+        collide_2d(F, A.rho[c], A.u[c], A.v[c], A.T[c], P, FP, Fx, Fy);
+        A.Fx[c] = Fx;
+        A.Fy[c] = Fy;
+#pragma unroll
+        for (int a = 0; a < 9; ++a) A.fpost[a * n + c] = FP[a];
+    } else {
+        double F[19], FP[19];
+#pragma unroll
+        for (int a = 0; a < 19; ++a) F[a] = A.f[a * n + c];
+        collide_3d(F, A.rho[c], A.u[c], A.v[c], A.w[c], A.T[c], P, FP);
+#pragma unroll
+        for (int a = 0; a < 19; ++a) A.fpost[a * n + c] = FP[a];
+    }
+}
+
+// streaming: pull from the ghost-padded f_post; ghost cells are zero (2DRB.F90:787-795).
+template <int Q>
+__global__ void k_streaming(Geo g, const double* __restrict__ src, double* __restrict__ dst) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    const long long n = g.ncell;
+#pragma unroll
+    for (int a = 0; a < Q; ++a) {
+        const int si = i - Lat<Q>::ex(a), sj = j - Lat<Q>::ey(a), sk = k - Lat<Q>::ez(a);
+        double val = 0.0;
+        if (si >= 0 && si < g.nx && sj >= 0 && sj < g.ny && sk >= 0 && sk < g.nz) val = src[a * n + cell_index(g, si, sj, sk)];
+        dst[a * n + c] = val;
+    }
+}
+
+// bounceback / bouncebackT: the face rules applied in the reference's order to the
+// cells of the boundary faces only.
+template <int Q>
+__global__ void k_bounceback(Geo g, const double* __restrict__ fpost, double* __restrict__ f) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    const bool onface = i == 0 || i == g.nx - 1 || j == 0 || j == g.ny - 1 || (Lat<Q>::D == 3 && (k == 0 || k == g.nz - 1));
+    if (!onface) return;
+    const long long n = g.ncell;
+    auto load = [&](int a, long long cc) { return fpost[a * n + cc]; };
+#pragma unroll
+    for (int a = 1; a < Q; ++a) {
+        const int si = i - Lat<Q>::ex(a), sj = j - Lat<Q>::ey(a), sk = k - Lat<Q>::ez(a);
+        const bool out = si < 0 || si >= g.nx || sj < 0 || sj >= g.ny || sk < 0 || sk >= g.nz;
+        if (out) f[a * n + c] = pull_flow<Q, double>(g, a, i, j, k, c, load);
+    }
+}
+
+template <int QT>
+__global__ void k_bouncebackT(Geo g, const double* __restrict__ gpost, double* __restrict__ gg) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    const bool onface = i == 0 || i == g.nx - 1 || j == 0 || j == g.ny - 1 || (Lat<QT>::D == 3 && (k == 0 || k == g.nz - 1));
+    if (!onface) return;
+    const long long n = g.ncell;
+    auto load = [&](int a, long long cc) { return gpost[a * n + cc]; };
+#pragma unroll
+    for (int a = 1; a < QT; ++a) {
+        const int si = i - Lat<QT>::ex(a), sj = j - Lat<QT>::ey(a), sk = k - Lat<QT>::ez(a);
+        const bool out = si < 0 || si >= g.nx || sj < 0 || sj >= g.ny || sk < 0 || sk >= g.nz;
+        if (out) gg[a * n + c] = pull_thermal<QT, double>(g, a, i, j, k, c, load);
+    }
+}
+
+template <int D>
+__global__ void k_macro(Geo g, PhysC P, ExactArrays A) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    const long long n = g.ncell;
+    if (D == 2) {
+        double F[9], rho, u, v;
+#pragma unroll
+        for (int a = 0; a < 9; ++a) F[a] = A.f[a * n + c];
+        macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
+        A.rho[c] = rho;
+        A.u[c] = u;
+        A.v[c] = v;
+    } else {
+        double F[19], rho, u, v, w;
+#pragma unroll
+        for (int a = 0; a < 19; ++a) F[a] = A.f[a * n + c];
+        macro_3d(F, A.T[c], P, rho, u, v, w);
+        A.rho[c] = rho;
+        A.u[c] = u;
+        A.v[c] = v;
+        A.w[c] = w;
+    }
+}
+
+template <int D>
+__global__ void k_collisionT(Geo g, PhysC P, ExactArrays A) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    const long long n = g.ncell;
+    if (D == 2) {
+        double G[5], GP[5], Bx, By;
+#pragma unroll
+        for (int a = 0; a < 5; ++a) G[a] = A.g[a * n + c];
+        collideT_2d(G, A.u[c], A.v[c], A.T[c], A.Bx[c], A.By[c], P, GP, Bx, By);
+        if (P.use_g) {
+            A.Bx[c] = Bx;
+            A.By[c] = By;
+        }
+#pragma unroll
+        for (int a = 0; a < 5; ++a) A.gpost[a * n + c] = GP[a];
+    } else {
+        double G[7], GP[7], Bx, By, Bz;
+#pragma unroll
+        for (int a = 0; a < 7; ++a) G[a] = A.g[a * n + c];
+        collideT_3d(G, A.u[c], A.v[c], A.w[c], A.T[c], A.Bx[c], A.By[c], A.Bz[c], P, GP, Bx, By, Bz);
+        if (P.use_g) {
+            A.Bx[c] = Bx;
+            A.By[c] = By;
+            A.Bz[c] = Bz;
+        }
+#pragma unroll
+        for (int a = 0; a < 7; ++a) A.gpost[a * n + c] = GP[a];
+    }
+}
+
+template <int QT>
+__global__ void k_macroT(Geo g, const double* __restrict__ gg, double* __restrict__ T) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    const long long n = g.ncell;
+    double G[QT];
+#pragma unroll
+    for (int a = 0; a < QT; ++a) G[a] = gg[a * n + c];
+    T[c] = sumT<QT>(G);
+}
+
+// ------------------------------------------------------------------------------------
+// Fused step kernels
+// ------------------------------------------------------------------------------------
+// Flow collision of step n (A_n in the reference's order).  FIRST: the inputs are the
+// reference's module arrays after `initial` or after a materialisation; otherwise they
+// are rebuilt from the fused buffers: f_{n-1} = pull(f_post_{n-1}), T_{n-1} =
+// sum pull(g_post_{n-1}), and u_{n-1} from f_{n-1} with the lag (3D: T_{n-2}; 2D: the
+// force F_{n-1} stored by the previous flow collision).
+template <int D, bool FIRST>
+__global__ void __launch_bounds__(128) k_flow(Geo g, PhysC P, ExactArrays A, const double* __restrict__ fin,
+                                              const double* __restrict__ gin, double* __restrict__ fout) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
+    const long long n = g.ncell;
+    double F[Q], FP[Q], rho, u, v, w = 0.0, T;
+    if (FIRST) {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) F[a] = A.f[a * n + c];
+        rho = A.rho[c];
+        u = A.u[c];
+        v = A.v[c];
+        if (D == 3) w = A.w[c];
+        T = A.T[c];
+    } else {
+        auto lf = [&](int a, long long cc) { return fin[a * n + cc]; };
+        auto lg = [&](int a, long long cc) { return gin[a * n + cc]; };
+#pragma unroll
+        for (int a = 0; a < Q; ++a) F[a] = pull_flow<Q, double>(g, a, i, j, k, c, lf);
+        double G[QT];
+#pragma unroll
+        for (int a = 0; a < QT; ++a) G[a] = pull_thermal<QT, double>(g, a, i, j, k, c, lg);
+        T = sumT<QT>(G);
+        if (D == 2) macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
+        else macro_3d(F, A.Tlag[c], P, rho, u, v, w);
+    }
+    if (D == 2) {
+        double Fx, Fy;
+        collide_2d(F, rho, u, v, T, P, FP, Fx, Fy);
+        A.Fx[c] = Fx;
+        A.Fy[c] = Fy;
+    } else {
+        collide_3d(F, rho, u, v, w, T, P, FP);
+    }
+#pragma unroll
+    for (int a = 0; a < Q; ++a) fout[a * n + c] = FP[a];
+}
+
+// Streaming + boundary + macro of the flow and thermal collision of step n
+// (B_n .. D_n).  FIRST: g_{n-1} and T_{n-1} are the module arrays.
+template <int D, bool FIRST>
+__global__ void __launch_bounds__(128) k_thermal(Geo g, PhysC P, ExactArrays A, const double* __restrict__ fin,
+                                                 const double* __restrict__ gin, double* __restrict__ gout) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
+    const long long n = g.ncell;
+    double F[Q], G[QT], GP[QT];
+    auto lf = [&](int a, long long cc) { return fin[a * n + cc]; };
+#pragma unroll
+    for (int a = 0; a < Q; ++a) F[a] = pull_flow<Q, double>(g, a, i, j, k, c, lf);
+    double Tprev;
+    if (FIRST) {
+#pragma unroll
+        for (int a = 0; a < QT; ++a) G[a] = A.g[a * n + c];
+        Tprev = A.T[c];
+    } else {
+        auto lg = [&](int a, long long cc) { return gin[a * n + cc]; };
+#pragma unroll
+        for (int a = 0; a < QT; ++a) G[a] = pull_thermal<QT, double>(g, a, i, j, k, c, lg);
+        Tprev = sumT<QT>(G);
+    }
+    if (D == 2) {
+        double rho, u, v, Bx, By;
+        macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
+        collideT_2d(G, u, v, Tprev, A.Bx[c], A.By[c], P, GP, Bx, By);
+        if (P.use_g) {
+            A.Bx[c] = Bx;
+            A.By[c] = By;
+        }
+    } else {
+        double rho, u, v, w, Bx, By, Bz;
+        macro_3d(F, Tprev, P, rho, u, v, w);
+        collideT_3d(G, u, v, w, Tprev, A.Bx[c], A.By[c], A.Bz[c], P, GP, Bx, By, Bz);
+        if (P.use_g) {
+            A.Bx[c] = Bx;
+            A.By[c] = By;
+            A.Bz[c] = Bz;
+        }
+        A.Tlag[c] = Tprev;
+    }
+#pragma unroll
+    for (int a = 0; a < QT; ++a) gout[a * n + c] = GP[a];
+}
+
+// Rebuild the reference's module arrays after fused step N: f_N, g_N (streamed, with
+// boundaries), rho_N, u_N (with the lag), T_N.
+template <int D>
+__global__ void k_materialize(Geo g, PhysC P, ExactArrays A, const double* __restrict__ fin,
+                              const double* __restrict__ gin) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
+    const long long n = g.ncell;
+    double F[Q], G[QT];
+    auto lf = [&](int a, long long cc) { return fin[a * n + cc]; };
+    auto lg = [&](int a, long long cc) { return gin[a * n + cc]; };
+#pragma unroll
+    for (int a = 0; a < Q; ++a) F[a] = pull_flow<Q, double>(g, a, i, j, k, c, lf);
+#pragma unroll
+    for (int a = 0; a < QT; ++a) G[a] = pull_thermal<QT, double>(g, a, i, j, k, c, lg);
+    double rho, u, v, w;
+    if (D == 2) {
+        macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
+    } else {
+        macro_3d(F, A.Tlag[c], P, rho, u, v, w);
+        A.w[c] = w;
+    }
+    A.rho[c] = rho;
+    A.u[c] = u;
+    A.v[c] = v;
+    A.T[c] = sumT<QT>(G);
+#pragma unroll
+    for (int a = 0; a < Q; ++a) A.f[a * n + c] = F[a];
+#pragma unroll
+    for (int a = 0; a < QT; ++a) A.g[a * n + c] = G[a];
+}
+
+// ------------------------------------------------------------------------------------
+// host launchers
+// ------------------------------------------------------------------------------------
+static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+void exact_initial(const Geo& g, const PhysC& P, const InitC& I, const ExactArrays& A, int dim, cudaStream_t s) {
+    if (dim == 2) k_initial<2><<<nblocks(g.ncell, 256), 256, 0, s>>>(g, P, I, A);
+    else k_initial<3><<<nblocks(g.ncell, 256), 256, 0, s>>>(g, P, I, A);
+}
+
+void exact_stage(int stage, const Geo& g, const PhysC& P, const ExactArrays& A, int dim, cudaStream_t s) {
+    const unsigned nb = nblocks(g.ncell, 128);
+    const bool d3 = dim == 3;
+    switch (stage) {
+        case STAGE_COLLISION:
+            if (d3) k_collision<3><<<nb, 128, 0, s>>>(g, P, A); else k_collision<2><<<nb, 128, 0, s>>>(g, P, A);
+            break;
+        case STAGE_STREAMING:
+            if (d3) k_streaming<19><<<nb, 128, 0, s>>>(g, A.fpost, A.f); else k_streaming<9><<<nb, 128, 0, s>>>(g, A.fpost, A.f);
+            break;
+        case STAGE_BOUNCEBACK:
+            if (d3) k_bounceback<19><<<nb, 128, 0, s>>>(g, A.fpost, A.f); else k_bounceback<9><<<nb, 128, 0, s>>>(g, A.fpost, A.f);
+            break;
+        case STAGE_MACRO:
+            if (d3) k_macro<3><<<nb, 128, 0, s>>>(g, P, A); else k_macro<2><<<nb, 128, 0, s>>>(g, P, A);
+            break;
+        case STAGE_COLLISIONT:
+            if (d3) k_collisionT<3><<<nb, 128, 0, s>>>(g, P, A); else k_collisionT<2><<<nb, 128, 0, s>>>(g, P, A);
+            break;
+        case STAGE_STREAMINGT:
+            if (d3) k_streaming<7><<<nb, 128, 0, s>>>(g, A.gpost, A.g); else k_streaming<5><<<nb, 128, 0, s>>>(g, A.gpost, A.g);
+            break;
+        case STAGE_BOUNCEBACKT:
+            if (d3) k_bouncebackT<7><<<nb, 128, 0, s>>>(g, A.gpost, A.g); else k_bouncebackT<5><<<nb, 128, 0, s>>>(g, A.gpost, A.g);
+            break;
+        case STAGE_MACROT:
+            if (d3) k_macroT<7><<<nb, 128, 0, s>>>(g, A.g, A.T); else k_macroT<5><<<nb, 128, 0, s>>>(g, A.g, A.T);
+            break;
+        default: break;
+    }
+}
+
+void exact_fused_step(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, bool first, const double* fprev,
+                      const double* gprev, double* fnext, double* gnext, cudaStream_t s, int part) {
+    const unsigned nb = nblocks(g.ncell, 128);
+    const bool fl = part != 1, th = part != 0;
+    if (dim == 2) {
+        if (first) {
+            if (fl) k_flow<2, true><<<nb, 128, 0, s>>>(g, P, A, fprev, gprev, fnext);
+            if (th) k_thermal<2, true><<<nb, 128, 0, s>>>(g, P, A, fnext, gprev, gnext);
+        } else {
+            if (fl) k_flow<2, false><<<nb, 128, 0, s>>>(g, P, A, fprev, gprev, fnext);
+            if (th) k_thermal<2, false><<<nb, 128, 0, s>>>(g, P, A, fnext, gprev, gnext);
+        }
+    } else {
+        if (first) {
+            if (fl) k_flow<3, true><<<nb, 128, 0, s>>>(g, P, A, fprev, gprev, fnext);
+            if (th) k_thermal<3, true><<<nb, 128, 0, s>>>(g, P, A, fnext, gprev, gnext);
+        } else {
+            if (fl) k_flow<3, false><<<nb, 128, 0, s>>>(g, P, A, fprev, gprev, fnext);
+            if (th) k_thermal<3, false><<<nb, 128, 0, s>>>(g, P, A, fnext, gprev, gnext);
+        }
+    }
+}
+
+void exact_materialize(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, const double* fcur,
+                       const double* gcur, cudaStream_t s) {
+    const unsigned nb = nblocks(g.ncell, 128);
+    if (dim == 2) k_materialize<2><<<nb, 128, 0, s>>>(g, P, A, fcur, gcur);
+    else k_materialize<3><<<nb, 128, 0, s>>>(g, P, A, fcur, gcur);
+}
+
+}  // namespace lbm

@@ -1,0 +1,91 @@
+// lbm_internal.h - structures and launchers shared by the kernels and the host API.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "lbm_device.cuh"
+
+namespace lbm {
+
+// Physics constants of one run, in the form the kernels consume (all from commondata).
+struct PhysC {
+    double gBeta, Tref;
+    double Snu, Sq, Se, Seps, Spi, Sm;  // flow relaxation rates
+    double Qk, Qnu, SG, paraA;          // thermal relaxation, M1G factor, legacy a_T
+    double omegaT0, omegaT1, geqc;      // thermal weights and g^eq coefficient
+    int use_g, legacy;
+};
+
+// Inputs of `initial` that depend on host-side math (sin/cos of the RB perturbation).
+struct InitC {
+    double L, Thot, Tcold;
+    int perturb;
+    double pert_amp;
+    const double* sx;  // sin(2 pi x/xLen) (2D) or cos(...) (3D), per i
+    const double* sy;  // sin(pi y/yLen), per j
+    double noise_amp;
+    uint64_t seed;
+};
+
+// FP64 device arrays: the reference's module state (f, g, f_post, g_post, rho, u, v, w,
+// T, B_prev, F, up..Tp) plus the lag field of the fused path.
+struct ExactArrays {
+    double *f, *g, *fpost, *gpost;
+    double *rho, *u, *v, *w, *T;
+    double *Bx, *By, *Bz;
+    double *Fx, *Fy;   // 2D: force stored by collision
+    double *Tlag;      // 3D fused: T of the previous step
+    double *up, *vp, *wp, *Tp;
+};
+
+enum Stage {
+    STAGE_COLLISION = 0, STAGE_STREAMING, STAGE_BOUNCEBACK, STAGE_MACRO,
+    STAGE_COLLISIONT, STAGE_STREAMINGT, STAGE_BOUNCEBACKT, STAGE_MACROT
+};
+
+// ---- exact FP64 kernels (lbm_exact.cu) ------------------------------------------------
+void exact_initial(const Geo& g, const PhysC& P, const InitC& I, const ExactArrays& A, int dim, cudaStream_t s);
+void exact_stage(int stage, const Geo& g, const PhysC& P, const ExactArrays& A, int dim, cudaStream_t s);
+// part: 0 = flow kernel only, 1 = thermal kernel only, 2 = both (one full step)
+void exact_fused_step(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, bool first, const double* fprev,
+                      const double* gprev, double* fnext, double* gnext, cudaStream_t s, int part = 2);
+void exact_materialize(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, const double* fcur,
+                       const double* gcur, cudaStream_t s);
+
+// ---- reductions (lbm_reduce.cu) ---------------------------------------------------------
+// Fields read by the diagnostics (FP64 or FP32 device arrays of ncell values).
+template <class S>
+struct DiagFields {
+    const S *u, *v, *w, *T, *rho;
+    S *up, *vp, *wp, *Tp;
+};
+
+enum DiagOp { DIAG_CHECK = 0, DIAG_NURE = 1, DIAG_NU_GLOBAL = 2, DIAG_NU_COLD_MID = 3 };
+
+// Number of partial-sum slots a reduction launch writes: nblocks * DIAG_NSUM doubles.
+constexpr int DIAG_NSUM = 5;
+int diag_blocks(long long ncell);
+
+struct DiagScalars {
+    double Thot, Tcold, Tref, dy, coef, deltaT;
+    int side;  // side-heated cell: Nu uses u instead of v
+    int d3;
+};
+
+// Launch one reduction; partial sums (DIAG_NSUM per block, fixed order) go to `partials`.
+template <class S>
+void diag_reduce(DiagOp op, const Geo& g, const DiagScalars& D, const DiagFields<S>& F, double* partials,
+                 int nblocks, cudaStream_t s);
+// Per-column wall profile for RBcalc_Nu_wall_avg: Tb[i] = mean_k T(i,1,k) and
+// Nu_bot[i] = mean_k (8Thot - 9T(i,1,k) + T(i,2,k))/(3dy)/deltaT, k summed in order.
+template <class S>
+void diag_wall_columns(const Geo& g, const DiagScalars& D, const S* T, double* Tb, double* Nub, cudaStream_t s);
+
+// ---- layout transforms (lbm_reduce.cu) -------------------------------------------------
+// Fortran AoS f(0:q-1, cells) <-> device SoA f[q][cells], FP64.
+void aos_to_soa(const double* aos, double* soa, int q, long long ncell, cudaStream_t s);
+void soa_to_aos(const double* soa, double* aos, int q, long long ncell, cudaStream_t s);
+
+}  // namespace lbm

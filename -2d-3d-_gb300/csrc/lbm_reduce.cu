@@ -1,0 +1,211 @@
+// lbm_reduce.cu - FP64 diagnostics reductions and layout transforms.
+//
+// Each diagnostic of the reference (check, calNuRe, RBcalc_Nu_global, the sums of
+// RBcalc_Nu_wall_avg) is a sum over cells of a per-cell term.  Here every thread forms
+// the reference's per-cell term in FP64 (from FP64 or FP32 fields), accumulates a
+// grid-stride slice, the warp folds its partials with __shfl_down_sync, the block folds
+// the warps through shared memory, and block b writes its partials to slot b.  The host
+// adds the per-block partials in block order, so results are reproducible run to run
+// (the reference's OpenMP reductions combine thread partials in an unspecified order,
+// so only the per-cell terms, not the sums, can match it bit for bit).
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "lbm_internal.h"
+
+namespace lbm {
+
+constexpr int kRedThreads = 256;
+constexpr int kRedMaxBlocks = 152 * 8;  // 8 blocks of 256 threads per SM on 152 SMs
+
+int diag_blocks(long long ncell) {
+    long long nb = (ncell + kRedThreads - 1) / kRedThreads;
+    if (nb > kRedMaxBlocks) nb = kRedMaxBlocks;
+    if (nb < 1) nb = 1;
+    return (int)nb;
+}
+
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    return x;
+}
+
+template <int N>
+__device__ __forceinline__ void block_store(double (&acc)[N], double* out) {
+    __shared__ double sh[kRedThreads / 32][N];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int s = 0; s < N; ++s) acc[s] = warp_sum(acc[s]);
+    if (lane == 0) {
+#pragma unroll
+        for (int s = 0; s < N; ++s) sh[wid][s] = acc[s];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int s = 0; s < N; ++s) {
+            double x = (lane < kRedThreads / 32) ? sh[lane][s] : 0.0;
+            x = warp_sum(x);
+            if (lane == 0) out[(long long)blockIdx.x * N + s] = x;
+        }
+    }
+}
+
+template <class S>
+__device__ __forceinline__ double ld(const S* p, long long c) {
+    return (double)p[c];
+}
+
+// A cell is "bad" when it holds a non-finite temperature or velocity or a density <= 0
+// (the reference's restart check, 3DRB.F90:1423, extended to the running state).
+template <class S>
+__device__ __forceinline__ double bad_cell(const DiagFields<S>& F, long long c, bool d3) {
+    const double u = ld(F.u, c), v = ld(F.v, c), T = ld(F.T, c);
+    const double w = d3 ? ld(F.w, c) : 0.0;
+    const double r = F.rho ? ld(F.rho, c) : 1.0;
+    return (isfinite(u) && isfinite(v) && isfinite(w) && isfinite(T) && r > 0.0) ? 0.0 : 1.0;
+}
+
+template <class S, int OP>
+__global__ void __launch_bounds__(kRedThreads) k_diag(Geo g, DiagScalars D, DiagFields<S> F, double* partials) {
+    double acc[DIAG_NSUM] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    const bool d3 = D.d3 != 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    if (OP == DIAG_NU_COLD_MID) {
+        // one thread per (i,k) column: cold wall term and mid-plane term
+        const long long ncol = (long long)g.nx * g.nz;
+        for (long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x; col < ncol; col += stride) {
+            const int i = (int)(col % g.nx), k = (int)(col / g.nx);
+            auto T = [&](int j) { return ld(F.T, cell_index(g, i, j, k)); };
+            auto V = [&](int j) { return ld(F.v, cell_index(g, i, j, k)); };
+            const int ny = g.ny;
+            // Nu_cold (2DRB.F90:2423-2428, 3DRB.F90:2145-2152)
+            const double qy_wall = (-8.0 * D.Tcold + 9.0 * T(ny - 1) - T(ny - 2)) / (3.0 * D.dy);
+            acc[0] += qy_wall / D.deltaT;
+            // Nu_middle (2DRB.F90:2433-2457, 3DRB.F90:2156-2180)
+            if (ny % 2 == 1) {
+                const int jm = (ny + 1) / 2 - 1;
+                acc[1] += (D.coef * V(jm) * (T(jm) - D.Tref) - (T(jm + 1) - T(jm - 1)) / (2.0 * D.dy)) / D.deltaT;
+            } else {
+                const int jB = ny / 2 - 1, jT = jB + 1;
+                if (d3)
+                    acc[1] += (D.coef * 0.5 * (V(jB) * (T(jB) - D.Tref) + V(jT) * (T(jT) - D.Tref)) + (T(jB) - T(jT)) / D.dy) / D.deltaT;
+                else
+                    acc[1] += (D.coef * (0.5 * (V(jB) * (T(jB) - D.Tref) + V(jT) * (T(jT) - D.Tref))) + (T(jB) - T(jT)) / D.dy) / D.deltaT;
+            }
+        }
+        block_store(acc, partials);
+        return;
+    }
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < g.ncell; c += stride) {
+        if (OP == DIAG_CHECK) {
+            // check (2DRB.F90:1233-1246, 3DRB.F90:1491-1520)
+            const double u = ld(F.u, c), v = ld(F.v, c), T = ld(F.T, c);
+            const double du = u - ld(F.up, c), dv = v - ld(F.vp, c);
+            double e1 = du * du + dv * dv, e2 = u * u + v * v;
+            if (d3) {
+                const double w = ld(F.w, c), dw = w - ld(F.wp, c);
+                e1 = e1 + dw * dw;
+                e2 = e2 + w * w;
+                F.wp[c] = F.w[c];
+            }
+            acc[0] += e1;
+            acc[1] += e2;
+            acc[2] += fabs(T - ld(F.Tp, c));
+            acc[3] += fabs(T);
+            acc[4] += bad_cell(F, c, d3);
+            F.up[c] = F.u[c];
+            F.vp[c] = F.v[c];
+            F.Tp[c] = F.T[c];
+        } else if (OP == DIAG_NURE) {
+            // calNuRe (2DRB.F90:1631-1663, 3DRB.F90:1731-1768)
+            const double u = ld(F.u, c), v = ld(F.v, c), T = ld(F.T, c);
+            acc[0] += (D.side ? u : v) * T;
+            double r = u * u + v * v;
+            if (d3) {
+                const double w = ld(F.w, c);
+                r = r + w * w;
+            }
+            acc[1] += r;
+            acc[4] += bad_cell(F, c, d3);
+        } else {
+            // RBcalc_Nu_global (2DRB.F90:2268-2288, 3DRB.F90:1851-1866)
+            int i, j, k;
+            cell_coords(g, c, i, j, k);
+            auto T = [&](int jj) { return ld(F.T, cell_index(g, i, jj, k)); };
+            double dTdy;
+            if (j == 0) dTdy = (3.0 * T(0) + T(1) - 4.0 * D.Thot) / (3.0 * D.dy);
+            else if (j == g.ny - 1) dTdy = (4.0 * D.Tcold - 3.0 * T(g.ny - 1) - T(g.ny - 2)) / (3.0 * D.dy);
+            else dTdy = (T(j + 1) - T(j - 1)) / (2.0 * D.dy);
+            acc[0] += D.coef * ld(F.v, c) * (T(j) - D.Tref) - dTdy;
+        }
+    }
+    block_store(acc, partials);
+}
+
+template <class S>
+void diag_reduce(DiagOp op, const Geo& g, const DiagScalars& D, const DiagFields<S>& F, double* partials, int nb,
+                 cudaStream_t s) {
+    switch (op) {
+        case DIAG_CHECK: k_diag<S, DIAG_CHECK><<<nb, kRedThreads, 0, s>>>(g, D, F, partials); break;
+        case DIAG_NURE: k_diag<S, DIAG_NURE><<<nb, kRedThreads, 0, s>>>(g, D, F, partials); break;
+        case DIAG_NU_GLOBAL: k_diag<S, DIAG_NU_GLOBAL><<<nb, kRedThreads, 0, s>>>(g, D, F, partials); break;
+        case DIAG_NU_COLD_MID: k_diag<S, DIAG_NU_COLD_MID><<<nb, kRedThreads, 0, s>>>(g, D, F, partials); break;
+    }
+}
+
+template <class S>
+__global__ void k_wall_columns(Geo g, DiagScalars D, const S* __restrict__ T, double* Tb, double* Nub) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.nx) return;
+    // 3DRB.F90:2067-2087 (2D: 2DRB.F90:2330-2336 is the nz = 1 case of the same sums)
+    double tb = 0.0, nb = 0.0;
+    for (int k = 0; k < g.nz; ++k) tb = tb + (double)T[cell_index(g, i, 0, k)];
+    for (int k = 0; k < g.nz; ++k) {
+        const double qy_wall = (8.0 * D.Thot - 9.0 * (double)T[cell_index(g, i, 0, k)] + (double)T[cell_index(g, i, 1, k)]) / (3.0 * D.dy);
+        nb = nb + qy_wall / D.deltaT;
+    }
+    Tb[i] = tb / (double)g.nz;
+    Nub[i] = nb / (double)g.nz;
+}
+
+template <class S>
+void diag_wall_columns(const Geo& g, const DiagScalars& D, const S* T, double* Tb, double* Nub, cudaStream_t s) {
+    k_wall_columns<S><<<(g.nx + 127) / 128, 128, 0, s>>>(g, D, T, Tb, Nub);
+}
+
+template void diag_reduce<double>(DiagOp, const Geo&, const DiagScalars&, const DiagFields<double>&, double*, int, cudaStream_t);
+template void diag_reduce<float>(DiagOp, const Geo&, const DiagScalars&, const DiagFields<float>&, double*, int, cudaStream_t);
+template void diag_wall_columns<double>(const Geo&, const DiagScalars&, const double*, double*, double*, cudaStream_t);
+template void diag_wall_columns<float>(const Geo&, const DiagScalars&, const float*, double*, double*, cudaStream_t);
+
+// ---- layout transforms ----------------------------------------------------------------
+__global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict__ soa, int q, long long n) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)q * n) return;
+    const long long c = e / q;
+    const int a = (int)(e - c * q);
+    soa[(long long)a * n + c] = aos[e];
+}
+
+__global__ void k_soa_to_aos(const double* __restrict__ soa, double* __restrict__ aos, int q, long long n) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)q * n) return;
+    const long long c = e / q;
+    const int a = (int)(e - c * q);
+    aos[e] = soa[(long long)a * n + c];
+}
+
+void aos_to_soa(const double* aos, double* soa, int q, long long ncell, cudaStream_t s) {
+    const long long tot = (long long)q * ncell;
+    k_aos_to_soa<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(aos, soa, q, ncell);
+}
+
+void soa_to_aos(const double* soa, double* aos, int q, long long ncell, cudaStream_t s) {
+    const long long tot = (long long)q * ncell;
+    k_soa_to_aos<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(soa, aos, q, ncell);
+}
+
+}  // namespace lbm

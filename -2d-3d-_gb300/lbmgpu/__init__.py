@@ -1,0 +1,232 @@
+"""lbmgpu - Python mirror of the reference's subroutine surface over the C ABI.
+
+The reference (2DRB/2DRB.F90, 2DRB/3DRB.F90) is a Fortran program whose hot path is a
+fixed sequence of argument-less subroutines acting on module arrays:
+
+    initial; do: collision, streaming, bounceback, macro,
+                 collisionT, streamingT, bouncebackT, macroT; check every 2000 steps
+    RBcalc_Nu_global, RBcalc_Nu_wall_avg, calNuRe at the end
+
+`Lattice` keeps that surface (same names, same meaning) on top of liblbmgpu.so, whose
+kernels are hand-written CUDA for sm_103a.  There is no CPU fallback: every method calls
+the library, and a missing library or GPU raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import (FIELDS, LBM_FP64, LBM_OK, STATUS_NAMES, LbmConstants, LbmNuWall, LbmParams, field_shape,
+                  field_size, rb_params)
+
+__all__ = ["Lattice", "LbmError", "LbmDiverged", "LbmParams", "rb_params", "load_library", "library_path",
+           "params_default", "derive_constants", "FIELDS"]
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_NAME = "liblbmgpu.so"
+
+# Every entry point of include/lbm_gpu.h with its ctypes signature.
+_vp, _i32, _i64, _dp, _sz = C.c_void_p, C.c_int, C.c_int64, C.POINTER(C.c_double), C.c_size_t
+SIGNATURES = {
+    "lbm_params_default": ([_i32, _vp], _i32),
+    "lbm_derive_constants": ([_vp, _vp], _i32),
+    "lbm_create": ([_vp, _i32, C.POINTER(_vp)], _i32),
+    "lbm_destroy": ([_vp], _i32),
+    "lbm_initial": ([_vp], _i32),
+    "lbm_last_error": ([_vp], C.c_char_p),
+    "lbm_status_string": ([_i32], C.c_char_p),
+    "lbm_get_constants": ([_vp, _vp], _i32),
+    "lbm_itc": ([_vp], _i64),
+    "lbm_sync": ([_vp], _i32),
+    "lbm_collision": ([_vp], _i32),
+    "lbm_streaming": ([_vp], _i32),
+    "lbm_bounceback": ([_vp], _i32),
+    "lbm_macro": ([_vp], _i32),
+    "lbm_collisionT": ([_vp], _i32),
+    "lbm_streamingT": ([_vp], _i32),
+    "lbm_bouncebackT": ([_vp], _i32),
+    "lbm_macroT": ([_vp], _i32),
+    "lbm_step": ([_vp, _i64], _i32),
+    "lbm_check": ([_vp, _dp, _dp], _i32),
+    "lbm_calNuRe": ([_vp, _dp, _dp], _i32),
+    "lbm_RBcalc_Nu_global": ([_vp, _dp], _i32),
+    "lbm_RBcalc_Nu_wall_avg": ([_vp, _vp], _i32),
+    "lbm_get_state": ([_vp, _i32, _dp, _sz], _i32),
+    "lbm_set_state": ([_vp, _i32, _dp, _sz], _i32),
+    "lbm_get_stream": ([_vp, C.POINTER(_vp)], _i32),
+    "lbm_time_kernels": ([_vp, _i64, _dp, _dp], _i32),
+}
+
+_lib = None
+
+
+def library_path():
+    return os.path.join(_PKG, LIB_NAME)
+
+
+def load_library(path=None):
+    """Load liblbmgpu.so from the package directory (built in-tree by lbmgpu.build)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or library_path()
+    if not os.path.exists(p):
+        raise RuntimeError("%s is not built; run lbmgpu.build.build() (nvcc, sm_103a)" % p)
+    lib = C.CDLL(p)
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class LbmError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+class LbmDiverged(LbmError):
+    pass
+
+
+def params_default(dim):
+    p = LbmParams()
+    st = load_library().lbm_params_default(int(dim), C.byref(p))
+    if st != LBM_OK:
+        raise LbmError(st, "lbm_params_default")
+    return p
+
+
+def derive_constants(params):
+    c = LbmConstants()
+    st = load_library().lbm_derive_constants(C.byref(params), C.byref(c))
+    if st != LBM_OK:
+        raise LbmError(st, "invalid parameters")
+    return c
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Lattice:
+    """One lattice resident on one GPU; methods are the reference's subroutines."""
+
+    def __init__(self, params, device=0):
+        self.lib = load_library()
+        self.params = params.copy()
+        h = C.c_void_p()
+        st = self.lib.lbm_create(C.byref(self.params), int(device), C.byref(h))
+        if st != LBM_OK:
+            raise LbmError(st, "lbm_create failed (parameters, device %d or memory)" % device)
+        self._h = h
+
+    # -- lifecycle -------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.lbm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _ck(self, st, what):
+        if st != LBM_OK:
+            msg = self.lib.lbm_last_error(self._h)
+            msg = msg.decode() if msg else what
+            cls = LbmDiverged if st == 4 else LbmError
+            raise cls(st, "%s: %s" % (what, msg))
+
+    @property
+    def itc(self):
+        return int(self.lib.lbm_itc(self._h))
+
+    def constants(self):
+        c = LbmConstants()
+        self._ck(self.lib.lbm_get_constants(self._h, C.byref(c)), "lbm_get_constants")
+        return c.as_dict()
+
+    def sync(self):
+        self._ck(self.lib.lbm_sync(self._h), "lbm_sync")
+
+    # -- the reference's subroutines ---------------------------------------------------
+    def initial(self):
+        self._ck(self.lib.lbm_initial(self._h), "initial")
+
+    def collision(self): self._ck(self.lib.lbm_collision(self._h), "collision")
+    def streaming(self): self._ck(self.lib.lbm_streaming(self._h), "streaming")
+    def bounceback(self): self._ck(self.lib.lbm_bounceback(self._h), "bounceback")
+    def macro(self): self._ck(self.lib.lbm_macro(self._h), "macro")
+    def collisionT(self): self._ck(self.lib.lbm_collisionT(self._h), "collisionT")
+    def streamingT(self): self._ck(self.lib.lbm_streamingT(self._h), "streamingT")
+    def bouncebackT(self): self._ck(self.lib.lbm_bouncebackT(self._h), "bouncebackT")
+    def macroT(self): self._ck(self.lib.lbm_macroT(self._h), "macroT")
+
+    def stage_step(self):
+        """One iteration of the reference's loop body through the eight stage kernels."""
+        for s in (self.collision, self.streaming, self.bounceback, self.macro,
+                  self.collisionT, self.streamingT, self.bouncebackT, self.macroT):
+            s()
+
+    def step(self, nsteps=1):
+        """nsteps iterations with the fused kernels (asynchronous)."""
+        self._ck(self.lib.lbm_step(self._h, int(nsteps)), "lbm_step")
+
+    def check(self):
+        a, b = C.c_double(), C.c_double()
+        self._ck(self.lib.lbm_check(self._h, C.byref(a), C.byref(b)), "check")
+        return a.value, b.value
+
+    def calNuRe(self):
+        a, b = C.c_double(), C.c_double()
+        self._ck(self.lib.lbm_calNuRe(self._h, C.byref(a), C.byref(b)), "calNuRe")
+        return a.value, b.value
+
+    def RBcalc_Nu_global(self):
+        a = C.c_double()
+        self._ck(self.lib.lbm_RBcalc_Nu_global(self._h, C.byref(a)), "RBcalc_Nu_global")
+        return a.value
+
+    def RBcalc_Nu_wall_avg(self):
+        w = LbmNuWall()
+        self._ck(self.lib.lbm_RBcalc_Nu_wall_avg(self._h, C.byref(w)), "RBcalc_Nu_wall_avg")
+        return w.as_dict()
+
+    # -- measurement ----------------------------------------------------------------------
+    def stream_handle(self):
+        """The cudaStream_t the handle enqueues on (as an integer), e.g. for torch.cuda.ExternalStream."""
+        s = C.c_void_p()
+        self._ck(self.lib.lbm_get_stream(self._h, C.byref(s)), "lbm_get_stream")
+        return s.value or 0
+
+    def time_kernels(self, nsteps):
+        """Mean device ms per launch of the (flow, thermal) fused kernels over nsteps steps."""
+        a, b = C.c_double(), C.c_double()
+        self._ck(self.lib.lbm_time_kernels(self._h, int(nsteps), C.byref(a), C.byref(b)), "lbm_time_kernels")
+        return a.value, b.value
+
+    # -- state transfer (Fortran layout) ------------------------------------------------
+    def get_state(self, field):
+        fid = FIELDS[field] if isinstance(field, str) else int(field)
+        a = np.empty(field_shape(self.params, fid), dtype=np.float64)
+        self._ck(self.lib.lbm_get_state(self._h, fid, _dptr(a), a.size), "get_state(%s)" % field)
+        return a
+
+    def set_state(self, field, arr):
+        fid = FIELDS[field] if isinstance(field, str) else int(field)
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        if a.size != field_size(self.params, fid):
+            raise ValueError("set_state(%s): expected %d values, got %d" % (field, field_size(self.params, fid), a.size))
+        self._ck(self.lib.lbm_set_state(self._h, fid, _dptr(a), a.size), "set_state(%s)" % field)

@@ -1,0 +1,323 @@
+#!/usr/bin/env python3
+"""Benchmark of the coupled thermal MRT-LBM time step on GB300.
+
+Workload: 3D Rayleigh-Benard cube, D3Q19 MRT flow + D3Q7 MRT temperature, 128^3 cells,
+no-slip walls, adiabatic side walls, hot bottom (+0.5) / cold top (-0.5), Ra = 1e7,
+Pr = 0.71, free-fall velocity U = 0.1, linear T + seeded 1e-3 noise.  A "step" is one
+coupled (flow + thermal) time step over the whole lattice; MLUPS counts one coupled cell
+update as one, as the reference's runtime print does (3DRB.F90:303-305).
+
+Headline `value`: the plain method (FP64, the reference's arithmetic) through the fused
+kernels, inputs resident in HBM.  The FP32 / FP16 storage forms of the same workload are
+reported beside it.  `e2e` is the same metric through the C ABI with host buffers in the
+reference's Fortran layout (state in, steps, T field and Nu/Re out).  `cpu_baseline` is
+the C++ restatement of the reference's OpenMP CPU path timed on this host's cores.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.join(ROOT, "-2d-3d-_gb300")
+for _p in (ROOT, PKG_ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "coupled MLUPS (D3Q19/D3Q7 MRT-LBM step)"
+UNIT = "MLUPS"
+N_CELL_EDGE = 128
+BYTES_PER_CELL = {"fp64": 416, "fp32": 208, "fp16": 104}  # populations read + written once
+DTYPE = {"fp64": "f64", "fp32": "f32", "fp16": "f16-storage/f32-arith"}
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload_params(precision="fp64", n=N_CELL_EDGE):
+    from lbmgpu.abi import rb_params
+    return rb_params(dim=3, n=n, Ra=1e7, Pr=0.71, U=0.1, noise_amp=1e-3, seed=20261203, precision=precision)
+
+
+def workload_config(n=N_CELL_EDGE):
+    return {
+        "workload": "3D Rayleigh-Benard cube D3Q19/D3Q7 MRT, %d^3 cells, Ra=1e7, Pr=0.71, U=0.1, no-slip walls, "
+                    "adiabatic sides, T linear + 1e-3 seeded noise (seed 20261203)" % n,
+        "cells": n ** 3,
+        "l2": "inputs larger than L2 (FP64 populations 872 MB, FP32 436 MB, FP16 218 MB per step)",
+        "step": "one coupled flow+thermal time step over the whole lattice",
+    }
+
+
+def measured_hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of each fused kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(steps=None, budget_s=12.0, n=N_CELL_EDGE):
+    """C++ restatement of the reference's 8-pass OpenMP CPU step, all host cores, bounded sample."""
+    from oracle import oracle as ora
+    threads = ora.set_threads(os.cpu_count() or 1)
+    o = ora.Oracle(workload_params("fp64", n))
+    o.initial()
+    o.step(1)
+    t0 = time.perf_counter()
+    done = 0
+    if steps is not None:
+        o.step(steps)
+        done = steps
+    else:
+        while time.perf_counter() - t0 < budget_s:
+            o.step(2)
+            done += 2
+    dt = time.perf_counter() - t0
+    cells = n ** 3
+    return {"value": cells * done / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d steps of the %d^3 workload (%.1f s), C++ restatement of the reference's OpenMP "
+                      "8-pass step (-O3 -fopenmp), %d threads" % (done, n, dt, threads)}
+
+
+def run_reference(args):
+    rank, world, local, pg = dist_setup(args)
+    if rank != 0:
+        return 0
+    from oracle import oracle as ora
+    ora.build()
+    threads = ora.set_threads(os.cpu_count() or 1)
+    o = ora.Oracle(workload_params("fp64"))
+    o.initial()
+    o.step(args.warmup)
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    cells = N_CELL_EDGE ** 3
+    value = cells * args.steps / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d steps of the %d^3 workload after %d warm-up steps; C++ restatement of the "
+                                   "reference's OpenMP CPU path (the Fortran cannot be compiled here)"
+                                   % (args.steps, N_CELL_EDGE, args.warmup)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def time_precision(prec, args, pg, local):
+    import torch
+    import lbmgpu
+    p = workload_params(prec)
+    lat = lbmgpu.Lattice(p, device=local)
+    lat.initial()
+    lat.step(args.warmup)
+    lat.sync()
+    stream = torch.cuda.ExternalStream(lat.stream_handle(), device=torch.device("cuda", local))
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(pg)
+    torch.cuda.synchronize()
+    start.record(stream)
+    lat.step(args.steps)
+    end.record(stream)
+    end.synchronize()
+    torch.cuda.synchronize()
+    barrier(pg)
+    ms = start.elapsed_time(end)
+    ms = max_over_ranks(pg, ms)
+    # per-kernel device times (no graph), for the roofline of the fused step
+    ms_flow, ms_thermal = lat.time_kernels(min(args.steps, 20))
+    nu, re = lat.calNuRe()
+    lat.close()
+    cells = p.nx * p.ny * p.nz
+    return {"ms_total": ms, "ms_per_step": ms / args.steps, "mlups": cells * args.steps / (ms / 1e3) / 1e6,
+            "ms_flow": ms_flow, "ms_thermal": ms_thermal, "Nu": nu, "Re": re}
+
+
+def e2e_run(prec, args, local):
+    """State in from host arrays (Fortran layout), K steps, T field and Nu/Re out, via the C ABI."""
+    import numpy as np
+    import lbmgpu
+    p = workload_params(prec)
+    lat = lbmgpu.Lattice(p, device=local)
+    lat.initial()
+    names = ["f", "g", "rho", "u", "v", "w", "T", "Bx_prev", "By_prev", "Bz_prev"]
+    host = {k: np.ascontiguousarray(lat.get_state(k)) for k in names}
+    lat.step(args.warmup)
+    lat.sync()
+    t0 = time.perf_counter()
+    for k in names:
+        lat.set_state(k, host[k])
+    lat.step(args.steps)
+    T = lat.get_state("T")
+    nu, re = lat.calNuRe()
+    dt = time.perf_counter() - t0
+    lat.close()
+    h2d = sum(a.nbytes for a in host.values())
+    d2h = T.nbytes + 16
+    cells = p.nx * p.ny * p.nz
+    return {"value": cells * args.steps / dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+            "d2h_bytes_per_step": d2h / args.steps,
+            "job": "lbm_set_state x%d (Fortran-layout host arrays) + lbm_step(%d) + lbm_get_state(T) + lbm_calNuRe"
+                   % (len(names), args.steps)}
+
+
+def run_gpu(args):
+    rank, world, local, pg = dist_setup(args)
+    import torch
+    torch.cuda.set_device(local)
+    from lbmgpu import build as lbuild
+    lbuild.build()
+    peak, peak_kind = measured_hbm_peak()
+    traffic = ncu_traffic()
+    results = {}
+    with ClockSampler(local) as clk:
+        for prec in ("fp64", "fp32", "fp16"):
+            results[prec] = time_precision(prec, args, pg, local)
+    clocks = clk.summary()
+    e2e = e2e_run("fp64", args, local)
+    cells = N_CELL_EDGE ** 3
+
+    def roof(prec):
+        r = results[prec]
+        step_ms = r["ms_flow"] + r["ms_thermal"]
+        achieved = BYTES_PER_CELL[prec] * cells / (step_ms / 1e3) / 1e9
+        t = traffic.get(prec)
+        return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": t, "peak_kind": peak_kind,
+                "kernel": "fused step = flow kernel %.3f ms + thermal kernel %.3f ms per launch"
+                          % (r["ms_flow"], r["ms_thermal"]),
+                "algorithmic_bytes_per_cell": BYTES_PER_CELL[prec]}
+
+    head = results["fp64"]
+    line = {
+        "metric": METRIC, "value": head["mlups"] * world, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": DTYPE["fp64"], "data": "synthetic", "config": workload_config(),
+        "parallelism": "replicas" if world > 1 else "single GPU",
+        "roofline": roof("fp64"),
+        "e2e": e2e,
+        "gpu_launches": 2 * args.steps,
+        "clocks": clocks,
+        "forms": {prec: {"mlups": results[prec]["mlups"] * world, "ms_per_step": results[prec]["ms_per_step"],
+                         "dtype": DTYPE[prec], "roofline": roof(prec), "Nu": results[prec]["Nu"],
+                         "Re": results[prec]["Re"]} for prec in results},
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,184 @@
+/*
+ * lbm_gpu.h - C ABI of the GB300 (sm_103a) coupled thermal MRT lattice-Boltzmann library.
+ *
+ * The reference (Fortran, 2DRB/2DRB.F90 and 2DRB/3DRB.F90) keeps its state in module
+ * globals and advances it with argument-less subroutines called in a fixed order from
+ * `program main` (2DRB.F90:236-277, 3DRB.F90:225-264).  This header replaces that
+ * surface one to one: a handle owns the lattice (all of it resident in HBM on one
+ * GPU), every reference subroutine on the time-step path has an entry point of the
+ * same name, and `lbm_step` runs the fused GB300 kernels for many steps at once.
+ *
+ * Conventions
+ *  - Every call returns an `int` status (LBM_OK = 0).  The library never exits the
+ *    process; `lbm_last_error` gives the message of the last failure on a handle.
+ *  - Calls enqueue work on the handle's own CUDA stream.  Only calls that return
+ *    host data (getters and diagnostics) synchronise.  A handle is not thread safe:
+ *    use one handle per host thread.
+ *  - Host arrays exchanged with `lbm_get_state` / `lbm_set_state` use the reference's
+ *    Fortran layout: populations f(0:q-1, 1:nx, 1:ny, 1:nz) with the direction index
+ *    fastest, scalar fields T(1:nx, 1:ny, 1:nz) column major (x fastest).
+ *  - 2D lattices have dim = 2 and nz = 1.
+ */
+#ifndef LBM_GPU_H
+#define LBM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------ */
+#define LBM_OK            0
+#define LBM_ERR_PARAM     1 /* invalid parameters (reference: `stop` after a log line) */
+#define LBM_ERR_CUDA      2 /* a CUDA runtime call failed                              */
+#define LBM_ERR_OOM       3 /* device allocation refused                               */
+#define LBM_ERR_DIVERGED  4 /* non-finite value or rho <= 0 found by a diagnostic      */
+#define LBM_ERR_TIMEOUT   5 /* a bounded device-side wait gave up                      */
+#define LBM_ERR_STATE     6 /* call not valid for this handle (e.g. precision)         */
+
+/* ---- cell type: CPP switches RayleighBenardCell / SideHeatedCell (3DRB.F90:23-37) --- */
+#define LBM_CELL_RB   0 /* heated from below: lengthUnit = ny                            */
+#define LBM_CELL_SIDE 1 /* heated side walls: lengthUnit = nx                            */
+
+/* ---- flow boundary per axis: *WallsNoslip / *WallsPeriodicalU (3DRB.F90:14-18) ------ */
+#define LBM_BC_NOSLIP   0
+#define LBM_BC_PERIODIC 1
+
+/* ---- thermal boundary per axis: *WallsConstT / *Adiabatic / *PeriodicalT ------------ */
+#define LBM_BCT_CONST     0 /* low face at Thot, high face at Tcold (anti-bounce-back)   */
+#define LBM_BCT_ADIABATIC 1
+#define LBM_BCT_PERIODIC  2
+
+/* ---- population storage precision --------------------------------------------------- */
+#define LBM_FP64 0 /* plain method: FP64 storage and arithmetic, reference expression order */
+#define LBM_FP32 1 /* FP32 storage of deviations from rest weights, FP32 arithmetic          */
+#define LBM_FP16 2 /* FP16 storage of deviations from rest weights, FP32 arithmetic          */
+
+/* ---- streaming pattern ---------------------------------------------------------------- */
+#define LBM_PATTERN_AB 0 /* two population buffers (ping-pong)                              */
+#define LBM_PATTERN_AA 1 /* one buffer, in-place even/odd (AA) access pattern               */
+
+/* ---- fields for lbm_get_state / lbm_set_state --------------------------------------- */
+#define LBM_FIELD_F       0  /* f(0:q-1,nx,ny,nz), q = 9 (2D) or 19 (3D)                 */
+#define LBM_FIELD_G       1  /* g(0:qt-1,nx,ny,nz), qt = 5 (2D) or 7 (3D)                */
+#define LBM_FIELD_RHO     2
+#define LBM_FIELD_U       3
+#define LBM_FIELD_V       4
+#define LBM_FIELD_W       5  /* 3D only                                                  */
+#define LBM_FIELD_T       6
+#define LBM_FIELD_BX_PREV 7
+#define LBM_FIELD_BY_PREV 8
+#define LBM_FIELD_BZ_PREV 9  /* 3D only                                                  */
+#define LBM_FIELD_FX      10 /* 2D only: body force stored by collision (2DRB.F90:718)   */
+#define LBM_FIELD_FY      11 /* 2D only                                                  */
+#define LBM_FIELD_F_POST  12 /* interior of f_post(0:q-1,0:nx+1,0:ny+1[,0:nz+1])         */
+#define LBM_FIELD_G_POST  13 /* interior of g_post                                       */
+
+/* Run parameters: the runtime form of the reference's compile-time `commondata` module
+ * (2DRB.F90:48-194, 3DRB.F90:55-187) and of its CPP boundary switches.  Mach follows the
+ * reference's definition (tauf = 0.5 + Mach*L*sqrt(3*Pr/Ra)); a free-fall velocity U in
+ * lattice units corresponds to Mach = U*sqrt(3). */
+typedef struct lbm_params {
+    int32_t dim;            /* 2 or 3                                                      */
+    int32_t nx, ny, nz;     /* lattice cells; nz = 1 in 2D                                  */
+    double  Ra, Pr, Mach;   /* Rayleigh, Prandtl, Mach                                      */
+    double  Thot, Tcold;    /* wall temperatures (Tref = (Thot+Tcold)/2)                    */
+    int32_t cell;           /* LBM_CELL_RB or LBM_CELL_SIDE                                 */
+    int32_t bc_flow[3];     /* per axis x,y,z: LBM_BC_*                                     */
+    int32_t bc_thermal[3];  /* per axis x,y,z: LBM_BCT_*                                    */
+    int32_t use_g;          /* EnableUseG: M1G heat-flux correction (default 1)            */
+    int32_t legacy_thermal; /* EnableLegacyThermalScheme (default 0)                        */
+    int32_t precision;      /* LBM_FP64 / LBM_FP32 / LBM_FP16                               */
+    int32_t pattern;        /* LBM_PATTERN_AB / LBM_PATTERN_AA                              */
+    uint64_t seed;          /* seed of the initial temperature noise                        */
+    double  noise_amp;      /* T += noise_amp*(2*xi-1), xi = splitmix64(seed ^ cell) in [0,1) */
+} lbm_params;
+
+/* Derived constants, computed exactly as the reference's `parameter` statements
+ * (2DRB.F90:61-115, 3DRB.F90:73-123). */
+typedef struct lbm_constants {
+    double lengthUnit, Tref, tauf, viscosity, diffusivity, paraA;
+    double gBeta, timeUnit, velocityUnit, heatFluxScale, velocityScaleCompare;
+    double Snu, Sq, Se, Seps, Spi, Sm;      /* flow MRT rates (2D uses Snu, Sq)         */
+    double taug, Qk, Qnu, SG, thermalGeqCoeff, cs2T;
+    double omegaT0, omegaT1;                /* thermal weights: rest, moving             */
+} lbm_constants;
+
+/* Wall Nusselt numbers of RBcalc_Nu_wall_avg (2DRB.F90:2308-2473, 3DRB.F90:2049-2210). */
+typedef struct lbm_nu_wall {
+    double Nu_hot, Nu_cold, Nu_middle;
+    double Nu_hot_max, Nu_hot_max_position;
+    double Nu_hot_min, Nu_hot_min_position;
+} lbm_nu_wall;
+
+typedef struct lbm_handle lbm_handle;
+
+/* ---- parameters ------------------------------------------------------------------------ */
+/* Defaults of a Rayleigh-Benard cell: 2D = 2DRB.F90:11-38 (x periodic, y walls at Thot/Tcold,
+ * Ra 5e4, Pr 0.71, Mach 0.1, 320x160); 3D = RB variant of 3DRB.F90:9-47 (no-slip everywhere,
+ * adiabatic x/z walls, 120^3, Ra 1e7). */
+int lbm_params_default(int dim, lbm_params* out);
+/* commondata derivation; replaces the `parameter` block (3DRB.F90:73-123). */
+int lbm_derive_constants(const lbm_params* p, lbm_constants* out);
+
+/* ---- lifecycle ------------------------------------------------------------------------- */
+/* Allocates every device array the run needs (replaces the `allocate` statements of
+ * `initial`, 3DRB.F90:467-473) and a CUDA stream; `device` selects the GPU. */
+int lbm_create(const lbm_params* p, int device, lbm_handle** out);
+int lbm_destroy(lbm_handle* h);
+/* subroutine initial (2DRB.F90:371-663, 3DRB.F90:342-679) with loadInitField = 0. */
+int lbm_initial(lbm_handle* h);
+const char* lbm_last_error(const lbm_handle* h);
+const char* lbm_status_string(int status);
+int lbm_get_constants(const lbm_handle* h, lbm_constants* out);
+int64_t lbm_itc(const lbm_handle* h);   /* time steps taken since lbm_initial (itc)     */
+int lbm_sync(lbm_handle* h);            /* wait for all queued work of the handle       */
+
+/* ---- stage entries: one CUDA kernel per reference subroutine (FP64 handles only) -------- */
+int lbm_collision(lbm_handle* h);   /* 2DRB.F90:675-766   3DRB.F90:689-949   */
+int lbm_streaming(lbm_handle* h);   /* 2DRB.F90:777-798   3DRB.F90:957-979   */
+int lbm_bounceback(lbm_handle* h);  /* 2DRB.F90:811-866   3DRB.F90:987-1058  */
+int lbm_macro(lbm_handle* h);       /* 2DRB.F90:878-894   3DRB.F90:1066-1098 */
+int lbm_collisionT(lbm_handle* h);  /* 2DRB.F90:906-980   3DRB.F90:1106-1198 */
+int lbm_streamingT(lbm_handle* h);  /* 2DRB.F90:993-1014  3DRB.F90:1209-1232 */
+int lbm_bouncebackT(lbm_handle* h); /* 2DRB.F90:1026-1107 3DRB.F90:1243-1351 */
+int lbm_macroT(lbm_handle* h);      /* 2DRB.F90:1120-1134 3DRB.F90:1362-1381 */
+
+/* ---- fused time stepping ---------------------------------------------------------------- */
+/* Advances nsteps time steps (the body of the `do while` loop, 3DRB.F90:225-241) with the
+ * fused pull-stream + MRT-collide kernels of the handle's precision, replayed from a
+ * captured CUDA graph.  Asynchronous. */
+int lbm_step(lbm_handle* h, int64_t nsteps);
+
+/* ---- diagnostics (FP64 reductions on the device; synchronise) --------------------------- */
+/* subroutine check: errU = ||u-up||_2/||u||_2, errT = ||T-Tp||_1/||T||_1, then up <- u
+ * (2DRB.F90:1213-1260, 3DRB.F90:1475-1528).  Returns LBM_ERR_DIVERGED on a non-finite field. */
+int lbm_check(lbm_handle* h, double* errU, double* errT);
+/* subroutine calNuRe: volume Nu = 1 + <v T> L/kappa (RB) or <u T> (side heated) and
+ * Re = sqrt(<|u|^2>) L/nu (2DRB.F90:1610-1675, 3DRB.F90:1712-1778). */
+int lbm_calNuRe(lbm_handle* h, double* Nu, double* Re);
+/* subroutine RBcalc_Nu_global (2DRB.F90:2251-2297, 3DRB.F90:1839-1878). */
+int lbm_RBcalc_Nu_global(lbm_handle* h, double* Nu_global);
+/* subroutine RBcalc_Nu_wall_avg (2DRB.F90:2308-2473, 3DRB.F90:2049-2210). */
+int lbm_RBcalc_Nu_wall_avg(lbm_handle* h, lbm_nu_wall* out);
+
+/* ---- state transfer (Fortran layout, FP64 host arrays) ---------------------------------- */
+/* `count` is the number of doubles in `host` and must equal the field's size. */
+int lbm_get_state(lbm_handle* h, int field, double* host, size_t count);
+int lbm_set_state(lbm_handle* h, int field, const double* host, size_t count);
+
+/* ---- measurement hooks (no counterpart in the reference, which times its loop with
+ *      CPU_TIME / OMP_get_wtime, 3DRB.F90:222-223, 266-267) -------------------------------- */
+/* The handle's CUDA stream (a cudaStream_t), for callers that record their own events. */
+int lbm_get_stream(lbm_handle* h, void** stream);
+/* Advance nsteps fused steps without graph replay, recording CUDA events around each
+ * kernel; returns the mean device time per launch of the flow and thermal kernels. */
+int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, double* ms_thermal);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GPU_H */
