@@ -1,0 +1,145 @@
+!=====================================================================================
+! lbm_gpu_mod.F90 - ISO_C_BINDING interface to liblbmgpu.so (include/lbm_gpu.h).
+!
+! A Fortran driver shaped like `program main3d` (3DRB.F90:198-330) keeps its loop and
+! replaces the module-array subroutines with calls into the GB300 library:
+!
+!   type(c_ptr) :: h
+!   type(lbm_params), target :: p
+!   ist = lbm_params_default(3, p)
+!   p%nx = nx; p%ny = ny; p%nz = nz; p%Ra = Rayleigh; p%Pr = Prandtl; p%Mach = Mach
+!   ist = lbm_create(p, 0, h)
+!   ist = lbm_initial(h)                          ! call initial()
+!   do while (...)
+!     ist = lbm_step(h, 2000_c_int64_t)           ! 2000 x (collision ... macroT)
+!     ist = lbm_check(h, errorU, errorT)          ! call check()
+!   enddo
+!   ist = lbm_RBcalc_Nu_global(h, Nu_global)
+!   ist = lbm_calNuRe(h, Nu, Re)
+!   ist = lbm_destroy(h)
+!
+! Shipped as source: no Fortran compiler was available where the library was built, so
+! this module is not compiled or tested here.
+!=====================================================================================
+module lbm_gpu_mod
+  use, intrinsic :: iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: LBM_OK = 0, LBM_ERR_PARAM = 1, LBM_ERR_CUDA = 2, LBM_ERR_OOM = 3
+  integer(c_int), parameter :: LBM_ERR_DIVERGED = 4, LBM_ERR_TIMEOUT = 5, LBM_ERR_STATE = 6
+  integer(c_int), parameter :: LBM_CELL_RB = 0, LBM_CELL_SIDE = 1
+  integer(c_int), parameter :: LBM_BC_NOSLIP = 0, LBM_BC_PERIODIC = 1
+  integer(c_int), parameter :: LBM_BCT_CONST = 0, LBM_BCT_ADIABATIC = 1, LBM_BCT_PERIODIC = 2
+  integer(c_int), parameter :: LBM_FP64 = 0, LBM_FP32 = 1, LBM_FP16 = 2
+  integer(c_int), parameter :: LBM_FIELD_F = 0, LBM_FIELD_G = 1, LBM_FIELD_RHO = 2, LBM_FIELD_U = 3
+  integer(c_int), parameter :: LBM_FIELD_V = 4, LBM_FIELD_W = 5, LBM_FIELD_T = 6
+
+  type, bind(C) :: lbm_params
+    integer(c_int32_t) :: dim, nx, ny, nz
+    real(c_double)     :: Ra, Pr, Mach, Thot, Tcold
+    integer(c_int32_t) :: cell
+    integer(c_int32_t) :: bc_flow(3), bc_thermal(3)
+    integer(c_int32_t) :: use_g, legacy_thermal, precision, pattern
+    integer(c_int64_t) :: seed
+    real(c_double)     :: noise_amp
+  end type lbm_params
+
+  type, bind(C) :: lbm_nu_wall
+    real(c_double) :: Nu_hot, Nu_cold, Nu_middle
+    real(c_double) :: Nu_hot_max, Nu_hot_max_position, Nu_hot_min, Nu_hot_min_position
+  end type lbm_nu_wall
+
+  interface
+    integer(c_int) function lbm_params_default(dim, p) bind(C, name="lbm_params_default")
+      import :: c_int, lbm_params
+      integer(c_int), value :: dim
+      type(lbm_params) :: p
+    end function
+    integer(c_int) function lbm_create(p, device, h) bind(C, name="lbm_create")
+      import :: c_int, c_ptr, lbm_params
+      type(lbm_params), intent(in) :: p
+      integer(c_int), value :: device
+      type(c_ptr) :: h
+    end function
+    integer(c_int) function lbm_destroy(h) bind(C, name="lbm_destroy")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int) function lbm_initial(h) bind(C, name="lbm_initial")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int) function lbm_collision(h) bind(C, name="lbm_collision")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int) function lbm_streaming(h) bind(C, name="lbm_streaming")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int) function lbm_bounceback(h) bind(C, name="lbm_bounceback")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int) function lbm_macro(h) bind(C, name="lbm_macro")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int) function lbm_collisionT(h) bind(C, name="lbm_collisionT")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int) function lbm_streamingT(h) bind(C, name="lbm_streamingT")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int) function lbm_bouncebackT(h) bind(C, name="lbm_bouncebackT")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int) function lbm_macroT(h) bind(C, name="lbm_macroT")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int) function lbm_step(h, nsteps) bind(C, name="lbm_step")
+      import :: c_int, c_ptr, c_int64_t
+      type(c_ptr), value :: h
+      integer(c_int64_t), value :: nsteps
+    end function
+    integer(c_int) function lbm_check(h, errU, errT) bind(C, name="lbm_check")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double) :: errU, errT
+    end function
+    integer(c_int) function lbm_calNuRe(h, Nu, Re) bind(C, name="lbm_calNuRe")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double) :: Nu, Re
+    end function
+    integer(c_int) function lbm_RBcalc_Nu_global(h, Nu) bind(C, name="lbm_RBcalc_Nu_global")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double) :: Nu
+    end function
+    integer(c_int) function lbm_RBcalc_Nu_wall_avg(h, w) bind(C, name="lbm_RBcalc_Nu_wall_avg")
+      import :: c_int, c_ptr, lbm_nu_wall
+      type(c_ptr), value :: h
+      type(lbm_nu_wall) :: w
+    end function
+    ! state arrays in the reference's own layout, e.g. f(0:qf-1,nx,ny,nz)
+    integer(c_int) function lbm_get_state(h, field, host, count) bind(C, name="lbm_get_state")
+      import :: c_int, c_ptr, c_double, c_size_t
+      type(c_ptr), value :: h
+      integer(c_int), value :: field
+      real(c_double) :: host(*)
+      integer(c_size_t), value :: count
+    end function
+    integer(c_int) function lbm_set_state(h, field, host, count) bind(C, name="lbm_set_state")
+      import :: c_int, c_ptr, c_double, c_size_t
+      type(c_ptr), value :: h
+      integer(c_int), value :: field
+      real(c_double), intent(in) :: host(*)
+      integer(c_size_t), value :: count
+    end function
+  end interface
+end module lbm_gpu_mod

@@ -1,0 +1,67 @@
+"""C-ABI checks that need no GPU: the library loads, exports every symbol the headers
+declare, fills the parameter struct consistently with the Python mirror, and derives the
+same constants as the oracle (host-only calls; no kernel is launched)."""
+import ctypes as C
+import glob
+import os
+import re
+
+import pytest
+
+from lbmgpu.abi import LbmConstants, LbmParams, rb_params
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s+\**\s*(lbm_[A-Za-z0-9_]+)\s*\(", text, re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declares_the_reference_surface():
+    names = declared_functions()
+    for sub in ("collision", "streaming", "bounceback", "macro", "collisionT", "streamingT", "bouncebackT",
+                "macroT", "initial", "check", "calNuRe", "RBcalc_Nu_global", "RBcalc_Nu_wall_avg"):
+        assert "lbm_" + sub in names
+
+
+def test_library_exports_every_declared_symbol(gpu_lib):
+    missing = [n for n in sorted(declared_functions()) if not hasattr(gpu_lib, n)]
+    assert not missing, missing
+
+
+def test_params_struct_layout(gpu_lib):
+    import lbmgpu
+    p = lbmgpu.params_default(2)
+    assert (p.dim, p.nx, p.ny, p.nz) == (2, 320, 160, 1)
+    assert p.Ra == 5e4 and p.Pr == 0.71 and p.Mach == 0.1 and p.Thot == 0.5 and p.Tcold == -0.5
+    assert list(p.bc_flow) == [1, 0, 0] and list(p.bc_thermal) == [2, 0, 1]
+    assert p.use_g == 1 and p.legacy_thermal == 0 and p.seed == 20261203 and p.noise_amp == 0.0
+    p3 = lbmgpu.params_default(3)
+    assert (p3.nx, p3.ny, p3.nz, p3.Ra) == (120, 120, 120, 1e7)
+    assert C.sizeof(LbmParams) == 120
+
+
+@pytest.mark.parametrize("dim,legacy", [(2, False), (3, False), (2, True), (3, True)])
+def test_constants_equal_oracle(gpu_lib, oracle_mod, dim, legacy):
+    import lbmgpu
+    p = rb_params(dim=dim, n=64, ny=64, Ra=1e6, U=0.02 if legacy else 0.1, legacy_thermal=legacy)
+    c_lib = lbmgpu.derive_constants(p).as_dict()
+    c_ora = oracle_mod.Oracle(p).constants(LbmConstants).as_dict()
+    assert c_lib == c_ora
+
+
+def test_invalid_parameters_rejected(gpu_lib):
+    import lbmgpu
+    for mutate in (lambda p: setattr(p, "nx", 2), lambda p: setattr(p, "Ra", -1.0),
+                   lambda p: p.bc_flow.__setitem__(1, 1), lambda p: setattr(p, "precision", 7),
+                   lambda p: setattr(p, "Tcold", 1.0)):
+        p = rb_params(dim=3, n=16)
+        mutate(p)
+        with pytest.raises(lbmgpu.LbmError):
+            lbmgpu.derive_constants(p)
