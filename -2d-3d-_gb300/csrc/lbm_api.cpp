@@ -406,6 +406,7 @@ extern "C" const char* lbm_status_string(int s) {
         case LBM_ERR_DIVERGED: return "LBM_ERR_DIVERGED";
         case LBM_ERR_TIMEOUT: return "LBM_ERR_TIMEOUT";
         case LBM_ERR_STATE: return "LBM_ERR_STATE";
+        case LBM_ERR_TOO_LARGE: return "LBM_ERR_TOO_LARGE";
         default: return "unknown status";
     }
 }

@@ -28,6 +28,7 @@ UNITS = [
     ("lbm_reduce.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
     ("lbm_fast.cu", ["-fmad=true"]),
     ("lbm_api.cpp", []),
+    ("lbm_noalloc.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
 ]
 
 

@@ -177,22 +177,22 @@ def run_reference(args):
     from oracle import oracle as ora
     ora.build()
     threads = ora.set_threads(os.cpu_count() or 1)
-    o = ora.Oracle(workload_params("fp64"))
+    o = ora.Oracle(workload_params("fp64", args.size))
     o.initial()
     o.step(args.warmup)
     t0 = time.perf_counter()
     o.step(args.steps)
     dt = time.perf_counter() - t0
-    cells = N_CELL_EDGE ** 3
+    cells = args.size ** 3
     value = cells * args.steps / dt / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(),
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args.size),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "%d steps of the %d^3 workload after %d warm-up steps; C++ restatement of the "
                                    "reference's OpenMP CPU path (the Fortran cannot be compiled here)"
-                                   % (args.steps, N_CELL_EDGE, args.warmup)},
+                                   % (args.steps, args.size, args.warmup)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -202,7 +202,7 @@ def run_reference(args):
 def time_precision(prec, args, pg, local):
     import torch
     import lbmgpu
-    p = workload_params(prec)
+    p = workload_params(prec, args.size)
     lat = lbmgpu.Lattice(p, device=local)
     lat.initial()
     lat.step(args.warmup)
@@ -232,7 +232,7 @@ def e2e_run(prec, args, local):
     """State in from host arrays (Fortran layout), K steps, T field and Nu/Re out, via the C ABI."""
     import numpy as np
     import lbmgpu
-    p = workload_params(prec)
+    p = workload_params(prec, args.size)
     lat = lbmgpu.Lattice(p, device=local)
     lat.initial()
     names = ["f", "g", "rho", "u", "v", "w", "T", "Bx_prev", "By_prev", "Bz_prev"]
@@ -265,12 +265,13 @@ def run_gpu(args):
     peak, peak_kind = measured_hbm_peak()
     traffic = ncu_traffic()
     results = {}
+    precs = [x for x in args.precisions.split(",") if x]
     with ClockSampler(local) as clk:
-        for prec in ("fp64", "fp32", "fp16"):
+        for prec in precs:
             results[prec] = time_precision(prec, args, pg, local)
     clocks = clk.summary()
-    e2e = e2e_run("fp64", args, local)
-    cells = N_CELL_EDGE ** 3
+    e2e = None if args.no_e2e else e2e_run(precs[0], args, local)
+    cells = args.size ** 3
 
     def roof(prec):
         r = results[prec]
@@ -283,13 +284,13 @@ def run_gpu(args):
                           % (r["ms_flow"], r["ms_thermal"]),
                 "algorithmic_bytes_per_cell": BYTES_PER_CELL[prec]}
 
-    head = results["fp64"]
+    head = results[precs[0]]
     line = {
         "metric": METRIC, "value": head["mlups"] * world, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": DTYPE["fp64"], "data": "synthetic", "config": workload_config(),
+        "vs_baseline": None, "dtype": DTYPE[precs[0]], "data": "synthetic", "config": workload_config(args.size),
         "parallelism": "replicas" if world > 1 else "single GPU",
-        "roofline": roof("fp64"),
+        "roofline": roof(precs[0]),
         "e2e": e2e,
         "gpu_launches": 2 * args.steps,
         "clocks": clocks,
@@ -298,7 +299,7 @@ def run_gpu(args):
                          "Re": results[prec]["Re"]} for prec in results},
     }
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline()
+        line["cpu_baseline"] = cpu_baseline(n=args.size)
     if rank == 0:
         print(json.dumps(line))
     return 0
@@ -311,6 +312,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) leg")
+    ap.add_argument("--size", type=int, default=N_CELL_EDGE, help="cube edge (cells); 128 is the benchmark")
+    ap.add_argument("--precisions", default="fp64,fp32,fp16",
+                    help="comma list; the first is the headline form")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

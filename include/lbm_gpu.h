@@ -177,6 +177,33 @@ int lbm_get_stream(lbm_handle* h, void** stream);
  * kernel; returns the mean device time per launch of the flow and thermal kernels. */
 int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, double* ms_thermal);
 
+/* ---- allocation-free diagnostic (no counterpart in the reference) -----------------------
+ * For callers that cannot let a library call cudaMalloc: programs whose device memory is
+ * already owned by their own allocator (the Fortran driver's OpenACC data region or pool,
+ * a framework's caching allocator, a server admitting lattices against a fixed HBM
+ * budget).  There a library cudaMalloc can fail while the owner's pool still has room,
+ * it escapes the owner's accounting, and cudaFree synchronises the whole device.
+ *
+ * Computes the calNuRe volume averages (Nu = 1 + <v T> L/kappa, or <u T> for a side-heated
+ * cell; Re = sqrt(<|u|^2>) L/nu) of caller-provided FP64 device fields of `ncell` values
+ * (w = NULL in 2D) on `stream` (a cudaStream_t, NULL = default stream), and returns the
+ * two numbers in host memory; the call synchronises that stream.  It allocates nothing:
+ * its per-block partial sums live in one fixed array compiled into the library, of
+ * 3*LBM_NOALLOC_MAX_BLOCKS+3 doubles (about 29 KB on every GPU that loads the library,
+ * held until the process exits).  Lattices larger than LBM_NOALLOC_MAX_CELLS cells are
+ * rejected with LBM_ERR_TOO_LARGE before anything is launched.  The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call outside any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller.  A non-finite
+ * field value gives LBM_ERR_DIVERGED. */
+#define LBM_ERR_TOO_LARGE            7
+#define LBM_NOALLOC_MAX_BLOCKS       1216
+#define LBM_NOALLOC_CELLS_PER_BLOCK  65536
+#define LBM_NOALLOC_MAX_CELLS        (1216LL * 65536LL) /* 79,691,776 cells, e.g. 430^3 */
+int lbm_calNuRe_noalloc(const double* u, const double* v, const double* w, const double* T, int64_t ncell,
+                        int side_heated, double lengthUnit, double diffusivity, double viscosity,
+                        void* stream, double* Nu, double* Re);
+
 #ifdef __cplusplus
 }
 #endif
