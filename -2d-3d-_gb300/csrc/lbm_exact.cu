@@ -26,6 +26,21 @@ namespace lbm {
 // Per-cell arithmetic, verbatim from the reference.
 // ------------------------------------------------------------------------------------
 
+// Division by one of the reference's integer constants c (all below 2^12), as the
+// reference writes it (x / c), rounded exactly like IEEE division but in 3 FP64
+// operations: q = x*rc with rc = RN(1/c), the exact remainder r = x - q*c (one fma),
+// then RN(q + r*rc) (Markstein's correction).  For an integer divisor c < 2^12 the exact
+// quotient is never closer than ulp/(2c) to a rounding midpoint, while the corrected
+// value differs from it by less than 1.5 ulp * 2^-53, so the result is the correctly
+// rounded quotient for every normal x (checked against CUDA's division by
+// lbm_selftest_const_division).
+__device__ __forceinline__ double divc(double x, double c) {
+    const double rc = 1.0 / c;  // folded at compile time
+    const double q = __dmul_rn(x, rc);
+    const double r = __fma_rn(-q, c, x);
+    return __fma_rn(r, rc, q);
+}
+
 // collision (2DRB.F90:688-759).  Writes f_post and the stored body force (Fx, Fy).
 __device__ __forceinline__ void collide_2d(const double* F, double rho, double u, double v, double T,
                                            const PhysC& P, double* FP, double& FxOut, double& FyOut) {
@@ -71,19 +86,19 @@ __device__ __forceinline__ void collide_2d(const double* F, double rho, double u
 #pragma unroll
     for (int a = 0; a < 9; ++a) m_post[a] = m[a] - s[a] * (m[a] - meq[a]) + fSource[a];
 
-    FP[0] = m_post[0] / 9.0 - m_post[1] / 9.0 + m_post[2] / 9.0;
-    FP[1] = m_post[0] / 9.0 - m_post[1] / 36.0 - m_post[2] / 18.0 + m_post[3] / 6.0 - m_post[4] / 6.0 + m_post[7] / 4.0;
-    FP[2] = m_post[0] / 9.0 - m_post[1] / 36.0 - m_post[2] / 18.0 + m_post[5] / 6.0 - m_post[6] / 6.0 - m_post[7] / 4.0;
-    FP[3] = m_post[0] / 9.0 - m_post[1] / 36.0 - m_post[2] / 18.0 - m_post[3] / 6.0 + m_post[4] / 6.0 + m_post[7] / 4.0;
-    FP[4] = m_post[0] / 9.0 - m_post[1] / 36.0 - m_post[2] / 18.0 - m_post[5] / 6.0 + m_post[6] / 6.0 - m_post[7] / 4.0;
-    FP[5] = m_post[0] / 9.0 + m_post[1] / 18.0 + m_post[2] / 36.0 + m_post[3] / 6.0 + m_post[4] / 12.0
-            + m_post[5] / 6.0 + m_post[6] / 12.0 + m_post[8] / 4.0;
-    FP[6] = m_post[0] / 9.0 + m_post[1] / 18.0 + m_post[2] / 36.0 - m_post[3] / 6.0 - m_post[4] / 12.0
-            + m_post[5] / 6.0 + m_post[6] / 12.0 - m_post[8] / 4.0;
-    FP[7] = m_post[0] / 9.0 + m_post[1] / 18.0 + m_post[2] / 36.0 - m_post[3] / 6.0 - m_post[4] / 12.0
-            - m_post[5] / 6.0 - m_post[6] / 12.0 + m_post[8] / 4.0;
-    FP[8] = m_post[0] / 9.0 + m_post[1] / 18.0 + m_post[2] / 36.0 + m_post[3] / 6.0 + m_post[4] / 12.0
-            - m_post[5] / 6.0 - m_post[6] / 12.0 - m_post[8] / 4.0;
+    FP[0] = divc(m_post[0], 9.0) - divc(m_post[1], 9.0) + divc(m_post[2], 9.0);
+    FP[1] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) + divc(m_post[3], 6.0) - divc(m_post[4], 6.0) + m_post[7] / 4.0;
+    FP[2] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) + divc(m_post[5], 6.0) - divc(m_post[6], 6.0) - m_post[7] / 4.0;
+    FP[3] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) - divc(m_post[3], 6.0) + divc(m_post[4], 6.0) + m_post[7] / 4.0;
+    FP[4] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) - divc(m_post[5], 6.0) + divc(m_post[6], 6.0) - m_post[7] / 4.0;
+    FP[5] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) + divc(m_post[3], 6.0) + divc(m_post[4], 12.0)
+            + divc(m_post[5], 6.0) + divc(m_post[6], 12.0) + m_post[8] / 4.0;
+    FP[6] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) - divc(m_post[3], 6.0) - divc(m_post[4], 12.0)
+            + divc(m_post[5], 6.0) + divc(m_post[6], 12.0) - m_post[8] / 4.0;
+    FP[7] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) - divc(m_post[3], 6.0) - divc(m_post[4], 12.0)
+            - divc(m_post[5], 6.0) - divc(m_post[6], 12.0) + m_post[8] / 4.0;
+    FP[8] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) + divc(m_post[3], 6.0) + divc(m_post[4], 12.0)
+            - divc(m_post[5], 6.0) - divc(m_post[6], 12.0) - m_post[8] / 4.0;
 }
 
 // collision (3DRB.F90:704-943).
@@ -120,11 +135,11 @@ __device__ __forceinline__ void collide_3d(const double* f, double rhoLoc, doubl
     meq[1] = rhoLoc * (-11.0 + 19.0 * u2);
     meq[2] = rhoLoc * (3.0 - 11.0 * u2 / 2.0);
     meq[3] = rhoLoc * uLoc;
-    meq[4] = -2.0 * rhoLoc * uLoc / 3.0;
+    meq[4] = divc(-2.0 * rhoLoc * uLoc, 3.0);
     meq[5] = rhoLoc * vLoc;
-    meq[6] = -2.0 * rhoLoc * vLoc / 3.0;
+    meq[6] = divc(-2.0 * rhoLoc * vLoc, 3.0);
     meq[7] = rhoLoc * wLoc;
-    meq[8] = -2.0 * rhoLoc * wLoc / 3.0;
+    meq[8] = divc(-2.0 * rhoLoc * wLoc, 3.0);
     meq[9] = rhoLoc * (2.0 * uLoc * uLoc - vLoc * vLoc - wLoc * wLoc);
     meq[10] = -0.5 * meq[9];
     meq[11] = rhoLoc * (vLoc * vLoc - wLoc * wLoc);
@@ -141,69 +156,74 @@ __device__ __forceinline__ void collide_3d(const double* f, double rhoLoc, doubl
     s[10] = P.Spi; s[11] = P.Snu; s[12] = P.Spi; s[13] = P.Snu; s[14] = P.Snu;
     s[15] = P.Snu; s[16] = P.Sm;  s[17] = P.Sm;  s[18] = P.Sm;
 
-    const double FxLoc = 0.0;
+    // Guo source (3DRB.F90:826-849) with the body force F = (0, F_y, 0).  Terms that the
+    // reference multiplies by F_x = F_z = 0 or by a zero rate are left out: they only add
+    // or subtract a zero, so every value is unchanged (at most the sign of a zero result
+    // differs, and no result is ever divided by it).
     const double FyLoc = rhoLoc * P.gBeta * (Tc - P.Tref);
-    const double FzLoc = 0.0;
-    const double uDotF = uLoc * FxLoc + vLoc * FyLoc + wLoc * FzLoc;
+    const double uDotF = vLoc * FyLoc;
 
-    fSource[0] = 0.0;
     fSource[1] = (1.0 - 0.5 * s[1]) * 38.0 * uDotF;
     fSource[2] = (1.0 - 0.5 * s[2]) * (-11.0) * uDotF;
-    fSource[3] = (1.0 - 0.5 * s[3]) * FxLoc;
-    fSource[4] = (1.0 - 0.5 * s[4]) * (-2.0 / 3.0) * FxLoc;
-    fSource[5] = (1.0 - 0.5 * s[5]) * FyLoc;
     fSource[6] = (1.0 - 0.5 * s[6]) * (-2.0 / 3.0) * FyLoc;
-    fSource[7] = (1.0 - 0.5 * s[7]) * FzLoc;
-    fSource[8] = (1.0 - 0.5 * s[8]) * (-2.0 / 3.0) * FzLoc;
-    fSource[9] = (1.0 - 0.5 * s[9]) * (4.0 * uLoc * FxLoc - 2.0 * vLoc * FyLoc - 2.0 * wLoc * FzLoc);
-    fSource[10] = (1.0 - 0.5 * s[10]) * (-2.0 * uLoc * FxLoc + vLoc * FyLoc + wLoc * FzLoc);
-    fSource[11] = (1.0 - 0.5 * s[11]) * (2.0 * vLoc * FyLoc - 2.0 * wLoc * FzLoc);
-    fSource[12] = (1.0 - 0.5 * s[12]) * (-(vLoc * FyLoc) + wLoc * FzLoc);
-    fSource[13] = (1.0 - 0.5 * s[13]) * (uLoc * FyLoc + vLoc * FxLoc);
-    fSource[14] = (1.0 - 0.5 * s[14]) * (vLoc * FzLoc + wLoc * FyLoc);
-    fSource[15] = (1.0 - 0.5 * s[15]) * (uLoc * FzLoc + wLoc * FxLoc);
-    fSource[16] = 0.0;
-    fSource[17] = 0.0;
-    fSource[18] = 0.0;
+    fSource[9] = (1.0 - 0.5 * s[9]) * (-(2.0 * vLoc * FyLoc));
+    fSource[10] = (1.0 - 0.5 * s[10]) * (vLoc * FyLoc);
+    fSource[11] = (1.0 - 0.5 * s[11]) * (2.0 * vLoc * FyLoc);
+    fSource[12] = (1.0 - 0.5 * s[12]) * (-(vLoc * FyLoc));
+    fSource[13] = (1.0 - 0.5 * s[13]) * (uLoc * FyLoc);
+    fSource[14] = (1.0 - 0.5 * s[14]) * (wLoc * FyLoc);
 
+    // m_post = m - S(m - meq) + source; conserved moments (s = 0) keep m plus the force.
+    mp[0] = m[0];
+    mp[3] = m[3];
+    mp[5] = m[5] + FyLoc;
+    mp[7] = m[7];
+    mp[1] = m[1] - s[1] * (m[1] - meq[1]) + fSource[1];
+    mp[2] = m[2] - s[2] * (m[2] - meq[2]) + fSource[2];
+    mp[4] = m[4] - s[4] * (m[4] - meq[4]);
+    mp[6] = m[6] - s[6] * (m[6] - meq[6]) + fSource[6];
+    mp[8] = m[8] - s[8] * (m[8] - meq[8]);
 #pragma unroll
-    for (int a = 0; a < 19; ++a) mp[a] = m[a] - s[a] * (m[a] - meq[a]) + fSource[a];
+    for (int a = 9; a <= 14; ++a) mp[a] = m[a] - s[a] * (m[a] - meq[a]) + fSource[a];
+    mp[15] = m[15] - s[15] * (m[15] - meq[15]);
+#pragma unroll
+    for (int a = 16; a <= 18; ++a) mp[a] = m[a] - s[a] * m[a];
 
-    fp[0] = mp[0] / 19.0 - 5.0 * mp[1] / 399.0 + mp[2] / 21.0;
-    fp[1] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 + mp[3] / 10.0 - mp[4] / 10.0 + mp[9] / 18.0 - mp[10] / 18.0;
-    fp[2] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 - mp[3] / 10.0 + mp[4] / 10.0 + mp[9] / 18.0 - mp[10] / 18.0;
-    fp[3] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 + mp[5] / 10.0 - mp[6] / 10.0 - mp[9] / 36.0 + mp[10] / 36.0
-            + mp[11] / 12.0 - mp[12] / 12.0;
-    fp[4] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 - mp[5] / 10.0 + mp[6] / 10.0 - mp[9] / 36.0 + mp[10] / 36.0
-            + mp[11] / 12.0 - mp[12] / 12.0;
-    fp[5] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 + mp[7] / 10.0 - mp[8] / 10.0 - mp[9] / 36.0 + mp[10] / 36.0
-            - mp[11] / 12.0 + mp[12] / 12.0;
-    fp[6] = mp[0] / 19.0 - 11.0 * mp[1] / 2394.0 - mp[2] / 63.0 - mp[7] / 10.0 + mp[8] / 10.0 - mp[9] / 36.0 + mp[10] / 36.0
-            - mp[11] / 12.0 + mp[12] / 12.0;
-    fp[7] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[3] / 10.0 + mp[4] / 40.0 + mp[5] / 10.0 + mp[6] / 40.0
-            + mp[9] / 36.0 + mp[10] / 72.0 + mp[11] / 12.0 + mp[12] / 24.0 + mp[13] / 4.0 + mp[16] / 8.0 - mp[17] / 8.0;
-    fp[8] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[3] / 10.0 - mp[4] / 40.0 + mp[5] / 10.0 + mp[6] / 40.0
-            + mp[9] / 36.0 + mp[10] / 72.0 + mp[11] / 12.0 + mp[12] / 24.0 - mp[13] / 4.0 - mp[16] / 8.0 - mp[17] / 8.0;
-    fp[9] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[3] / 10.0 + mp[4] / 40.0 - mp[5] / 10.0 - mp[6] / 40.0
-            + mp[9] / 36.0 + mp[10] / 72.0 + mp[11] / 12.0 + mp[12] / 24.0 - mp[13] / 4.0 + mp[16] / 8.0 + mp[17] / 8.0;
-    fp[10] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[3] / 10.0 - mp[4] / 40.0 - mp[5] / 10.0 - mp[6] / 40.0
-             + mp[9] / 36.0 + mp[10] / 72.0 + mp[11] / 12.0 + mp[12] / 24.0 + mp[13] / 4.0 - mp[16] / 8.0 + mp[17] / 8.0;
-    fp[11] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[3] / 10.0 + mp[4] / 40.0 + mp[7] / 10.0 + mp[8] / 40.0
-             + mp[9] / 36.0 + mp[10] / 72.0 - mp[11] / 12.0 - mp[12] / 24.0 + mp[15] / 4.0 - mp[16] / 8.0 + mp[18] / 8.0;
-    fp[12] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[3] / 10.0 - mp[4] / 40.0 + mp[7] / 10.0 + mp[8] / 40.0
-             + mp[9] / 36.0 + mp[10] / 72.0 - mp[11] / 12.0 - mp[12] / 24.0 - mp[15] / 4.0 + mp[16] / 8.0 + mp[18] / 8.0;
-    fp[13] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[3] / 10.0 + mp[4] / 40.0 - mp[7] / 10.0 - mp[8] / 40.0
-             + mp[9] / 36.0 + mp[10] / 72.0 - mp[11] / 12.0 - mp[12] / 24.0 - mp[15] / 4.0 - mp[16] / 8.0 - mp[18] / 8.0;
-    fp[14] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[3] / 10.0 - mp[4] / 40.0 - mp[7] / 10.0 - mp[8] / 40.0
-             + mp[9] / 36.0 + mp[10] / 72.0 - mp[11] / 12.0 - mp[12] / 24.0 + mp[15] / 4.0 + mp[16] / 8.0 - mp[18] / 8.0;
-    fp[15] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[5] / 10.0 + mp[6] / 40.0 + mp[7] / 10.0 + mp[8] / 40.0
-             - mp[9] / 18.0 - mp[10] / 36.0 + mp[14] / 4.0 + mp[17] / 8.0 - mp[18] / 8.0;
-    fp[16] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[5] / 10.0 - mp[6] / 40.0 + mp[7] / 10.0 + mp[8] / 40.0
-             - mp[9] / 18.0 - mp[10] / 36.0 - mp[14] / 4.0 - mp[17] / 8.0 - mp[18] / 8.0;
-    fp[17] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 + mp[5] / 10.0 + mp[6] / 40.0 - mp[7] / 10.0 - mp[8] / 40.0
-             - mp[9] / 18.0 - mp[10] / 36.0 - mp[14] / 4.0 + mp[17] / 8.0 + mp[18] / 8.0;
-    fp[18] = mp[0] / 19.0 + 4.0 * mp[1] / 1197.0 + mp[2] / 252.0 - mp[5] / 10.0 - mp[6] / 40.0 - mp[7] / 10.0 - mp[8] / 40.0
-             - mp[9] / 18.0 - mp[10] / 36.0 + mp[14] / 4.0 - mp[17] / 8.0 + mp[18] / 8.0;
+    fp[0] = divc(mp[0], 19.0) - divc(5.0 * mp[1], 399.0) + divc(mp[2], 21.0);
+    fp[1] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) + divc(mp[3], 10.0) - divc(mp[4], 10.0) + divc(mp[9], 18.0) - divc(mp[10], 18.0);
+    fp[2] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) - divc(mp[3], 10.0) + divc(mp[4], 10.0) + divc(mp[9], 18.0) - divc(mp[10], 18.0);
+    fp[3] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) + divc(mp[5], 10.0) - divc(mp[6], 10.0) - divc(mp[9], 36.0) + divc(mp[10], 36.0)
+            + divc(mp[11], 12.0) - divc(mp[12], 12.0);
+    fp[4] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) - divc(mp[5], 10.0) + divc(mp[6], 10.0) - divc(mp[9], 36.0) + divc(mp[10], 36.0)
+            + divc(mp[11], 12.0) - divc(mp[12], 12.0);
+    fp[5] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) + divc(mp[7], 10.0) - divc(mp[8], 10.0) - divc(mp[9], 36.0) + divc(mp[10], 36.0)
+            - divc(mp[11], 12.0) + divc(mp[12], 12.0);
+    fp[6] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) - divc(mp[7], 10.0) + divc(mp[8], 10.0) - divc(mp[9], 36.0) + divc(mp[10], 36.0)
+            - divc(mp[11], 12.0) + divc(mp[12], 12.0);
+    fp[7] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0)
+            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) + mp[13] / 4.0 + mp[16] / 8.0 - mp[17] / 8.0;
+    fp[8] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0)
+            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) - mp[13] / 4.0 - mp[16] / 8.0 - mp[17] / 8.0;
+    fp[9] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0)
+            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) - mp[13] / 4.0 + mp[16] / 8.0 + mp[17] / 8.0;
+    fp[10] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0)
+             + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) + mp[13] / 4.0 - mp[16] / 8.0 + mp[17] / 8.0;
+    fp[11] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
+             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) + mp[15] / 4.0 - mp[16] / 8.0 + mp[18] / 8.0;
+    fp[12] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
+             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) - mp[15] / 4.0 + mp[16] / 8.0 + mp[18] / 8.0;
+    fp[13] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
+             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) - mp[15] / 4.0 - mp[16] / 8.0 - mp[18] / 8.0;
+    fp[14] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
+             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) + mp[15] / 4.0 + mp[16] / 8.0 - mp[18] / 8.0;
+    fp[15] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
+             - divc(mp[9], 18.0) - divc(mp[10], 36.0) + mp[14] / 4.0 + mp[17] / 8.0 - mp[18] / 8.0;
+    fp[16] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
+             - divc(mp[9], 18.0) - divc(mp[10], 36.0) - mp[14] / 4.0 - mp[17] / 8.0 - mp[18] / 8.0;
+    fp[17] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
+             - divc(mp[9], 18.0) - divc(mp[10], 36.0) - mp[14] / 4.0 + mp[17] / 8.0 + mp[18] / 8.0;
+    fp[18] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
+             - divc(mp[9], 18.0) - divc(mp[10], 36.0) + mp[14] / 4.0 - mp[17] / 8.0 + mp[18] / 8.0;
 }
 
 // collisionT (2DRB.F90:921-974).  B = (u T, v T); returns g_post and the new B.
@@ -286,13 +306,13 @@ __device__ __forceinline__ void collideT_3d(const double* g, double u, double v,
     n_post[4] = n[4] - q[4] * (n[4] - neq[4]);
     n_post[5] = n[5] - q[5] * (n[5] - neq[5]);
     n_post[6] = n[6] - q[6] * (n[6] - neq[6]);
-    gp[0] = n_post[0] / 7.0 - n_post[4] / 7.0;
-    gp[1] = n_post[0] / 7.0 + n_post[1] / 2.0 + n_post[4] / 42.0 + n_post[5] / 6.0;
-    gp[2] = n_post[0] / 7.0 - n_post[1] / 2.0 + n_post[4] / 42.0 + n_post[5] / 6.0;
-    gp[3] = n_post[0] / 7.0 + n_post[2] / 2.0 + n_post[4] / 42.0 - n_post[5] / 12.0 + n_post[6] / 4.0;
-    gp[4] = n_post[0] / 7.0 - n_post[2] / 2.0 + n_post[4] / 42.0 - n_post[5] / 12.0 + n_post[6] / 4.0;
-    gp[5] = n_post[0] / 7.0 + n_post[3] / 2.0 + n_post[4] / 42.0 - n_post[5] / 12.0 - n_post[6] / 4.0;
-    gp[6] = n_post[0] / 7.0 - n_post[3] / 2.0 + n_post[4] / 42.0 - n_post[5] / 12.0 - n_post[6] / 4.0;
+    gp[0] = divc(n_post[0], 7.0) - divc(n_post[4], 7.0);
+    gp[1] = divc(n_post[0], 7.0) + n_post[1] / 2.0 + divc(n_post[4], 42.0) + divc(n_post[5], 6.0);
+    gp[2] = divc(n_post[0], 7.0) - n_post[1] / 2.0 + divc(n_post[4], 42.0) + divc(n_post[5], 6.0);
+    gp[3] = divc(n_post[0], 7.0) + n_post[2] / 2.0 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) + n_post[6] / 4.0;
+    gp[4] = divc(n_post[0], 7.0) - n_post[2] / 2.0 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) + n_post[6] / 4.0;
+    gp[5] = divc(n_post[0], 7.0) + n_post[3] / 2.0 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) - n_post[6] / 4.0;
+    gp[6] = divc(n_post[0], 7.0) - n_post[3] / 2.0 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) - n_post[6] / 4.0;
 }
 
 // macro (2DRB.F90:884-889): u = (sum e f + Fx/2)/rho with the force stored by collision.
@@ -753,3 +773,56 @@ void exact_materialize(const Geo& g, const PhysC& P, const ExactArrays& A, int d
 }
 
 }  // namespace lbm
+
+// ------------------------------------------------------------------------------------
+// self-test of divc against CUDA's IEEE double division
+// ------------------------------------------------------------------------------------
+namespace lbm {
+
+__constant__ double kDivisors[19] = {3.0, 6.0, 7.0, 9.0, 10.0, 12.0, 18.0, 19.0, 21.0, 24.0,
+                                     36.0, 40.0, 42.0, 63.0, 72.0, 252.0, 399.0, 1197.0, 2394.0};
+
+__global__ void k_selftest_divc(long long n, uint64_t seed, unsigned long long* mismatches) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    // random sign, normal exponent in [2^-923, 2^900], random 52-bit significand; every
+    // 8th sample is an exact multiple c*k so that exact quotients are covered too
+    uint64_t z = (seed ^ (uint64_t)i) + 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z = z ^ (z >> 31);
+    const uint64_t expo = 100 + (z >> 52) % 1824;
+    const uint64_t bits = (z & 0x8000000000000000ULL) | (expo << 52) | (z & 0x000FFFFFFFFFFFFFULL);
+    double x = __longlong_as_double((long long)bits);
+    unsigned long long bad = 0;
+#pragma unroll 1
+    for (int d = 0; d < 19; ++d) {
+        const double c = kDivisors[d];
+        double xx = x;
+        if ((i & 7) == 0) xx = c * (double)(long long)((z >> 11) & 0xFFFFFFFFFFULL);
+        const double q_ieee = xx / c;
+        const double rc = 1.0 / c;
+        const double q = __dmul_rn(xx, rc);
+        const double r = __fma_rn(-q, c, xx);
+        const double q_fast = __fma_rn(r, rc, q);
+        if (q_fast != q_ieee) bad += 1;
+    }
+    if (bad) atomicAdd(mismatches, bad);
+}
+
+}  // namespace lbm
+
+extern "C" int lbm_selftest_const_division(int64_t n, uint64_t seed, int64_t* mismatches) {
+    if (n <= 0 || !mismatches) return LBM_ERR_PARAM;
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, sizeof(*d)) != cudaSuccess) return LBM_ERR_OOM;
+    cudaMemset(d, 0, sizeof(*d));
+    lbm::k_selftest_divc<<<(unsigned)((n + 255) / 256), 256>>>((long long)n, seed, d);
+    unsigned long long h = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return LBM_ERR_CUDA;
+    *mismatches = (int64_t)h;
+    return LBM_OK;
+}

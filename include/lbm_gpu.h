@@ -176,6 +176,11 @@ int lbm_get_stream(lbm_handle* h, void** stream);
 /* Advance nsteps fused steps without graph replay, recording CUDA events around each
  * kernel; returns the mean device time per launch of the flow and thermal kernels. */
 int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, double* ms_thermal);
+/* Self-test (no counterpart in the reference): the plain method divides by the reference's
+ * integer constants (x/19, x/2394, ...) with a 3-operation correctly rounded sequence; this
+ * compares it bitwise with CUDA's IEEE division on n random normal doubles for each of the
+ * 19 constants and returns the number of mismatches (expected 0). */
+int lbm_selftest_const_division(int64_t n, uint64_t seed, int64_t* mismatches);
 
 /* ---- allocation-free diagnostic (no counterpart in the reference) -----------------------
  * For callers that cannot let a library call cudaMalloc: programs whose device memory is
