@@ -523,14 +523,23 @@ extern "C" int lbm_macroT(lbm_handle* h) { return stage(h, STAGE_MACROT); }
 // ------------------------------------------------------------------------------------
 // fused stepping
 // ------------------------------------------------------------------------------------
+// FP32/FP16 handles advance with the single fused kernel (lbm_fused.cu) unless it is
+// switched off or the geometry needs whole tiles it does not have.
+static bool use_single(const lbm_handle* h) {
+    return h->p.precision != LBM_FP64 && h->F.single_kernel && fast_fused_supported(h->geo, h->dim);
+}
+
 static void enqueue_one(lbm_handle* h, bool first) {
     const int nxt = h->cur ^ 1;
     if (h->p.precision == LBM_FP64) {
         exact_fused_step(h->geo, h->phys, h->A, h->dim, first, h->fbuf[h->cur], h->gbuf[h->cur], h->fbuf[nxt],
                          h->gbuf[nxt], h->stream);
         h->cur = nxt;
-    } else {
+    } else if (first || !use_single(h)) {
         fast_step(h->F, h->geo, h->phys, h->dim, first, h->stream);
+    } else {
+        if (!h->F.ahead) fast_enter(h->F, h->geo, h->phys, h->dim, h->stream);
+        fast_fused_step(h->F, h->geo, h->phys, h->dim, h->stream);
     }
 }
 
@@ -562,6 +571,8 @@ extern "C" int lbm_step(lbm_handle* h, int64_t nsteps) {
         if (h->p.precision == LBM_FP64) h->fused_valid = true;
         done = 1;
     }
+    // enter the single-kernel phase outside any captured graph
+    if (use_single(h) && !h->F.ahead && done < nsteps) fast_enter(h->F, h->geo, h->phys, h->dim, h->stream);
     while (done < nsteps) {
         if (at_graph_origin(h) && nsteps - done >= kChunkSteps) {
             if (!h->graph_exec) {
@@ -920,6 +931,11 @@ extern "C" int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, 
             exact_fused_step(h->geo, h->phys, h->A, h->dim, false, h->fbuf[h->cur], h->gbuf[h->cur], h->fbuf[nxt],
                              h->gbuf[nxt], h->stream, 1);
             h->cur = nxt;
+        } else if (use_single(h)) {
+            // one kernel per step: its time goes to the first slot, the second is empty
+            if (!h->F.ahead) fast_enter(h->F, h->geo, h->phys, h->dim, h->stream);
+            CK(h, cudaEventRecord(ev[2 * k + 1], h->stream));
+            fast_fused_step(h->F, h->geo, h->phys, h->dim, h->stream);
         } else {
             fast_step(h->F, h->geo, h->phys, h->dim, false, h->stream, 0);
             CK(h, cudaEventRecord(ev[2 * k + 1], h->stream));
@@ -934,12 +950,46 @@ extern "C" int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, 
         float a = 0.f, b = 0.f;
         CK(h, cudaEventElapsedTime(&a, ev[2 * k], ev[2 * k + 1]));
         CK(h, cudaEventElapsedTime(&b, ev[2 * k + 1], ev[2 * k + 2]));
-        tf += a;
-        tt += b;
+        if (use_single(h)) {
+            tf += b;  // the fused kernel sits between the middle and the last event
+        } else {
+            tf += a;
+            tt += b;
+        }
     }
     for (auto& e : ev) cudaEventDestroy(e);
     *ms_flow = tf / (double)nsteps;
     *ms_thermal = tt / (double)nsteps;
     h->itc += nsteps;
+    return LBM_OK;
+}
+
+extern "C" int lbm_set_option(lbm_handle* h, int option, int value) {
+    if (!h) return LBM_ERR_PARAM;
+    switch (option) {
+        case LBM_OPT_SINGLE_KERNEL:
+            if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the plain FP64 method has no single-kernel form");
+            if (h->F.single_kernel != (value != 0)) {
+                // leave the one-ahead phase and drop the graph captured for the other form
+                h->F.ahead = false;
+                h->F.single_kernel = value != 0;
+            }
+            break;
+        case LBM_OPT_KCHUNK:
+            if (value < 1) return fail(h, LBM_ERR_PARAM, "kchunk must be >= 1");
+            h->F.kchunk = value;
+            break;
+        default:
+            return fail(h, LBM_ERR_PARAM, "unknown option");
+    }
+    if (h->graph_exec) {
+        CK(h, cudaStreamSynchronize(h->stream));
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+    }
+    if (h->graph) {
+        cudaGraphDestroy(h->graph);
+        h->graph = nullptr;
+    }
     return LBM_OK;
 }

@@ -76,6 +76,13 @@ struct Geo {
     double bcT_hi[3];    // ... and at the high face
 };
 
+// Select element `axis` of a 3-array without a runtime-indexed access (which would copy a
+// by-value kernel parameter to local memory).
+template <class T>
+__host__ __device__ __forceinline__ T pick3(const T (&a)[3], int axis) {
+    return axis == 0 ? a[0] : (axis == 1 ? a[1] : a[2]);
+}
+
 __host__ __device__ inline long long cell_index(const Geo& g, int i, int j, int k) {
     return (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
 }
@@ -103,7 +110,7 @@ __device__ __forceinline__ T pull_flow(const Geo& g, int a, int i, int j, int k,
         const long long off = (long long)(-Lat<Q>::ex(a)) + (long long)g.nx * ((long long)(-Lat<Q>::ey(a)) + (long long)g.ny * (long long)(-Lat<Q>::ez(a)));
         return load(a, c + off);
     }
-    if (g.bcf[axis] == LBM_BC_NOSLIP) return load(Lat<Q>::opp(a), c);
+    if (pick3(g.bcf, axis) == LBM_BC_NOSLIP) return load(Lat<Q>::opp(a), c);
     if (axis == 0) return load(a, cell_index(g, si < 0 ? g.nx - 1 : 0, j, k));
     if (axis == 1) return load(a, cell_index(g, i, sj < 0 ? g.ny - 1 : 0, k));
     return load(a, cell_index(g, i, j, sk < 0 ? g.nz - 1 : 0));
@@ -127,8 +134,8 @@ __device__ __forceinline__ T pull_thermal(const Geo& g, int a, int i, int j, int
         const long long off = (long long)(-Lat<QT>::ex(a)) + (long long)g.nx * ((long long)(-Lat<QT>::ey(a)) + (long long)g.ny * (long long)(-Lat<QT>::ez(a)));
         return load(a, c + off);
     }
-    const int bt = g.bct[axis];
-    if (bt == LBM_BCT_CONST) return -load(Lat<QT>::opp(a), c) + (T)(low ? g.bcT_lo[axis] : g.bcT_hi[axis]);
+    const int bt = pick3(g.bct, axis);
+    if (bt == LBM_BCT_CONST) return -load(Lat<QT>::opp(a), c) + (T)(low ? pick3(g.bcT_lo, axis) : pick3(g.bcT_hi, axis));
     if (bt == LBM_BCT_ADIABATIC) return load(Lat<QT>::opp(a), c);
     if (axis == 0) return load(a, cell_index(g, si < 0 ? g.nx - 1 : 0, j, k));
     if (axis == 1) return load(a, cell_index(g, i, sj < 0 ? g.ny - 1 : 0, k));

@@ -1,338 +1,50 @@
 // lbm_fast.cu - the reduced-storage forms: FP32 or FP16 populations (deviations from the
 // rest state), FP32 arithmetic, FMA contraction allowed.
 //
-// Same time-step structure as the plain method (two kernels per step, see lbm_exact.cu)
-// and the same moment space: the forward transform is the reference's integer matrix
+// This unit holds the two-kernel step (used for the first step after `initial` or a
+// state load, and to enter the single-kernel mode of lbm_fused.cu), the materialisation
+// of the module arrays, and the conversions to and from the reference's FP64 layout.
+// The moment space is the reference's: the forward transform is its integer matrix
 // applied to the deviations, the relaxation acts on non-equilibrium moments
-// m_k - meq_k = M_k d - (meq_k(rho,u) - meq_k(1,0)), and the inverse transform is the
-// reference's M^-1 with the divisions by constants turned into multiplications.
+// m_k - meq_k = M_k d - (meq_k(rho,u) - meq_k(1,0)), and the inverse transform is its
+// M^-1 with the divisions by constants turned into multiplications.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "lbm_fast.h"
+#include "lbm_fast_math.cuh"
 
 namespace lbm {
 
-// ------------------------------------------------------------------------------------
-// storage conversions
-// ------------------------------------------------------------------------------------
-template <class S> __device__ __forceinline__ float ldS(const S* p, long long i);
-template <> __device__ __forceinline__ float ldS<float>(const float* p, long long i) { return __ldg(p + i); }
-template <> __device__ __forceinline__ float ldS<__half>(const __half* p, long long i) { return __half2float(__ldg(p + i)); }
-template <class S> __device__ __forceinline__ S toS(float x);
-template <> __device__ __forceinline__ float toS<float>(float x) { return x; }
-template <> __device__ __forceinline__ __half toS<__half>(float x) { return __float2half_rn(x); }
-
-// Rest weights (D2Q9 2DRB.F90:506-512, D3Q19 3DRB.F90:669-671).
-template <int Q>
-__host__ __device__ constexpr double wrest(int a) {
-    return Q == 9 ? (a == 0 ? 4.0 / 9.0 : (a <= 4 ? 1.0 / 9.0 : 1.0 / 36.0))
-                  : (a == 0 ? 1.0 / 3.0 : (a <= 6 ? 1.0 / 18.0 : 1.0 / 36.0));
-}
-
-struct PhysF {
-    float gBeta, Tref;
-    float Snu, Sq, Se, Seps, Spi, Sm;
-    float Qk, Qnu, SG, paraA;
-    float omegaT0, omegaT1, geqc;
-    int use_g, legacy;
-};
-
-static PhysF to_physf(const PhysC& P) {
-    PhysF F;
-    F.gBeta = (float)P.gBeta; F.Tref = (float)P.Tref;
-    F.Snu = (float)P.Snu; F.Sq = (float)P.Sq; F.Se = (float)P.Se; F.Seps = (float)P.Seps;
-    F.Spi = (float)P.Spi; F.Sm = (float)P.Sm;
-    F.Qk = (float)P.Qk; F.Qnu = (float)P.Qnu; F.SG = (float)P.SG; F.paraA = (float)P.paraA;
-    F.omegaT0 = (float)P.omegaT0; F.omegaT1 = (float)P.omegaT1; F.geqc = (float)P.geqc;
-    F.use_g = P.use_g; F.legacy = P.legacy;
-    return F;
-}
-
-// Thermal wall terms for deviations: e_a = -e_opp + 2 wT (Tw - Tref).
-static Geo dev_geo(const Geo& g, const PhysC& P) {
-    Geo d = g;
-    for (int a = 0; a < 3; ++a) {
-        d.bcT_lo[a] = g.bcT_lo[a] - 2.0 * P.omegaT1 * P.Tref;
-        d.bcT_hi[a] = g.bcT_hi[a] - 2.0 * P.omegaT1 * P.Tref;
-    }
-    return d;
-}
-
+// Pointers of one launch: module arrays plus the B_prev / lag buffers to read and write.
 template <class S>
-struct FastArrays {
+struct FastArgs {
     S *fref, *gref;
-    float *rho, *u, *v, *w, *T, *Bx, *By, *Bz, *lag;
+    float *rho, *u, *v, *w, *T;
+    const float *Bin0, *Bin1, *Bin2;
+    float *Bout0, *Bout1, *Bout2;
+    const float* lag_in;
+    float* lag_out;
 };
 
 template <class S>
-static FastArrays<S> arrays(const FastState& F) {
-    return FastArrays<S>{(S*)F.fref, (S*)F.gref, F.rho, F.u, F.v, F.w, F.T, F.Bx, F.By, F.Bz, F.lag};
-}
-
-// ------------------------------------------------------------------------------------
-// per-cell arithmetic (FP32, deviations)
-// ------------------------------------------------------------------------------------
-// D2Q9 MRT collision with Guo forcing (2DRB.F90:688-759) on deviations d.
-__device__ __forceinline__ void fcollide_2d(const float* d, float dr, float rho, float u, float v, float Fy,
-                                            const PhysF& P, float* dp) {
-    const float m1 = -4.0f * d[0] - d[1] - d[2] - d[3] - d[4] + 2.0f * (d[5] + d[6] + d[7] + d[8]);
-    const float m2 = 4.0f * d[0] - 2.0f * (d[1] + d[2] + d[3] + d[4]) + d[5] + d[6] + d[7] + d[8];
-    const float m3 = d[1] - d[3] + d[5] - d[6] - d[7] + d[8];
-    const float m4 = -2.0f * d[1] + 2.0f * d[3] + d[5] - d[6] - d[7] + d[8];
-    const float m5 = d[2] - d[4] + d[5] + d[6] - d[7] - d[8];
-    const float m6 = -2.0f * d[2] + 2.0f * d[4] + d[5] + d[6] - d[7] - d[8];
-    const float m7 = d[1] - d[2] + d[3] - d[4];
-    const float m8 = d[5] - d[6] + d[7] - d[8];
-    const float uu = u * u, vv = v * v, q2 = uu + vv;
-    // equilibrium moments relative to rest: meq_k(rho,u) - meq_k(1,0)
-    const float e1 = -2.0f * dr + 3.0f * rho * q2;
-    const float e2 = dr - 3.0f * rho * q2;
-    const float e4 = -rho * u, e6 = -rho * v;
-    const float e7 = rho * (uu - vv), e8 = rho * (u * v);
-    // Guo source with Fx = 0
-    const float s1 = (6.0f - 3.0f * P.Snu) * (v * Fy);
-    const float s2 = -(6.0f - 3.0f * P.Snu) * (v * Fy);
-    const float s6 = -(1.0f - 0.5f * P.Sq) * Fy;
-    const float s7 = (2.0f - P.Snu) * (-v * Fy);
-    const float s8 = (1.0f - 0.5f * P.Snu) * (u * Fy);
-    const float mp0 = dr;
-    const float mp1 = m1 - P.Snu * (m1 - e1) + s1;
-    const float mp2 = m2 - P.Snu * (m2 - e2) + s2;
-    const float mp3 = m3;
-    const float mp4 = m4 - P.Sq * (m4 - e4);
-    const float mp5 = m5 + Fy;
-    const float mp6 = m6 - P.Sq * (m6 - e6) + s6;
-    const float mp7 = m7 - P.Snu * (m7 - e7) + s7;
-    const float mp8 = m8 - P.Snu * (m8 - e8) + s8;
-    // M^-1 (2DRB.F90:743-759)
-    const float A = mp0 * (1.0f / 9.0f);
-    const float B9 = mp1 * (1.0f / 9.0f), B36 = mp1 * (1.0f / 36.0f), B18 = mp1 * (1.0f / 18.0f);
-    const float C9 = mp2 * (1.0f / 9.0f), C18 = mp2 * (1.0f / 18.0f), C36 = mp2 * (1.0f / 36.0f);
-    const float X6 = mp3 * (1.0f / 6.0f), Xq6 = mp4 * (1.0f / 6.0f), Xq12 = mp4 * (1.0f / 12.0f);
-    const float Y6 = mp5 * (1.0f / 6.0f), Yq6 = mp6 * (1.0f / 6.0f), Yq12 = mp6 * (1.0f / 12.0f);
-    const float P7 = mp7 * 0.25f, P8 = mp8 * 0.25f;
-    const float ax = A - B36 - C18, dg = A + B18 + C36;
-    dp[0] = A - B9 + C9;
-    dp[1] = ax + X6 - Xq6 + P7;
-    dp[2] = ax + Y6 - Yq6 - P7;
-    dp[3] = ax - X6 + Xq6 + P7;
-    dp[4] = ax - Y6 + Yq6 - P7;
-    dp[5] = dg + X6 + Xq12 + Y6 + Yq12 + P8;
-    dp[6] = dg - X6 - Xq12 + Y6 + Yq12 - P8;
-    dp[7] = dg - X6 - Xq12 - Y6 - Yq12 + P8;
-    dp[8] = dg + X6 + Xq12 - Y6 - Yq12 - P8;
-}
-
-// D3Q19 MRT collision with Guo forcing (3DRB.F90:714-943) on deviations d.
-__device__ __forceinline__ void fcollide_3d(const float* d, float dr, float rho, float u, float v, float w,
-                                            float Fy, const PhysF& P, float* dp) {
-    const float s16 = d[1] + d[2] + d[3] + d[4] + d[5] + d[6];
-    const float e712 = d[7] + d[8] + d[9] + d[10] + d[11] + d[12] + d[13] + d[14];
-    const float e1518 = d[15] + d[16] + d[17] + d[18];
-    const float s718 = e712 + e1518;
-    const float m1 = -30.0f * d[0] - 11.0f * s16 + 8.0f * s718;
-    const float m2 = 12.0f * d[0] - 4.0f * s16 + s718;
-    const float xs = d[7] - d[8] + d[9] - d[10] + d[11] - d[12] + d[13] - d[14];
-    const float m3 = d[1] - d[2] + xs;
-    const float m4 = -4.0f * d[1] + 4.0f * d[2] + xs;
-    const float ys = d[7] + d[8] - d[9] - d[10] + d[15] - d[16] + d[17] - d[18];
-    const float m5 = d[3] - d[4] + ys;
-    const float m6 = -4.0f * d[3] + 4.0f * d[4] + ys;
-    const float zs = d[11] + d[12] - d[13] - d[14] + d[15] + d[16] - d[17] - d[18];
-    const float m7 = d[5] - d[6] + zs;
-    const float m8 = -4.0f * d[5] + 4.0f * d[6] + zs;
-    const float m9 = 2.0f * (d[1] + d[2]) - (d[3] + d[4] + d[5] + d[6]) + e712 - 2.0f * e1518;
-    const float m10 = -4.0f * (d[1] + d[2]) + 2.0f * (d[3] + d[4] + d[5] + d[6]) + e712 - 2.0f * e1518;
-    const float q710 = d[7] + d[8] + d[9] + d[10], q1114 = d[11] + d[12] + d[13] + d[14];
-    const float m11 = (d[3] + d[4]) - (d[5] + d[6]) + q710 - q1114;
-    const float m12 = -2.0f * (d[3] + d[4]) + 2.0f * (d[5] + d[6]) + q710 - q1114;
-    const float m13 = d[7] - d[8] - d[9] + d[10];
-    const float m14 = d[15] - d[16] - d[17] + d[18];
-    const float m15 = d[11] - d[12] - d[13] + d[14];
-    const float m16 = d[7] - d[8] + d[9] - d[10] - d[11] + d[12] - d[13] + d[14];
-    const float m17 = -d[7] - d[8] + d[9] + d[10] + d[15] - d[16] + d[17] - d[18];
-    const float m18 = d[11] + d[12] - d[13] - d[14] - d[15] - d[16] + d[17] + d[18];
-
-    const float uu = u * u, vv = v * v, ww = w * w, u2 = uu + vv + ww;
-    const float e1 = -11.0f * dr + 19.0f * rho * u2;
-    const float e2 = 3.0f * dr - 5.5f * rho * u2;
-    const float e4 = (-2.0f / 3.0f) * rho * u, e6 = (-2.0f / 3.0f) * rho * v, e8 = (-2.0f / 3.0f) * rho * w;
-    const float e9 = rho * (2.0f * uu - vv - ww), e10 = -0.5f * e9;
-    const float e11 = rho * (vv - ww), e12 = -0.5f * e11;
-    const float e13 = rho * u * v, e14 = rho * v * w, e15 = rho * u * w;
-    const float vF = v * Fy;  // u.F with F = (0, Fy, 0)
-    const float anu = 1.0f - 0.5f * P.Snu, api = 1.0f - 0.5f * P.Spi;
-    const float src1 = (1.0f - 0.5f * P.Se) * 38.0f * vF;
-    const float src2 = (1.0f - 0.5f * P.Seps) * (-11.0f) * vF;
-    const float src6 = (1.0f - 0.5f * P.Sq) * (-2.0f / 3.0f) * Fy;
-    const float src9 = anu * (-2.0f * vF), src10 = api * vF, src11 = anu * (2.0f * vF), src12 = api * (-vF);
-    const float src13 = anu * (u * Fy), src14 = anu * (w * Fy);
-
-    const float mp0 = dr;
-    const float mp1 = m1 - P.Se * (m1 - e1) + src1;
-    const float mp2 = m2 - P.Seps * (m2 - e2) + src2;
-    const float mp3 = m3;
-    const float mp4 = m4 - P.Sq * (m4 - e4);
-    const float mp5 = m5 + Fy;
-    const float mp6 = m6 - P.Sq * (m6 - e6) + src6;
-    const float mp7 = m7;
-    const float mp8 = m8 - P.Sq * (m8 - e8);
-    const float mp9 = m9 - P.Snu * (m9 - e9) + src9;
-    const float mp10 = m10 - P.Spi * (m10 - e10) + src10;
-    const float mp11 = m11 - P.Snu * (m11 - e11) + src11;
-    const float mp12 = m12 - P.Spi * (m12 - e12) + src12;
-    const float mp13 = m13 - P.Snu * (m13 - e13) + src13;
-    const float mp14 = m14 - P.Snu * (m14 - e14) + src14;
-    const float mp15 = m15 - P.Snu * (m15 - e15);
-    const float mp16 = m16 - P.Sm * m16;
-    const float mp17 = m17 - P.Sm * m17;
-    const float mp18 = m18 - P.Sm * m18;
-
-    // M^-1 (3DRB.F90:861-943) with the divisions folded into constants
-    const float A = mp0 * (1.0f / 19.0f);
-    const float B1 = mp1 * (5.0f / 399.0f), B2 = mp1 * (11.0f / 2394.0f), B3 = mp1 * (4.0f / 1197.0f);
-    const float C1 = mp2 * (1.0f / 21.0f), C2 = mp2 * (1.0f / 63.0f), C3 = mp2 * (1.0f / 252.0f);
-    const float X3 = mp3 * 0.1f, X4 = mp4 * 0.1f, X4b = mp4 * 0.025f;
-    const float Y5 = mp5 * 0.1f, Y6 = mp6 * 0.1f, Y6b = mp6 * 0.025f;
-    const float Z7 = mp7 * 0.1f, Z8 = mp8 * 0.1f, Z8b = mp8 * 0.025f;
-    const float P9a = mp9 * (1.0f / 18.0f), P9b = mp9 * (1.0f / 36.0f);
-    const float P10a = mp10 * (1.0f / 18.0f), P10b = mp10 * (1.0f / 36.0f), P10c = mp10 * (1.0f / 72.0f);
-    const float P11 = mp11 * (1.0f / 12.0f), P12a = mp12 * (1.0f / 12.0f), P12b = mp12 * (1.0f / 24.0f);
-    const float Q13 = mp13 * 0.25f, Q14 = mp14 * 0.25f, Q15 = mp15 * 0.25f;
-    const float R16 = mp16 * 0.125f, R17 = mp17 * 0.125f, R18 = mp18 * 0.125f;
-    const float ax = A - B2 - C2;
-    const float axx = ax + P9a - P10a;
-    const float ayz = ax - P9b + P10b;
-    const float dgc = A + B3 + C3;
-    const float dxy = dgc + P9b + P10c + P11 + P12b;
-    const float dxz = dgc + P9b + P10c - P11 - P12b;
-    const float dyz = dgc - P9a - P10b;
-    dp[0] = A - B1 + C1;
-    dp[1] = axx + X3 - X4;
-    dp[2] = axx - X3 + X4;
-    dp[3] = ayz + Y5 - Y6 + P11 - P12a;
-    dp[4] = ayz - Y5 + Y6 + P11 - P12a;
-    dp[5] = ayz + Z7 - Z8 - P11 + P12a;
-    dp[6] = ayz - Z7 + Z8 - P11 + P12a;
-    const float xp = X3 + X4b, yp = Y5 + Y6b, zp = Z7 + Z8b;
-    dp[7] = dxy + xp + yp + Q13 + R16 - R17;
-    dp[8] = dxy - xp + yp - Q13 - R16 - R17;
-    dp[9] = dxy + xp - yp - Q13 + R16 + R17;
-    dp[10] = dxy - xp - yp + Q13 - R16 + R17;
-    dp[11] = dxz + xp + zp + Q15 - R16 + R18;
-    dp[12] = dxz - xp + zp - Q15 + R16 + R18;
-    dp[13] = dxz + xp - zp - Q15 - R16 - R18;
-    dp[14] = dxz - xp - zp + Q15 + R16 - R18;
-    dp[15] = dyz + yp + zp + Q14 + R17 - R18;
-    dp[16] = dyz - yp + zp - Q14 - R17 - R18;
-    dp[17] = dyz + yp - zp - Q14 + R17 + R18;
-    dp[18] = dyz - yp - zp + Q14 - R17 + R18;
-}
-
-// D2Q5 thermal MRT with the M1G term (2DRB.F90:921-974), full g in FP32.
-__device__ __forceinline__ void fcollideT_2d(const float* G, float u, float v, float T, float& Bx, float& By,
-                                             const PhysF& P, float* GP) {
-    const float bx = u * T, by = v * T;
-    const float dBx = P.use_g ? bx - Bx : 0.0f, dBy = P.use_g ? by - By : 0.0f;
-    if (P.use_g) {
-        Bx = bx;
-        By = by;
-    }
-    const float n0 = G[0] + G[1] + G[2] + G[3] + G[4];
-    const float n1 = G[1] - G[3], n2 = G[2] - G[4];
-    const float n3 = -4.0f * G[0] + G[1] + G[2] + G[3] + G[4];
-    const float n4 = G[1] - G[2] + G[3] - G[4];
-    const float neq3 = P.legacy ? T * P.paraA : T * (-2.0f / 3.0f);
-    const float p0 = n0;
-    const float p1 = n1 - P.Qk * (n1 - T * u) + P.SG * dBx;
-    const float p2 = n2 - P.Qk * (n2 - T * v) + P.SG * dBy;
-    const float p3 = n3 - P.Qnu * (n3 - neq3);
-    const float p4 = n4 - P.Qnu * n4;
-    GP[0] = 0.2f * p0 - 0.2f * p3;
-    GP[1] = 0.2f * p0 + 0.5f * p1 + 0.05f * p3 + 0.25f * p4;
-    GP[2] = 0.2f * p0 + 0.5f * p2 + 0.05f * p3 - 0.25f * p4;
-    GP[3] = 0.2f * p0 - 0.5f * p1 + 0.05f * p3 + 0.25f * p4;
-    GP[4] = 0.2f * p0 - 0.5f * p2 + 0.05f * p3 - 0.25f * p4;
-}
-
-// D3Q7 thermal MRT with the M1G term (3DRB.F90:1121-1191).
-__device__ __forceinline__ void fcollideT_3d(const float* g, float u, float v, float w, float T, float& Bx, float& By,
-                                             float& Bz, const PhysF& P, float* gp) {
-    const float bx = u * T, by = v * T, bz = w * T;
-    const float dBx = P.use_g ? bx - Bx : 0.0f, dBy = P.use_g ? by - By : 0.0f, dBz = P.use_g ? bz - Bz : 0.0f;
-    if (P.use_g) {
-        Bx = bx;
-        By = by;
-        Bz = bz;
-    }
-    const float n0 = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6];
-    const float n1 = g[1] - g[2], n2 = g[3] - g[4], n3 = g[5] - g[6];
-    const float n4 = -6.0f * g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6];
-    const float n5 = 2.0f * g[1] + 2.0f * g[2] - g[3] - g[4] - g[5] - g[6];
-    const float n6 = g[3] + g[4] - g[5] - g[6];
-    const float neq4 = P.legacy ? P.paraA * T : -0.75f * T;
-    const float p0 = n0;
-    const float p1 = n1 - P.Qk * (n1 - bx) + P.SG * dBx;
-    const float p2 = n2 - P.Qk * (n2 - by) + P.SG * dBy;
-    const float p3 = n3 - P.Qk * (n3 - bz) + P.SG * dBz;
-    const float p4 = n4 - P.Qnu * (n4 - neq4);
-    const float p5 = n5 - P.Qnu * n5;
-    const float p6 = n6 - P.Qnu * n6;
-    const float a = p0 * (1.0f / 7.0f), b = p4 * (1.0f / 42.0f);
-    gp[0] = a - p4 * (1.0f / 7.0f);
-    gp[1] = a + 0.5f * p1 + b + p5 * (1.0f / 6.0f);
-    gp[2] = a - 0.5f * p1 + b + p5 * (1.0f / 6.0f);
-    const float c = a + b - p5 * (1.0f / 12.0f);
-    gp[3] = c + 0.5f * p2 + 0.25f * p6;
-    gp[4] = c - 0.5f * p2 + 0.25f * p6;
-    gp[5] = c + 0.5f * p3 - 0.25f * p6;
-    gp[6] = c - 0.5f * p3 - 0.25f * p6;
-}
-
-__device__ __forceinline__ bool fcell(const Geo& g, long long& c, int& i, int& j, int& k) {
-    c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.ncell) return false;
-    cell_coords(g, c, i, j, k);
-    return true;
-}
-
-template <int QT>
-__device__ __forceinline__ float wT(const PhysF& P, int a) {
-    return a == 0 ? P.omegaT0 : P.omegaT1;
-}
-
-// macro on deviations: rho = 1 + sum d; u = (j + F/2)/rho (3D: F_y from the lagged T)
-template <int D>
-__device__ __forceinline__ void fmacro(const float* d, float lag, const PhysF& P, float& dr, float& rho, float& u,
-                                       float& v, float& w, float& Fy) {
-    if (D == 2) {
-        dr = d[0] + d[1] + d[2] + d[3] + d[4] + d[5] + d[6] + d[7] + d[8];
-        rho = 1.0f + dr;
-        Fy = lag;  // force stored by the previous collision (2DRB.F90:719, 888)
-        const float inv = 1.0f / rho;
-        u = (d[1] - d[3] + d[5] - d[6] - d[7] + d[8]) * inv;
-        v = (d[2] - d[4] + d[5] + d[6] - d[7] - d[8] + 0.5f * Fy) * inv;
-        w = 0.0f;
-    } else {
-        float s = 0.0f;
-#pragma unroll
-        for (int a = 0; a < 19; ++a) s += d[a];
-        dr = s;
-        rho = 1.0f + dr;
-        Fy = rho * P.gBeta * (lag - P.Tref);  // 3DRB.F90:1083
-        const float inv = 1.0f / rho;
-        u = (d[1] - d[2] + d[7] - d[8] + d[9] - d[10] + d[11] - d[12] + d[13] - d[14]) * inv;
-        v = (d[3] - d[4] + d[7] + d[8] - d[9] - d[10] + d[15] - d[16] + d[17] - d[18] + 0.5f * Fy) * inv;
-        w = (d[5] - d[6] + d[11] + d[12] - d[13] - d[14] + d[15] + d[16] - d[17] - d[18]) * inv;
-    }
+static FastArgs<S> args_for(const FastState& F, int bin, int bout, int lin, int lout) {
+    FastArgs<S> a;
+    a.fref = (S*)F.fref;
+    a.gref = (S*)F.gref;
+    a.rho = F.rho; a.u = F.u; a.v = F.v; a.w = F.w; a.T = F.T;
+    a.Bin0 = F.B[bin][0]; a.Bin1 = F.B[bin][1]; a.Bin2 = F.B[bin][2];
+    a.Bout0 = F.B[bout][0]; a.Bout1 = F.B[bout][1]; a.Bout2 = F.B[bout][2];
+    a.lag_in = F.L[lin];
+    a.lag_out = F.L[lout];
+    return a;
 }
 
 // ------------------------------------------------------------------------------------
 // kernels
 // ------------------------------------------------------------------------------------
 template <int D, class S>
-__global__ void k_fast_initial(Geo g, PhysF P, InitC I, FastArrays<S> A) {
+__global__ void k_fast_initial(Geo g, PhysF P, InitC I, FastArgs<S> A) {
     long long c;
     int i, j, k;
     if (!fcell(g, c, i, j, k)) return;
@@ -350,20 +62,23 @@ __global__ void k_fast_initial(Geo g, PhysF P, InitC I, FastArrays<S> A) {
 #pragma unroll
     for (int a = 0; a < Q; ++a) A.fref[a * n + c] = toS<S>(0.0f);  // f = w at rest
 #pragma unroll
-    for (int a = 0; a < QT; ++a) A.gref[a * n + c] = toS<S>((float)((a == 0 ? (double)P.omegaT0 : (double)P.omegaT1) * (T - (double)P.Tref)));
+    for (int a = 0; a < QT; ++a)
+        A.gref[a * n + c] = toS<S>((float)((a == 0 ? (double)P.omegaT0 : (double)P.omegaT1) * (T - (double)P.Tref)));
     A.rho[c] = 1.0f;
     A.u[c] = 0.0f;
     A.v[c] = 0.0f;
     if (D == 3) A.w[c] = 0.0f;
     A.T[c] = (float)T;
-    A.Bx[c] = 0.0f;
-    A.By[c] = 0.0f;
-    if (D == 3) A.Bz[c] = 0.0f;
-    A.lag[c] = 0.0f;
+    A.Bout0[c] = 0.0f;
+    A.Bout1[c] = 0.0f;
+    if (D == 3) A.Bout2[c] = 0.0f;
+    A.lag_out[c] = 0.0f;
 }
 
+// Flow collision of step n: f_post_n from f_post_{n-1} (or the module arrays when FIRST).
+// Reads lag_in (3D: T_{n-2}; 2D: F_y,n-1); writes lag_out (2D: F_y,n).
 template <int D, bool FIRST, class S>
-__global__ void __launch_bounds__(128) k_fast_flow(Geo g, PhysF P, FastArrays<S> A, const S* __restrict__ fin,
+__global__ void __launch_bounds__(128) k_fast_flow(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
                                                    const S* __restrict__ gin, S* __restrict__ fout) {
     long long c;
     int i, j, k;
@@ -390,11 +105,11 @@ __global__ void __launch_bounds__(128) k_fast_flow(Geo g, PhysF P, FastArrays<S>
         for (int a = 0; a < QT; ++a) ts += pull_thermal<QT, float>(g, a, i, j, k, c, lg);
         T = ts + P.Tref;  // sum of deviations + Tref * sum(wT)
         float Fy;
-        fmacro<D>(d, A.lag[c], P, dr, rho, u, v, w, Fy);
+        fmacro<D>(d, A.lag_in[c], P, dr, rho, u, v, w, Fy);
     }
     const float Fy = rho * P.gBeta * (T - P.Tref);
     if (D == 2) {
-        A.lag[c] = Fy;
+        A.lag_out[c] = Fy;
         fcollide_2d(d, dr, rho, u, v, Fy, P, dp);
     } else {
         fcollide_3d(d, dr, rho, u, v, w, Fy, P, dp);
@@ -403,8 +118,10 @@ __global__ void __launch_bounds__(128) k_fast_flow(Geo g, PhysF P, FastArrays<S>
     for (int a = 0; a < Q; ++a) fout[a * n + c] = toS<S>(dp[a]);
 }
 
+// Streaming, boundary and macro of the flow, and thermal collision of step n.
+// 2D reads lag_in = F_y,n; 3D writes lag_out = T_{n-1}.
 template <int D, bool FIRST, class S>
-__global__ void __launch_bounds__(128) k_fast_thermal(Geo g, PhysF P, FastArrays<S> A, const S* __restrict__ fin,
+__global__ void __launch_bounds__(128) k_fast_thermal(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
                                                       const S* __restrict__ gin, S* __restrict__ gout) {
     long long c;
     int i, j, k;
@@ -431,26 +148,27 @@ __global__ void __launch_bounds__(128) k_fast_thermal(Geo g, PhysF P, FastArrays
         Tprev = ts;
     }
     float dr, rho, u, v, w, Fy;
-    fmacro<D>(d, D == 2 ? A.lag[c] : Tprev, P, dr, rho, u, v, w, Fy);
+    fmacro<D>(d, D == 2 ? A.lag_in[c] : Tprev, P, dr, rho, u, v, w, Fy);
     if (D == 2) {
-        float Bx = A.Bx[c], By = A.By[c];
+        float Bx = A.Bin0[c], By = A.Bin1[c];
         fcollideT_2d(G, u, v, Tprev, Bx, By, P, GP);
-        A.Bx[c] = Bx;
-        A.By[c] = By;
+        A.Bout0[c] = Bx;
+        A.Bout1[c] = By;
     } else {
-        float Bx = A.Bx[c], By = A.By[c], Bz = A.Bz[c];
+        float Bx = A.Bin0[c], By = A.Bin1[c], Bz = A.Bin2[c];
         fcollideT_3d(G, u, v, w, Tprev, Bx, By, Bz, P, GP);
-        A.Bx[c] = Bx;
-        A.By[c] = By;
-        A.Bz[c] = Bz;
-        A.lag[c] = Tprev;
+        A.Bout0[c] = Bx;
+        A.Bout1[c] = By;
+        A.Bout2[c] = Bz;
+        A.lag_out[c] = Tprev;
     }
 #pragma unroll
     for (int a = 0; a < QT; ++a) gout[a * n + c] = toS<S>(GP[a] - wT<QT>(P, a) * P.Tref);
 }
 
+// Module arrays of step N from F[cur] = f_post_N, G[cur] = g_post_N, L[cur] (lag_in).
 template <int D, class S>
-__global__ void k_fast_materialize(Geo g, PhysF P, FastArrays<S> A, const S* __restrict__ fin,
+__global__ void k_fast_materialize(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
                                    const S* __restrict__ gin) {
     long long c;
     int i, j, k;
@@ -473,7 +191,7 @@ __global__ void k_fast_materialize(Geo g, PhysF P, FastArrays<S> A, const S* __r
         ts += e + wT<QT>(P, a) * P.Tref;
     }
     float dr, rho, u, v, w, Fy;
-    fmacro<D>(d, A.lag[c], P, dr, rho, u, v, w, Fy);
+    fmacro<D>(d, A.lag_in[c], P, dr, rho, u, v, w, Fy);
     A.rho[c] = rho;
     A.u[c] = u;
     A.v[c] = v;
@@ -530,18 +248,22 @@ int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn
     for (int b = 0; b < 2; ++b) {
         if ((st = alloc(&F.fbuf[b], F.esize * F.q * n)) != LBM_OK) return st;
         if ((st = alloc(&F.gbuf[b], F.esize * F.qt * n)) != LBM_OK) return st;
+        for (int c = 0; c < (p.dim == 3 ? 3 : 2); ++c)
+            if ((st = alloc((void**)&F.B[b][c], sizeof(float) * n)) != LBM_OK) return st;
+        if ((st = alloc((void**)&F.L[b], sizeof(float) * n)) != LBM_OK) return st;
     }
     if ((st = alloc(&F.fref, F.esize * F.q * n)) != LBM_OK) return st;
     if ((st = alloc(&F.gref, F.esize * F.qt * n)) != LBM_OK) return st;
-    float** scal[] = {&F.rho, &F.u, &F.v, &F.T, &F.up, &F.vp, &F.Tp, &F.Bx, &F.By, &F.lag};
+    float** scal[] = {&F.rho, &F.u, &F.v, &F.T, &F.up, &F.vp, &F.Tp};
     for (float** s : scal)
         if ((st = alloc((void**)s, sizeof(float) * n)) != LBM_OK) return st;
     if (p.dim == 3) {
-        float** s3[] = {&F.w, &F.wp, &F.Bz};
+        float** s3[] = {&F.w, &F.wp};
         for (float** s : s3)
             if ((st = alloc((void**)s, sizeof(float) * n)) != LBM_OK) return st;
     }
     F.fused_valid = false;
+    F.ahead = false;
     F.cur = 0;
     return LBM_OK;
 }
@@ -559,16 +281,18 @@ int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn
 
 void fast_initial(FastState& F, const Geo& g, const PhysC& P, const InitC& I, int dim, cudaStream_t s) {
     const PhysF pf = to_physf(P);
+    F.cur = 0;
+    F.fused_valid = false;
+    F.ahead = false;
     DISPATCH_S(F, {
-        if (dim == 2) k_fast_initial<2, S><<<nb(g.ncell, 256), 256, 0, s>>>(g, pf, I, arrays<S>(F));
-        else k_fast_initial<3, S><<<nb(g.ncell, 256), 256, 0, s>>>(g, pf, I, arrays<S>(F));
+        FastArgs<S> A = args_for<S>(F, 0, 0, 0, 0);
+        if (dim == 2) k_fast_initial<2, S><<<nb(g.ncell, 256), 256, 0, s>>>(g, pf, I, A);
+        else k_fast_initial<3, S><<<nb(g.ncell, 256), 256, 0, s>>>(g, pf, I, A);
     });
     cudaMemsetAsync(F.up, 0, sizeof(float) * g.ncell, s);
     cudaMemsetAsync(F.vp, 0, sizeof(float) * g.ncell, s);
     cudaMemsetAsync(F.Tp, 0, sizeof(float) * g.ncell, s);
     if (dim == 3) cudaMemsetAsync(F.wp, 0, sizeof(float) * g.ncell, s);
-    F.fused_valid = false;
-    F.cur = 0;
 }
 
 void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first, cudaStream_t s, int part) {
@@ -576,28 +300,30 @@ void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first,
     const Geo g = dev_geo(g0, P);
     const int cur = F.cur, nxt = F.cur ^ 1;
     const unsigned blocks = nb(g.ncell, 128);
+    F.ahead = false;
     DISPATCH_S(F, {
         const S* fin = (const S*)F.fbuf[cur];
         const S* gin = (const S*)F.gbuf[cur];
         S* fout = (S*)F.fbuf[nxt];
         S* gout = (S*)F.gbuf[nxt];
-        FastArrays<S> A = arrays<S>(F);
+        FastArgs<S> Af = args_for<S>(F, cur, nxt, cur, nxt);  // flow: lag_in = L[cur], lag_out = L[nxt]
+        FastArgs<S> At = args_for<S>(F, cur, nxt, nxt, nxt);  // thermal: 2D reads F_y,n from L[nxt]
         const bool fl = part != 1, th = part != 0;
         if (dim == 2) {
             if (first) {
-                if (fl) k_fast_flow<2, true, S><<<blocks, 128, 0, s>>>(g, pf, A, fin, gin, fout);
-                if (th) k_fast_thermal<2, true, S><<<blocks, 128, 0, s>>>(g, pf, A, fout, gin, gout);
+                if (fl) k_fast_flow<2, true, S><<<blocks, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
+                if (th) k_fast_thermal<2, true, S><<<blocks, 128, 0, s>>>(g, pf, At, fout, gin, gout);
             } else {
-                if (fl) k_fast_flow<2, false, S><<<blocks, 128, 0, s>>>(g, pf, A, fin, gin, fout);
-                if (th) k_fast_thermal<2, false, S><<<blocks, 128, 0, s>>>(g, pf, A, fout, gin, gout);
+                if (fl) k_fast_flow<2, false, S><<<blocks, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
+                if (th) k_fast_thermal<2, false, S><<<blocks, 128, 0, s>>>(g, pf, At, fout, gin, gout);
             }
         } else {
             if (first) {
-                if (fl) k_fast_flow<3, true, S><<<blocks, 128, 0, s>>>(g, pf, A, fin, gin, fout);
-                if (th) k_fast_thermal<3, true, S><<<blocks, 128, 0, s>>>(g, pf, A, fout, gin, gout);
+                if (fl) k_fast_flow<3, true, S><<<blocks, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
+                if (th) k_fast_thermal<3, true, S><<<blocks, 128, 0, s>>>(g, pf, At, fout, gin, gout);
             } else {
-                if (fl) k_fast_flow<3, false, S><<<blocks, 128, 0, s>>>(g, pf, A, fin, gin, fout);
-                if (th) k_fast_thermal<3, false, S><<<blocks, 128, 0, s>>>(g, pf, A, fout, gin, gout);
+                if (fl) k_fast_flow<3, false, S><<<blocks, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
+                if (th) k_fast_thermal<3, false, S><<<blocks, 128, 0, s>>>(g, pf, At, fout, gin, gout);
             }
         }
     });
@@ -607,6 +333,12 @@ void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first,
     }
 }
 
+void fast_enter(FastState& F, const Geo& g0, const PhysC& P, int dim, cudaStream_t s) {
+    // one flow collision ahead: F[cur^1] = f_post_{N+1}, 2D L[cur^1] = F_y,N+1
+    fast_step(F, g0, P, dim, false, s, 0);
+    F.ahead = true;
+}
+
 void fast_materialize(FastState& F, const Geo& g0, const PhysC& P, int dim, cudaStream_t s) {
     if (!F.fused_valid) return;
     const PhysF pf = to_physf(P);
@@ -614,10 +346,10 @@ void fast_materialize(FastState& F, const Geo& g0, const PhysC& P, int dim, cuda
     DISPATCH_S(F, {
         const S* fin = (const S*)F.fbuf[F.cur];
         const S* gin = (const S*)F.gbuf[F.cur];
-        if (dim == 2) k_fast_materialize<2, S><<<nb(g.ncell, 128), 128, 0, s>>>(g, pf, arrays<S>(F), fin, gin);
-        else k_fast_materialize<3, S><<<nb(g.ncell, 128), 128, 0, s>>>(g, pf, arrays<S>(F), fin, gin);
+        FastArgs<S> A = args_for<S>(F, F.cur, F.cur, F.cur, F.cur);
+        if (dim == 2) k_fast_materialize<2, S><<<nb(g.ncell, 128), 128, 0, s>>>(g, pf, A, fin, gin);
+        else k_fast_materialize<3, S><<<nb(g.ncell, 128), 128, 0, s>>>(g, pf, A, fin, gin);
     });
-    F.fused_valid = false;
 }
 
 DiagFields<float> fast_diag_fields(const FastState& F) {
@@ -645,17 +377,18 @@ int fast_export(const FastState& F, const Geo& g, const PhysC& P, int dim, int f
         return LBM_OK;
     }
     const float* src = nullptr;
+    const int c = F.cur;
     switch (field) {
         case LBM_FIELD_RHO: src = F.rho; break;
         case LBM_FIELD_U: src = F.u; break;
         case LBM_FIELD_V: src = F.v; break;
         case LBM_FIELD_W: if (!d3) return LBM_ERR_PARAM; src = F.w; break;
         case LBM_FIELD_T: src = F.T; break;
-        case LBM_FIELD_BX_PREV: src = F.Bx; break;
-        case LBM_FIELD_BY_PREV: src = F.By; break;
-        case LBM_FIELD_BZ_PREV: if (!d3) return LBM_ERR_PARAM; src = F.Bz; break;
+        case LBM_FIELD_BX_PREV: src = F.B[c][0]; break;
+        case LBM_FIELD_BY_PREV: src = F.B[c][1]; break;
+        case LBM_FIELD_BZ_PREV: if (!d3) return LBM_ERR_PARAM; src = F.B[c][2]; break;
         case LBM_FIELD_FX: if (d3) return LBM_ERR_PARAM; src = nullptr; break;
-        case LBM_FIELD_FY: if (d3) return LBM_ERR_PARAM; src = F.lag; break;
+        case LBM_FIELD_FY: if (d3) return LBM_ERR_PARAM; src = F.L[c]; break;
         default: return LBM_ERR_PARAM;
     }
     k_f2d<<<nb(n, 256), 256, 0, s>>>(src, out, n);
@@ -679,22 +412,27 @@ int fast_import(FastState& F, const Geo& g, const PhysC& P, int dim, int field, 
                 else k_import_pop<9, S><<<nb(q * n, 256), 256, 0, s>>>(in, (S*)dst, n, 0, 0, 0);
             }
         });
+        F.fused_valid = false;
+        F.ahead = false;
         return LBM_OK;
     }
     float* dst = nullptr;
+    const int c = F.cur;
     switch (field) {
         case LBM_FIELD_RHO: dst = F.rho; break;
         case LBM_FIELD_U: dst = F.u; break;
         case LBM_FIELD_V: dst = F.v; break;
         case LBM_FIELD_W: if (!d3) return LBM_ERR_PARAM; dst = F.w; break;
         case LBM_FIELD_T: dst = F.T; break;
-        case LBM_FIELD_BX_PREV: dst = F.Bx; break;
-        case LBM_FIELD_BY_PREV: dst = F.By; break;
-        case LBM_FIELD_BZ_PREV: if (!d3) return LBM_ERR_PARAM; dst = F.Bz; break;
-        case LBM_FIELD_FY: if (d3) return LBM_ERR_PARAM; dst = F.lag; break;
+        case LBM_FIELD_BX_PREV: dst = F.B[c][0]; break;
+        case LBM_FIELD_BY_PREV: dst = F.B[c][1]; break;
+        case LBM_FIELD_BZ_PREV: if (!d3) return LBM_ERR_PARAM; dst = F.B[c][2]; break;
+        case LBM_FIELD_FY: if (d3) return LBM_ERR_PARAM; dst = F.L[c]; break;
         default: return LBM_ERR_STATE;
     }
     k_d2f<<<nb(n, 256), 256, 0, s>>>(in, dst, n);
+    F.fused_valid = false;
+    F.ahead = false;
     return LBM_OK;
 }
 

@@ -5,6 +5,12 @@
 // signal and FP16 keeps ~3 significant digits of it.  Arithmetic is FP32 in the same
 // moment space as the reference (same M, same relaxation, same Guo source); the lag
 // state (B_prev, and the 3D T lag / 2D stored force) is kept in FP32.
+//
+// Buffers come in pairs indexed by one parity `cur`:
+//   F[cur] = f_post_N, G[cur] = g_post_N, B[cur] = B_prev_N,
+//   L[cur] = lag (3D: T_{N-1}; 2D: the force F_y,N stored by the flow collision).
+// In single-kernel mode the handle runs one flow collision ahead ("ahead"):
+//   F[cur^1] = f_post_{N+1} and, in 2D, L[cur^1] = F_y,N+1.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -19,32 +25,41 @@ struct FastState {
     int precision = LBM_FP32;  // LBM_FP32 or LBM_FP16
     int dim = 3, q = 19, qt = 7;
     size_t esize = 4;          // bytes per stored population
-    // fused buffers (type float or __half, stored as raw bytes)
     void* fbuf[2] = {nullptr, nullptr};
     void* gbuf[2] = {nullptr, nullptr};
+    float* B[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    float* L[2] = {nullptr, nullptr};
     // module form (after initial / materialisation): populations as deviations
     void* fref = nullptr;
     void* gref = nullptr;
     float *rho = nullptr, *u = nullptr, *v = nullptr, *w = nullptr, *T = nullptr;
     float *up = nullptr, *vp = nullptr, *wp = nullptr, *Tp = nullptr;
-    float *Bx = nullptr, *By = nullptr, *Bz = nullptr;
-    float* lag = nullptr;  // 3D: T of the previous step; 2D: stored force F_y
-    bool fused_valid = false;
     int cur = 0;
+    bool fused_valid = false;   // the fused buffers hold the current state
+    bool ahead = false;         // single-kernel phase: F[cur^1] already holds f_post_{N+1}
+    bool single_kernel = false; // one-launch fused step (lbm_fused.cu); off: the two-kernel step is faster today
+    int kchunk = 16;            // z planes per block of the fused kernel (3D)
 };
 
 using AllocFn = std::function<int(void**, size_t)>;
 
 int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn& alloc);
 void fast_initial(FastState& F, const Geo& g, const PhysC& P, const InitC& I, int dim, cudaStream_t s);
-// part: 0 = flow kernel only, 1 = thermal kernel only (then advances the buffers), 2 = both
+// Two-kernel step (flow collision, then thermal).  first: read the module arrays.
+// part: 0 = flow kernel only, 1 = thermal kernel only, 2 = both.
 void fast_step(FastState& F, const Geo& g, const PhysC& P, int dim, bool first, cudaStream_t s, int part = 2);
+// Single-kernel mode: enter (one flow collision ahead), then one launch per step.
+void fast_enter(FastState& F, const Geo& g, const PhysC& P, int dim, cudaStream_t s);
+void fast_fused_step(FastState& F, const Geo& g, const PhysC& P, int dim, cudaStream_t s);
+bool fast_fused_supported(const Geo& g, int dim);
+// Rebuild the module arrays (f, g, rho, u, v, w, T) of the current step; leaves the fused
+// buffers valid.
 void fast_materialize(FastState& F, const Geo& g, const PhysC& P, int dim, cudaStream_t s);
 inline bool fast_fused_valid(const FastState& F) { return F.fused_valid; }
 inline bool fast_at_origin(const FastState& F) { return F.cur == 0; }
 DiagFields<float> fast_diag_fields(const FastState& F);
 // Export a field to an FP64 device buffer in the reference's Fortran layout (AoS for
-// populations); import the reverse.  Return LBM_OK or LBM_ERR_STATE.
+// populations); import the reverse.  Return LBM_OK or LBM_ERR_STATE / LBM_ERR_PARAM.
 int fast_export(const FastState& F, const Geo& g, const PhysC& P, int dim, int field, double* out, cudaStream_t s);
 int fast_import(FastState& F, const Geo& g, const PhysC& P, int dim, int field, const double* in, cudaStream_t s);
 

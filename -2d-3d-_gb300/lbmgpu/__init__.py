@@ -55,7 +55,10 @@ SIGNATURES = {
     "lbm_set_state": ([_vp, _i32, _dp, _sz], _i32),
     "lbm_get_stream": ([_vp, C.POINTER(_vp)], _i32),
     "lbm_time_kernels": ([_vp, _i64, _dp, _dp], _i32),
+    "lbm_set_option": ([_vp, _i32, _i32], _i32),
 }
+LBM_OPT_SINGLE_KERNEL = 1
+LBM_OPT_KCHUNK = 2
 
 _lib = None
 
@@ -210,6 +213,10 @@ class Lattice:
         s = C.c_void_p()
         self._ck(self.lib.lbm_get_stream(self._h, C.byref(s)), "lbm_get_stream")
         return s.value or 0
+
+    def set_option(self, option, value):
+        """LBM_OPT_SINGLE_KERNEL (0/1) or LBM_OPT_KCHUNK (z planes per block of the fused kernel)."""
+        self._ck(self.lib.lbm_set_option(self._h, int(option), int(value)), "lbm_set_option")
 
     def time_kernels(self, nsteps):
         """Mean device ms per launch of the (flow, thermal) fused kernels over nsteps steps."""

@@ -278,10 +278,13 @@ def run_gpu(args):
         step_ms = r["ms_flow"] + r["ms_thermal"]
         achieved = BYTES_PER_CELL[prec] * cells / (step_ms / 1e3) / 1e9
         t = traffic.get(prec)
+        if r["ms_thermal"] == 0.0:
+            desc = "single fused kernel k_fused, %.4f ms per launch (one launch per step)" % r["ms_flow"]
+        else:
+            desc = "two-kernel step: flow kernel %.4f ms + thermal kernel %.4f ms per launch" % (
+                r["ms_flow"], r["ms_thermal"])
         return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": t, "peak_kind": peak_kind,
-                "kernel": "fused step = flow kernel %.3f ms + thermal kernel %.3f ms per launch"
-                          % (r["ms_flow"], r["ms_thermal"]),
+                "traffic": t, "peak_kind": peak_kind, "kernel": desc,
                 "algorithmic_bytes_per_cell": BYTES_PER_CELL[prec]}
 
     head = results[precs[0]]

@@ -169,6 +169,14 @@ int lbm_RBcalc_Nu_wall_avg(lbm_handle* h, lbm_nu_wall* out);
 int lbm_get_state(lbm_handle* h, int field, double* host, size_t count);
 int lbm_set_state(lbm_handle* h, int field, const double* host, size_t count);
 
+/* ---- execution options (no counterpart in the reference) --------------------------------
+ * LBM_OPT_SINGLE_KERNEL: FP32/FP16 handles advance with one fused kernel per step (1) or
+ *   with the two-kernel form (0, default).  Both give the same arithmetic.
+ * LBM_OPT_KCHUNK: z planes marched by one block of the fused 3D kernel (default 16). */
+#define LBM_OPT_SINGLE_KERNEL 1
+#define LBM_OPT_KCHUNK        2
+int lbm_set_option(lbm_handle* h, int option, int value);
+
 /* ---- measurement hooks (no counterpart in the reference, which times its loop with
  *      CPU_TIME / OMP_get_wtime, 3DRB.F90:222-223, 266-267) -------------------------------- */
 /* The handle's CUDA stream (a cudaStream_t), for callers that record their own events. */
