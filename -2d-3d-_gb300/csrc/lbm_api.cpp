@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/lbm_gpu.h"
+#include "lbm_ensemble.h"
 #include "lbm_fast.h"
 #include "lbm_internal.h"
 
@@ -69,6 +70,10 @@ struct lbm_handle {
     double* d_sx = nullptr;
     double* d_sy = nullptr;
     std::vector<void*> allocs;
+
+    // batched stepping
+    lbm_ensemble* ensemble = nullptr;  // the ensemble this handle is a member of
+    cudaEvent_t order_ev = nullptr;    // orders the handle's stream against the ensemble's
 };
 
 // ------------------------------------------------------------------------------------
@@ -129,7 +134,7 @@ static int validate(const lbm_params* p) {
         if (p->bc_thermal[2] != LBM_BCT_ADIABATIC && p->bc_thermal[2] != LBM_BCT_PERIODIC) return LBM_ERR_PARAM;
     }
     if (p->precision < LBM_FP64 || p->precision > LBM_FP16) return LBM_ERR_PARAM;
-    if (p->pattern != LBM_PATTERN_AB && p->pattern != LBM_PATTERN_AA) return LBM_ERR_PARAM;
+    if (p->pattern != LBM_PATTERN_AB) return LBM_ERR_PARAM;  // the in-place AA pattern is not built yet
     return LBM_OK;
 }
 
@@ -388,8 +393,12 @@ extern "C" int lbm_create(const lbm_params* p, int device, lbm_handle** out) {
     return LBM_OK;
 }
 
+extern "C" int lbm_ensemble_remove(lbm_ensemble* e, lbm_handle* h);
+
 extern "C" int lbm_destroy(lbm_handle* h) {
     if (!h) return LBM_ERR_PARAM;
+    if (h->ensemble) lbm_ensemble_remove(h->ensemble, h);
+    if (h->order_ev) cudaEventDestroy(h->order_ev);
     release(h);
     delete h;
     return LBM_OK;
@@ -991,5 +1000,255 @@ extern "C" int lbm_set_option(lbm_handle* h, int option, int value) {
         cudaGraphDestroy(h->graph);
         h->graph = nullptr;
     }
+    return LBM_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// device footprint (for admission against an HBM budget)
+// ------------------------------------------------------------------------------------
+extern "C" int lbm_footprint(const lbm_params* p, size_t* bytes) {
+    if (!bytes || validate(p) != LBM_OK) return LBM_ERR_PARAM;
+    const size_t n = (size_t)p->nx * p->ny * (size_t)(p->dim == 3 ? p->nz : 1);
+    const size_t q = p->dim == 3 ? 19 : 9, qt = p->dim == 3 ? 7 : 5;
+    size_t b = 0;
+    if (p->precision == LBM_FP64) {
+        b += 8 * n * (3 * q + 3 * qt);                       // f_post A/B, g_post A/B, f, g
+        b += 8 * n * (p->dim == 3 ? 13 : 11);                // rho u v T Bx By up vp Tp (+w Bz wp Tlag | Fx Fy)
+    } else {
+        const size_t es = p->precision == LBM_FP16 ? 2 : 4;
+        b += es * n * (3 * q + 3 * qt);                      // F A/B, G A/B, f, g (module)
+        b += 4 * n * (2 * (p->dim == 3 ? 3 : 2) + 2);        // B_prev A/B, lag A/B
+        b += 4 * n * (p->dim == 3 ? 9 : 7);                  // rho u v T up vp Tp (+w wp)
+    }
+    b += 8 * ((size_t)diag_blocks((long long)n) * DIAG_NSUM + 3 * (size_t)p->nx + (size_t)p->ny);
+    *bytes = b;
+    return LBM_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// batched stepping of many lattices
+// ------------------------------------------------------------------------------------
+struct lbm_ensemble {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    std::vector<lbm_handle*> members;
+    EnsPlan plan;
+    EnsLaunchCfg cfg;
+    bool dirty = true;
+    int flip = 0;
+    int sms = 152;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::string err;
+};
+
+static int efail(lbm_ensemble* e, int st, const std::string& m) {
+    if (e) e->err = m;
+    return st;
+}
+
+#define ECK(e, call)                                                                              \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return efail((e), e_ == cudaErrorMemoryAllocation ? LBM_ERR_OOM : LBM_ERR_CUDA,        \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+    } while (0)
+
+static void drop_graph(lbm_ensemble* e) {
+    if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
+    if (e->graph) cudaGraphDestroy(e->graph);
+    e->graph_exec = nullptr;
+    e->graph = nullptr;
+}
+
+extern "C" int lbm_ensemble_create(int device, lbm_ensemble** out) {
+    if (!out) return LBM_ERR_PARAM;
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) return LBM_ERR_CUDA;
+    lbm_ensemble* e = new (std::nothrow) lbm_ensemble();
+    if (!e) return LBM_ERR_OOM;
+    e->device = device;
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming) != cudaSuccess) {
+        delete e;
+        return LBM_ERR_CUDA;
+    }
+    cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, device);
+    *out = e;
+    return LBM_OK;
+}
+
+extern "C" int lbm_ensemble_destroy(lbm_ensemble* e) {
+    if (!e) return LBM_ERR_PARAM;
+    cudaSetDevice(e->device);
+    cudaStreamSynchronize(e->stream);
+    for (lbm_handle* h : e->members) h->ensemble = nullptr;
+    drop_graph(e);
+    ens_free(e->plan);
+    cudaEventDestroy(e->done);
+    cudaStreamDestroy(e->stream);
+    delete e;
+    return LBM_OK;
+}
+
+extern "C" const char* lbm_ensemble_last_error(const lbm_ensemble* e) { return e ? e->err.c_str() : "null ensemble"; }
+
+extern "C" int lbm_ensemble_add(lbm_ensemble* e, lbm_handle* h) {
+    if (!e || !h) return LBM_ERR_PARAM;
+    if (h->p.precision == LBM_FP64) return efail(e, LBM_ERR_STATE, "the batched form takes FP32/FP16 handles");
+    if (h->device != e->device) return efail(e, LBM_ERR_PARAM, "handle is on another device");
+    if (!h->initialised) return efail(e, LBM_ERR_STATE, "lbm_initial has not been called on the handle");
+    if (h->ensemble) return efail(e, LBM_ERR_STATE, "handle already belongs to an ensemble");
+    if (!e->members.empty() && e->members[0]->p.precision != h->p.precision)
+        return efail(e, LBM_ERR_PARAM, "all members of an ensemble share one storage precision");
+    if (!h->order_ev && cudaEventCreateWithFlags(&h->order_ev, cudaEventDisableTiming) != cudaSuccess)
+        return efail(e, LBM_ERR_CUDA, "cudaEventCreate");
+    // wait for the ensemble's queued work before the member is used again on its own stream
+    cudaSetDevice(e->device);
+    ECK(e, cudaStreamSynchronize(e->stream));
+    e->members.push_back(h);
+    h->ensemble = e;
+    e->dirty = true;
+    return LBM_OK;
+}
+
+extern "C" int lbm_ensemble_remove(lbm_ensemble* e, lbm_handle* h) {
+    if (!e || !h) return LBM_ERR_PARAM;
+    for (size_t i = 0; i < e->members.size(); ++i) {
+        if (e->members[i] == h) {
+            cudaSetDevice(e->device);
+            cudaStreamSynchronize(e->stream);
+            e->members.erase(e->members.begin() + (long)i);
+            h->ensemble = nullptr;
+            e->dirty = true;
+            return LBM_OK;
+        }
+    }
+    return efail(e, LBM_ERR_PARAM, "handle is not a member");
+}
+
+extern "C" int lbm_ensemble_size(const lbm_ensemble* e) { return e ? (int)e->members.size() : -1; }
+
+extern "C" int lbm_ensemble_get_stream(lbm_ensemble* e, void** stream) {
+    if (!e || !stream) return LBM_ERR_PARAM;
+    *stream = (void*)e->stream;
+    return LBM_OK;
+}
+
+static int ens_rebuild(lbm_ensemble* e) {
+    std::vector<EnsMemberHost> mh;
+    for (lbm_handle* h : e->members) mh.push_back(EnsMemberHost{h->geo, h->phys, &h->F, h->dim});
+    drop_graph(e);
+    ECK(e, ens_build(e->plan, mh, e->cfg, e->sms));
+    e->flip = 0;
+    e->dirty = false;
+    return LBM_OK;
+}
+
+extern "C" int lbm_ensemble_step(lbm_ensemble* e, int64_t nsteps) {
+    if (!e || nsteps < 0) return LBM_ERR_PARAM;
+    if (e->members.empty() || nsteps == 0) return LBM_OK;
+    ECK(e, cudaSetDevice(e->device));
+    // a member not in the fused form takes its first step (reading the module arrays) alone
+    for (lbm_handle* h : e->members) {
+        if (!h->F.fused_valid) {
+            enqueue_one(h, true);
+            h->itc += 1;
+            e->dirty = true;
+        }
+        h->F.ahead = false;
+    }
+    if (e->dirty) {
+        int st = ens_rebuild(e);
+        if (st != LBM_OK) return st;
+    }
+    for (lbm_handle* h : e->members) {
+        ECK(e, cudaEventRecord(h->order_ev, h->stream));
+        ECK(e, cudaStreamWaitEvent(e->stream, h->order_ev, 0));
+    }
+    int64_t done = 0;
+    while (done < nsteps) {
+        if (e->flip == 0 && nsteps - done >= kChunkSteps) {
+            if (!e->graph_exec) {
+                ECK(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+                for (int s = 0; s < kChunkSteps; ++s) ens_step(e->plan, s & 1, e->stream);
+                cudaGraph_t g = nullptr;
+                ECK(e, cudaStreamEndCapture(e->stream, &g));
+                e->graph = g;
+                ECK(e, cudaGraphInstantiate(&e->graph_exec, g, 0));
+            }
+            ECK(e, cudaGraphLaunch(e->graph_exec, e->stream));
+            done += kChunkSteps;
+        } else {
+            ens_step(e->plan, e->flip, e->stream);
+            e->flip ^= 1;
+            done += 1;
+        }
+    }
+    ECK(e, cudaGetLastError());
+    ECK(e, cudaEventRecord(e->done, e->stream));
+    for (lbm_handle* h : e->members) {
+        ECK(e, cudaStreamWaitEvent(h->stream, e->done, 0));
+        h->F.cur ^= (int)(nsteps & 1);
+        h->F.fused_valid = true;
+        h->itc += nsteps;
+    }
+    return LBM_OK;
+}
+
+extern "C" int lbm_ensemble_sync(lbm_ensemble* e) {
+    if (!e) return LBM_ERR_PARAM;
+    ECK(e, cudaSetDevice(e->device));
+    ECK(e, cudaStreamSynchronize(e->stream));
+    return LBM_OK;
+}
+
+// Time `nsteps` batched steps per launch configuration and keep the fastest.  The steps
+// are real steps: every member advances by ncand * nsteps steps.
+extern "C" int lbm_ensemble_autotune(lbm_ensemble* e, int nsteps, int* best_block, int* best_tile, int* best_grid) {
+    if (!e || nsteps <= 0) return LBM_ERR_PARAM;
+    if (e->members.empty()) return LBM_OK;
+    const EnsLaunchCfg cands[] = {{128, 512, 8}, {128, 1024, 16}, {256, 1024, 4}, {256, 2048, 8},
+                                  {256, 4096, 8}, {128, 2048, 8}};
+    ECK(e, cudaSetDevice(e->device));
+    int st = lbm_ensemble_step(e, 1);  // first steps and ordering
+    if (st != LBM_OK) return st;
+    cudaEvent_t a, b;
+    ECK(e, cudaEventCreate(&a));
+    ECK(e, cudaEventCreate(&b));
+    float best = 1e30f;
+    EnsLaunchCfg bestc = e->cfg;
+    for (const EnsLaunchCfg& c : cands) {
+        e->cfg = c;
+        if ((st = ens_rebuild(e)) != LBM_OK) return st;
+        ens_step(e->plan, 0, e->stream);  // warm
+        ens_step(e->plan, 1, e->stream);
+        ECK(e, cudaEventRecord(a, e->stream));
+        for (int s = 0; s < nsteps; ++s) ens_step(e->plan, s & 1, e->stream);
+        ECK(e, cudaEventRecord(b, e->stream));
+        ECK(e, cudaEventSynchronize(b));
+        float ms = 0.f;
+        ECK(e, cudaEventElapsedTime(&ms, a, b));
+        if (ms < best) {
+            best = ms;
+            bestc = c;
+        }
+        const int adv = 2 + nsteps;
+        for (lbm_handle* h : e->members) {
+            h->F.cur ^= (adv & 1);
+            h->itc += adv;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    ECK(e, cudaEventRecord(e->done, e->stream));
+    for (lbm_handle* h : e->members) ECK(e, cudaStreamWaitEvent(h->stream, e->done, 0));
+    e->cfg = bestc;
+    e->dirty = true;
+    if (best_block) *best_block = bestc.block;
+    if (best_tile) *best_tile = bestc.tile_cells;
+    if (best_grid) *best_grid = bestc.grid_mul;
     return LBM_OK;
 }

@@ -12,20 +12,9 @@
 #include <cuda_runtime.h>
 
 #include "lbm_fast.h"
-#include "lbm_fast_math.cuh"
+#include "lbm_fast_cells.cuh"
 
 namespace lbm {
-
-// Pointers of one launch: module arrays plus the B_prev / lag buffers to read and write.
-template <class S>
-struct FastArgs {
-    S *fref, *gref;
-    float *rho, *u, *v, *w, *T;
-    const float *Bin0, *Bin1, *Bin2;
-    float *Bout0, *Bout1, *Bout2;
-    const float* lag_in;
-    float* lag_out;
-};
 
 template <class S>
 static FastArgs<S> args_for(const FastState& F, int bin, int bout, int lin, int lout) {
@@ -75,95 +64,23 @@ __global__ void k_fast_initial(Geo g, PhysF P, InitC I, FastArgs<S> A) {
     A.lag_out[c] = 0.0f;
 }
 
-// Flow collision of step n: f_post_n from f_post_{n-1} (or the module arrays when FIRST).
-// Reads lag_in (3D: T_{n-2}; 2D: F_y,n-1); writes lag_out (2D: F_y,n).
+// Flow collision and thermal kernels of the two-kernel step (bodies in lbm_fast_cells.cuh).
 template <int D, bool FIRST, class S>
 __global__ void __launch_bounds__(128) k_fast_flow(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
                                                    const S* __restrict__ gin, S* __restrict__ fout) {
     long long c;
     int i, j, k;
     if (!fcell(g, c, i, j, k)) return;
-    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
-    const long long n = g.ncell;
-    float d[Q], dp[Q], dr, rho, u, v, w = 0.0f, T;
-    if (FIRST) {
-#pragma unroll
-        for (int a = 0; a < Q; ++a) d[a] = ldS(A.fref, a * n + c);
-        rho = A.rho[c];
-        dr = rho - 1.0f;
-        u = A.u[c];
-        v = A.v[c];
-        if (D == 3) w = A.w[c];
-        T = A.T[c];
-    } else {
-        auto lf = [&](int a, long long cc) { return ldS(fin, a * n + cc); };
-        auto lg = [&](int a, long long cc) { return ldS(gin, a * n + cc); };
-#pragma unroll
-        for (int a = 0; a < Q; ++a) d[a] = pull_flow<Q, float>(g, a, i, j, k, c, lf);
-        float ts = 0.0f;
-#pragma unroll
-        for (int a = 0; a < QT; ++a) ts += pull_thermal<QT, float>(g, a, i, j, k, c, lg);
-        T = ts + P.Tref;  // sum of deviations + Tref * sum(wT)
-        float Fy;
-        fmacro<D>(d, A.lag_in[c], P, dr, rho, u, v, w, Fy);
-    }
-    const float Fy = rho * P.gBeta * (T - P.Tref);
-    if (D == 2) {
-        A.lag_out[c] = Fy;
-        fcollide_2d(d, dr, rho, u, v, Fy, P, dp);
-    } else {
-        fcollide_3d(d, dr, rho, u, v, w, Fy, P, dp);
-    }
-#pragma unroll
-    for (int a = 0; a < Q; ++a) fout[a * n + c] = toS<S>(dp[a]);
+    flow_cell_2k<D, FIRST, S>(g, P, A, fin, gin, fout, c, i, j, k);
 }
 
-// Streaming, boundary and macro of the flow, and thermal collision of step n.
-// 2D reads lag_in = F_y,n; 3D writes lag_out = T_{n-1}.
 template <int D, bool FIRST, class S>
 __global__ void __launch_bounds__(128) k_fast_thermal(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
                                                       const S* __restrict__ gin, S* __restrict__ gout) {
     long long c;
     int i, j, k;
     if (!fcell(g, c, i, j, k)) return;
-    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
-    const long long n = g.ncell;
-    float d[Q], G[QT], GP[QT];
-    auto lf = [&](int a, long long cc) { return ldS(fin, a * n + cc); };
-#pragma unroll
-    for (int a = 0; a < Q; ++a) d[a] = pull_flow<Q, float>(g, a, i, j, k, c, lf);
-    float Tprev;
-    if (FIRST) {
-#pragma unroll
-        for (int a = 0; a < QT; ++a) G[a] = ldS(A.gref, a * n + c) + wT<QT>(P, a) * P.Tref;
-        Tprev = A.T[c];
-    } else {
-        auto lg = [&](int a, long long cc) { return ldS(gin, a * n + cc); };
-        float ts = 0.0f;
-#pragma unroll
-        for (int a = 0; a < QT; ++a) {
-            G[a] = pull_thermal<QT, float>(g, a, i, j, k, c, lg) + wT<QT>(P, a) * P.Tref;
-            ts += G[a];
-        }
-        Tprev = ts;
-    }
-    float dr, rho, u, v, w, Fy;
-    fmacro<D>(d, D == 2 ? A.lag_in[c] : Tprev, P, dr, rho, u, v, w, Fy);
-    if (D == 2) {
-        float Bx = A.Bin0[c], By = A.Bin1[c];
-        fcollideT_2d(G, u, v, Tprev, Bx, By, P, GP);
-        A.Bout0[c] = Bx;
-        A.Bout1[c] = By;
-    } else {
-        float Bx = A.Bin0[c], By = A.Bin1[c], Bz = A.Bin2[c];
-        fcollideT_3d(G, u, v, w, Tprev, Bx, By, Bz, P, GP);
-        A.Bout0[c] = Bx;
-        A.Bout1[c] = By;
-        A.Bout2[c] = Bz;
-        A.lag_out[c] = Tprev;
-    }
-#pragma unroll
-    for (int a = 0; a < QT; ++a) gout[a * n + c] = toS<S>(GP[a] - wT<QT>(P, a) * P.Tref);
+    thermal_cell_2k<D, FIRST, S>(g, P, A, fin, gin, gout, c, i, j, k);
 }
 
 // Module arrays of step N from F[cur] = f_post_N, G[cur] = g_post_N, L[cur] (lag_in).

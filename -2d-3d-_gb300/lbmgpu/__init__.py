@@ -19,8 +19,8 @@ import numpy as np
 from .abi import (FIELDS, LBM_FP64, LBM_OK, STATUS_NAMES, LbmConstants, LbmNuWall, LbmParams, field_shape,
                   field_size, rb_params)
 
-__all__ = ["Lattice", "LbmError", "LbmDiverged", "LbmParams", "rb_params", "load_library", "library_path",
-           "params_default", "derive_constants", "FIELDS"]
+__all__ = ["Lattice", "Ensemble", "LbmError", "LbmDiverged", "LbmParams", "rb_params", "load_library",
+           "library_path", "params_default", "derive_constants", "footprint", "FIELDS"]
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_NAME = "liblbmgpu.so"
@@ -56,6 +56,17 @@ SIGNATURES = {
     "lbm_get_stream": ([_vp, C.POINTER(_vp)], _i32),
     "lbm_time_kernels": ([_vp, _i64, _dp, _dp], _i32),
     "lbm_set_option": ([_vp, _i32, _i32], _i32),
+    "lbm_footprint": ([_vp, C.POINTER(_sz)], _i32),
+    "lbm_ensemble_create": ([_i32, C.POINTER(_vp)], _i32),
+    "lbm_ensemble_destroy": ([_vp], _i32),
+    "lbm_ensemble_add": ([_vp, _vp], _i32),
+    "lbm_ensemble_remove": ([_vp, _vp], _i32),
+    "lbm_ensemble_size": ([_vp], _i32),
+    "lbm_ensemble_step": ([_vp, _i64], _i32),
+    "lbm_ensemble_sync": ([_vp], _i32),
+    "lbm_ensemble_get_stream": ([_vp, C.POINTER(_vp)], _i32),
+    "lbm_ensemble_last_error": ([_vp], C.c_char_p),
+    "lbm_ensemble_autotune": ([_vp, _i32, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32)], _i32),
 }
 LBM_OPT_SINGLE_KERNEL = 1
 LBM_OPT_KCHUNK = 2
@@ -109,6 +120,15 @@ def derive_constants(params):
     if st != LBM_OK:
         raise LbmError(st, "invalid parameters")
     return c
+
+
+def footprint(params):
+    """Device bytes a Lattice with these parameters allocates."""
+    b = C.c_size_t()
+    st = load_library().lbm_footprint(C.byref(params), C.byref(b))
+    if st != LBM_OK:
+        raise LbmError(st, "invalid parameters")
+    return int(b.value)
 
 
 def _dptr(a):
@@ -237,3 +257,63 @@ class Lattice:
         if a.size != field_size(self.params, fid):
             raise ValueError("set_state(%s): expected %d values, got %d" % (field, field_size(self.params, fid), a.size))
         self._ck(self.lib.lbm_set_state(self._h, fid, _dptr(a), a.size), "set_state(%s)" % field)
+
+
+class Ensemble:
+    """Many FP32/FP16 lattices advanced together: one flow and one thermal launch per step
+    over a packed tile table of all members (the batched form)."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        st = self.lib.lbm_ensemble_create(int(device), C.byref(h))
+        if st != LBM_OK:
+            raise LbmError(st, "lbm_ensemble_create")
+        self._h = h
+        self.members = []
+
+    def _ck(self, st, what):
+        if st != LBM_OK:
+            msg = self.lib.lbm_ensemble_last_error(self._h)
+            raise LbmError(st, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    def add(self, lattice):
+        self._ck(self.lib.lbm_ensemble_add(self._h, lattice._h), "lbm_ensemble_add")
+        self.members.append(lattice)
+
+    def remove(self, lattice):
+        self._ck(self.lib.lbm_ensemble_remove(self._h, lattice._h), "lbm_ensemble_remove")
+        self.members.remove(lattice)
+
+    def __len__(self):
+        return int(self.lib.lbm_ensemble_size(self._h))
+
+    def step(self, nsteps):
+        self._ck(self.lib.lbm_ensemble_step(self._h, int(nsteps)), "lbm_ensemble_step")
+
+    def sync(self):
+        self._ck(self.lib.lbm_ensemble_sync(self._h), "lbm_ensemble_sync")
+
+    def stream_handle(self):
+        s = C.c_void_p()
+        self._ck(self.lib.lbm_ensemble_get_stream(self._h, C.byref(s)), "lbm_ensemble_get_stream")
+        return s.value or 0
+
+    def autotune(self, nsteps=4):
+        """Pick the tile / block / grid configuration by timing; members advance meanwhile."""
+        b, t, g = C.c_int(), C.c_int(), C.c_int()
+        self._ck(self.lib.lbm_ensemble_autotune(self._h, int(nsteps), C.byref(b), C.byref(t), C.byref(g)),
+                 "lbm_ensemble_autotune")
+        return {"block": b.value, "tile_cells": t.value, "grid_per_sm": g.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.lbm_ensemble_destroy(self._h)
+            self._h = None
+            self.members = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -27,7 +27,8 @@ UNITS = [
     ("lbm_exact.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
     ("lbm_reduce.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
     ("lbm_fast.cu", ["-fmad=true"]),
-    ("lbm_fused.cu", ["-fmad=true", "-Xptxas", "-v"]),
+    ("lbm_fused.cu", ["-fmad=true"]),
+    ("lbm_ensemble.cu", ["-fmad=true"]),
     ("lbm_api.cpp", []),
     ("lbm_noalloc.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
 ]

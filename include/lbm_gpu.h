@@ -169,6 +169,31 @@ int lbm_RBcalc_Nu_wall_avg(lbm_handle* h, lbm_nu_wall* out);
 int lbm_get_state(lbm_handle* h, int field, double* host, size_t count);
 int lbm_set_state(lbm_handle* h, int field, const double* host, size_t count);
 
+/* ---- batched form: many lattices in one launch per stage (no counterpart in the
+ *      reference, which runs one case per executable) ---------------------------------------
+ * An ensemble advances any number of FP32/FP16 handles (one storage precision, any mix of
+ * sizes, Ra, Pr, 2D and 3D) with one flow and one thermal launch per step over a packed
+ * tile table, replayed from captured CUDA graphs.  Members stay ordinary handles: their
+ * diagnostics and state transfer work as usual (the handle's stream waits for the
+ * ensemble's work).  A member that is not yet in the fused form (after lbm_initial or
+ * lbm_set_state) takes that first step alone at the next lbm_ensemble_step. */
+typedef struct lbm_ensemble lbm_ensemble;
+int lbm_ensemble_create(int device, lbm_ensemble** out);
+int lbm_ensemble_destroy(lbm_ensemble* e);            /* does not destroy the members      */
+int lbm_ensemble_add(lbm_ensemble* e, lbm_handle* h);
+int lbm_ensemble_remove(lbm_ensemble* e, lbm_handle* h);  /* lbm_destroy also removes     */
+int lbm_ensemble_size(const lbm_ensemble* e);
+int lbm_ensemble_step(lbm_ensemble* e, int64_t nsteps);
+int lbm_ensemble_sync(lbm_ensemble* e);
+int lbm_ensemble_get_stream(lbm_ensemble* e, void** stream);
+const char* lbm_ensemble_last_error(const lbm_ensemble* e);
+/* Tile/block autotuner: times `nsteps` steps of each launch configuration and keeps the
+ * fastest (members advance by those steps); outputs may be NULL. */
+int lbm_ensemble_autotune(lbm_ensemble* e, int nsteps, int* best_block, int* best_tile, int* best_grid);
+/* Device bytes lbm_create allocates for these parameters (for admission against an HBM
+ * budget). */
+int lbm_footprint(const lbm_params* p, size_t* bytes);
+
 /* ---- execution options (no counterpart in the reference) --------------------------------
  * LBM_OPT_SINGLE_KERNEL: FP32/FP16 handles advance with one fused kernel per step (1) or
  *   with the two-kernel form (0, default).  Both give the same arithmetic.
