@@ -17,6 +17,7 @@ the C++ restatement of the reference's OpenMP CPU path timed on this host's core
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -256,6 +257,130 @@ def e2e_run(prec, args, local):
                    % (len(names), args.steps)}
 
 
+def plain_rate_2d(local, ny=128):
+    """FP64 plain-method MLUPS on a 2D cell (for the served-form comparison)."""
+    import lbmgpu
+    from lbmgpu.abi import rb_params
+    lat = lbmgpu.Lattice(rb_params(dim=2, ny=ny, Ra=1e5, noise_amp=1e-3), device=local)
+    lat.initial()
+    lat.step(64)
+    lat.sync()
+    t0 = time.perf_counter()
+    lat.step(3200)
+    lat.sync()
+    dt = time.perf_counter() - t0
+    lat.close()
+    return 2 * ny * ny * 3200 / dt / 1e6
+
+
+def ensemble_run(args, local, steps_total=13000):
+    """Batched form (BASELINE config 3): 64 D2Q9/D2Q5 RB instances, aspect 2, ny drawn from
+    {64,...,512}, Ra log-uniform in [1e4, 1e8], Pr in {0.71, 7}, U = 0.1, FP32 storage, one
+    launch per stage over a packed tile table, graph replay, autotuned tiles.  |dNu| is
+    measured against FP64 plain solves of the four smallest instances."""
+    import random
+    import torch
+    import lbmgpu
+    from lbmgpu.abi import rb_params
+    rng = random.Random(20261203)
+    specs = []
+    for m in range(64):
+        ny = rng.choice([64, 96, 128, 192, 256, 384, 512])
+        ra = math.exp(rng.uniform(math.log(1e4), math.log(1e8)))
+        pr = rng.choice([0.71, 7.0])
+        specs.append(dict(dim=2, ny=ny, nx=2 * ny, Ra=ra, Pr=pr, U=0.1, noise_amp=1e-3, seed=20261203 + m))
+    ens = lbmgpu.Ensemble(device=local)
+    lats = []
+    for sp in specs:
+        lat = lbmgpu.Lattice(rb_params(precision="fp32", **sp), device=local)
+        lat.initial()
+        ens.add(lat)
+        lats.append(lat)
+    cells = sum(2 * sp["ny"] * sp["ny"] for sp in specs)
+    cfg = ens.autotune(3)
+    ens.step(10)
+    ens.sync()
+    stream = torch.cuda.ExternalStream(ens.stream_handle(), device=torch.device("cuda", local))
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k = 320
+    a.record(stream)
+    ens.step(k)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b)
+    mlups = cells * k / (ms / 1e3) / 1e6
+    # run on to a developed flow and compare the four smallest instances with FP64 solves
+    done = lats[0].itc
+    if steps_total > done:
+        ens.step(steps_total - done)
+    ens.sync()
+    small = sorted(range(len(specs)), key=lambda m: (specs[m]["ny"], m))[:4]
+    dnu = []
+    for m in small:
+        nu32, _ = lats[m].calNuRe()
+        ref = lbmgpu.Lattice(rb_params(precision="fp64", **specs[m]), device=local)
+        ref.initial()
+        ref.step(lats[m].itc)
+        nu64, _ = ref.calNuRe()
+        ref.close()
+        dnu.append({"ny": specs[m]["ny"], "Ra": specs[m]["Ra"], "Pr": specs[m]["Pr"], "steps": lats[m].itc,
+                    "Nu_fp32_batched": nu32, "Nu_fp64_plain": nu64, "rel_dNu": abs(nu32 - nu64) / abs(nu64)})
+    ens.close()
+    for lat in lats:
+        lat.close()
+    return {"workload": "64 D2Q9/D2Q5 RB instances, aspect 2, ny in {64..512}, Ra log-uniform 1e4..1e8, "
+                        "Pr in {0.71,7}, FP32 storage, %d cells" % cells,
+            "aggregate_mlups": mlups, "ms_per_step": ms / k, "steps_timed": k, "autotuned": cfg,
+            "launches_per_step": 2, "dNu_vs_fp64": dnu}
+
+
+def served_run(args, local, plain3d_mlups, duration=20.0, drain=40.0):
+    """Served form (BASELINE config 4), shortened: Poisson arrivals at 2/s for `duration`
+    seconds (the configuration asks for 600 s), half 2D (ny 64..512) half 3D (n 64..192),
+    Ra log-uniform 1e4..1e8, Pr in {0.71, 7}, FP32, admission by an 80% HBM budget, stop at
+    |dNu| < 0.1% over 5000 steps or at 20000 steps."""
+    import lbmgpu
+    from lbmgpu import server as srv
+    reqs = srv.poisson_requests(2.0, duration)
+    s = srv.SolveServer(device=local, chunk_steps=500, check_every=5000, rel_tol=1e-3, max_steps=20000,
+                        autotune=False)
+    t0 = time.perf_counter()
+    results = s.run(reqs, time_limit=duration + drain)
+    wall = time.perf_counter() - t0
+    unfinished = len(s.active) + len(s.queue) + (len(reqs) - len(results) - len(s.active) - len(s.queue))
+    summary = srv.summarize(results, wall)
+    peak = (s.peak_active, s.peak_queue)
+    s.close()
+    # plain FP64 method, one solve at a time, on the same completed work
+    plain2d = plain_rate_2d(local)
+    by_id = {r.rid: r for r in reqs}
+    done = [r for r in results if r.steps > 0]
+    plain_s = sum(r.cells * r.steps / ((plain2d if by_id[r.rid].dim == 2 else plain3d_mlups) * 1e6) for r in done)
+    # |dNu| of the two smallest completed solves against FP64 plain solves of the same length
+    dnu = []
+    for r in sorted(done, key=lambda r: r.cells)[:2]:
+        q = by_id[r.rid]
+        p64 = q.params()
+        p64.precision = 0
+        ref = lbmgpu.Lattice(p64, device=local)
+        ref.initial()
+        ref.step(r.steps)
+        nu64, _ = ref.calNuRe()
+        ref.close()
+        dnu.append({"rid": r.rid, "dim": q.dim, "n": q.n, "Ra": q.Ra, "steps": r.steps, "Nu_fp32_served": r.Nu,
+                    "Nu_fp64_plain": nu64, "rel_dNu": abs(r.Nu - nu64) / abs(nu64)})
+    summary.update({
+        "workload": "Poisson arrivals 2/s for %.0f s (shortened from 600 s), 50/50 2D (ny 64..512, aspect 2) / 3D "
+                    "(n 64..192), Ra log-uniform 1e4..1e8, Pr {0.71,7}, FP32, 80%% HBM budget, stop at |dNu|<0.1%% "
+                    "over 5000 steps or 20000 steps" % duration,
+        "arrived": len(reqs), "unfinished_at_limit": unfinished, "wall_s": wall,
+        "peak_active": peak[0], "peak_queue": peak[1],
+        "plain_fp64_solves_per_hour_same_work": 3600.0 * len(done) / plain_s if plain_s > 0 else None,
+        "dNu_vs_fp64": dnu,
+    })
+    return summary
+
+
 def run_gpu(args):
     rank, world, local, pg = dist_setup(args)
     import torch
@@ -301,6 +426,10 @@ def run_gpu(args):
                          "dtype": DTYPE[prec], "roofline": roof(prec), "Nu": results[prec]["Nu"],
                          "Re": results[prec]["Re"]} for prec in results},
     }
+    if rank == 0 and not args.no_ensemble:
+        line["batched"] = ensemble_run(args, local)
+    if rank == 0 and not args.no_served:
+        line["served"] = served_run(args, local, results["fp64"]["mlups"] if "fp64" in results else 700.0)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n=args.size)
     if rank == 0:
@@ -316,6 +445,8 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) leg")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-form leg (64 2D instances)")
+    ap.add_argument("--no-served", action="store_true", help="skip the served-stream leg")
     ap.add_argument("--size", type=int, default=N_CELL_EDGE, help="cube edge (cells); 128 is the benchmark")
     ap.add_argument("--precisions", default="fp64,fp32,fp16",
                     help="comma list; the first is the headline form")
