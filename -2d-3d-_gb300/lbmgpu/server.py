@@ -15,7 +15,7 @@ import math
 import time
 from dataclasses import dataclass, field
 
-from . import Ensemble, Lattice, footprint
+from . import Ensemble, Lattice, LbmDiverged, footprint
 from .abi import rb_params
 
 
@@ -54,6 +54,7 @@ class Result:
     finished: float
     cells: int
     nu_history: list = field(default_factory=list)
+    diverged: bool = False
 
     @property
     def time_to_solution(self):
@@ -124,9 +125,10 @@ class SolveServer:
         self.peak_active = max(self.peak_active, len(self.active))
         return admitted
 
-    def _finish(self, rid, now, converged, nu, re):
+    def _finish(self, rid, now, converged, nu, re, diverged=False):
         req, lat, need, adm, _, hist = self.active.pop(rid)
-        self.results.append(Result(rid, nu, re, lat.itc, converged, req.arrival, adm, now, req.cells, hist))
+        self.results.append(Result(rid, nu, re, lat.itc, converged, req.arrival, adm, now, req.cells, hist,
+                                   diverged))
         self.ens.remove(lat)
         lat.close()
         self.used -= need
@@ -138,7 +140,12 @@ class SolveServer:
             due = steps >= (len(hist) + 1) * self.check_every
             if not due and steps < self.max_steps:
                 continue
-            nu, re = lat.calNuRe()
+            try:
+                nu, re = lat.calNuRe()
+            except LbmDiverged:
+                # non-finite field or rho <= 0: end this solve, keep serving the others
+                self._finish(rid, now, False, float("nan"), float("nan"), diverged=True)
+                continue
             hist.append((steps, nu))
             if last is not None and abs(nu - last) <= self.rel_tol * abs(last):
                 self._finish(rid, now, True, nu, re)
@@ -196,7 +203,8 @@ def summarize(results, wall_seconds):
     return {
         "completed": len(done),
         "converged": sum(1 for r in done if r.converged),
-        "capped": sum(1 for r in done if not r.converged),
+        "capped": sum(1 for r in done if not r.converged and not r.diverged),
+        "diverged": sum(1 for r in done if r.diverged),
         "solves_per_hour": 3600.0 * len(done) / wall_seconds if wall_seconds > 0 else None,
         "p50_s": pct(50),
         "p99_s": pct(99),

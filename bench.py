@@ -314,10 +314,18 @@ def ensemble_run(args, local, steps_total=13000):
     if steps_total > done:
         ens.step(steps_total - done)
     ens.sync()
-    small = sorted(range(len(specs)), key=lambda m: (specs[m]["ny"], m))[:4]
+    diverged = []
+    nus = {}
+    for m, lat in enumerate(lats):
+        try:
+            nus[m] = lat.calNuRe()[0]
+        except lbmgpu.LbmDiverged:
+            diverged.append({"ny": specs[m]["ny"], "Ra": specs[m]["Ra"], "Pr": specs[m]["Pr"],
+                             "tauf": lat.constants()["tauf"]})
+    small = sorted(nus, key=lambda m: (specs[m]["ny"], m))[:4]
     dnu = []
     for m in small:
-        nu32, _ = lats[m].calNuRe()
+        nu32 = nus[m]
         ref = lbmgpu.Lattice(rb_params(precision="fp64", **specs[m]), device=local)
         ref.initial()
         ref.step(lats[m].itc)
@@ -331,18 +339,23 @@ def ensemble_run(args, local, steps_total=13000):
     return {"workload": "64 D2Q9/D2Q5 RB instances, aspect 2, ny in {64..512}, Ra log-uniform 1e4..1e8, "
                         "Pr in {0.71,7}, FP32 storage, %d cells" % cells,
             "aggregate_mlups": mlups, "ms_per_step": ms / k, "steps_timed": k, "autotuned": cfg,
-            "launches_per_step": 2, "dNu_vs_fp64": dnu}
+            "launches_per_step": 2, "dNu_vs_fp64": dnu,
+            "diverged": {"count": len(diverged), "cases": diverged,
+                         "note": "under-resolved draws (tau_f close to 1/2) reported as LBM_ERR_DIVERGED"}}
 
 
-def served_run(args, local, plain3d_mlups, duration=20.0, drain=40.0):
-    """Served form (BASELINE config 4), shortened: Poisson arrivals at 2/s for `duration`
-    seconds (the configuration asks for 600 s), half 2D (ny 64..512) half 3D (n 64..192),
-    Ra log-uniform 1e4..1e8, Pr in {0.71, 7}, FP32, admission by an 80% HBM budget, stop at
-    |dNu| < 0.1% over 5000 steps or at 20000 steps."""
+def served_run(args, local, plain3d_mlups):
+    """Served form (BASELINE config 4): Poisson arrivals at 2/s, half 2D (ny 64..512, aspect 2)
+    half 3D (n 64..192), Ra log-uniform 1e4..1e8, Pr in {0.71, 7}, FP32, admission by an 80%
+    HBM budget, each solve run until Nu changes by < 0.1% over a window of steps or a step cap.
+    The default run is scaled to fit a bench (20 s of arrivals, 1000-step window, 4000-step
+    cap); --served-full runs the configuration as stated (600 s, 5000-step window)."""
     import lbmgpu
     from lbmgpu import server as srv
+    duration, drain = args.served_seconds, args.served_drain
+    window, cap = args.served_window, args.served_cap
     reqs = srv.poisson_requests(2.0, duration)
-    s = srv.SolveServer(device=local, chunk_steps=500, check_every=5000, rel_tol=1e-3, max_steps=20000,
+    s = srv.SolveServer(device=local, chunk_steps=500, check_every=window, rel_tol=1e-3, max_steps=cap,
                         autotune=False)
     t0 = time.perf_counter()
     results = s.run(reqs, time_limit=duration + drain)
@@ -358,7 +371,7 @@ def served_run(args, local, plain3d_mlups, duration=20.0, drain=40.0):
     plain_s = sum(r.cells * r.steps / ((plain2d if by_id[r.rid].dim == 2 else plain3d_mlups) * 1e6) for r in done)
     # |dNu| of the two smallest completed solves against FP64 plain solves of the same length
     dnu = []
-    for r in sorted(done, key=lambda r: r.cells)[:2]:
+    for r in sorted([r for r in done if not r.diverged], key=lambda r: r.cells)[:2]:
         q = by_id[r.rid]
         p64 = q.params()
         p64.precision = 0
@@ -370,9 +383,11 @@ def served_run(args, local, plain3d_mlups, duration=20.0, drain=40.0):
         dnu.append({"rid": r.rid, "dim": q.dim, "n": q.n, "Ra": q.Ra, "steps": r.steps, "Nu_fp32_served": r.Nu,
                     "Nu_fp64_plain": nu64, "rel_dNu": abs(r.Nu - nu64) / abs(nu64)})
     summary.update({
-        "workload": "Poisson arrivals 2/s for %.0f s (shortened from 600 s), 50/50 2D (ny 64..512, aspect 2) / 3D "
-                    "(n 64..192), Ra log-uniform 1e4..1e8, Pr {0.71,7}, FP32, 80%% HBM budget, stop at |dNu|<0.1%% "
-                    "over 5000 steps or 20000 steps" % duration,
+        "workload": "Poisson arrivals 2/s for %.0f s, 50/50 2D (ny 64..512, aspect 2) / 3D (n 64..192), Ra "
+                    "log-uniform 1e4..1e8, Pr {0.71,7}, FP32, 80%% HBM budget, stop at |dNu|<0.1%% over %d steps or "
+                    "at %d steps; drain limit %.0f s%s" % (duration, window, cap, drain,
+                    "" if args.served_full else " (scaled from 600 s / 5000-step window: the stated stream "
+                    "oversubscribes one GPU several times)"),
         "arrived": len(reqs), "unfinished_at_limit": unfinished, "wall_s": wall,
         "peak_active": peak[0], "peak_queue": peak[1],
         "plain_fp64_solves_per_hour_same_work": 3600.0 * len(done) / plain_s if plain_s > 0 else None,
@@ -447,12 +462,19 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-form leg (64 2D instances)")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream leg")
+    ap.add_argument("--served-full", action="store_true", help="served leg as configured: 600 s, 5000-step window")
+    ap.add_argument("--served-seconds", type=float, default=20.0)
+    ap.add_argument("--served-drain", type=float, default=40.0)
+    ap.add_argument("--served-window", type=int, default=1000)
+    ap.add_argument("--served-cap", type=int, default=4000)
     ap.add_argument("--size", type=int, default=N_CELL_EDGE, help="cube edge (cells); 128 is the benchmark")
     ap.add_argument("--precisions", default="fp64,fp32,fp16",
                     help="comma list; the first is the headline form")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.served_full:
+        args.served_seconds, args.served_drain, args.served_window, args.served_cap = 600.0, 1200.0, 5000, 50000
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

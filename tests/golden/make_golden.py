@@ -15,6 +15,7 @@ read as independent statements of the same transforms.
 """
 import argparse
 import json
+import math
 import os
 import re
 
@@ -126,6 +127,193 @@ def main():
     with open(os.path.join(HERE, "reference_matrices.json"), "w") as fh:
         json.dump(out, fh)
     print("wrote reference_matrices.json")
+    make_step_fixtures(args.ref)
+
+
+
+
+# ---------------------------------------------------------------------------------------
+# step fixtures: the reference's own subroutines executed on small perturbed states
+# ---------------------------------------------------------------------------------------
+def module_constants(src_lines, module_name, defines, overrides):
+    """Evaluate the `parameter` declarations of the reference's commondata module in order,
+    with the lattice size and physics numbers overridden."""
+    from transliterate import convert_expr, join_continuations, preprocess
+    start = next(k for k, ln in enumerate(src_lines) if re.match(r"\s*module\s+%s\b" % module_name, ln, re.I))
+    end = next(k for k in range(start, len(src_lines)) if re.match(r"\s*end\s+module", src_lines[k], re.I))
+    lines = join_continuations(preprocess(src_lines[start + 1:end], defines))
+    ns = {"math": math}
+    for s in lines:
+        m = re.match(r".*parameter\s*::\s*(.+)$", s, re.I)
+        if not m:
+            continue
+        rhs, depth, cur, parts = m.group(1), 0, "", []
+        for ch in rhs:
+            if ch == "(":
+                depth += 1
+            elif ch == ")":
+                depth -= 1
+            if ch == "," and depth == 0:
+                parts.append(cur)
+                cur = ""
+            else:
+                cur += ch
+        parts.append(cur)
+        for part in parts:
+            name, expr = part.split("=", 1)
+            name = name.strip()
+            if name in overrides:
+                ns[name] = overrides[name]
+                continue
+            expr = convert_expr(expr).replace("acos(", "math.acos(")
+            ns[name] = eval(expr, ns)
+    return ns
+
+
+def lattice_tables(src_text, dim):
+    def vec(name):
+        if dim == 3:
+            m = re.search(r"^\s*%s\s*=\s*\(/(.*?)/\)" % name, src_text, re.M)
+        else:
+            m = re.search(r"data\s+%s\s*/(.*?)/" % name, src_text)
+        return np.array([int(x) for x in m.group(1).split(",")])
+    if dim == 3:
+        return {k: vec(k) for k in ("ex", "ey", "ez", "opp", "exT", "eyT", "ezT", "oppT")}
+    return {"ex": vec("ex"), "ey": vec("ey")}
+
+
+def make_state(dim, nx, ny, nz, consts, tables, rng):
+    """A perturbed module state: near-equilibrium populations with random deviations, random
+    T, consistent rho/u, random B_prev.  Arrays carry the Fortran index ranges."""
+    q, qt = (19, 7) if dim == 3 else (9, 5)
+    shp = (nx + 2, ny + 2, nz + 2) if dim == 3 else (nx + 2, ny + 2)
+    ns = dict(consts)
+    ns.update(tables)
+    ns["f"] = np.zeros((q,) + shp)
+    ns["f_post"] = np.zeros((q,) + shp)
+    ns["g"] = np.zeros((qt,) + shp)
+    ns["g_post"] = np.zeros((qt,) + shp)
+    for a in ("rho", "u", "v", "w", "T", "Bx_prev", "By_prev", "Bz_prev", "Fx", "Fy", "up", "vp", "wp", "Tp"):
+        ns[a] = np.zeros(shp)
+    if dim == 3:
+        w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+        wT = np.array([consts["omegaT0"]] + [consts["omegaT1"]] * 6)
+        exs = (tables["ex"], tables["ey"], tables["ez"])
+        exT = (tables["exT"], tables["eyT"], tables["ezT"])
+    else:
+        w = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+        wT = np.array([consts["omegaT0"]] + [consts["omegaT1"]] * 4)
+        exs = (tables["ex"], tables["ey"])
+        exT = (tables["ex"][:5], tables["ey"][:5])
+    inner = tuple(slice(1, n + 1) for n in ((nx, ny, nz) if dim == 3 else (nx, ny)))
+    ishape = tuple(s.stop - 1 for s in inner)
+    rho = 1.0 + 1e-3 * rng.standard_normal(ishape)
+    vel = [0.03 * rng.standard_normal(ishape) for _ in range(dim)]
+    T = 0.5 * rng.uniform(-1, 1, ishape)
+    for a in range(q):
+        eu = sum(exs[d][a] * vel[d] for d in range(dim))
+        u2 = sum(vv * vv for vv in vel)
+        ns["f"][(a,) + inner] = w[a] * rho * (1 + 3 * eu + 4.5 * eu * eu - 1.5 * u2) + 1e-4 * rng.standard_normal(ishape)
+    for a in range(qt):
+        eu = sum(exT[d][a] * vel[d] for d in range(dim))
+        ns["g"][(a,) + inner] = wT[a] * T * (1 + 3 * eu) + 1e-4 * rng.standard_normal(ishape)
+    ns["rho"][inner] = rho
+    ns["u"][inner] = vel[0]
+    ns["v"][inner] = vel[1]
+    if dim == 3:
+        ns["w"][inner] = vel[2]
+    ns["T"][inner] = T
+    ns["Bx_prev"][inner] = vel[0] * T + 1e-4 * rng.standard_normal(ishape)
+    ns["By_prev"][inner] = vel[1] * T + 1e-4 * rng.standard_normal(ishape)
+    if dim == 3:
+        ns["Bz_prev"][inner] = vel[2] * T + 1e-4 * rng.standard_normal(ishape)
+    return ns, inner
+
+
+FIELDS_OUT = {2: ["f", "g", "rho", "u", "v", "T", "Bx_prev", "By_prev", "Fx", "Fy", "f_post", "g_post"],
+              3: ["f", "g", "rho", "u", "v", "w", "T", "Bx_prev", "By_prev", "Bz_prev", "f_post", "g_post"]}
+
+
+def to_fortran_layout(arr, inner, pop):
+    """numpy array with Fortran index ranges -> the (nz,)ny,nx(,q) C-order layout of
+    lbm_get_state (direction fastest, x next)."""
+    if pop:
+        sub = arr[(slice(None),) + inner]
+        return np.ascontiguousarray(np.transpose(sub, tuple(range(sub.ndim - 1, 0, -1)) + (0,)))
+    sub = arr[inner]
+    return np.ascontiguousarray(np.transpose(sub))
+
+
+def step_fixture(ref_dir, case):
+    from transliterate import ReferenceSubroutines
+    dim = case["dim"]
+    path = os.path.join(ref_dir, "2DRB.F90" if dim == 2 else "3DRB.F90")
+    src_lines = open(path, encoding="utf-8-sig").read().splitlines()
+    src_text = "\n".join(src_lines)
+    defines = set(case["defines"])
+    over = {"nx": case["nx"], "ny": case["ny"], "Rayleigh": case["Ra"], "Prandtl": case["Pr"], "Mach": case["Mach"]}
+    if dim == 3:
+        over["nz"] = case["nz"]
+    consts = module_constants(src_lines, "commondata3d" if dim == 3 else "commondata", defines, over)
+    legacy = "EnableLegacyThermalScheme" in defines
+    if dim == 3:
+        consts["omegaT0"] = (1.0 - consts["paraA"]) / 7.0 if legacy else 1.0 / 4.0
+        consts["omegaT1"] = (6.0 + consts["paraA"]) / 42.0 if legacy else 1.0 / 8.0
+    else:
+        consts["omegaT0"] = (1.0 - consts["paraA"]) / 5.0 if legacy else 1.0 / 3.0
+        consts["omegaT1"] = (consts["paraA"] + 4.0) / 20.0 if legacy else 1.0 / 6.0
+    tables = lattice_tables(src_text, dim)
+    rng = np.random.default_rng(case["seed"])
+    ns, inner = make_state(dim, case["nx"], case["ny"], case.get("nz", 1), consts, tables, rng)
+    q, qt = (19, 7) if dim == 3 else (9, 5)
+    ns["omega"] = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12) if dim == 3 else \
+        np.array([4.0 / 9.0] + [1.0 / 9.0] * 4 + [1.0 / 36.0] * 4)
+    ns["omegaT"] = np.array([consts["omegaT0"]] + [consts["omegaT1"]] * (qt - 1))
+    ns["qf"], ns["qt"] = q, qt
+    out = {}
+    for name in FIELDS_OUT[dim]:
+        out["in_" + name] = to_fortran_layout(ns[name], inner, name in ("f", "g", "f_post", "g_post"))
+    subs = ReferenceSubroutines(path, defines)
+    for _ in range(case["steps"]):
+        subs.step(ns)
+    for name in FIELDS_OUT[dim]:
+        out["out_" + name] = to_fortran_layout(ns[name], inner, name in ("f", "g", "f_post", "g_post"))
+    meta = {k: v for k, v in case.items() if k != "defines"}
+    meta["defines"] = sorted(defines)
+    meta["constants"] = {k: consts[k] for k in ("tauf", "viscosity", "diffusivity", "gBeta", "Qk", "paraA")}
+    return out, meta
+
+
+STEP_CASES = [
+    dict(name="rb2d_periodic", dim=2, nx=10, ny=6, Ra=1e5, Pr=0.71, Mach=0.1 * math.sqrt(3.0), steps=4, seed=7,
+         defines=["steadyFlow", "HorizontalWallsNoslip", "VerticalWallsPeriodicalU", "RayleighBenardCell",
+                  "HorizontalWallsConstT", "VerticalWallsPeriodicalT", "EnableUseG"]),
+    dict(name="rb3d_noslip", dim=3, nx=6, ny=5, nz=4, Ra=1e6, Pr=0.71, Mach=0.1 * math.sqrt(3.0), steps=3, seed=8,
+         defines=["steadyFlow", "HorizontalWallsNoslip", "VerticalWallsNoslip", "SpanwiseWallsNoslip",
+                  "RayleighBenardCell", "HorizontalWallsConstT", "VerticalWallsAdiabatic", "SpanwiseWallsAdiabatic",
+                  "EnableUseG"]),
+    dict(name="side3d_default", dim=3, nx=5, ny=6, nz=4, Ra=1e5, Pr=0.71, Mach=0.1, steps=3, seed=9,
+         defines=["steadyFlow", "HorizontalWallsNoslip", "VerticalWallsNoslip", "SpanwiseWallsNoslip",
+                  "SideHeatedCell", "VerticalWallsConstT", "HorizontalWallsAdiabatic", "SpanwiseWallsAdiabatic",
+                  "EnableUseG"]),
+    dict(name="rb3d_periodic_legacy", dim=3, nx=6, ny=5, nz=4, Ra=1e5, Pr=0.71, Mach=0.02, steps=3, seed=10,
+         defines=["steadyFlow", "HorizontalWallsNoslip", "VerticalWallsPeriodicalU", "SpanwiseWallsPeriodicalU",
+                  "RayleighBenardCell", "HorizontalWallsConstT", "VerticalWallsPeriodicalT",
+                  "SpanwiseWallsPeriodicalT", "EnableUseG", "EnableLegacyThermalScheme"]),
+]
+
+
+def make_step_fixtures(ref_dir):
+    import sys
+    sys.path.insert(0, HERE)
+    index = {}
+    for case in STEP_CASES:
+        out, meta = step_fixture(ref_dir, case)
+        np.savez_compressed(os.path.join(HERE, "step_%s.npz" % case["name"]), **out)
+        index[case["name"]] = meta
+        print("wrote step_%s.npz" % case["name"])
+    with open(os.path.join(HERE, "step_cases.json"), "w") as fh:
+        json.dump(index, fh, indent=1)
 
 
 if __name__ == "__main__":
