@@ -23,6 +23,7 @@
 #include "lbm_ensemble.h"
 #include "lbm_fast.h"
 #include "lbm_internal.h"
+#include "lbm_records.h"
 
 using namespace lbm;
 
@@ -74,6 +75,8 @@ struct lbm_handle {
     // batched stepping
     lbm_ensemble* ensemble = nullptr;  // the ensemble this handle is a member of
     cudaEvent_t order_ev = nullptr;    // orders the handle's stream against the ensemble's
+
+    int reload_form = -1;  // form used by the last lbm_reload (0 reference, 1 continuation)
 };
 
 // ------------------------------------------------------------------------------------
@@ -909,6 +912,370 @@ extern "C" int lbm_set_state(lbm_handle* h, int field, const double* host, size_
     if (!host) return LBM_ERR_PARAM;
     return state_io(h, field, nullptr, host, count);
 }
+
+// ------------------------------------------------------------------------------------
+// restart files: backupData / reload (3DRB.F90:1638-1665, 602-623; 2DRB.F90:1402-1430,
+// 621-637) with reconstruct_macro_from_fg (3DRB.F90:1392-1463, 2DRB.F90:1144-1200)
+// ------------------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t kContMagic = 0x31544E4F434D424CLL;  // "LBMCONT1" read as little-endian bytes
+constexpr int64_t kContVersion = 1;
+constexpr int kContHeader = 16;                       // int64 words of the header record
+constexpr size_t kIoChunk = size_t(64) << 20;         // host staging per copy
+
+// forms of the continuation records
+constexpr int kFormExact = 0;      // FP64 module arrays (f, g come from the two reference records)
+constexpr int kFormFastFused = 1;  // FP32/FP16 fused buffers F[cur], G[cur], B[cur], L[cur]
+constexpr int kFormFastModule = 2; // FP32/FP16 module arrays fref, gref, rho, u, v, w, T, B, L
+
+struct Pinned {
+    void* p = nullptr;
+    size_t cap = 0;
+    ~Pinned() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+struct ContArray {
+    void* dptr;
+    size_t bytes;
+};
+
+struct FileCloser {
+    FILE* fp = nullptr;
+    ~FileCloser() {
+        if (fp) std::fclose(fp);
+    }
+};
+
+}  // namespace
+
+// Device arrays of the continuation records, in file order, for one form.
+static std::vector<ContArray> cont_arrays(lbm_handle* h, int form) {
+    const size_t n = (size_t)h->geo.ncell;
+    const bool d3 = h->dim == 3;
+    std::vector<ContArray> v;
+    if (form == kFormExact) {
+        ExactArrays& A = h->A;
+        const size_t b = n * sizeof(double);
+        v = {{A.rho, b}, {A.u, b}, {A.v, b}};
+        if (d3) v.push_back({A.w, b});
+        v.push_back({A.T, b});
+        v.push_back({A.Bx, b});
+        v.push_back({A.By, b});
+        if (d3) v.push_back({A.Bz, b});
+        else {
+            v.push_back({A.Fx, b});
+            v.push_back({A.Fy, b});
+        }
+        v.push_back({A.up, b});
+        v.push_back({A.vp, b});
+        if (d3) v.push_back({A.wp, b});
+        v.push_back({A.Tp, b});
+        return v;
+    }
+    FastState& F = h->F;
+    const size_t b = n * sizeof(float);
+    const int c = F.cur;
+    if (form == kFormFastFused) {
+        v = {{F.fbuf[c], (size_t)h->q * n * F.esize}, {F.gbuf[c], (size_t)h->qt * n * F.esize}};
+    } else {
+        v = {{F.fref, (size_t)h->q * n * F.esize}, {F.gref, (size_t)h->qt * n * F.esize}, {F.rho, b}, {F.u, b},
+             {F.v, b}};
+        if (d3) v.push_back({F.w, b});
+        v.push_back({F.T, b});
+    }
+    for (int a = 0; a < h->dim; ++a) v.push_back({F.B[c][a], b});
+    v.push_back({F.L[c], b});
+    v.push_back({F.up, b});
+    v.push_back({F.vp, b});
+    if (d3) v.push_back({F.wp, b});
+    v.push_back({F.Tp, b});
+    return v;
+}
+
+static int pinned_for(lbm_handle* h, Pinned& pin, size_t largest) {
+    const size_t want = largest < kIoChunk ? largest : kIoChunk;
+    CK(h, cudaMallocHost(&pin.p, want > 0 ? want : 1));
+    pin.cap = want > 0 ? want : 1;
+    return LBM_OK;
+}
+
+// One record of `bytes` bytes of device memory, staged through pinned host memory.
+static int write_device_record(lbm_handle* h, FILE* fp, const void* dptr, size_t bytes, Pinned& pin) {
+    RecordWriter w;
+    if (!w.begin(fp, bytes)) return fail(h, LBM_ERR_IO, "write failed");
+    for (size_t off = 0; off < bytes;) {
+        const size_t k = bytes - off < pin.cap ? bytes - off : pin.cap;
+        CK(h, cudaMemcpyAsync(pin.p, (const char*)dptr + off, k, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        if (!w.put(pin.p, k)) return fail(h, LBM_ERR_IO, "write failed");
+        off += k;
+    }
+    if (!w.end()) return fail(h, LBM_ERR_IO, "write failed");
+    return LBM_OK;
+}
+
+static int read_device_record(lbm_handle* h, FILE* fp, void* dptr, size_t bytes, Pinned& pin) {
+    RecordReader r;
+    if (!r.begin(fp)) return fail(h, LBM_ERR_IO, "restart file truncated");
+    for (size_t off = 0; off < bytes;) {
+        const size_t k = bytes - off < pin.cap ? bytes - off : pin.cap;
+        if (r.get(pin.p, k) != k) return fail(h, LBM_ERR_IO, "restart record shorter than the lattice");
+        CK(h, cudaMemcpyAsync((char*)dptr + off, pin.p, k, cudaMemcpyHostToDevice, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        off += k;
+    }
+    if (!r.ok || !r.at_end()) return fail(h, LBM_ERR_IO, "restart record longer than the lattice");
+    return LBM_OK;
+}
+
+static void cont_header(const lbm_handle* h, int form, size_t narrays, int64_t hdr[kContHeader]) {
+    for (int k = 0; k < kContHeader; ++k) hdr[k] = 0;
+    hdr[0] = kContMagic;
+    hdr[1] = kContVersion;
+    hdr[2] = h->dim;
+    hdr[3] = h->geo.nx;
+    hdr[4] = h->geo.ny;
+    hdr[5] = h->geo.nz;
+    hdr[6] = h->p.precision;
+    hdr[7] = form;
+    hdr[8] = h->itc;
+    hdr[9] = (int64_t)narrays;
+    hdr[10] = h->p.precision == LBM_FP64 ? 8 : (int64_t)h->F.esize;
+}
+
+extern "C" int lbm_backupData(lbm_handle* h, const char* path, int flags) {
+    if (!h || !path) return LBM_ERR_PARAM;
+    if (flags != LBM_BACKUP_REFERENCE && flags != LBM_BACKUP_CONTINUE) return fail(h, LBM_ERR_PARAM, "unknown flags");
+    if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
+    CK(h, cudaSetDevice(h->device));
+    int st = materialize(h);
+    if (st != LBM_OK) return st;
+    const size_t n = (size_t)h->geo.ncell;
+    const bool fp64 = h->p.precision == LBM_FP64;
+    Pinned pin;
+    if ((st = pinned_for(h, pin, (size_t)h->q * n * sizeof(double))) != LBM_OK) return st;
+    FileCloser file;
+    file.fp = std::fopen(path, "wb");
+    if (!file.fp) return fail(h, LBM_ERR_IO, std::string("cannot open ") + path + " for writing");
+    // the reference's two records: f then g, direction outermost, x fastest, FP64
+    for (int which = 0; which < 2; ++which) {
+        const int qq = which == 0 ? h->q : h->qt;
+        const double* src = nullptr;
+        if (fp64) {
+            src = which == 0 ? h->A.f : h->A.g;
+        } else {
+            if ((st = ensure_stage(h, (size_t)qq * n)) != LBM_OK) return st;
+            st = fast_export(h->F, h->geo, h->phys, h->dim, which == 0 ? LBM_FIELD_F : LBM_FIELD_G, h->d_stage,
+                             h->stream, true);
+            if (st != LBM_OK) return fail(h, st, "population export failed");
+            CK_LAUNCH(h, "export");
+            src = h->d_stage;
+        }
+        if ((st = write_device_record(h, file.fp, src, (size_t)qq * n * sizeof(double), pin)) != LBM_OK) return st;
+    }
+    if (flags == LBM_BACKUP_CONTINUE) {
+        const int form = fp64 ? kFormExact : (h->F.fused_valid ? kFormFastFused : kFormFastModule);
+        std::vector<ContArray> arrays = cont_arrays(h, form);
+        int64_t hdr[kContHeader];
+        cont_header(h, form, arrays.size(), hdr);
+        RecordWriter w;
+        if (!(w.begin(file.fp, sizeof(hdr)) && w.put(hdr, sizeof(hdr)) && w.end()))
+            return fail(h, LBM_ERR_IO, "write failed");
+        for (const ContArray& a : arrays)
+            if ((st = write_device_record(h, file.fp, a.dptr, a.bytes, pin)) != LBM_OK) return st;
+    }
+    const int rc = std::fclose(file.fp);
+    file.fp = nullptr;
+    if (rc != 0) return fail(h, LBM_ERR_IO, "write failed");
+    return LBM_OK;
+}
+
+// Record layout of a restart file, read without touching the handle.
+struct RestartScan {
+    size_t len_f = 0, len_g = 0;
+    bool has_cont = false;
+    int64_t hdr[kContHeader] = {};
+    std::vector<size_t> lens;
+};
+
+static bool scan_restart(FILE* fp, RestartScan& s) {
+    RecordReader r;
+    if (!r.begin(fp) || !r.skip_rest()) return false;
+    s.len_f = r.total;
+    RecordReader r2;
+    if (!r2.begin(fp) || !r2.skip_rest()) return false;
+    s.len_g = r2.total;
+    RecordReader r3;
+    if (!r3.begin(fp)) return true;  // end of file: the reference's two records only
+    if (r3.get(s.hdr, sizeof(s.hdr)) != sizeof(s.hdr) || !r3.ok || !r3.at_end()) return true;
+    if (s.hdr[0] != kContMagic) return true;
+    for (int64_t k = 0; k < s.hdr[9] && k < 64; ++k) {
+        RecordReader ra;
+        if (!ra.begin(fp) || !ra.skip_rest()) return true;
+        s.lens.push_back(ra.total);
+    }
+    s.has_cont = (int64_t)s.lens.size() == s.hdr[9];
+    return true;
+}
+
+static std::string cont_mismatch(lbm_handle* h, const RestartScan& s) {
+    const int64_t* H = s.hdr;
+    if (H[1] != kContVersion) return "unknown continuation version";
+    if (H[2] != h->dim || H[3] != h->geo.nx || H[4] != h->geo.ny || H[5] != h->geo.nz)
+        return "continuation records were written for another lattice size";
+    if (H[6] != h->p.precision) return "continuation records were written for another storage precision";
+    const bool fp64 = h->p.precision == LBM_FP64;
+    if (fp64 ? H[7] != kFormExact : (H[7] != kFormFastFused && H[7] != kFormFastModule))
+        return "unknown continuation form";
+    std::vector<ContArray> arrays = cont_arrays(h, (int)H[7]);
+    if (arrays.size() != s.lens.size()) return "continuation record count differs";
+    for (size_t k = 0; k < arrays.size(); ++k)
+        if (arrays[k].bytes != s.lens[k]) return "continuation record length differs";
+    return "";
+}
+
+extern "C" int lbm_reload(lbm_handle* h, const char* path, int mode) {
+    if (!h || !path) return LBM_ERR_PARAM;
+    if (mode != LBM_RELOAD_REFERENCE && mode != LBM_RELOAD_CONTINUE && mode != LBM_RELOAD_AUTO)
+        return fail(h, LBM_ERR_PARAM, "unknown reload mode");
+    if (h->ensemble) return fail(h, LBM_ERR_STATE, "remove the handle from its ensemble before reloading it");
+    CK(h, cudaSetDevice(h->device));
+    FileCloser file;
+    file.fp = std::fopen(path, "rb");
+    if (!file.fp) return fail(h, LBM_ERR_IO, std::string("cannot open ") + path);
+    // check the whole file before the state is touched
+    RestartScan scan;
+    if (!scan_restart(file.fp, scan)) return fail(h, LBM_ERR_IO, "not a restart file (two Fortran records expected)");
+    const size_t n = (size_t)h->geo.ncell;
+    if (scan.len_f != (size_t)h->q * n * sizeof(double) || scan.len_g != (size_t)h->qt * n * sizeof(double))
+        return fail(h, LBM_ERR_IO, "restart records do not match the lattice size");
+    std::string why = scan.has_cont ? cont_mismatch(h, scan) : "no continuation records in the file";
+    bool cont = false;
+    if (mode == LBM_RELOAD_CONTINUE) {
+        if (!scan.has_cont) return fail(h, LBM_ERR_IO, why);
+        if (!why.empty()) return fail(h, LBM_ERR_PARAM, why);
+        cont = true;
+    } else if (mode == LBM_RELOAD_AUTO) {
+        cont = scan.has_cont && why.empty();
+    }
+    int st;
+    if (!h->initialised && (st = lbm_initial(h)) != LBM_OK) return st;
+    CK(h, cudaStreamSynchronize(h->stream));
+    std::rewind(file.fp);
+    const bool fp64 = h->p.precision == LBM_FP64;
+    Pinned pin;
+    if ((st = pinned_for(h, pin, (size_t)h->q * n * sizeof(double))) != LBM_OK) return st;
+    // from here on a failure leaves the state partly overwritten
+    h->initialised = false;
+    auto lost = [h](int s) {
+        h->err = "reload failed, lattice state lost: " + h->err;
+        return s;
+    };
+    // a temporary set of FP64 module arrays for FP32/FP16 handles (reference reconstruction)
+    std::vector<void*> tmp;
+    struct TmpFree {
+        std::vector<void*>& v;
+        ~TmpFree() {
+            for (void* p : v) cudaFree(p);
+        }
+    } tmp_free{tmp};
+    ExactArrays X = h->A;
+    if (!fp64 && !cont) {
+        auto talloc = [&](double** p, size_t cnt) {
+            void* q = nullptr;
+            cudaError_t e = cudaMalloc(&q, cnt * sizeof(double));
+            if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc");
+            tmp.push_back(q);
+            *p = (double*)q;
+            return LBM_OK;
+        };
+        X = ExactArrays{};
+        double** scal[] = {&X.rho, &X.u, &X.v, &X.w, &X.T, &X.Bx, &X.By, &X.Bz, &X.Fx, &X.Fy};
+        if ((st = talloc(&X.f, (size_t)h->q * n)) != LBM_OK || (st = talloc(&X.g, (size_t)h->qt * n)) != LBM_OK)
+            return lost(st);
+        for (double** p : scal)
+            if ((st = talloc(p, n)) != LBM_OK) return lost(st);
+    }
+    // records 1 and 2: f and g
+    if (fp64 || !cont) {
+        if ((st = read_device_record(h, file.fp, X.f, (size_t)h->q * n * sizeof(double), pin)) != LBM_OK) return lost(st);
+        if ((st = read_device_record(h, file.fp, X.g, (size_t)h->qt * n * sizeof(double), pin)) != LBM_OK) return lost(st);
+    } else {
+        RecordReader r1, r2;
+        if (!(r1.begin(file.fp) && r1.skip_rest() && r2.begin(file.fp) && r2.skip_rest()))
+            return lost(fail(h, LBM_ERR_IO, "restart file truncated"));
+    }
+    if (fp64) {
+        h->A.fpost = h->fbuf[0];
+        h->A.gpost = h->gbuf[0];
+        h->cur = 0;
+        h->fused_valid = false;
+    } else {
+        h->F.cur = 0;
+        h->F.ahead = false;
+    }
+    if (cont) {
+        RecordReader rh;
+        if (!(rh.begin(file.fp) && rh.skip_rest())) return lost(fail(h, LBM_ERR_IO, "restart file truncated"));
+        const int form = (int)scan.hdr[7];
+        for (const ContArray& a : cont_arrays(h, form))
+            if ((st = read_device_record(h, file.fp, a.dptr, a.bytes, pin)) != LBM_OK) return lost(st);
+        if (!fp64) h->F.fused_valid = form == kFormFastFused;
+        h->itc = scan.hdr[8];
+        h->reload_form = 1;
+        h->initialised = true;
+        return LBM_OK;
+    }
+    // reference reconstruction
+    unsigned int* bad = (unsigned int*)h->d_part;
+    CK(h, cudaMemsetAsync(bad, 0, sizeof(unsigned int), h->stream));
+    exact_reconstruct(h->geo, h->phys, X, h->dim, bad, h->stream);
+    CK_LAUNCH(h, "reconstruct");
+    if (!fp64) {
+        const bool d3 = h->dim == 3;
+        FastState& F = h->F;
+        if ((st = fast_import(F, h->geo, h->phys, h->dim, LBM_FIELD_F, X.f, h->stream, true)) != LBM_OK ||
+            (st = fast_import(F, h->geo, h->phys, h->dim, LBM_FIELD_G, X.g, h->stream, true)) != LBM_OK)
+            return lost(fail(h, st, "population import failed"));
+        std::vector<std::pair<int, const double*>> fields = {
+            {LBM_FIELD_RHO, X.rho}, {LBM_FIELD_U, X.u}, {LBM_FIELD_V, X.v}, {LBM_FIELD_T, X.T}};
+        if (d3) {
+            fields.push_back({LBM_FIELD_W, X.w});
+            fields.push_back({LBM_FIELD_BX_PREV, X.Bx});
+            fields.push_back({LBM_FIELD_BY_PREV, X.By});
+            fields.push_back({LBM_FIELD_BZ_PREV, X.Bz});
+        } else {
+            fields.push_back({LBM_FIELD_FY, X.Fy});
+            if (h->p.use_g) {
+                fields.push_back({LBM_FIELD_BX_PREV, X.Bx});
+                fields.push_back({LBM_FIELD_BY_PREV, X.By});
+            }
+        }
+        for (auto& fv : fields)
+            if ((st = fast_import(F, h->geo, h->phys, h->dim, fv.first, fv.second, h->stream)) != LBM_OK)
+                return lost(fail(h, st, "field import failed"));
+        CK_LAUNCH(h, "import");
+    }
+    // initial after a reload: up = vp = wp = Tp = 0 (3DRB.F90:627-632, steadyFlow)
+    const size_t es = fp64 ? sizeof(double) : sizeof(float);
+    void* prev[4] = {fp64 ? (void*)h->A.up : (void*)h->F.up, fp64 ? (void*)h->A.vp : (void*)h->F.vp,
+                     fp64 ? (void*)h->A.wp : (void*)h->F.wp, fp64 ? (void*)h->A.Tp : (void*)h->F.Tp};
+    for (void* p : prev)
+        if (p) CK(h, cudaMemsetAsync(p, 0, n * es, h->stream));
+    unsigned int hbad = 0;
+    CK(h, cudaMemcpyAsync(&hbad, bad, sizeof(hbad), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (hbad) return fail(h, LBM_ERR_DIVERGED, "non-positive rho found during restart reconstruction");
+    h->itc = 0;
+    h->reload_form = 0;
+    h->initialised = true;
+    return LBM_OK;
+}
+
+extern "C" int lbm_reload_form(const lbm_handle* h) { return h ? h->reload_form : -1; }
 
 // ------------------------------------------------------------------------------------
 // measurement hooks

@@ -701,6 +701,76 @@ __global__ void k_materialize(Geo g, PhysC P, ExactArrays A, const double* __res
 }
 
 // ------------------------------------------------------------------------------------
+// restart reconstruction (reconstruct_macro_from_fg, 2DRB.F90:1144-1200,
+// 3DRB.F90:1392-1463): T = sum g (the macroT call), rho = sum f, u = (mom + F/2)/rho with
+// F = rho gBeta (T - Tref).  The reference iterates that assignment three times; the
+// right-hand side does not depend on u, so one evaluation gives the same value.
+// ------------------------------------------------------------------------------------
+template <int D>
+__global__ void k_reconstruct(Geo g, PhysC P, ExactArrays A, unsigned int* bad) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    const long long n = g.ncell;
+    constexpr int QT = (D == 2) ? 5 : 7;
+    double G[QT];
+#pragma unroll
+    for (int a = 0; a < QT; ++a) G[a] = A.g[a * n + c];
+    const double T = sumT<QT>(G);
+    A.T[c] = T;
+    if (D == 2) {
+        double F[9];
+#pragma unroll
+        for (int a = 0; a < 9; ++a) F[a] = A.f[a * n + c];
+        const double rho = F[0] + F[1] + F[2] + F[3] + F[4] + F[5] + F[6] + F[7] + F[8];
+        const double momx = F[1] - F[3] + F[5] - F[6] - F[7] + F[8];
+        const double momy = F[2] - F[4] + F[5] + F[6] - F[7] - F[8];
+        double u = 0.0, v = 0.0, Fx = 0.0, Fy = 0.0;
+        if (rho > 0.0) {
+            Fy = rho * P.gBeta * (T - P.Tref);
+            u = (momx + 0.5 * Fx) / rho;
+            v = (momy + 0.5 * Fy) / rho;
+        } else {
+            *bad = 1u;
+        }
+        A.rho[c] = rho;
+        A.u[c] = u;
+        A.v[c] = v;
+        A.Fx[c] = Fx;
+        A.Fy[c] = Fy;
+        if (P.use_g) {  // without EnableUseG the 2D reconstruction leaves B_prev as it is
+            A.Bx[c] = u * T;
+            A.By[c] = v * T;
+        }
+    } else {
+        double f[19];
+#pragma unroll
+        for (int a = 0; a < 19; ++a) f[a] = A.f[a * n + c];
+        const double rho = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8] + f[9] + f[10] + f[11] + f[12]
+                           + f[13] + f[14] + f[15] + f[16] + f[17] + f[18];
+        const double momx = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+        const double momy = f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
+        const double momz = f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
+        double u = 0.0, v = 0.0, w = 0.0;
+        if (rho > 0.0) {
+            const double FxLoc = 0.0, FyLoc = rho * P.gBeta * (T - P.Tref), FzLoc = 0.0;
+            u = (momx + 0.5 * FxLoc) / rho;
+            v = (momy + 0.5 * FyLoc) / rho;
+            w = (momz + 0.5 * FzLoc) / rho;
+        } else {
+            *bad = 1u;
+        }
+        A.rho[c] = rho;
+        A.u[c] = u;
+        A.v[c] = v;
+        A.w[c] = w;
+        A.Bx[c] = P.use_g ? u * T : 0.0;
+        A.By[c] = P.use_g ? v * T : 0.0;
+        A.Bz[c] = P.use_g ? w * T : 0.0;
+    }
+}
+
+// ------------------------------------------------------------------------------------
 // host launchers
 // ------------------------------------------------------------------------------------
 static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -763,6 +833,13 @@ void exact_fused_step(const Geo& g, const PhysC& P, const ExactArrays& A, int di
             if (th) k_thermal<3, false><<<nb, 128, 0, s>>>(g, P, A, fnext, gprev, gnext);
         }
     }
+}
+
+void exact_reconstruct(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, unsigned int* bad,
+                       cudaStream_t s) {
+    const unsigned nb = nblocks(g.ncell, 128);
+    if (dim == 2) k_reconstruct<2><<<nb, 128, 0, s>>>(g, P, A, bad);
+    else k_reconstruct<3><<<nb, 128, 0, s>>>(g, P, A, bad);
 }
 
 void exact_materialize(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, const double* fcur,

@@ -118,25 +118,25 @@ __global__ void k_fast_materialize(Geo g, PhysF P, FastArgs<S> A, const S* __res
 
 // export / import (FP64 Fortran layout)
 template <int Q, class S>
-__global__ void k_export_pop(const S* __restrict__ soa, double* __restrict__ aos, long long n, int thermal, double w0,
-                             double w1) {
+__global__ void k_export_pop(const S* __restrict__ soa, double* __restrict__ out, long long n, int thermal, double w0,
+                             double w1, int out_soa) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)Q * n) return;
     const long long c = e / Q;
     const int a = (int)(e - c * Q);
     const double rest = thermal ? (a == 0 ? w0 : w1) : wrest<(Q == 9 || Q == 5) ? 9 : 19>(a);
-    aos[e] = rest + (double)ldS(soa, (long long)a * n + c);
+    out[out_soa ? (long long)a * n + c : e] = rest + (double)ldS(soa, (long long)a * n + c);
 }
 
 template <int Q, class S>
-__global__ void k_import_pop(const double* __restrict__ aos, S* __restrict__ soa, long long n, int thermal, double w0,
-                             double w1) {
+__global__ void k_import_pop(const double* __restrict__ in, S* __restrict__ soa, long long n, int thermal, double w0,
+                             double w1, int in_soa) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)Q * n) return;
     const long long c = e / Q;
     const int a = (int)(e - c * Q);
     const double rest = thermal ? (a == 0 ? w0 : w1) : wrest<(Q == 9 || Q == 5) ? 9 : 19>(a);
-    soa[(long long)a * n + c] = toS<S>((float)(aos[e] - rest));
+    soa[(long long)a * n + c] = toS<S>((float)(in[in_soa ? (long long)a * n + c : e] - rest));
 }
 
 __global__ void k_f2d(const float* __restrict__ x, double* __restrict__ y, long long n) {
@@ -273,7 +273,8 @@ DiagFields<float> fast_diag_fields(const FastState& F) {
     return DiagFields<float>{F.u, F.v, F.w, F.T, F.rho, F.up, F.vp, F.wp, F.Tp};
 }
 
-int fast_export(const FastState& F, const Geo& g, const PhysC& P, int dim, int field, double* out, cudaStream_t s) {
+int fast_export(const FastState& F, const Geo& g, const PhysC& P, int dim, int field, double* out, cudaStream_t s,
+                bool soa) {
     const long long n = g.ncell;
     const bool d3 = dim == 3;
     const double wt0 = P.omegaT0 * P.Tref, wt1 = P.omegaT1 * P.Tref;
@@ -284,11 +285,11 @@ int fast_export(const FastState& F, const Geo& g, const PhysC& P, int dim, int f
         const int q = th ? F.qt : F.q;
         DISPATCH_S(F, {
             if (d3) {
-                if (th) k_export_pop<7, S><<<nb(q * n, 256), 256, 0, s>>>((const S*)src, out, n, 1, wt0, wt1);
-                else k_export_pop<19, S><<<nb(q * n, 256), 256, 0, s>>>((const S*)src, out, n, 0, 0, 0);
+                if (th) k_export_pop<7, S><<<nb(q * n, 256), 256, 0, s>>>((const S*)src, out, n, 1, wt0, wt1, soa);
+                else k_export_pop<19, S><<<nb(q * n, 256), 256, 0, s>>>((const S*)src, out, n, 0, 0, 0, soa);
             } else {
-                if (th) k_export_pop<5, S><<<nb(q * n, 256), 256, 0, s>>>((const S*)src, out, n, 1, wt0, wt1);
-                else k_export_pop<9, S><<<nb(q * n, 256), 256, 0, s>>>((const S*)src, out, n, 0, 0, 0);
+                if (th) k_export_pop<5, S><<<nb(q * n, 256), 256, 0, s>>>((const S*)src, out, n, 1, wt0, wt1, soa);
+                else k_export_pop<9, S><<<nb(q * n, 256), 256, 0, s>>>((const S*)src, out, n, 0, 0, 0, soa);
             }
         });
         return LBM_OK;
@@ -312,7 +313,8 @@ int fast_export(const FastState& F, const Geo& g, const PhysC& P, int dim, int f
     return LBM_OK;
 }
 
-int fast_import(FastState& F, const Geo& g, const PhysC& P, int dim, int field, const double* in, cudaStream_t s) {
+int fast_import(FastState& F, const Geo& g, const PhysC& P, int dim, int field, const double* in, cudaStream_t s,
+                bool soa) {
     const long long n = g.ncell;
     const bool d3 = dim == 3;
     const double wt0 = P.omegaT0 * P.Tref, wt1 = P.omegaT1 * P.Tref;
@@ -322,11 +324,11 @@ int fast_import(FastState& F, const Geo& g, const PhysC& P, int dim, int field, 
         const int q = th ? F.qt : F.q;
         DISPATCH_S(F, {
             if (d3) {
-                if (th) k_import_pop<7, S><<<nb(q * n, 256), 256, 0, s>>>(in, (S*)dst, n, 1, wt0, wt1);
-                else k_import_pop<19, S><<<nb(q * n, 256), 256, 0, s>>>(in, (S*)dst, n, 0, 0, 0);
+                if (th) k_import_pop<7, S><<<nb(q * n, 256), 256, 0, s>>>(in, (S*)dst, n, 1, wt0, wt1, soa);
+                else k_import_pop<19, S><<<nb(q * n, 256), 256, 0, s>>>(in, (S*)dst, n, 0, 0, 0, soa);
             } else {
-                if (th) k_import_pop<5, S><<<nb(q * n, 256), 256, 0, s>>>(in, (S*)dst, n, 1, wt0, wt1);
-                else k_import_pop<9, S><<<nb(q * n, 256), 256, 0, s>>>(in, (S*)dst, n, 0, 0, 0);
+                if (th) k_import_pop<5, S><<<nb(q * n, 256), 256, 0, s>>>(in, (S*)dst, n, 1, wt0, wt1, soa);
+                else k_import_pop<9, S><<<nb(q * n, 256), 256, 0, s>>>(in, (S*)dst, n, 0, 0, 0, soa);
             }
         });
         F.fused_valid = false;

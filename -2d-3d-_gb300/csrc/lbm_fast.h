@@ -59,8 +59,11 @@ inline bool fast_fused_valid(const FastState& F) { return F.fused_valid; }
 inline bool fast_at_origin(const FastState& F) { return F.cur == 0; }
 DiagFields<float> fast_diag_fields(const FastState& F);
 // Export a field to an FP64 device buffer in the reference's Fortran layout (AoS for
-// populations); import the reverse.  Return LBM_OK or LBM_ERR_STATE / LBM_ERR_PARAM.
-int fast_export(const FastState& F, const Geo& g, const PhysC& P, int dim, int field, double* out, cudaStream_t s);
-int fast_import(FastState& F, const Geo& g, const PhysC& P, int dim, int field, const double* in, cudaStream_t s);
+// populations, or direction-major SoA with soa = true); import the reverse.  Return LBM_OK
+// or LBM_ERR_STATE / LBM_ERR_PARAM.
+int fast_export(const FastState& F, const Geo& g, const PhysC& P, int dim, int field, double* out, cudaStream_t s,
+                bool soa = false);
+int fast_import(FastState& F, const Geo& g, const PhysC& P, int dim, int field, const double* in, cudaStream_t s,
+                bool soa = false);
 
 }  // namespace lbm

@@ -54,6 +54,11 @@ void exact_fused_step(const Geo& g, const PhysC& P, const ExactArrays& A, int di
 void exact_materialize(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, const double* fcur,
                        const double* gcur, cudaStream_t s);
 
+// Restart: rebuild T, rho, u, v, w, B_prev and the 2D force from the SoA populations A.f,
+// A.g (reconstruct_macro_from_fg); sets *bad = 1 when some cell has rho <= 0.
+void exact_reconstruct(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, unsigned int* bad,
+                       cudaStream_t s);
+
 // ---- reductions (lbm_reduce.cu) ---------------------------------------------------------
 // Fields read by the diagnostics (FP64 or FP32 device arrays of ncell values).
 template <class S>

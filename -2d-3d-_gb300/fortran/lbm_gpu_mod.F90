@@ -27,6 +27,9 @@ module lbm_gpu_mod
 
   integer(c_int), parameter :: LBM_OK = 0, LBM_ERR_PARAM = 1, LBM_ERR_CUDA = 2, LBM_ERR_OOM = 3
   integer(c_int), parameter :: LBM_ERR_DIVERGED = 4, LBM_ERR_TIMEOUT = 5, LBM_ERR_STATE = 6
+  integer(c_int), parameter :: LBM_ERR_TOO_LARGE = 7, LBM_ERR_IO = 8
+  integer(c_int), parameter :: LBM_BACKUP_REFERENCE = 0, LBM_BACKUP_CONTINUE = 1
+  integer(c_int), parameter :: LBM_RELOAD_REFERENCE = 0, LBM_RELOAD_CONTINUE = 1, LBM_RELOAD_AUTO = 2
   integer(c_int), parameter :: LBM_CELL_RB = 0, LBM_CELL_SIDE = 1
   integer(c_int), parameter :: LBM_BC_NOSLIP = 0, LBM_BC_PERIODIC = 1
   integer(c_int), parameter :: LBM_BCT_CONST = 0, LBM_BCT_ADIABATIC = 1, LBM_BCT_PERIODIC = 2
@@ -140,6 +143,20 @@ module lbm_gpu_mod
       integer(c_int), value :: field
       real(c_double), intent(in) :: host(*)
       integer(c_size_t), value :: count
+    end function
+    ! restart files: call lbm_backupData(h, 'backupFile3D-'//trim(filename)//'.bin'//c_null_char, LBM_BACKUP_CONTINUE)
+    ! replaces backupData; lbm_reload replaces the loadInitField = 1 branch of initial
+    integer(c_int) function lbm_backupData(h, path, flags) bind(C, name="lbm_backupData")
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: h
+      character(kind=c_char), intent(in) :: path(*)
+      integer(c_int), value :: flags
+    end function
+    integer(c_int) function lbm_reload(h, path, mode) bind(C, name="lbm_reload")
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: h
+      character(kind=c_char), intent(in) :: path(*)
+      integer(c_int), value :: mode
     end function
   end interface
 end module lbm_gpu_mod

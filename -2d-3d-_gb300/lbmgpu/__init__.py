@@ -16,8 +16,9 @@ import os
 
 import numpy as np
 
-from .abi import (FIELDS, LBM_FP64, LBM_OK, STATUS_NAMES, LbmConstants, LbmNuWall, LbmParams, field_shape,
-                  field_size, rb_params)
+from .abi import (FIELDS, LBM_BACKUP_CONTINUE, LBM_BACKUP_REFERENCE, LBM_FP64, LBM_OK, LBM_RELOAD_AUTO,
+                  LBM_RELOAD_CONTINUE, LBM_RELOAD_REFERENCE, STATUS_NAMES, LbmConstants, LbmNuWall, LbmParams,
+                  field_shape, field_size, rb_params)
 
 __all__ = ["Lattice", "Ensemble", "LbmError", "LbmDiverged", "LbmParams", "rb_params", "load_library",
            "library_path", "params_default", "derive_constants", "footprint", "FIELDS"]
@@ -67,6 +68,12 @@ SIGNATURES = {
     "lbm_ensemble_get_stream": ([_vp, C.POINTER(_vp)], _i32),
     "lbm_ensemble_last_error": ([_vp], C.c_char_p),
     "lbm_ensemble_autotune": ([_vp, _i32, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32)], _i32),
+    "lbm_backupData": ([_vp, C.c_char_p, _i32], _i32),
+    "lbm_reload": ([_vp, C.c_char_p, _i32], _i32),
+    "lbm_reload_form": ([_vp], _i32),
+    "lbm_fortran_record_write": ([C.c_char_p, _i32, _vp, _sz], _i32),
+    "lbm_fortran_record_read": ([C.c_char_p, C.c_uint64, _vp, _sz, C.POINTER(_sz), C.POINTER(C.c_uint64)], _i32),
+    "lbm_fortran_set_subrecord_limit": ([_sz], _i32),
 }
 LBM_OPT_SINGLE_KERNEL = 1
 LBM_OPT_KCHUNK = 2
@@ -243,6 +250,21 @@ class Lattice:
         a, b = C.c_double(), C.c_double()
         self._ck(self.lib.lbm_time_kernels(self._h, int(nsteps), C.byref(a), C.byref(b)), "lbm_time_kernels")
         return a.value, b.value
+
+    # -- restart files (backupData / loadInitField = 1) --------------------------------------
+    def backupData(self, path, continuation=True):
+        """Write the reference's restart file (f and g records, 3DRB.F90:1638-1665); with
+        continuation=True also the records that make a reload bit-continuous."""
+        flags = LBM_BACKUP_CONTINUE if continuation else LBM_BACKUP_REFERENCE
+        self._ck(self.lib.lbm_backupData(self._h, os.fsencode(path), flags), "backupData")
+
+    def reload(self, path, mode="auto"):
+        """Replace the state from a restart file.  mode: "reference" (f, g and
+        reconstruct_macro_from_fg), "continue" (bit-continuous records required) or "auto".
+        Returns the form used: "reference" or "continue"."""
+        m = {"reference": LBM_RELOAD_REFERENCE, "continue": LBM_RELOAD_CONTINUE, "auto": LBM_RELOAD_AUTO}[mode]
+        self._ck(self.lib.lbm_reload(self._h, os.fsencode(path), m), "reload")
+        return "continue" if self.lib.lbm_reload_form(self._h) == 1 else "reference"
 
     # -- state transfer (Fortran layout) ------------------------------------------------
     def get_state(self, field):

@@ -8,7 +8,11 @@ import math
 
 LBM_OK, LBM_ERR_PARAM, LBM_ERR_CUDA, LBM_ERR_OOM, LBM_ERR_DIVERGED, LBM_ERR_TIMEOUT, LBM_ERR_STATE = range(7)
 STATUS_NAMES = {0: "LBM_OK", 1: "LBM_ERR_PARAM", 2: "LBM_ERR_CUDA", 3: "LBM_ERR_OOM",
-                4: "LBM_ERR_DIVERGED", 5: "LBM_ERR_TIMEOUT", 6: "LBM_ERR_STATE", 7: "LBM_ERR_TOO_LARGE"}
+                4: "LBM_ERR_DIVERGED", 5: "LBM_ERR_TIMEOUT", 6: "LBM_ERR_STATE", 7: "LBM_ERR_TOO_LARGE",
+                8: "LBM_ERR_IO"}
+LBM_ERR_IO = 8
+LBM_BACKUP_REFERENCE, LBM_BACKUP_CONTINUE = 0, 1
+LBM_RELOAD_REFERENCE, LBM_RELOAD_CONTINUE, LBM_RELOAD_AUTO = 0, 1, 2
 
 LBM_CELL_RB, LBM_CELL_SIDE = 0, 1
 LBM_BC_NOSLIP, LBM_BC_PERIODIC = 0, 1

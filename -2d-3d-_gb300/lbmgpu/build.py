@@ -5,6 +5,7 @@ Translation units and their floating-point flags:
   lbm_reduce.cu -fmad=false : FP64 diagnostics, per-cell terms rounded as in the reference
   lbm_fast.cu               : FP32 arithmetic on FP32/FP16 storage, FMA contraction allowed
   lbm_api.cpp               : host code (-ffp-contract=off for the host-side fits)
+  lbm_checkpoint.cpp        : Fortran unformatted sequential records (restart files)
 The units compile in parallel; a full build takes well under two minutes.
 """
 import concurrent.futures as cf
@@ -30,6 +31,7 @@ UNITS = [
     ("lbm_fused.cu", ["-fmad=true"]),
     ("lbm_ensemble.cu", ["-fmad=true"]),
     ("lbm_api.cpp", []),
+    ("lbm_checkpoint.cpp", []),
     ("lbm_noalloc.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
 ]
 

@@ -37,6 +37,7 @@ extern "C" {
 #define LBM_ERR_DIVERGED  4 /* non-finite value or rho <= 0 found by a diagnostic      */
 #define LBM_ERR_TIMEOUT   5 /* a bounded device-side wait gave up                      */
 #define LBM_ERR_STATE     6 /* call not valid for this handle (e.g. precision)         */
+#define LBM_ERR_IO        8 /* a file could not be opened, written or parsed            */
 
 /* ---- cell type: CPP switches RayleighBenardCell / SideHeatedCell (3DRB.F90:23-37) --- */
 #define LBM_CELL_RB   0 /* heated from below: lengthUnit = ny                            */
@@ -241,6 +242,51 @@ int lbm_selftest_const_division(int64_t n, uint64_t seed, int64_t* mismatches);
 int lbm_calNuRe_noalloc(const double* u, const double* v, const double* w, const double* T, int64_t ncell,
                         int side_heated, double lengthUnit, double diffusivity, double viscosity,
                         void* stream, double* Nu, double* Re);
+
+/* ---- restart files (backupData, 3DRB.F90:1638-1665 / 2DRB.F90:1402-1430; reload,
+ *      3DRB.F90:602-623 / 2DRB.F90:621-637; reconstruct_macro_from_fg,
+ *      3DRB.F90:1392-1463 / 2DRB.F90:1144-1200) -----------------------------------------
+ * lbm_backupData writes the reference's file: two Fortran unformatted sequential records
+ * (gfortran framing: 4-byte length markers, subrecords above 2^31-9 bytes) holding
+ * f(alpha,i,j,k) and g(alpha,i,j,k) as FP64, direction outermost and x fastest.  FP32/FP16
+ * handles write their populations converted to FP64.  With LBM_BACKUP_CONTINUE the file
+ * continues with extra records (a 16 x int64 header, then one record per array in the
+ * handle's own storage type) that make the restart bit-continuous: the reference's own
+ * reader reads the first two records and never sees them.  The reference's file name is
+ * backupFile-<n>.bin (2D) / backupFile3D-<n>.bin (3D); the caller passes the path.
+ *
+ * lbm_reload replaces the state of a handle (initialised or not, not an ensemble member):
+ *   LBM_RELOAD_REFERENCE  read f and g, then rebuild T = sum g, rho, u (3 fixed-point
+ *                         passes with F = rho gBeta (T - Tref)), B_prev = u T, 2D Fx/Fy, as
+ *                         reconstruct_macro_from_fg does; zero up..Tp and itc.  Not bit-
+ *                         continuous: the running solver's u and B_prev used T of the
+ *                         previous step.  A cell with rho <= 0 gives LBM_ERR_DIVERGED (the
+ *                         reference stops) and leaves the handle uninitialised.
+ *   LBM_RELOAD_CONTINUE   read the continuation records too (error LBM_ERR_IO if absent,
+ *                         LBM_ERR_PARAM if they were written for another lattice size or
+ *                         precision); the next lbm_step continues the saved run bit for bit
+ *                         and lbm_itc resumes from the saved count.
+ *   LBM_RELOAD_AUTO       CONTINUE when the records are there and match, else REFERENCE. */
+#define LBM_BACKUP_REFERENCE 0
+#define LBM_BACKUP_CONTINUE  1
+#define LBM_RELOAD_REFERENCE 0
+#define LBM_RELOAD_CONTINUE  1
+#define LBM_RELOAD_AUTO      2
+int lbm_backupData(lbm_handle* h, const char* path, int flags);
+int lbm_reload(lbm_handle* h, const char* path, int mode);
+/* Which form lbm_reload used last on this handle: 0 reference reconstruction, 1 continuation. */
+int lbm_reload_form(const lbm_handle* h);
+
+/* Fortran record I/O underneath (host only, no GPU needed).  lbm_fortran_record_write
+ * writes one record (append != 0 adds it at the end of the file).  lbm_fortran_record_read
+ * reads the record that starts at byte `offset` into `data` (up to `capacity` bytes) and
+ * returns its length and the offset of the next record; LBM_ERR_TOO_LARGE if the record
+ * is longer than `capacity`.  lbm_fortran_set_subrecord_limit lowers the subrecord size
+ * (default and maximum 2^31-9) so the subrecord framing can be exercised on small data. */
+int lbm_fortran_record_write(const char* path, int append, const void* data, size_t nbytes);
+int lbm_fortran_record_read(const char* path, uint64_t offset, void* data, size_t capacity, size_t* nbytes,
+                            uint64_t* next_offset);
+int lbm_fortran_set_subrecord_limit(size_t max_subrecord_bytes);
 
 #ifdef __cplusplus
 }

@@ -16,6 +16,7 @@
 
 #include "lbm_oracle.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -1044,6 +1045,77 @@ extern "C" void ora_collisionT(ora_handle* h) { h->d3 ? collisionT3d(h) : collis
 extern "C" void ora_streamingT(ora_handle* h) { h->d3 ? streamingT3d(h) : streamingT2d(h); }
 extern "C" void ora_bouncebackT(ora_handle* h) { h->d3 ? bouncebackT3d(h) : bouncebackT2d(h); }
 extern "C" void ora_macroT(ora_handle* h) { h->d3 ? macroT3d(h) : macroT2d(h); }
+
+// ------------------------------------------------------------------------------------
+// restart: reconstruct_macro_from_fg (2DRB.F90:1144-1200, 3DRB.F90:1392-1463), called by
+// initial after loadInitField = 1 has read f and g (2DRB.F90:621-637, 3DRB.F90:602-623);
+// initial then zeroes up, vp, wp, Tp (steadyFlow, 3DRB.F90:627-632) and the time loop
+// starts from itc = 0.  The three fixed-point iterations of the reference do not depend
+// on u, so one pass gives the same values.  Returns 1 if some cell had rho <= 0 (the
+// reference stops there), else 0.
+// ------------------------------------------------------------------------------------
+extern "C" int ora_reconstruct_macro_from_fg(ora_handle* h) {
+    ora_macroT(h);
+    const double gBeta = h->c.gBeta, Tref = h->c.Tref;
+    const bool useG = h->p.use_g != 0;
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (long long ci = 0; ci < (long long)h->ncell; ++ci) {
+        const double T = h->T[ci];
+        if (h->d3) {
+            const double* f = &h->f[19 * ci];
+            const double rho = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8] + f[9] + f[10] + f[11]
+                               + f[12] + f[13] + f[14] + f[15] + f[16] + f[17] + f[18];
+            const double momx = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+            const double momy = f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
+            const double momz = f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
+            h->rho[ci] = rho;
+            double u = 0.0, v = 0.0, w = 0.0;
+            if (rho > 0.0) {
+                const double FxLoc = 0.0, FyLoc = rho * gBeta * (T - Tref), FzLoc = 0.0;
+                u = (momx + 0.5 * FxLoc) / rho;
+                v = (momy + 0.5 * FyLoc) / rho;
+                w = (momz + 0.5 * FzLoc) / rho;
+            } else {
+                bad = 1;
+            }
+            h->u[ci] = u;
+            h->v[ci] = v;
+            h->w[ci] = w;
+            h->Bx[ci] = useG ? u * T : 0.0;
+            h->By[ci] = useG ? v * T : 0.0;
+            h->Bz[ci] = useG ? w * T : 0.0;
+        } else {
+            const double* f = &h->f[9 * ci];
+            const double rho = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8];
+            const double momx = f[1] - f[3] + f[5] - f[6] - f[7] + f[8];
+            const double momy = f[2] - f[4] + f[5] + f[6] - f[7] - f[8];
+            h->rho[ci] = rho;
+            double u = 0.0, v = 0.0, Fx = 0.0, Fy = 0.0;
+            if (rho > 0.0) {
+                Fy = rho * gBeta * (T - Tref);
+                u = (momx + 0.5 * Fx) / rho;
+                v = (momy + 0.5 * Fy) / rho;
+            } else {
+                bad = 1;
+            }
+            h->u[ci] = u;
+            h->v[ci] = v;
+            h->Fx[ci] = Fx;
+            h->Fy[ci] = Fy;
+            if (useG) {  // 2DRB.F90:1189-1192: without EnableUseG B_prev is left as it is
+                h->Bx[ci] = u * T;
+                h->By[ci] = v * T;
+            }
+        }
+    }
+    std::fill(h->up.begin(), h->up.end(), 0.0);
+    std::fill(h->vp.begin(), h->vp.end(), 0.0);
+    std::fill(h->wp.begin(), h->wp.end(), 0.0);
+    std::fill(h->Tp.begin(), h->Tp.end(), 0.0);
+    h->itc = 0;
+    return bad;
+}
 
 extern "C" void ora_step(ora_handle* h, long long nsteps) {
     for (long long s = 0; s < nsteps; ++s) {

@@ -42,6 +42,10 @@ void ora_macroT(ora_handle* h);
 /* nsteps iterations of the time loop body (3DRB.F90:227-243), without check/output. */
 void ora_step(ora_handle* h, long long nsteps);
 
+/* Restart: rebuild T, rho, u, v, w, B_prev (and the 2D force) from f and g as
+ * reconstruct_macro_from_fg does; zero up..Tp and itc.  Returns 1 if some rho <= 0. */
+int ora_reconstruct_macro_from_fg(ora_handle* h);
+
 int ora_check(ora_handle* h, double* errU, double* errT);
 int ora_calNuRe(ora_handle* h, double* Nu, double* Re);
 int ora_RBcalc_Nu_global(ora_handle* h, double* Nu);

@@ -63,6 +63,8 @@ def lib():
             fn.restype = None
         L.ora_step.argtypes = [vp, C.c_longlong]
         L.ora_step.restype = None
+        L.ora_reconstruct_macro_from_fg.argtypes = [vp]
+        L.ora_reconstruct_macro_from_fg.restype = i32
         L.ora_check.argtypes = [vp, dp, dp]
         L.ora_calNuRe.argtypes = [vp, dp, dp]
         L.ora_RBcalc_Nu_global.argtypes = [vp, dp]
@@ -130,6 +132,10 @@ class Oracle:
 
     def step(self, n=1):
         lib().ora_step(self._h, int(n))
+
+    def reconstruct_macro_from_fg(self):
+        """Restart reconstruction (2DRB.F90:1144-1200, 3DRB.F90:1392-1463); True if some rho <= 0."""
+        return bool(lib().ora_reconstruct_macro_from_fg(self._h))
 
     def check(self):
         a, b = C.c_double(), C.c_double()

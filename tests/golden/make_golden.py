@@ -234,6 +234,10 @@ FIELDS_OUT = {2: ["f", "g", "rho", "u", "v", "T", "Bx_prev", "By_prev", "Fx", "F
               3: ["f", "g", "rho", "u", "v", "w", "T", "Bx_prev", "By_prev", "Bz_prev", "f_post", "g_post"]}
 
 
+RESTART_OUT = {2: ["rho", "u", "v", "T", "Bx_prev", "By_prev", "Fx", "Fy"],
+               3: ["rho", "u", "v", "w", "T", "Bx_prev", "By_prev", "Bz_prev"]}
+
+
 def to_fortran_layout(arr, inner, pop):
     """numpy array with Fortran index ranges -> the (nz,)ny,nx(,q) C-order layout of
     lbm_get_state (direction fastest, x next)."""
@@ -273,11 +277,17 @@ def step_fixture(ref_dir, case):
     out = {}
     for name in FIELDS_OUT[dim]:
         out["in_" + name] = to_fortran_layout(ns[name], inner, name in ("f", "g", "f_post", "g_post"))
-    subs = ReferenceSubroutines(path, defines)
+    subs = ReferenceSubroutines(path, defines, extra=("reconstruct_macro_from_fg",))
     for _ in range(case["steps"]):
         subs.step(ns)
     for name in FIELDS_OUT[dim]:
         out["out_" + name] = to_fortran_layout(ns[name], inner, name in ("f", "g", "f_post", "g_post"))
+    # restart from the stepped f and g: initial with loadInitField = 1 reads them and calls
+    # reconstruct_macro_from_fg, whose first statement (call macroT) the translation drops
+    subs.run("macroT", ns)
+    subs.run("reconstruct_macro_from_fg", ns)
+    for name in RESTART_OUT[dim]:
+        out["rst_" + name] = to_fortran_layout(ns[name], inner, False)
     meta = {k: v for k, v in case.items() if k != "defines"}
     meta["defines"] = sorted(defines)
     meta["constants"] = {k: consts[k] for k in ("tauf", "viscosity", "diffusivity", "gBeta", "Qk", "paraA")}
@@ -288,6 +298,9 @@ STEP_CASES = [
     dict(name="rb2d_periodic", dim=2, nx=10, ny=6, Ra=1e5, Pr=0.71, Mach=0.1 * math.sqrt(3.0), steps=4, seed=7,
          defines=["steadyFlow", "HorizontalWallsNoslip", "VerticalWallsPeriodicalU", "RayleighBenardCell",
                   "HorizontalWallsConstT", "VerticalWallsPeriodicalT", "EnableUseG"]),
+    dict(name="rb2d_noslip_nog", dim=2, nx=8, ny=7, Ra=2e4, Pr=7.0, Mach=0.1, steps=2, seed=11,
+         defines=["steadyFlow", "HorizontalWallsNoslip", "VerticalWallsNoslip", "RayleighBenardCell",
+                  "HorizontalWallsConstT", "VerticalWallsAdiabatic"]),
     dict(name="rb3d_noslip", dim=3, nx=6, ny=5, nz=4, Ra=1e6, Pr=0.71, Mach=0.1 * math.sqrt(3.0), steps=3, seed=8,
          defines=["steadyFlow", "HorizontalWallsNoslip", "VerticalWallsNoslip", "SpanwiseWallsNoslip",
                   "RayleighBenardCell", "HorizontalWallsConstT", "VerticalWallsAdiabatic", "SpanwiseWallsAdiabatic",

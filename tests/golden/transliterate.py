@@ -144,6 +144,7 @@ def to_python(body_lines, defines):
             py.append(pad() + "for %s in range(%s, (%s) + 1):" % (mdo.group(1), convert_expr(mdo.group(2)),
                                                                 convert_expr(mdo.group(3))))
             ind += 1
+            py.append(pad() + "pass")
             continue
         if re.match(r"end\s*do$", t, re.I):
             ind -= 1
@@ -152,17 +153,20 @@ def to_python(body_lines, defines):
         if mif:
             py.append(pad() + "if %s:" % convert_expr(mif.group(1)))
             ind += 1
+            py.append(pad() + "pass")  # blocks whose only statements (I/O, stop) were dropped
             continue
         melif = re.match(r"else\s*if\s*\((.*)\)\s*then$", t, re.I)
         if melif:
             ind -= 1
             py.append(pad() + "elif %s:" % convert_expr(melif.group(1)))
             ind += 1
+            py.append(pad() + "pass")
             continue
         if re.match(r"else$", t, re.I):
             ind -= 1
             py.append(pad() + "else:")
             ind += 1
+            py.append(pad() + "pass")
             continue
         if re.match(r"end\s*if$", t, re.I):
             ind -= 1
@@ -201,11 +205,11 @@ class ReferenceSubroutines:
 
     NAMES = ("collision", "streaming", "bounceback", "macro", "collisionT", "streamingT", "bouncebackT", "macroT")
 
-    def __init__(self, path, defines):
+    def __init__(self, path, defines, extra=()):
         src = open(path, encoding="utf-8-sig").read().splitlines()
         self.source = {}
         self.fn = {}
-        for name in self.NAMES:
+        for name in self.NAMES + tuple(extra):
             code = compile_subroutine(src, name, defines)
             self.source[name] = code
             glb = {"math": math, "np": np}

@@ -51,3 +51,7 @@ def field_names(data):
 
 def field_id(name):
     return FIELDS[name]
+
+
+def restart_names(data):
+    return sorted(k[4:] for k in data if k.startswith("rst_"))

@@ -37,3 +37,36 @@ def test_fixture_constants_match_derivation(oracle_mod):
         c = oracle_mod.Oracle(gc.params_for(meta)).constants(LbmConstants)
         for k, v in meta["constants"].items():
             assert getattr(c, k) == v, (name, k, getattr(c, k), v)
+
+
+@pytest.mark.parametrize("name", sorted(gc.cases()))
+def test_oracle_reproduces_reference_restart(oracle_mod, name):
+    """Restart: f and g after the steps, then macroT + reconstruct_macro_from_fg
+    (2DRB.F90:1144-1200, 3DRB.F90:1392-1463) executed from the reference's statements."""
+    meta = gc.cases()[name]
+    p = gc.params_for(meta)
+    data = gc.load(name)
+    o = oracle_mod.Oracle(p)
+    o.initial()
+    for f in gc.field_names(data):
+        o.set(gc.field_id(f), data["in_" + f])
+    o.step(meta["steps"])
+    assert not o.reconstruct_macro_from_fg()
+    for f in gc.restart_names(data):
+        got = o.get(gc.field_id(f), field_shape(p, f))
+        want = data["rst_" + f]
+        assert np.array_equal(got, want), (name, f, float(np.abs(got - want).max()))
+
+
+def test_oracle_restart_flags_nonpositive_rho(oracle_mod):
+    name = "rb2d_periodic"
+    meta = gc.cases()[name]
+    p = gc.params_for(meta)
+    data = gc.load(name)
+    o = oracle_mod.Oracle(p)
+    o.initial()
+    f = data["in_f"].copy()
+    f[2, 3, :] = 0.0  # one cell with rho = 0
+    o.set(gc.field_id("f"), f)
+    o.set(gc.field_id("g"), data["in_g"])
+    assert o.reconstruct_macro_from_fg()
