@@ -431,11 +431,20 @@ extern "C" int lbm_get_constants(const lbm_handle* h, lbm_constants* out) {
 
 extern "C" int64_t lbm_itc(const lbm_handle* h) { return h ? h->itc : -1; }
 
+// A staged FP32/FP16 kernel whose bounded wait gave up leaves a device flag set.
+static int take_device_error(lbm_handle* h) {
+    if (h->p.precision == LBM_FP64) return LBM_OK;
+    const int st = fast_take_error(h->F, h->stream);
+    if (st == LBM_ERR_TIMEOUT) return fail(h, st, "a staged kernel timed out waiting for its bulk copies");
+    if (st != LBM_OK) return fail(h, st, "reading the device error flag failed");
+    return LBM_OK;
+}
+
 extern "C" int lbm_sync(lbm_handle* h) {
     if (!h) return LBM_ERR_PARAM;
     CK(h, cudaSetDevice(h->device));
     CK(h, cudaStreamSynchronize(h->stream));
-    return LBM_OK;
+    return take_device_error(h);
 }
 
 // ------------------------------------------------------------------------------------
@@ -629,6 +638,8 @@ static int diag_prologue(lbm_handle* h) {
     if (!h) return LBM_ERR_PARAM;
     if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
     CK(h, cudaSetDevice(h->device));
+    int st = take_device_error(h);
+    if (st != LBM_OK) return st;
     return materialize(h);
 }
 
@@ -1354,6 +1365,14 @@ extern "C" int lbm_set_option(lbm_handle* h, int option, int value) {
         case LBM_OPT_KCHUNK:
             if (value < 1) return fail(h, LBM_ERR_PARAM, "kchunk must be >= 1");
             h->F.kchunk = value;
+            break;
+        case LBM_OPT_PAIRS:
+            if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the plain FP64 method has no paired form");
+            h->F.pairs = value != 0;
+            break;
+        case LBM_OPT_STAGED:
+            if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the plain FP64 method has no staged form");
+            h->F.tma = value != 0;
             break;
         default:
             return fail(h, LBM_ERR_PARAM, "unknown option");

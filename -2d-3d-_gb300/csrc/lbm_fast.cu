@@ -13,6 +13,7 @@
 
 #include "lbm_fast.h"
 #include "lbm_fast_cells.cuh"
+#include "lbm_fast_pairs.cuh"
 
 namespace lbm {
 
@@ -81,6 +82,44 @@ __global__ void __launch_bounds__(128) k_fast_thermal(Geo g, PhysF P, FastArgs<S
     int i, j, k;
     if (!fcell(g, c, i, j, k)) return;
     thermal_cell_2k<D, FIRST, S>(g, P, A, fin, gin, gout, c, i, j, k);
+}
+
+// Paired form of the two kernels (lbm_fast_pairs.cuh): thread (x, y) of a block holds the
+// cells 2t and 2t+1 of row (j, k); blockDim.x * blockDim.y = 128.  nx even.
+__device__ __forceinline__ bool pair_cell(const Geo& g, long long& c0, int& i0, int& j, int& k) {
+    i0 = 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    j = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    k = (int)blockIdx.z;
+    if (i0 >= g.nx || j >= g.ny) return false;
+    c0 = (long long)i0 + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
+    return true;
+}
+
+template <int D, class S>
+__global__ void __launch_bounds__(128) k_fast_flow_pair(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
+                                                        const S* __restrict__ gin, S* __restrict__ fout) {
+    long long c0;
+    int i0, j, k;
+    if (!pair_cell(g, c0, i0, j, k)) return;
+    flow_pair_2k<D, S>(g, P, A, fin, gin, fout, c0, i0, j, k);
+}
+
+template <int D, class S>
+__global__ void __launch_bounds__(128) k_fast_thermal_pair(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
+                                                           const S* __restrict__ gin, S* __restrict__ gout) {
+    long long c0;
+    int i0, j, k;
+    if (!pair_cell(g, c0, i0, j, k)) return;
+    thermal_pair_2k<D, S>(g, P, A, fin, gin, gout, c0, i0, j, k);
+}
+
+// Block shape of the paired kernels: as many pairs of a row as fit in 64 threads.
+static void pair_launch(const Geo& g, dim3& grid, dim3& block) {
+    const int pairs = g.nx / 2;
+    const int bx = pairs > 32 ? 64 : 32;
+    const int by = 128 / bx;
+    block = dim3(bx, by, 1);
+    grid = dim3((pairs + bx - 1) / bx, (g.ny + by - 1) / by, g.nz);
 }
 
 // Module arrays of step N from F[cur] = f_post_N, G[cur] = g_post_N, L[cur] (lag_in).
@@ -156,6 +195,11 @@ static inline unsigned nb(long long n, int bs) { return (unsigned)((n + bs - 1) 
 
 int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn& alloc) {
     F.precision = p.precision;
+    // Measured on GB300 (3D cubes 128^3 and 256^3, 2D 1024 x 512): 3D FP16 is fastest with
+    // staged rows (scalar 2-byte loads leave the one-cell kernel waiting on memory), 3D FP32
+    // with one cell per thread, 2D (lattices that live in L2) with two cells per thread.
+    F.tma = p.dim == 3 && p.precision == LBM_FP16;
+    F.pairs = p.dim == 2 || p.precision == LBM_FP16;
     F.dim = p.dim;
     F.q = p.dim == 3 ? 19 : 9;
     F.qt = p.dim == 3 ? 7 : 5;
@@ -169,6 +213,8 @@ int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn
             if ((st = alloc((void**)&F.B[b][c], sizeof(float) * n)) != LBM_OK) return st;
         if ((st = alloc((void**)&F.L[b], sizeof(float) * n)) != LBM_OK) return st;
     }
+    if ((st = alloc((void**)&F.err, sizeof(int))) != LBM_OK) return st;
+    if (cudaMemset(F.err, 0, sizeof(int)) != cudaSuccess) return LBM_ERR_CUDA;
     if ((st = alloc(&F.fref, F.esize * F.q * n)) != LBM_OK) return st;
     if ((st = alloc(&F.gref, F.esize * F.qt * n)) != LBM_OK) return st;
     float** scal[] = {&F.rho, &F.u, &F.v, &F.T, &F.up, &F.vp, &F.Tp};
@@ -212,11 +258,27 @@ void fast_initial(FastState& F, const Geo& g, const PhysC& P, const InitC& I, in
     if (dim == 3) cudaMemsetAsync(F.wp, 0, sizeof(float) * g.ncell, s);
 }
 
+bool fast_step_tma(FastState& F, const Geo& g, const PhysF& pf, int dim, const void* Af, const void* At,
+                   const void* fin, const void* gin, void* fout, void* gout, cudaStream_t s, int part);
+
+int fast_take_error(FastState& F, cudaStream_t s) {
+    if (!F.err) return LBM_OK;
+    int h = 0;
+    if (cudaMemcpyAsync(&h, F.err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return LBM_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return LBM_ERR_CUDA;
+    if (h == 0) return LBM_OK;
+    cudaMemsetAsync(F.err, 0, sizeof(int), s);
+    return LBM_ERR_TIMEOUT;
+}
+
 void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first, cudaStream_t s, int part) {
     const PhysF pf = to_physf(P);
     const Geo g = dev_geo(g0, P);
     const int cur = F.cur, nxt = F.cur ^ 1;
     const unsigned blocks = nb(g.ncell, 128);
+    const bool paired = F.pairs && g.nx % 2 == 0;
+    dim3 pgrid, pblock;
+    pair_launch(g, pgrid, pblock);
     F.ahead = false;
     DISPATCH_S(F, {
         const S* fin = (const S*)F.fbuf[cur];
@@ -226,10 +288,15 @@ void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first,
         FastArgs<S> Af = args_for<S>(F, cur, nxt, cur, nxt);  // flow: lag_in = L[cur], lag_out = L[nxt]
         FastArgs<S> At = args_for<S>(F, cur, nxt, nxt, nxt);  // thermal: 2D reads F_y,n from L[nxt]
         const bool fl = part != 1, th = part != 0;
-        if (dim == 2) {
+        if (!first && F.tma && fast_step_tma(F, g, pf, dim, &Af, &At, fin, gin, fout, gout, s, part)) {
+            // staged rows (lbm_fast_tma.cu)
+        } else if (dim == 2) {
             if (first) {
                 if (fl) k_fast_flow<2, true, S><<<blocks, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
                 if (th) k_fast_thermal<2, true, S><<<blocks, 128, 0, s>>>(g, pf, At, fout, gin, gout);
+            } else if (paired) {
+                if (fl) k_fast_flow_pair<2, S><<<pgrid, pblock, 0, s>>>(g, pf, Af, fin, gin, fout);
+                if (th) k_fast_thermal_pair<2, S><<<pgrid, pblock, 0, s>>>(g, pf, At, fout, gin, gout);
             } else {
                 if (fl) k_fast_flow<2, false, S><<<blocks, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
                 if (th) k_fast_thermal<2, false, S><<<blocks, 128, 0, s>>>(g, pf, At, fout, gin, gout);
@@ -238,6 +305,9 @@ void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first,
             if (first) {
                 if (fl) k_fast_flow<3, true, S><<<blocks, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
                 if (th) k_fast_thermal<3, true, S><<<blocks, 128, 0, s>>>(g, pf, At, fout, gin, gout);
+            } else if (paired) {
+                if (fl) k_fast_flow_pair<3, S><<<pgrid, pblock, 0, s>>>(g, pf, Af, fin, gin, fout);
+                if (th) k_fast_thermal_pair<3, S><<<pgrid, pblock, 0, s>>>(g, pf, At, fout, gin, gout);
             } else {
                 if (fl) k_fast_flow<3, false, S><<<blocks, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
                 if (th) k_fast_thermal<3, false, S><<<blocks, 128, 0, s>>>(g, pf, At, fout, gin, gout);

@@ -39,6 +39,12 @@ struct FastState {
     bool ahead = false;         // single-kernel phase: F[cur^1] already holds f_post_{N+1}
     bool single_kernel = false; // one-launch fused step (lbm_fused.cu); off: the two-kernel step is faster today
     int kchunk = 16;            // z planes per block of the fused kernel (3D)
+    // Form of the non-first two-kernel step, chosen by fast_allocate from GB300 timings:
+    // staged rows (lbm_fast_tma.cu) for 3D FP16; two cells per thread in 2D and as the 3D
+    // FP16 fallback; one cell per thread for 3D FP32.
+    bool pairs = false;
+    bool tma = false;
+    int* err = nullptr;         // device flag: a bounded wait of a staged kernel gave up
 };
 
 using AllocFn = std::function<int(void**, size_t)>;
@@ -52,6 +58,10 @@ void fast_step(FastState& F, const Geo& g, const PhysC& P, int dim, bool first, 
 void fast_enter(FastState& F, const Geo& g, const PhysC& P, int dim, cudaStream_t s);
 void fast_fused_step(FastState& F, const Geo& g, const PhysC& P, int dim, cudaStream_t s);
 bool fast_fused_supported(const Geo& g, int dim);
+// The staged two-kernel step applies (nx a multiple of 8, a tile row within the budget).
+bool fast_tma_supported(const Geo& g, int dim, int precision);
+// Read and clear the device error flag of the staged kernels (synchronises the stream).
+int fast_take_error(FastState& F, cudaStream_t s);
 // Rebuild the module arrays (f, g, rho, u, v, w, T) of the current step; leaves the fused
 // buffers valid.
 void fast_materialize(FastState& F, const Geo& g, const PhysC& P, int dim, cudaStream_t s);

@@ -14,7 +14,12 @@ namespace lbm {
 // ------------------------------------------------------------------------------------
 template <class S> __device__ __forceinline__ float ldS(const S* p, long long i);
 template <> __device__ __forceinline__ float ldS<float>(const float* p, long long i) { return __ldg(p + i); }
-template <> __device__ __forceinline__ float ldS<__half>(const __half* p, long long i) { return __half2float(__ldg(p + i)); }
+// FP16 values are fetched through the 16-bit integer __ldg builtin: the compiler schedules
+// it like any other load (hoisting it above the pull's boundary selects), which the
+// inline-assembly __half overload does not allow, and then reinterpreted.
+template <> __device__ __forceinline__ float ldS<__half>(const __half* p, long long i) {
+    return __half2float(__ushort_as_half(__ldg(reinterpret_cast<const unsigned short*>(p) + i)));
+}
 template <class S> __device__ __forceinline__ S toS(float x);
 template <> __device__ __forceinline__ float toS<float>(float x) { return x; }
 template <> __device__ __forceinline__ __half toS<__half>(float x) { return __float2half_rn(x); }

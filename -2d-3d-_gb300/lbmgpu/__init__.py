@@ -77,6 +77,8 @@ SIGNATURES = {
 }
 LBM_OPT_SINGLE_KERNEL = 1
 LBM_OPT_KCHUNK = 2
+LBM_OPT_PAIRS = 3
+LBM_OPT_STAGED = 4
 
 _lib = None
 

@@ -4,6 +4,7 @@ Translation units and their floating-point flags:
   lbm_exact.cu  -fmad=false : the plain FP64 method, one rounding per operation as in the reference
   lbm_reduce.cu -fmad=false : FP64 diagnostics, per-cell terms rounded as in the reference
   lbm_fast.cu               : FP32 arithmetic on FP32/FP16 storage, FMA contraction allowed
+  lbm_fast_tma.cu           : the same step with population rows staged by bulk copies
   lbm_api.cpp               : host code (-ffp-contract=off for the host-side fits)
   lbm_checkpoint.cpp        : Fortran unformatted sequential records (restart files)
 The units compile in parallel; a full build takes well under two minutes.
@@ -28,6 +29,7 @@ UNITS = [
     ("lbm_exact.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
     ("lbm_reduce.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
     ("lbm_fast.cu", ["-fmad=true"]),
+    ("lbm_fast_tma.cu", ["-fmad=true"]),
     ("lbm_fused.cu", ["-fmad=true"]),
     ("lbm_ensemble.cu", ["-fmad=true"]),
     ("lbm_api.cpp", []),

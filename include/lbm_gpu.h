@@ -198,9 +198,20 @@ int lbm_footprint(const lbm_params* p, size_t* bytes);
 /* ---- execution options (no counterpart in the reference) --------------------------------
  * LBM_OPT_SINGLE_KERNEL: FP32/FP16 handles advance with one fused kernel per step (1) or
  *   with the two-kernel form (0, default).  Both give the same arithmetic.
- * LBM_OPT_KCHUNK: z planes marched by one block of the fused 3D kernel (default 16). */
+ * LBM_OPT_KCHUNK: z planes marched by one block of the fused 3D kernel (default 16).
+ * LBM_OPT_PAIRS: the two-kernel FP32/FP16 step moves populations as 2-cell vectors, two
+ *   x-adjacent cells per thread (1; used when nx is even) or one cell per thread (0).
+ * LBM_OPT_STAGED: the two-kernel FP32/FP16 step stages tiles of x-rows in shared memory
+ *   with bulk asynchronous copies (1; used when nx is a multiple of 8; takes precedence
+ *   over LBM_OPT_PAIRS) or pulls every value from global memory (0).  A staged kernel
+ *   whose bounded wait for its copies gives up sets a device flag: the next lbm_sync or
+ *   diagnostic returns LBM_ERR_TIMEOUT.
+ * All forms give the same values bit for bit.  Defaults (fastest on GB300): 3D FP16
+ * staged, 3D FP32 one cell per thread, 2D two cells per thread. */
 #define LBM_OPT_SINGLE_KERNEL 1
 #define LBM_OPT_KCHUNK        2
+#define LBM_OPT_PAIRS         3
+#define LBM_OPT_STAGED        4
 int lbm_set_option(lbm_handle* h, int option, int value);
 
 /* ---- measurement hooks (no counterpart in the reference, which times its loop with
