@@ -12,8 +12,10 @@
 // holds after iteration N, so stepping resumes on the same trajectory).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <limits>
 #include <cstring>
 #include <new>
 #include <string>
@@ -66,6 +68,8 @@ struct lbm_handle {
     std::vector<double> h_part;
     double* d_tb = nullptr;
     double* d_nub = nullptr;
+    double* d_tl = nullptr;   // side-heated wall profile: mean T and Nu of the hot (left) wall per row
+    double* d_nul = nullptr;
     double* d_stage = nullptr;  // AoS staging for state transfer
     size_t stage_cap = 0;
     double* d_sx = nullptr;
@@ -302,6 +306,8 @@ static int allocate(lbm_handle* h) {
     AL(h->d_part, (size_t)diag_blocks(n) * DIAG_NSUM);
     AL(h->d_tb, h->geo.nx);
     AL(h->d_nub, h->geo.nx);
+    AL(h->d_tl, h->geo.ny);
+    AL(h->d_nul, h->geo.ny);
     AL(h->d_sx, h->geo.nx);
     AL(h->d_sy, h->geo.ny);
 #undef AL
@@ -823,6 +829,235 @@ extern "C" int lbm_RBcalc_Nu_wall_avg(lbm_handle* h, lbm_nu_wall* out) {
     return std::isfinite(out->Nu_hot) && std::isfinite(out->Nu_cold) ? LBM_OK
                                                                       : fail(h, LBM_ERR_DIVERGED, "non-finite wall Nu");
 }
+
+// ------------------------------------------------------------------------------------
+// side-heated cell diagnostics and mid-line / mid-plane velocity maxima
+// ------------------------------------------------------------------------------------
+// Node coordinates of one axis (3DRB.F90:444-465, 2DRB.F90:463-476): c[0] = 0,
+// c[n+1] = n/L, c[i] = (i - 1/2)/L.
+static std::vector<double> node_coords(int n, double L) {
+    std::vector<double> c((size_t)n + 2);
+    for (int i = 0; i <= n + 1; ++i) {
+        const double raw = i == 0 ? 0.0 : (i == n + 1 ? (double)n : (double)i - 0.5);
+        c[(size_t)i] = raw / L;
+    }
+    return c;
+}
+
+extern "C" int lbm_SideHeatedcalc_Nu_global(lbm_handle* h, double* Nu) {
+    int st = diag_prologue(h);
+    if (st != LBM_OK) return st;
+    if (!Nu) return fail(h, LBM_ERR_PARAM, "null output");
+    double s[DIAG_NSUM];
+    if ((st = run_reduce(h, DIAG_NU_GLOBAL_SIDE, s)) != LBM_OK) return st;
+    *Nu = (s[0] / (double)h->geo.ncell) / h->dsc.deltaT;
+    return std::isfinite(*Nu) ? LBM_OK : fail(h, LBM_ERR_DIVERGED, "non-finite Nu_global");
+}
+
+// SideHeatedcalc_Nu_wall_avg (2DRB.F90:1746-1941, 3DRB.F90:1889-2038): the hot wall is
+// the left face x = 0; its profile runs along y.
+extern "C" int lbm_SideHeatedcalc_Nu_wall_avg(lbm_handle* h, lbm_nu_wall* out) {
+    int st = diag_prologue(h);
+    if (st != LBM_OK) return st;
+    if (!out) return fail(h, LBM_ERR_PARAM, "null output");
+    const int ny = h->geo.ny, nz = h->geo.nz;
+    const bool d3 = h->dim == 3;
+    if (ny < 5) return fail(h, LBM_ERR_PARAM, "the wall fits need ny >= 5");
+    if (h->p.precision == LBM_FP64) diag_wall_rows<double>(h->geo, h->dsc, h->A.T, h->d_tl, h->d_nul, h->stream);
+    else diag_wall_rows<float>(h->geo, h->dsc, fast_diag_fields(h->F).T, h->d_tl, h->d_nul, h->stream);
+    CK_LAUNCH(h, "wall rows");
+    std::vector<double> Tl(ny + 2, 0.0), Nul(ny + 2, 0.0);
+    CK(h, cudaMemcpyAsync(Tl.data() + 1, h->d_tl, ny * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(Nul.data() + 1, h->d_nul, ny * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    const double dx = h->dsc.dy, deltaT = h->dsc.deltaT, Thot = h->p.Thot;
+    const std::vector<double> yp = node_coords(ny, h->c.lengthUnit);
+    double sum_hot = 0.0;
+    for (int j = 1; j <= ny; ++j) sum_hot = sum_hot + Nul[j];
+    out->Nu_hot = sum_hot / (double)ny;
+    double yf[4], Tf[4];
+    for (int m = 0; m < 4; ++m) { yf[m] = yp[1 + m]; Tf[m] = Tl[1 + m]; }
+    const double T_wb = fit_adiabatic_wall_T4(0.0, yf, Tf);
+    for (int m = 0; m < 4; ++m) { yf[m] = yp[ny - 3 + m]; Tf[m] = Tl[ny - 3 + m]; }
+    const double T_wt = fit_adiabatic_wall_T4(yp[ny + 1], yf, Tf);
+    std::vector<double> ext(Nul);
+    ext[0] = (2.0 * (Thot - T_wb) / dx) / deltaT;
+    ext[ny + 1] = (2.0 * (Thot - T_wt) / dx) / deltaT;
+    int jmax = 0, jmin = 0;
+    double vmax = ext[0], vmin = ext[0];
+    for (int j = 1; j <= ny + 1; ++j) {
+        if (ext[j] > vmax) { vmax = ext[j]; jmax = j; }
+        if (ext[j] < vmin) { vmin = ext[j]; jmin = j; }
+    }
+    int jj[5];
+    double yk[5], fk[5], fstar, ystar;
+    for (int m = 0; m < 5; ++m) jj[m] = jmax <= 2 ? m : (jmax >= ny - 1 ? ny - 3 + m : jmax - 2 + m);
+    for (int m = 0; m < 5; ++m) { yk[m] = yp[jj[m]]; fk[m] = ext[jj[m]]; }
+    fit_parabola_ls5(d3, yk, fk, +1, &fstar, &ystar);
+    out->Nu_hot_max = fstar;
+    out->Nu_hot_max_position = ystar;
+    // the minimum's window ends at it (2DRB.F90:1880-1884, 3DRB.F90:1974-1978)
+    for (int m = 0; m < 5; ++m) jj[m] = jmin >= 4 ? jmin - 4 + m : m;
+    for (int m = 0; m < 5; ++m) { yk[m] = yp[jj[m]]; fk[m] = ext[jj[m]]; }
+    fit_parabola_ls5(d3, yk, fk, -1, &fstar, &ystar);
+    out->Nu_hot_min = fstar;
+    out->Nu_hot_min_position = ystar;
+    double s[DIAG_NSUM];
+    if ((st = run_reduce(h, DIAG_NU_COLD_MID_SIDE, s)) != LBM_OK) return st;
+    out->Nu_cold = s[0] / (double)(ny * nz);
+    out->Nu_middle = s[1] / (double)(ny * nz);
+    return std::isfinite(out->Nu_hot) && std::isfinite(out->Nu_cold) ? LBM_OK
+                                                                      : fail(h, LBM_ERR_DIVERGED, "non-finite wall Nu");
+}
+
+static int ensure_stage(lbm_handle* h, size_t count);
+
+// The plane `idx` (0-based) normal to `axis` of velocity component `comp` (0 u, 1 v, 2 w),
+// to host memory.
+static int fetch_plane(lbm_handle* h, int comp, int axis, int idx, std::vector<double>& out) {
+    const Geo& g = h->geo;
+    const size_t n1 = axis == 0 ? g.ny : g.nx, n2 = axis == 2 ? g.ny : g.nz;
+    int st = ensure_stage(h, n1 * n2);
+    if (st != LBM_OK) return st;
+    if (h->p.precision == LBM_FP64) {
+        const double* f = comp == 0 ? h->A.u : (comp == 1 ? h->A.v : h->A.w);
+        diag_gather_plane<double>(g, f, axis, idx, h->d_stage, h->stream);
+    } else {
+        const DiagFields<float> F = fast_diag_fields(h->F);
+        const float* f = comp == 0 ? F.u : (comp == 1 ? F.v : F.w);
+        diag_gather_plane<float>(g, f, axis, idx, h->d_stage, h->stream);
+    }
+    CK_LAUNCH(h, "gather plane");
+    out.resize(n1 * n2);
+    CK(h, cudaMemcpyAsync(out.data(), h->d_stage, n1 * n2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return LBM_OK;
+}
+
+// calc_{u,v,w}mid_max_common (3DRB.F90:2399-2518): the grid maximum, over the mid plane
+// normal to the component's axis, of the component interpolated to that plane.
+static int mid_max_3d(lbm_handle* h, int comp, lbm_mid_max* out) {
+    const Geo& g = h->geo;
+    const double L = h->c.lengthUnit;
+    const int n[3] = {g.nx, g.ny, g.nz};
+    const std::vector<double> cx = node_coords(g.nx, L), cy = node_coords(g.ny, L), cz = node_coords(g.nz, L);
+    const std::vector<double>& c = comp == 0 ? cx : (comp == 1 ? cy : cz);
+    const int nn = n[comp];
+    // find_bracketing_index (3DRB.F90:2525-2545)
+    const double target = 0.5 * c[(size_t)nn + 1];
+    int iL = 1;
+    while (iL < nn && c[(size_t)iL + 1] < target) iL = iL + 1;
+    const int iR = iL + 1 < nn ? iL + 1 : nn;
+    double weight = std::fabs(c[(size_t)iR] - c[(size_t)iL]) <= 1.0e-14 ? 0.0 : (target - c[(size_t)iL]) / (c[(size_t)iR] - c[(size_t)iL]);
+    weight = std::max(0.0, std::min(1.0, weight));
+    std::vector<double> pL, pR;
+    int st = fetch_plane(h, comp, comp, iL - 1, pL);
+    if (st != LBM_OK) return st;
+    if (iR != iL && (st = fetch_plane(h, comp, comp, iR - 1, pR)) != LBM_OK) return st;
+    // loop order of the reference: outer over the later axis, inner over the earlier one
+    const int a1 = comp == 0 ? 1 : 0, a2 = comp == 2 ? 1 : 2;
+    const int n1 = n[a1], n2 = n[a2];
+    double vmax = -std::numeric_limits<double>::max();
+    int b1 = 1, b2 = 1;
+    for (int q2 = 1; q2 <= n2; ++q2)
+        for (int q1 = 1; q1 <= n1; ++q1) {
+            const size_t e = (size_t)(q1 - 1) + (size_t)n1 * (size_t)(q2 - 1);
+            const double val = iL == iR ? pL[e] : (1.0 - weight) * pL[e] + weight * pR[e];
+            if (val > vmax) {
+                vmax = val;
+                b1 = q1;
+                b2 = q2;
+            }
+        }
+    const std::vector<double>& c1 = a1 == 0 ? cx : cy;
+    const std::vector<double>& c2 = a2 == 1 ? cy : cz;
+    out->value = vmax * h->dsc.coef;
+    out->pos1 = c1[(size_t)b1];
+    out->pos2 = c2[(size_t)b2];
+    out->mid = target;
+    return std::isfinite(vmax) ? LBM_OK : fail(h, LBM_ERR_DIVERGED, "non-finite velocity");
+}
+
+// 2D mid-line maxima with the 5-point parabola (2DRB.F90:2081-2238, 2484-2575).
+// comp 0: u on the line x = mid (rb: x = 0.5, interpolated, maximum position folded into
+// the lower half); comp 1: v on the line y = mid.
+static int mid_max_2d(lbm_handle* h, int comp, bool rb, lbm_mid_max* out) {
+    const Geo& g = h->geo;
+    const int nx = g.nx, ny = g.ny;
+    const double L = h->c.lengthUnit;
+    const std::vector<double> xp = node_coords(nx, L), yp = node_coords(ny, L);
+    const int nline = comp == 0 ? ny : nx, nacross = comp == 0 ? nx : ny;
+    const std::vector<double>& along = comp == 0 ? yp : xp;   // coordinate along the line
+    const std::vector<double>& across = comp == 0 ? xp : yp;  // coordinate of the line
+    std::vector<double> line((size_t)nline + 1), pa, pb;
+    double mid;
+    int st;
+    if (comp == 0 && rb) {
+        const double targetX = 0.5;
+        mid = targetX;
+        int iL = 1;
+        while (iL < nx && xp[(size_t)iL + 1] < targetX) iL = iL + 1;
+        const int iR = iL + 1 < nx ? iL + 1 : nx;
+        if ((st = fetch_plane(h, 0, 0, iL - 1, pa)) != LBM_OK) return st;
+        if (std::fabs(xp[(size_t)iL] - targetX) <= 1.0e-14 || iR == iL) {
+            for (int j = 1; j <= ny; ++j) line[(size_t)j] = pa[(size_t)j - 1];
+        } else {
+            if ((st = fetch_plane(h, 0, 0, iR - 1, pb)) != LBM_OK) return st;
+            const double w = (targetX - xp[(size_t)iL]) / (xp[(size_t)iR] - xp[(size_t)iL]);
+            for (int j = 1; j <= ny; ++j) line[(size_t)j] = (1.0 - w) * pa[(size_t)j - 1] + w * pb[(size_t)j - 1];
+        }
+    } else if (nacross % 2 == 1) {
+        const int m = (nacross + 1) / 2;
+        mid = across[(size_t)m];
+        if ((st = fetch_plane(h, comp, comp, m - 1, pa)) != LBM_OK) return st;
+        for (int q = 1; q <= nline; ++q) line[(size_t)q] = pa[(size_t)q - 1];
+    } else {
+        const int mL = nacross / 2, mR = mL + 1;
+        mid = 0.5 * (across[(size_t)mL] + across[(size_t)mR]);
+        if ((st = fetch_plane(h, comp, comp, mL - 1, pa)) != LBM_OK) return st;
+        if ((st = fetch_plane(h, comp, comp, mR - 1, pb)) != LBM_OK) return st;
+        for (int q = 1; q <= nline; ++q) line[(size_t)q] = 0.5 * (pa[(size_t)q - 1] + pb[(size_t)q - 1]);
+    }
+    int q0 = 1;
+    double vmax = line[1];
+    for (int q = 2; q <= nline; ++q)
+        if (line[(size_t)q] > vmax) {
+            vmax = line[(size_t)q];
+            q0 = q;
+        }
+    double sk[5], fk[5], fstar, sstar;
+    for (int m = 0; m < 5; ++m) {
+        const int q = q0 <= 2 ? 1 + m : (q0 >= nline - 1 ? nline - 4 + m : q0 - 2 + m);
+        sk[m] = along[(size_t)q];
+        fk[m] = line[(size_t)q];
+    }
+    fit_parabola_ls5(false, sk, fk, +1, &fstar, &sstar);
+    if (comp == 0 && rb) {
+        const double yLen = yp[(size_t)ny + 1];
+        if (sstar > 0.5 * yLen) sstar = yLen - sstar;
+    }
+    out->value = fstar * h->dsc.coef;
+    out->pos1 = sstar;
+    out->pos2 = 0.0;
+    out->mid = mid;
+    return std::isfinite(fstar) ? LBM_OK : fail(h, LBM_ERR_DIVERGED, "non-finite velocity");
+}
+
+static int mid_max(lbm_handle* h, int comp, bool rb, lbm_mid_max* out) {
+    int st = diag_prologue(h);
+    if (st != LBM_OK) return st;
+    if (!out) return fail(h, LBM_ERR_PARAM, "null output");
+    if (comp == 2 && h->dim != 3) return fail(h, LBM_ERR_PARAM, "w exists in 3D only");
+    if (h->dim == 2 && (h->geo.nx < 5 || h->geo.ny < 5)) return fail(h, LBM_ERR_PARAM, "the fit needs 5 points");
+    return h->dim == 3 ? mid_max_3d(h, comp, out) : mid_max_2d(h, comp, rb, out);
+}
+
+extern "C" int lbm_SideHeatedcalc_umid_max(lbm_handle* h, lbm_mid_max* out) { return mid_max(h, 0, false, out); }
+extern "C" int lbm_SideHeatedcalc_vmid_max(lbm_handle* h, lbm_mid_max* out) { return mid_max(h, 1, false, out); }
+extern "C" int lbm_SideHeatedcalc_wmid_max(lbm_handle* h, lbm_mid_max* out) { return mid_max(h, 2, false, out); }
+extern "C" int lbm_RBcalc_umid_max(lbm_handle* h, lbm_mid_max* out) { return mid_max(h, 0, true, out); }
+extern "C" int lbm_RBcalc_vmid_max(lbm_handle* h, lbm_mid_max* out) { return mid_max(h, 1, true, out); }
+extern "C" int lbm_RBcalc_wmid_max(lbm_handle* h, lbm_mid_max* out) { return mid_max(h, 2, true, out); }
 
 // ------------------------------------------------------------------------------------
 // state transfer

@@ -67,7 +67,10 @@ struct DiagFields {
     S *up, *vp, *wp, *Tp;
 };
 
-enum DiagOp { DIAG_CHECK = 0, DIAG_NURE = 1, DIAG_NU_GLOBAL = 2, DIAG_NU_COLD_MID = 3 };
+enum DiagOp {
+    DIAG_CHECK = 0, DIAG_NURE = 1, DIAG_NU_GLOBAL = 2, DIAG_NU_COLD_MID = 3,
+    DIAG_NU_GLOBAL_SIDE = 4, DIAG_NU_COLD_MID_SIDE = 5
+};
 
 // Number of partial-sum slots a reduction launch writes: nblocks * DIAG_NSUM doubles.
 constexpr int DIAG_NSUM = 5;
@@ -87,6 +90,14 @@ void diag_reduce(DiagOp op, const Geo& g, const DiagScalars& D, const DiagFields
 // Nu_bot[i] = mean_k (8Thot - 9T(i,1,k) + T(i,2,k))/(3dy)/deltaT, k summed in order.
 template <class S>
 void diag_wall_columns(const Geo& g, const DiagScalars& D, const S* T, double* Tb, double* Nub, cudaStream_t s);
+
+// Per-row hot (left) wall profile for SideHeatedcalc_Nu_wall_avg: Tl[j] = mean_k T(1,j,k)
+// and Nu_left[j] = mean_k (8Thot - 9T(1,j,k) + T(2,j,k))/(3dx)/deltaT, k summed in order.
+template <class S>
+void diag_wall_rows(const Geo& g, const DiagScalars& D, const S* T, double* Tl, double* Nul, cudaStream_t s);
+// Copy the plane `idx` normal to `axis` of a field into `out` (FP64, contiguous).
+template <class S>
+void diag_gather_plane(const Geo& g, const S* f, int axis, int idx, double* out, cudaStream_t s);
 
 // ---- layout transforms (lbm_reduce.cu) -------------------------------------------------
 // Fortran AoS f(0:q-1, cells) <-> device SoA f[q][cells], FP64.

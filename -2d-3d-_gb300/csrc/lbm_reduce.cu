@@ -73,6 +73,32 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(Geo g, DiagScalars D, Diag
     double acc[DIAG_NSUM] = {0.0, 0.0, 0.0, 0.0, 0.0};
     const bool d3 = D.d3 != 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
+    if (OP == DIAG_NU_COLD_MID_SIDE) {
+        // one thread per (j,k) row: cold (right) wall term and x mid-plane term
+        const long long nrow = (long long)g.ny * g.nz;
+        for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < nrow; row += stride) {
+            const int j = (int)(row % g.ny), k = (int)(row / g.ny);
+            auto T = [&](int i) { return ld(F.T, cell_index(g, i, j, k)); };
+            auto U = [&](int i) { return ld(F.u, cell_index(g, i, j, k)); };
+            const int nx = g.nx;
+            // Nu_cold (2DRB.F90:1908-1912, 3DRB.F90:1990-1997)
+            const double qx_wall = (-8.0 * D.Tcold + 9.0 * T(nx - 1) - T(nx - 2)) / (3.0 * D.dy);
+            acc[0] += qx_wall / D.deltaT;
+            // Nu_middle (2DRB.F90:1916-1931, 3DRB.F90:2000-2021)
+            if (nx % 2 == 1) {
+                const int im = (nx + 1) / 2 - 1;
+                acc[1] += (D.coef * U(im) * (T(im) - D.Tref) + (T(im - 1) - T(im + 1)) / (2.0 * D.dy)) / D.deltaT;
+            } else {
+                const int iL = nx / 2 - 1, iR = iL + 1;
+                if (d3)
+                    acc[1] += (D.coef * 0.5 * (U(iL) * (T(iL) - D.Tref) + U(iR) * (T(iR) - D.Tref)) + (T(iL) - T(iR)) / D.dy) / D.deltaT;
+                else
+                    acc[1] += (D.coef * (0.5 * (U(iL) * (T(iL) - D.Tref) + U(iR) * (T(iR) - D.Tref))) + (T(iL) - T(iR)) / D.dy) / D.deltaT;
+            }
+        }
+        block_store(acc, partials);
+        return;
+    }
     if (OP == DIAG_NU_COLD_MID) {
         // one thread per (i,k) column: cold wall term and mid-plane term
         const long long ncol = (long long)g.nx * g.nz;
@@ -130,6 +156,16 @@ __global__ void __launch_bounds__(kRedThreads) k_diag(Geo g, DiagScalars D, Diag
             }
             acc[1] += r;
             acc[4] += bad_cell(F, c, d3);
+        } else if (OP == DIAG_NU_GLOBAL_SIDE) {
+            // SideHeatedcalc_Nu_global (2DRB.F90:1700-1720, 3DRB.F90:1801-1817)
+            int i, j, k;
+            cell_coords(g, c, i, j, k);
+            auto T = [&](int ii) { return ld(F.T, cell_index(g, ii, j, k)); };
+            double dTdx;
+            if (i == 0) dTdx = (-3.0 * T(0) - T(1) + 4.0 * D.Thot) / (3.0 * D.dy);
+            else if (i == g.nx - 1) dTdx = (-4.0 * D.Tcold + 3.0 * T(g.nx - 1) + T(g.nx - 2)) / (3.0 * D.dy);
+            else dTdx = (T(i - 1) - T(i + 1)) / (2.0 * D.dy);
+            acc[0] += D.coef * ld(F.u, c) * (T(i) - D.Tref) + dTdx;
         } else {
             // RBcalc_Nu_global (2DRB.F90:2268-2288, 3DRB.F90:1851-1866)
             int i, j, k;
@@ -153,6 +189,10 @@ void diag_reduce(DiagOp op, const Geo& g, const DiagScalars& D, const DiagFields
         case DIAG_NURE: k_diag<S, DIAG_NURE><<<nb, kRedThreads, 0, s>>>(g, D, F, partials); break;
         case DIAG_NU_GLOBAL: k_diag<S, DIAG_NU_GLOBAL><<<nb, kRedThreads, 0, s>>>(g, D, F, partials); break;
         case DIAG_NU_COLD_MID: k_diag<S, DIAG_NU_COLD_MID><<<nb, kRedThreads, 0, s>>>(g, D, F, partials); break;
+        case DIAG_NU_GLOBAL_SIDE: k_diag<S, DIAG_NU_GLOBAL_SIDE><<<nb, kRedThreads, 0, s>>>(g, D, F, partials); break;
+        case DIAG_NU_COLD_MID_SIDE:
+            k_diag<S, DIAG_NU_COLD_MID_SIDE><<<nb, kRedThreads, 0, s>>>(g, D, F, partials);
+            break;
     }
 }
 
@@ -176,10 +216,52 @@ void diag_wall_columns(const Geo& g, const DiagScalars& D, const S* T, double* T
     k_wall_columns<S><<<(g.nx + 127) / 128, 128, 0, s>>>(g, D, T, Tb, Nub);
 }
 
+template <class S>
+__global__ void k_wall_rows(Geo g, DiagScalars D, const S* __restrict__ T, double* Tl, double* Nul) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= g.ny) return;
+    // 3DRB.F90:1905-1925 (2D: 2DRB.F90:1776-1781 is the nz = 1 case of the same sums)
+    double tl = 0.0, nl = 0.0;
+    for (int k = 0; k < g.nz; ++k) tl = tl + (double)T[cell_index(g, 0, j, k)];
+    for (int k = 0; k < g.nz; ++k) {
+        const double qx_wall = (8.0 * D.Thot - 9.0 * (double)T[cell_index(g, 0, j, k)] + (double)T[cell_index(g, 1, j, k)]) / (3.0 * D.dy);
+        nl = nl + qx_wall / D.deltaT;
+    }
+    Tl[j] = tl / (double)g.nz;
+    Nul[j] = nl / (double)g.nz;
+}
+
+template <class S>
+void diag_wall_rows(const Geo& g, const DiagScalars& D, const S* T, double* Tl, double* Nul, cudaStream_t s) {
+    k_wall_rows<S><<<(g.ny + 127) / 128, 128, 0, s>>>(g, D, T, Tl, Nul);
+}
+
+// The plane `idx` normal to `axis` of a field, contiguous in FP64:
+//   axis 0: out[j + ny k] = f(idx, j, k);  axis 1: out[i + nx k];  axis 2: out[i + nx j].
+template <class S>
+__global__ void k_gather_plane(Geo g, const S* __restrict__ f, int axis, int idx, double* out) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n1 = axis == 0 ? g.ny : g.nx, n2 = axis == 2 ? g.ny : g.nz;
+    if (e >= n1 * n2) return;
+    const int a = (int)(e % n1), b = (int)(e / n1);
+    const long long c = axis == 0 ? cell_index(g, idx, a, b) : (axis == 1 ? cell_index(g, a, idx, b) : cell_index(g, a, b, idx));
+    out[e] = (double)f[c];
+}
+
+template <class S>
+void diag_gather_plane(const Geo& g, const S* f, int axis, int idx, double* out, cudaStream_t s) {
+    const long long n1 = axis == 0 ? g.ny : g.nx, n2 = axis == 2 ? g.ny : g.nz;
+    k_gather_plane<S><<<(unsigned)((n1 * n2 + 255) / 256), 256, 0, s>>>(g, f, axis, idx, out);
+}
+
 template void diag_reduce<double>(DiagOp, const Geo&, const DiagScalars&, const DiagFields<double>&, double*, int, cudaStream_t);
 template void diag_reduce<float>(DiagOp, const Geo&, const DiagScalars&, const DiagFields<float>&, double*, int, cudaStream_t);
 template void diag_wall_columns<double>(const Geo&, const DiagScalars&, const double*, double*, double*, cudaStream_t);
 template void diag_wall_columns<float>(const Geo&, const DiagScalars&, const float*, double*, double*, cudaStream_t);
+template void diag_wall_rows<double>(const Geo&, const DiagScalars&, const double*, double*, double*, cudaStream_t);
+template void diag_wall_rows<float>(const Geo&, const DiagScalars&, const float*, double*, double*, cudaStream_t);
+template void diag_gather_plane<double>(const Geo&, const double*, int, int, double*, cudaStream_t);
+template void diag_gather_plane<float>(const Geo&, const float*, int, int, double*, cudaStream_t);
 
 // ---- layout transforms ----------------------------------------------------------------
 __global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict__ soa, int q, long long n) {

@@ -17,8 +17,8 @@ import os
 import numpy as np
 
 from .abi import (FIELDS, LBM_BACKUP_CONTINUE, LBM_BACKUP_REFERENCE, LBM_FP64, LBM_OK, LBM_RELOAD_AUTO,
-                  LBM_RELOAD_CONTINUE, LBM_RELOAD_REFERENCE, STATUS_NAMES, LbmConstants, LbmNuWall, LbmParams,
-                  field_shape, field_size, rb_params)
+                  LBM_RELOAD_CONTINUE, LBM_RELOAD_REFERENCE, STATUS_NAMES, LbmConstants, LbmMidMax, LbmNuWall,
+                  LbmParams, field_shape, field_size, rb_params)
 
 __all__ = ["Lattice", "Ensemble", "LbmError", "LbmDiverged", "LbmParams", "rb_params", "load_library",
            "library_path", "params_default", "derive_constants", "footprint", "FIELDS"]
@@ -68,6 +68,14 @@ SIGNATURES = {
     "lbm_ensemble_get_stream": ([_vp, C.POINTER(_vp)], _i32),
     "lbm_ensemble_last_error": ([_vp], C.c_char_p),
     "lbm_ensemble_autotune": ([_vp, _i32, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32)], _i32),
+    "lbm_SideHeatedcalc_Nu_global": ([_vp, _dp], _i32),
+    "lbm_SideHeatedcalc_Nu_wall_avg": ([_vp, _vp], _i32),
+    "lbm_SideHeatedcalc_umid_max": ([_vp, _vp], _i32),
+    "lbm_SideHeatedcalc_vmid_max": ([_vp, _vp], _i32),
+    "lbm_SideHeatedcalc_wmid_max": ([_vp, _vp], _i32),
+    "lbm_RBcalc_umid_max": ([_vp, _vp], _i32),
+    "lbm_RBcalc_vmid_max": ([_vp, _vp], _i32),
+    "lbm_RBcalc_wmid_max": ([_vp, _vp], _i32),
     "lbm_backupData": ([_vp, C.c_char_p, _i32], _i32),
     "lbm_reload": ([_vp, C.c_char_p, _i32], _i32),
     "lbm_reload_form": ([_vp], _i32),
@@ -235,6 +243,28 @@ class Lattice:
         w = LbmNuWall()
         self._ck(self.lib.lbm_RBcalc_Nu_wall_avg(self._h, C.byref(w)), "RBcalc_Nu_wall_avg")
         return w.as_dict()
+
+    def SideHeatedcalc_Nu_global(self):
+        a = C.c_double()
+        self._ck(self.lib.lbm_SideHeatedcalc_Nu_global(self._h, C.byref(a)), "SideHeatedcalc_Nu_global")
+        return a.value
+
+    def SideHeatedcalc_Nu_wall_avg(self):
+        w = LbmNuWall()
+        self._ck(self.lib.lbm_SideHeatedcalc_Nu_wall_avg(self._h, C.byref(w)), "SideHeatedcalc_Nu_wall_avg")
+        return w.as_dict()
+
+    def _mid_max(self, name):
+        m = LbmMidMax()
+        self._ck(getattr(self.lib, "lbm_" + name)(self._h, C.byref(m)), name)
+        return m.as_dict()
+
+    def SideHeatedcalc_umid_max(self): return self._mid_max("SideHeatedcalc_umid_max")
+    def SideHeatedcalc_vmid_max(self): return self._mid_max("SideHeatedcalc_vmid_max")
+    def SideHeatedcalc_wmid_max(self): return self._mid_max("SideHeatedcalc_wmid_max")
+    def RBcalc_umid_max(self): return self._mid_max("RBcalc_umid_max")
+    def RBcalc_vmid_max(self): return self._mid_max("RBcalc_vmid_max")
+    def RBcalc_wmid_max(self): return self._mid_max("RBcalc_wmid_max")
 
     # -- measurement ----------------------------------------------------------------------
     def stream_handle(self):

@@ -71,6 +71,13 @@ class LbmNuWall(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class LbmMidMax(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("value", "pos1", "pos2", "mid")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 def rb_params(dim=3, n=None, nx=None, ny=None, nz=None, Ra=1e7, Pr=0.71, U=0.1, Mach=None,
               precision="fp64", pattern="AB", seed=20261203, noise_amp=1e-3,
               periodic_x=None, legacy_thermal=False, use_g=True):

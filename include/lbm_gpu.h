@@ -254,6 +254,34 @@ int lbm_calNuRe_noalloc(const double* u, const double* v, const double* w, const
                         int side_heated, double lengthUnit, double diffusivity, double viscosity,
                         void* stream, double* Nu, double* Re);
 
+/* ---- side-heated cell and mid-line diagnostics ---------------------------------------
+ * SideHeatedcalc_Nu_global (2DRB.F90:1686-1734, 3DRB.F90:1789-1828): mean over cells of
+ *   [(L/kappa) u (T - Tref) + dT/dx] / (Thot - Tcold), one-sided wall stencils at x faces.
+ * SideHeatedcalc_Nu_wall_avg (2DRB.F90:1746-1941, 3DRB.F90:1889-2038): hot (left) wall,
+ *   cold (right) wall and x mid-plane means, and the hot wall's extremes along y from the
+ *   adiabatic-corner extension and the 5-point least-squares parabola (the fields of
+ *   lbm_nu_wall; positions are y).
+ * {SideHeated,RB}calc_{u,v,w}mid_max: the largest velocity component on its mid line / plane:
+ *   2D (2DRB.F90:2081-2238, 2484-2657): the 5-point parabola through the grid maximum of
+ *     u on the vertical mid line (RB: on x = 0.5, interpolated, position folded into the
+ *     lower half) or of v on the horizontal mid line; pos1 = position along the line;
+ *   3D (3DRB.F90:2345-2518, SideHeated and RB alike): the grid maximum over the mid plane
+ *     of the component interpolated to it; pos1/pos2 = the two in-plane coordinates (y,z
+ *     for u; x,z for v; x,y for w).
+ *   value is in the reference's post-processing scale (times L/kappa); mid = the line /
+ *   plane coordinate.  w is 3D only. */
+typedef struct lbm_mid_max {
+    double value, pos1, pos2, mid;
+} lbm_mid_max;
+int lbm_SideHeatedcalc_Nu_global(lbm_handle* h, double* Nu_global);
+int lbm_SideHeatedcalc_Nu_wall_avg(lbm_handle* h, lbm_nu_wall* out);
+int lbm_SideHeatedcalc_umid_max(lbm_handle* h, lbm_mid_max* out);
+int lbm_SideHeatedcalc_vmid_max(lbm_handle* h, lbm_mid_max* out);
+int lbm_SideHeatedcalc_wmid_max(lbm_handle* h, lbm_mid_max* out);
+int lbm_RBcalc_umid_max(lbm_handle* h, lbm_mid_max* out);
+int lbm_RBcalc_vmid_max(lbm_handle* h, lbm_mid_max* out);
+int lbm_RBcalc_wmid_max(lbm_handle* h, lbm_mid_max* out);
+
 /* ---- restart files (backupData, 3DRB.F90:1638-1665 / 2DRB.F90:1402-1430; reload,
  *      3DRB.F90:602-623 / 2DRB.F90:621-637; reconstruct_macro_from_fg,
  *      3DRB.F90:1392-1463 / 2DRB.F90:1144-1200) -----------------------------------------

@@ -21,6 +21,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <new>
 #include <vector>
 #ifdef _OPENMP
@@ -1419,6 +1420,235 @@ extern "C" int ora_RBcalc_Nu_wall_avg(ora_handle* h, lbm_nu_wall* out) {
     }
     out->Nu_middle = sum_mid / (double)(nx * nz);
     return std::isfinite(out->Nu_hot) ? LBM_OK : LBM_ERR_DIVERGED;
+}
+
+// SideHeatedcalc_Nu_global (2DRB.F90:1686-1734, 3DRB.F90:1789-1828)
+extern "C" int ora_SideHeatedcalc_Nu_global(ora_handle* h, double* Nu) {
+    const lbm_constants& c = h->c;
+    const int nx = h->nx, ny = h->ny, nz = h->nz;
+    const double dx = 1.0 / c.lengthUnit;
+    const double deltaT = h->p.Thot - h->p.Tcold;
+    const double coef = c.velocityScaleCompare;
+    const double Thot = h->p.Thot, Tcold = h->p.Tcold, Tref = c.Tref;
+    double sum_qx = 0.0;
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                auto T = [h, j, k](int ii) { return h->T[h->C(ii, j, k)]; };
+                double dTdx;
+                if (i == 1)
+                    dTdx = (-3.0 * T(1) - T(2) + 4.0 * Thot) / (3.0 * dx);
+                else if (i == nx)
+                    dTdx = (-4.0 * Tcold + 3.0 * T(nx) + T(nx - 1)) / (3.0 * dx);
+                else
+                    dTdx = (T(i - 1) - T(i + 1)) / (2.0 * dx);
+                double qx = coef * h->u[h->C(i, j, k)] * (T(i) - Tref) + dTdx;
+                sum_qx = sum_qx + qx;
+            }
+    *Nu = (sum_qx / (double)(long long)h->ncell) / deltaT;
+    return std::isfinite(*Nu) ? LBM_OK : LBM_ERR_DIVERGED;
+}
+
+// SideHeatedcalc_Nu_wall_avg (2DRB.F90:1746-1941, 3DRB.F90:1889-2038)
+extern "C" int ora_SideHeatedcalc_Nu_wall_avg(ora_handle* h, lbm_nu_wall* out) {
+    const lbm_constants& c = h->c;
+    const int nx = h->nx, ny = h->ny, nz = h->nz;
+    const double dx = 1.0 / c.lengthUnit;
+    const double deltaT = h->p.Thot - h->p.Tcold;
+    const double Thot = h->p.Thot, Tcold = h->p.Tcold, Tref = c.Tref;
+    const double coef = h->d3 ? c.heatFluxScale : c.velocityScaleCompare;
+    const std::vector<double>& yp = h->yp;
+    auto T = [h](int i, int j, int k) { return h->T[h->C(i, j, k)]; };
+    auto U = [h](int i, int j, int k) { return h->u[h->C(i, j, k)]; };
+    std::vector<double> Nu_left(ny + 2, 0.0), Tl(ny + 2, 0.0);
+    double sum_hot = 0.0;
+    for (int j = 1; j <= ny; ++j) {
+        if (h->d3) {
+            double tl = 0.0;
+            for (int k = 1; k <= nz; ++k) tl = tl + T(1, j, k);
+            Tl[j] = tl / (double)nz;
+            double nl = 0.0;
+            for (int k = 1; k <= nz; ++k) {
+                double qx_wall = (8.0 * Thot - 9.0 * T(1, j, k) + T(2, j, k)) / (3.0 * dx);
+                nl = nl + qx_wall / deltaT;
+            }
+            Nu_left[j] = nl / (double)nz;
+        } else {
+            Tl[j] = T(1, j, 1);
+            double qx_wall = (8.0 * Thot - 9.0 * T(1, j, 1) + T(2, j, 1)) / (3.0 * dx);
+            Nu_left[j] = qx_wall / deltaT;
+        }
+        sum_hot = sum_hot + Nu_left[j];
+    }
+    out->Nu_hot = sum_hot / (double)ny;
+    double yfit[4], Tfit[4];
+    for (int m = 0; m < 4; ++m) { yfit[m] = yp[1 + m]; Tfit[m] = Tl[1 + m]; }
+    double T_wb = fit_adiabatic_wall_T4(0.0, yfit, Tfit);
+    for (int m = 0; m < 4; ++m) { yfit[m] = yp[ny - 3 + m]; Tfit[m] = Tl[ny - 3 + m]; }
+    double T_wt = fit_adiabatic_wall_T4(yp[ny + 1], yfit, Tfit);
+    std::vector<double> ext(Nu_left);
+    ext[0] = (2.0 * (Thot - T_wb) / dx) / deltaT;
+    ext[ny + 1] = (2.0 * (Thot - T_wt) / dx) / deltaT;
+    int jmax = 0, jmin = 0;
+    double vmax = ext[0], vmin = ext[0];
+    for (int j = 1; j <= ny + 1; ++j) {
+        if (ext[j] > vmax) { vmax = ext[j]; jmax = j; }
+        if (ext[j] < vmin) { vmin = ext[j]; jmin = j; }
+    }
+    int jj[5];
+    if (jmax <= 2) { for (int m = 0; m < 5; ++m) jj[m] = m; }
+    else if (jmax >= ny - 1) { for (int m = 0; m < 5; ++m) jj[m] = ny - 3 + m; }
+    else { for (int m = 0; m < 5; ++m) jj[m] = jmax - 2 + m; }
+    double yk[5], fk[5], fstar, ystar;
+    for (int m = 0; m < 5; ++m) { yk[m] = yp[jj[m]]; fk[m] = ext[jj[m]]; }
+    if (h->d3) fit_parabola_ls5_3d(yk, fk, +1, &fstar, &ystar); else fit_parabola_ls5_2d(yk, fk, +1, &fstar, &ystar);
+    out->Nu_hot_max = fstar;
+    out->Nu_hot_max_position = ystar;
+    if (jmin >= 4) { for (int m = 0; m < 5; ++m) jj[m] = jmin - 4 + m; }
+    else { for (int m = 0; m < 5; ++m) jj[m] = m; }
+    for (int m = 0; m < 5; ++m) { yk[m] = yp[jj[m]]; fk[m] = ext[jj[m]]; }
+    if (h->d3) fit_parabola_ls5_3d(yk, fk, -1, &fstar, &ystar); else fit_parabola_ls5_2d(yk, fk, -1, &fstar, &ystar);
+    out->Nu_hot_min = fstar;
+    out->Nu_hot_min_position = ystar;
+
+    double sum_cold = 0.0;
+    for (int j = 1; j <= ny; ++j)
+        for (int k = 1; k <= nz; ++k) {
+            double qx_wall = (-8.0 * Tcold + 9.0 * T(nx, j, k) - T(nx - 1, j, k)) / (3.0 * dx);
+            sum_cold = sum_cold + qx_wall / deltaT;
+        }
+    out->Nu_cold = sum_cold / (double)(ny * nz);
+
+    double sum_mid = 0.0;
+    if (nx % 2 == 1) {
+        int iMid = (nx + 1) / 2;
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                sum_mid = sum_mid + (coef * U(iMid, j, k) * (T(iMid, j, k) - Tref)
+                                     + (T(iMid - 1, j, k) - T(iMid + 1, j, k)) / (2.0 * dx)) / deltaT;
+    } else {
+        int iL = nx / 2, iR = iL + 1;
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j) {
+                if (h->d3)
+                    sum_mid = sum_mid + (coef * 0.5 * (U(iL, j, k) * (T(iL, j, k) - Tref) + U(iR, j, k) * (T(iR, j, k) - Tref))
+                                         + (T(iL, j, k) - T(iR, j, k)) / dx) / deltaT;
+                else
+                    sum_mid = sum_mid + (coef * (0.5 * (U(iL, j, k) * (T(iL, j, k) - Tref) + U(iR, j, k) * (T(iR, j, k) - Tref)))
+                                         + (T(iL, j, k) - T(iR, j, k)) / dx) / deltaT;
+            }
+    }
+    out->Nu_middle = sum_mid / (double)(ny * nz);
+    return std::isfinite(out->Nu_hot) ? LBM_OK : LBM_ERR_DIVERGED;
+}
+
+// Mid-line / mid-plane velocity maxima.  comp: 0 u, 1 v, 2 w; rb: the RB form of the 2D
+// u line.  out = {value * velocityScaleCompare, position 1, position 2, mid coordinate}.
+//   2D: SideHeatedcalc_umid_max / vmid_max (2DRB.F90:2081-2238), RBcalc_umid_max /
+//       vmid_max (2DRB.F90:2484-2655);
+//   3D: calc_{u,v,w}mid_max_common with find_bracketing_index and interp_scalar_*
+//       (3DRB.F90:2399-2617), shared by the SideHeated and RB entry points.
+extern "C" int ora_mid_max(ora_handle* h, int comp, int rb, lbm_mid_max* out) {
+    const double coef = h->c.velocityScaleCompare;
+    const int nx = h->nx, ny = h->ny, nz = h->nz;
+    const std::vector<double>& xp = h->xp;
+    const std::vector<double>& yp = h->yp;
+    const std::vector<double>& zp = h->zp;
+    const std::vector<double>& field = comp == 0 ? h->u : (comp == 1 ? h->v : h->w);
+    auto F = [h, &field](int i, int j, int k) { return field[h->C(i, j, k)]; };
+    if (h->d3) {
+        const std::vector<double>& cc = comp == 0 ? xp : (comp == 1 ? yp : zp);
+        const int n = comp == 0 ? nx : (comp == 1 ? ny : nz);
+        const double target = 0.5 * cc[n + 1];
+        int iL = 1;
+        while (iL < n && cc[iL + 1] < target) iL = iL + 1;
+        const int iR = std::min(iL + 1, n);
+        double weight;
+        if (std::fabs(cc[iR] - cc[iL]) <= 1.0e-14) weight = 0.0;
+        else weight = (target - cc[iL]) / (cc[iR] - cc[iL]);
+        weight = std::max(0.0, std::min(1.0, weight));
+        auto interp = [&](int a, int b) {
+            int iA, jA, kA, iB, jB, kB;
+            if (comp == 0) { iA = iL; iB = iR; jA = jB = a; kA = kB = b; }
+            else if (comp == 1) { jA = iL; jB = iR; iA = iB = a; kA = kB = b; }
+            else { kA = iL; kB = iR; iA = iB = a; jA = jB = b; }
+            if (iL == iR) return F(iA, jA, kA);
+            return (1.0 - weight) * F(iA, jA, kA) + weight * F(iB, jB, kB);
+        };
+        double vmax = -std::numeric_limits<double>::max();
+        int b1 = 1, b2 = 1;
+        const int n1 = comp == 0 ? ny : nx, n2 = comp == 2 ? ny : nz;
+        for (int q2 = 1; q2 <= n2; ++q2)
+            for (int q1 = 1; q1 <= n1; ++q1) {
+                const double val = interp(q1, q2);
+                if (val > vmax) { vmax = val; b1 = q1; b2 = q2; }
+            }
+        out->value = vmax * coef;
+        out->pos1 = comp == 0 ? yp[b1] : xp[b1];
+        out->pos2 = comp == 2 ? yp[b2] : zp[b2];
+        out->mid = target;
+        return std::isfinite(vmax) ? LBM_OK : LBM_ERR_DIVERGED;
+    }
+    if (comp == 2) return LBM_ERR_PARAM;
+    std::vector<double> line;
+    double mid;
+    if (comp == 0) {
+        line.assign(ny + 1, 0.0);
+        if (rb) {
+            const double targetX = 0.5;
+            mid = targetX;
+            int iL = 1;
+            while (iL < nx && xp[iL + 1] < targetX) iL = iL + 1;
+            const int iR = std::min(iL + 1, nx);
+            if (std::fabs(xp[iL] - targetX) <= 1.0e-14 || iR == iL) {
+                for (int j = 1; j <= ny; ++j) line[j] = F(iL, j, 1);
+            } else {
+                const double w = (targetX - xp[iL]) / (xp[iR] - xp[iL]);
+                for (int j = 1; j <= ny; ++j) line[j] = (1.0 - w) * F(iL, j, 1) + w * F(iR, j, 1);
+            }
+        } else if (nx % 2 == 1) {
+            const int iMid = (nx + 1) / 2;
+            mid = xp[iMid];
+            for (int j = 1; j <= ny; ++j) line[j] = F(iMid, j, 1);
+        } else {
+            const int iL = nx / 2, iR = iL + 1;
+            mid = 0.5 * (xp[iL] + xp[iR]);
+            for (int j = 1; j <= ny; ++j) line[j] = 0.5 * (F(iL, j, 1) + F(iR, j, 1));
+        }
+    } else {
+        line.assign(nx + 1, 0.0);
+        if (ny % 2 == 1) {
+            const int jMid = (ny + 1) / 2;
+            mid = yp[jMid];
+            for (int i = 1; i <= nx; ++i) line[i] = F(i, jMid, 1);
+        } else {
+            const int jB = ny / 2, jT = jB + 1;
+            mid = 0.5 * (yp[jB] + yp[jT]);
+            for (int i = 1; i <= nx; ++i) line[i] = 0.5 * (F(i, jB, 1) + F(i, jT, 1));
+        }
+    }
+    const int nl = (int)line.size() - 1;
+    const std::vector<double>& along = comp == 0 ? yp : xp;
+    int q0 = 1;
+    double gmax = line[1];
+    for (int q = 2; q <= nl; ++q)
+        if (line[q] > gmax) { gmax = line[q]; q0 = q; }
+    int qq[5];
+    if (q0 <= 2) { for (int m = 0; m < 5; ++m) qq[m] = 1 + m; }
+    else if (q0 >= nl - 1) { for (int m = 0; m < 5; ++m) qq[m] = nl - 4 + m; }
+    else { for (int m = 0; m < 5; ++m) qq[m] = q0 - 2 + m; }
+    double sk[5], fk[5], fstar, sstar;
+    for (int m = 0; m < 5; ++m) { sk[m] = along[qq[m]]; fk[m] = line[qq[m]]; }
+    fit_parabola_ls5_2d(sk, fk, +1, &fstar, &sstar);
+    if (comp == 0 && rb) {
+        const double yLen = yp[ny + 1];
+        if (sstar > 0.5 * yLen) sstar = yLen - sstar;
+    }
+    out->value = fstar * coef;
+    out->pos1 = sstar;
+    out->pos2 = 0.0;
+    out->mid = mid;
+    return std::isfinite(fstar) ? LBM_OK : LBM_ERR_DIVERGED;
 }
 
 // ------------------------------------------------------------------------------------

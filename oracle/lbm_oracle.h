@@ -50,6 +50,10 @@ int ora_check(ora_handle* h, double* errU, double* errT);
 int ora_calNuRe(ora_handle* h, double* Nu, double* Re);
 int ora_RBcalc_Nu_global(ora_handle* h, double* Nu);
 int ora_RBcalc_Nu_wall_avg(ora_handle* h, lbm_nu_wall* out);
+int ora_SideHeatedcalc_Nu_global(ora_handle* h, double* Nu);
+int ora_SideHeatedcalc_Nu_wall_avg(ora_handle* h, lbm_nu_wall* out);
+/* comp: 0 u, 1 v, 2 w; rb: 1 for the RB form of the 2D u line (RBcalc_umid_max). */
+int ora_mid_max(ora_handle* h, int comp, int rb, lbm_mid_max* out);
 
 int ora_get_state(ora_handle* h, int field, double* dst, size_t count);
 int ora_set_state(ora_handle* h, int field, const double* src, size_t count);

@@ -69,6 +69,9 @@ def lib():
         L.ora_calNuRe.argtypes = [vp, dp, dp]
         L.ora_RBcalc_Nu_global.argtypes = [vp, dp]
         L.ora_RBcalc_Nu_wall_avg.argtypes = [vp, vp]
+        L.ora_SideHeatedcalc_Nu_global.argtypes = [vp, dp]
+        L.ora_SideHeatedcalc_Nu_wall_avg.argtypes = [vp, vp]
+        L.ora_mid_max.argtypes = [vp, i32, i32, vp]
         L.ora_get_state.argtypes = [vp, i32, dp, C.c_size_t]
         L.ora_set_state.argtypes = [vp, i32, dp, C.c_size_t]
         L.ora_transform_matrices.argtypes = [i32, dp, dp]
@@ -156,6 +159,22 @@ class Oracle:
         w = struct_type()
         st = lib().ora_RBcalc_Nu_wall_avg(self._h, C.byref(w))
         return w, st
+
+    def SideHeatedcalc_Nu_global(self):
+        a = C.c_double()
+        st = lib().ora_SideHeatedcalc_Nu_global(self._h, C.byref(a))
+        return a.value, st
+
+    def SideHeatedcalc_Nu_wall_avg(self, struct_type):
+        w = struct_type()
+        st = lib().ora_SideHeatedcalc_Nu_wall_avg(self._h, C.byref(w))
+        return w.as_dict(), st
+
+    def mid_max(self, comp, rb, struct_type):
+        """comp 0/1/2 = u/v/w; rb: the RB form of the 2D u line."""
+        m = struct_type()
+        st = lib().ora_mid_max(self._h, int(comp), int(rb), C.byref(m))
+        return m.as_dict(), st
 
     def get(self, field_id, shape):
         a = np.empty(shape, dtype=np.float64)

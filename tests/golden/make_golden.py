@@ -282,6 +282,7 @@ def step_fixture(ref_dir, case):
         subs.step(ns)
     for name in FIELDS_OUT[dim]:
         out["out_" + name] = to_fortran_layout(ns[name], inner, name in ("f", "g", "f_post", "g_post"))
+    diag = diagnostics(subs, ns, dim, case)
     # restart from the stepped f and g: initial with loadInitField = 1 reads them and calls
     # reconstruct_macro_from_fg, whose first statement (call macroT) the translation drops
     subs.run("macroT", ns)
@@ -291,7 +292,69 @@ def step_fixture(ref_dir, case):
     meta = {k: v for k, v in case.items() if k != "defines"}
     meta["defines"] = sorted(defines)
     meta["constants"] = {k: consts[k] for k in ("tauf", "viscosity", "diffusivity", "gBeta", "Qk", "paraA")}
+    meta["diagnostics"] = diag
     return out, meta
+
+
+def coords(n, L):
+    """xp(0:n+1) as the reference sets it (3DRB.F90:444-465, 2DRB.F90:463-476)."""
+    c = np.zeros(n + 2)
+    c[n + 1] = float(n)
+    for i in range(1, n + 1):
+        c[i] = float(i) - 0.5
+    return c / L
+
+
+def diagnostics(subs, ns0, dim, case):
+    """The reference's post-processing subroutines on the stepped state, each on a fresh
+    copy of the module namespace; returns their results by name."""
+    import copy
+    L = ns0["lengthUnit"]
+    base = dict(ns0)
+    base["xp"] = coords(case["nx"], L)
+    base["yp"] = coords(case["ny"], L)
+    if dim == 3:
+        base["zp"] = coords(case["nz"], L)
+    base["dimensionlessTime"] = 0
+    base["NuVolAvg"] = np.zeros(16)
+    base["ReVolAvg"] = np.zeros(16)
+    wall_keys = ("Nu_hot", "Nu_cold", "Nu_middle", "Nu_hot_max", "Nu_hot_max_position", "Nu_hot_min",
+                 "Nu_hot_min_position")
+    res = {}
+
+    def run(name, *args):
+        ns = {k: (copy.deepcopy(v) if isinstance(v, np.ndarray) else v) for k, v in base.items()}
+        if args:
+            subs.module = ns
+            subs._call(name, list(args))
+            return subs.last_ns
+        subs.run(name, ns)
+        return ns
+
+    ns = run("calNuRe")
+    res["calNuRe"] = {"Nu": float(ns["NuVolAvg"][1]), "Re": float(ns["ReVolAvg"][1])}
+    for name in ("RBcalc_Nu_global", "SideHeatedcalc_Nu_global"):
+        res[name] = {"Nu_global": float(run(name)["Nu_global"])}
+    for name in ("RBcalc_Nu_wall_avg", "SideHeatedcalc_Nu_wall_avg"):
+        ns = run(name)
+        res[name] = {k: float(ns[k]) for k in wall_keys}
+    vsc = base["velocityScaleCompare"]
+    if dim == 2:
+        for name, keys in (("SideHeatedcalc_umid_max", ("umax_fit", "y_fit", "xmid")),
+                           ("RBcalc_umid_max", ("umax_fit", "y_fit", "xmid")),
+                           ("SideHeatedcalc_vmid_max", ("vmax_fit", "x_fit", "ymid")),
+                           ("RBcalc_vmid_max", ("vmax_fit", "x_fit", "ymid"))):
+            ns = run(name)
+            res[name] = {"value": float(ns[keys[0]] * ns["coef"]), "pos1": float(ns[keys[1]]), "pos2": 0.0,
+                         "mid": float(ns[keys[2]])}
+    else:
+        for name, keys in (("calc_umid_max_common", ("umax", "yAtU", "zAtU", "targetX")),
+                           ("calc_vmid_max_common", ("vmax", "xAtV", "zAtV", "targetY")),
+                           ("calc_wmid_max_common", ("wmax", "xAtW", "yAtW", "targetZ"))):
+            ns = run(name, "tag")
+            res[name] = {"value": float(ns[keys[0]] * vsc), "pos1": float(ns[keys[1]]), "pos2": float(ns[keys[2]]),
+                         "mid": float(ns[keys[3]])}
+    return res
 
 
 STEP_CASES = [

@@ -1,17 +1,23 @@
-"""Mechanical Fortran -> Python transliteration of the reference's step subroutines.
+"""Mechanical Fortran -> Python transliteration of the reference's subroutines.
 
 Used only by tests/golden/make_golden.py, in a container where the reference source is
-mounted, to execute the reference's own statements (collision, streaming, bounceback,
-macro, collisionT, streamingT, bouncebackT, macroT of 2DRB.F90 / 3DRB.F90) on small
-inputs and store the results as fixtures.  The translation is syntactic:
+mounted, to execute the reference's own statements (the time-step subroutines, the
+restart reconstruction and the post-processing diagnostics of 2DRB.F90 / 3DRB.F90) on
+small inputs and store the results as fixtures.  The translation is syntactic:
 
 * the C preprocessor switches are resolved for a chosen set of #defines;
-* `do v = a, b` / `enddo`, `if (...) then` / `elseif` / `else` / `endif` and one-line
-  `if (...) stmt` become Python blocks; declarations, OpenMP directives, I/O and comments
-  are dropped; `real(kind=8), parameter :: X = expr` inside a body becomes `X = expr`;
+* `do v = a, b` / `do while (c)` / `enddo`, `if (...) then` / `elseif` / `else` /
+  `endif` and one-line `if (...) stmt` become Python blocks; OpenMP directives, I/O and
+  comments are dropped; `real(kind=8), parameter :: X = expr` inside a body becomes
+  `X = expr`;
+* declarations of local arrays allocate zero arrays large enough for their Fortran index
+  ranges (indices are used as written); dummy arguments are bound to the actual arguments
+  of each call, and after a call the actual arguments that are variables receive the
+  dummies' final values (Fortran passes by reference);
 * `1.0d0` literals become Python floats, `dble`/`dsqrt`/`dabs` map to float/math.sqrt/abs,
-  relational and logical operators map to Python's, array references `a(i,j)` become
-  `a[i,j]` on numpy arrays allocated with room for the Fortran index ranges.
+  `min`/`max`/`mod`/`huge` to their Python equivalents, relational and logical operators
+  map to Python's, array references `a(i,j)` become `a[i,j]`, a section `a(l:h)` becomes
+  `a[l:h+1]`, and an array constructor `a = (/ ... /)` fills `a` from its lower bound.
 
 Python evaluates + - * / left to right with one IEEE double rounding per operation and no
 fused multiply-add, which is how gfortran evaluates these expressions without -ffast-math,
@@ -22,10 +28,15 @@ import re
 
 import numpy as np
 
+# module arrays of commondata / commondata3d that the subroutines index
 ARRAYS = {"f", "f_post", "g", "g_post", "rho", "u", "v", "w", "T", "Bx_prev", "By_prev", "Bz_prev", "Fx", "Fy",
           "ex", "ey", "ez", "opp", "exT", "eyT", "ezT", "oppT", "omega", "omegaT", "m", "meq", "m_post", "s",
-          "fSource", "n", "neq", "q", "n_post", "up", "vp", "wp", "Tp", "un"}
+          "fSource", "n", "neq", "q", "n_post", "up", "vp", "wp", "Tp", "un", "xp", "yp", "zp", "NuVolAvg",
+          "ReVolAvg"}
 LOCAL_ARRAYS = ["m", "meq", "m_post", "s", "fSource", "n", "neq", "q", "n_post", "un"]
+INTRINSIC_SKIP = ("use ", "implicit ", "write", "open", "close", "stop", "print", "flush")
+# `return` hands the subroutine's variables back to the caller's namespace first
+RETURN = "ns.update({k: v for k, v in locals().items() if k != 'ns'}); return"
 
 
 def preprocess(lines, defines):
@@ -49,23 +60,39 @@ def preprocess(lines, defines):
 
 
 def extract(lines, name):
-    start = None
+    """(dummy argument names, body lines) of subroutine `name`."""
+    start, args = None, []
     for k, ln in enumerate(lines):
-        if re.match(r"\s*subroutine\s+%s\s*\(\s*\)" % re.escape(name), ln, re.I):
+        m = re.match(r"\s*subroutine\s+%s\s*\(([^)]*)\)" % re.escape(name), ln, re.I)
+        if m:
             start = k + 1
+            args = [a.strip() for a in m.group(1).split(",") if a.strip()]
             break
     if start is None:
         raise ValueError("subroutine %s not found" % name)
     for k in range(start, len(lines)):
         if re.match(r"\s*end\s+subroutine\s+%s\b" % re.escape(name), lines[k], re.I):
-            return lines[start:k]
+            return args, lines[start:k]
     raise ValueError("end of %s not found" % name)
 
 
 def strip_comment(ln):
     if ln.lstrip().startswith("!$"):
         return ""
-    return ln.split("!")[0]
+    # a '!' inside a string literal is not a comment
+    out, quote = [], None
+    for ch in ln:
+        if quote:
+            out.append(ch)
+            if ch == quote:
+                quote = None
+            continue
+        if ch in "'\"":
+            quote = ch
+        elif ch == "!":
+            break
+        out.append(ch)
+    return "".join(out)
 
 
 def join_continuations(lines):
@@ -73,8 +100,6 @@ def join_continuations(lines):
     for ln in lines:
         s = strip_comment(ln).rstrip()
         if not s.strip():
-            if buf:
-                continue
             continue
         if buf:
             s = buf + " " + s.strip().lstrip("&")
@@ -86,11 +111,28 @@ def join_continuations(lines):
     return out
 
 
-def convert_expr(e):
+def split_top(text, sep=","):
+    parts, depth, cur = [], 0, ""
+    for ch in text:
+        if ch in "([":
+            depth += 1
+        elif ch in ")]":
+            depth -= 1
+        if ch == sep and depth == 0:
+            parts.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    parts.append(cur)
+    return [p.strip() for p in parts]
+
+
+def convert_expr(e, arrays=ARRAYS):
     e = re.sub(r"(\d+\.\d*|\d+)[dD]([+-]?\d+)", lambda m: "%se%s" % (m.group(1), m.group(2)), e)
     for a, b in ((".EQ.", "=="), (".NE.", "!="), (".GT.", ">"), (".LT.", "<"), (".GE.", ">="), (".LE.", "<="),
                  (".AND.", " and "), (".OR.", " or "), (".NOT.", " not "), (".TRUE.", "True"), (".FALSE.", "False")):
         e = re.sub(re.escape(a), b, e, flags=re.I)
+    e = re.sub(r"/=", "!=", e)
     e = re.sub(r"\bdble\s*\(", "float(", e)
     e = re.sub(r"\bdsqrt\s*\(", "math.sqrt(", e)
     e = re.sub(r"\bdabs\s*\(", "abs(", e)
@@ -104,7 +146,7 @@ def convert_expr(e):
             j = k2
             while j < len(e) and e[j] == " ":
                 j += 1
-            if j < len(e) and e[j] == "(" and name in ARRAYS:
+            if j < len(e) and e[j] == "(" and name in arrays:
                 out.append(name + "[")
                 stack.append("]")
                 k = j + 1
@@ -121,28 +163,124 @@ def convert_expr(e):
         else:
             out.append(ch)
         k += 1
-    return "".join(out)
+    s = "".join(out)
+    # Fortran sections l:h are inclusive
+    return re.sub(r"\[([^\[\]:]*):([^\[\]:,]*)\]", lambda m: "[%s:(%s)+1]" % (m.group(1), m.group(2)), s)
 
 
-def to_python(body_lines, defines):
+def parse_declaration(t):
+    """(dummy?, integer?, [(name, dims or None)]) of a declaration line `spec :: list`."""
+    spec, rest = t.split("::", 1)
+    mdim = re.search(r"dimension\s*\((.*)\)", spec, re.I)
+    common = split_top(mdim.group(1)) if mdim else None
+    items = []
+    for part in split_top(rest):
+        if not part or "=" in part:
+            continue
+        m = re.match(r"(\w+)\s*(\((.*)\))?$", part)
+        if m:
+            items.append((m.group(1), split_top(m.group(3)) if m.group(3) else common))
+    return "intent" in spec.lower(), "integer" in spec.lower(), items
+
+
+def to_python(body_lines, defines, dummies=()):
     lines = join_continuations(preprocess(body_lines, defines))
-    py, ind = [], 1
-    pad = lambda: "    " * ind
+    # pass 1: array names (module, local, dummy)
+    arrays = set(ARRAYS)
+    local_alloc, local_scalars, ints, bounds = [], [], set(), {}
     for s in lines:
         t = s.strip()
+        if "::" in t and "parameter" not in t.lower().split("::")[0] and not t.lower().startswith("character"):
+            is_dummy, is_int, items = parse_declaration(t)
+            for name, dims in items:
+                if dims is None:
+                    if is_int:
+                        ints.add(name)
+                    if not is_dummy and name not in dummies:
+                        local_scalars.append((name, is_int))
+                    continue
+                arrays.add(name)
+                if len(dims) == 1:
+                    lo, hi = dims[0].split(":", 1) if ":" in dims[0] else ("1", dims[0])
+                    bounds[name] = (lo.strip(), hi.strip())
+                if not is_dummy and name not in dummies:
+                    local_alloc.append((name, dims, is_int))
+    py, ind = [], 1
+    pad = lambda: "    " * ind
+    cx = lambda e: convert_expr(e, arrays)
+    lower = {}
+    for name, dims, is_int in local_alloc:
+        if name in LOCAL_ARRAYS:
+            continue  # step work arrays come from the namespace
+        shape = []
+        for d in dims:
+            lo, hi = d.split(":", 1) if ":" in d else ("1", d)
+            shape.append("int(%s) + 1" % cx(hi))
+            lower.setdefault(name, cx(lo))
+        py.append(pad() + "%s = np.zeros((%s,)%s)" % (name, ", ".join(shape), ", dtype=np.int64" if is_int else ""))
+    # Fortran locals start undefined; outputs of calls must exist before the call
+    for name, is_int in local_scalars:
+        py.append(pad() + "%s = %s" % (name, "0" if is_int else "0.0"))
+    # module scalars the body assigns are locals of the Python function: start them from the
+    # module's values (a statement like `x = x + 1` reads them first)
+    declared = {n for n, _ in local_scalars} | set(dummies) | arrays
+    assigned = []
+    for s in lines:
+        m = re.match(r"^\s*(?:if\s*\(.*\)\s*)?(\w+)\s*=(?!=)", s.strip(), re.I)
+        if m and m.group(1) not in declared and m.group(1) not in assigned and m.group(1).lower() not in ("do", "if"):
+            assigned.append(m.group(1))
+    for name in assigned:
+        py.append(pad() + "if %r in ns: %s = ns[%r]" % (name, name, name))
+    local_names = ({n for n, _ in local_scalars} | set(dummies) | set(assigned)) - arrays
+
+    def assignment(stmt):
+        """`name = expr` with an integer target truncates like Fortran's integer assignment."""
+        m = re.match(r"^(\w+)\s*=(?!=)\s*(.+)$", stmt)
+        if m and m.group(1) in ints:
+            return "%s = int(%s)" % (m.group(1), cx(m.group(2)))
+        return cx(stmt)
+
+    def whole_array_reductions(t):
+        # minval(a) / maxval(a) over the declared index range of a 1-D array
+        return re.sub(r"\b(minval|maxval)\s*\(\s*(\w+)\s*\)",
+                      lambda m: "_%s(%s, %s, %s)" % (m.group(1).lower(), m.group(2), *bounds[m.group(2)]), t)
+
+    for s in lines:
+        t = whole_array_reductions(s.strip())
         low = t.lower()
-        if low.startswith(("use ", "implicit ", "return", "write", "open", "close", "call ", "stop")):
-            continue
-        mpar = re.match(r"real\s*\(\s*kind\s*=\s*8\s*\)\s*,\s*parameter\s*::\s*(\w+)\s*=\s*(.+)$", t, re.I)
+        if low.startswith(INTRINSIC_SKIP) or low.startswith("character") or "ctime(" in low:
+            continue  # I/O, declarations of strings, wall-clock time stamps
+        mpar = re.match(r"(real|integer)\s*\(\s*kind\s*=\s*\d\s*\)\s*,\s*parameter\s*::\s*(.+)$", t, re.I)
         if mpar:
-            py.append(pad() + "%s = %s" % (mpar.group(1), convert_expr(mpar.group(2))))
+            for item in split_top(mpar.group(2)):
+                name, expr = item.split("=", 1)
+                py.append(pad() + "%s = %s" % (name.strip(), cx(expr.strip())))
             continue
         if "::" in t:
             continue  # declaration
+        if re.match(r"return$", t, re.I):
+            py.append(pad() + RETURN)
+            continue
+        mcall = re.match(r"call\s+(\w+)\s*\((.*)\)\s*$", t, re.I)
+        if mcall:
+            actual = split_top(mcall.group(2))
+            py.append(pad() + "_r = _call(%r, [%s])" % (mcall.group(1), ", ".join(cx(a) for a in actual)))
+            for pos, a in enumerate(actual):
+                # write back into this subroutine's own scalars (module parameters stay)
+                if a in local_names:
+                    py.append(pad() + "%s = _r[%d]" % (a, pos))
+            continue
+        if re.match(r"call\s+\w+\s*$", t, re.I) or re.match(r"call\s+\w+\s*\(\s*\)\s*$", t, re.I):
+            continue  # argument-less calls (macroT, ...) are run by the caller
+        mwhile = re.match(r"do\s+while\s*\((.*)\)$", t, re.I)
+        if mwhile:
+            py.append(pad() + "while %s:" % cx(mwhile.group(1)))
+            ind += 1
+            py.append(pad() + "pass")
+            continue
         mdo = re.match(r"do\s+(\w+)\s*=\s*(.+?)\s*,\s*(.+)$", t, re.I)
         if mdo:
-            py.append(pad() + "for %s in range(%s, (%s) + 1):" % (mdo.group(1), convert_expr(mdo.group(2)),
-                                                                convert_expr(mdo.group(3))))
+            py.append(pad() + "for %s in range(%s, (%s) + 1):" % (mdo.group(1), cx(mdo.group(2)), cx(mdo.group(3))))
             ind += 1
             py.append(pad() + "pass")
             continue
@@ -151,14 +289,14 @@ def to_python(body_lines, defines):
             continue
         mif = re.match(r"if\s*\((.*)\)\s*then$", t, re.I)
         if mif:
-            py.append(pad() + "if %s:" % convert_expr(mif.group(1)))
+            py.append(pad() + "if %s:" % cx(mif.group(1)))
             ind += 1
             py.append(pad() + "pass")  # blocks whose only statements (I/O, stop) were dropped
             continue
         melif = re.match(r"else\s*if\s*\((.*)\)\s*then$", t, re.I)
         if melif:
             ind -= 1
-            py.append(pad() + "elif %s:" % convert_expr(melif.group(1)))
+            py.append(pad() + "elif %s:" % cx(melif.group(1)))
             ind += 1
             py.append(pad() + "pass")
             continue
@@ -170,6 +308,13 @@ def to_python(body_lines, defines):
             continue
         if re.match(r"end\s*if$", t, re.I):
             ind -= 1
+            continue
+        mctor = re.match(r"(\w+)\s*=\s*\(/(.*)/\)$", t)
+        if mctor:
+            items = split_top(mctor.group(2))
+            lo = lower.get(mctor.group(1), "1")
+            py.append(pad() + "%s[%s:%s + %d] = [%s]" % (mctor.group(1), lo, lo, len(items),
+                                                       ", ".join(cx(i) for i in items)))
             continue
         m1 = re.match(r"if\s*\((.*?)\)\s+(\w.*)$", t, re.I)
         if m1 and "=" in m1.group(2):
@@ -184,41 +329,72 @@ def to_python(body_lines, defines):
                         cut = k
                         break
             cond, stmt = t[t.index("(") + 1:cut], t[cut + 1:].strip()
-            py.append(pad() + "if %s: %s" % (convert_expr(cond), convert_expr(stmt)))
+            if stmt.lower().startswith(INTRINSIC_SKIP):
+                continue
+            if re.match(r"return$", stmt, re.I):
+                py.append(pad() + "if %s: %s" % (cx(cond), RETURN))
+                continue
+            py.append(pad() + "if %s: %s" % (cx(cond), assignment(stmt)))
             continue
-        py.append(pad() + convert_expr(t))
+        py.append(pad() + assignment(t))
     return py
 
 
 def compile_subroutine(src_lines, name, defines):
-    body = extract(src_lines, name)
+    args, body = extract(src_lines, name)
     code = ["def %s(ns):" % name, "    globals().update(ns)"]
     code += ["    %s = ns.get('%s')" % (a, a) for a in sorted(ARRAYS)]
-    code += to_python(body, defines)
+    code += ["    %s = ns['%s']" % (a, a) for a in args]
+    code += to_python(body, defines, dummies=args)
     code += ["    ns.update({k: v for k, v in locals().items() if k != 'ns'})"]
-    return "\n".join(code)
+    return args, "\n".join(code)
+
+
+def _huge(x):
+    return 1.7976931348623157e308
 
 
 class ReferenceSubroutines:
-    """The step subroutines of one reference file, executable on a namespace of module
-    variables (scalars and numpy arrays indexed with the Fortran bounds)."""
+    """Subroutines of one reference file, executable on a namespace of module variables
+    (scalars and numpy arrays indexed with the Fortran bounds)."""
 
     NAMES = ("collision", "streaming", "bounceback", "macro", "collisionT", "streamingT", "bouncebackT", "macroT")
 
     def __init__(self, path, defines, extra=()):
-        src = open(path, encoding="utf-8-sig").read().splitlines()
+        self.src = open(path, encoding="utf-8-sig").read().splitlines()
+        self.defines = defines
         self.source = {}
         self.fn = {}
+        self.args = {}
+        self.module = None
         for name in self.NAMES + tuple(extra):
-            code = compile_subroutine(src, name, defines)
-            self.source[name] = code
-            glb = {"math": math, "np": np}
-            exec(code, glb)
-            self.fn[name] = glb[name]
+            self.add(name)
+
+    def add(self, name):
+        args, code = compile_subroutine(self.src, name, self.defines)
+        self.source[name] = code
+        self.args[name] = args
+        glb = {"math": math, "np": np, "min": min, "max": max, "mod": lambda a, b: int(math.fmod(a, b)),
+               "_minval": lambda a, lo, hi: min(a[lo:hi + 1]), "_maxval": lambda a, lo, hi: max(a[lo:hi + 1]),
+               "huge": _huge, "ctime": lambda *a: "", "time": lambda *a: 0, "_call": self._call}
+        exec(code, glb)
+        self.fn[name] = glb[name]
+
+    def _call(self, name, actual):
+        if name not in self.fn:
+            self.add(name)
+        ns = dict(self.module)
+        ns.update(zip(self.args[name], actual))
+        self.fn[name](ns)
+        self.last_ns = ns
+        return [ns[a] for a in self.args[name]]
 
     def run(self, name, ns):
         for a in LOCAL_ARRAYS:
             ns.setdefault(a, np.zeros(32))
+        if name not in self.fn:
+            self.add(name)
+        self.module = ns
         self.fn[name](ns)
 
     def step(self, ns):
