@@ -142,6 +142,11 @@ static int validate(const lbm_params* p) {
     }
     if (p->precision < LBM_FP64 || p->precision > LBM_FP16) return LBM_ERR_PARAM;
     if (p->pattern != LBM_PATTERN_AB) return LBM_ERR_PARAM;  // the in-place AA pattern is not built yet
+    // the magnetic force exists in the 2D program only (2DRB.F90:88-92); the FP32/FP16 forms
+    // carry only F_y in their lag state
+    if (p->side_heated_ha && (p->dim != 2 || p->precision != LBM_FP64 || !std::isfinite(p->Ha) ||
+                              !std::isfinite(p->phi_deg)))
+        return LBM_ERR_PARAM;
     return LBM_OK;
 }
 
@@ -178,6 +183,9 @@ extern "C" int lbm_params_default(int dim, lbm_params* out) {
     out->pattern = LBM_PATTERN_AB;
     out->seed = 20261203ULL;
     out->noise_amp = 0.0;
+    out->side_heated_ha = 0;
+    out->Ha = 20.0;
+    out->phi_deg = 0.0;
     return LBM_OK;
 }
 
@@ -240,6 +248,14 @@ extern "C" int lbm_derive_constants(const lbm_params* p, lbm_constants* c) {
         }
     }
     c->SG = 1.0 - 0.5 * c->Qk;
+    if (p->side_heated_ha) {
+        // 2DRB.F90:67, 89-91: pi = acos(-1), phi = deg*(pi/180), B2sigemarho = Ha**2 nu / L^2
+        const double pi = std::acos(-1.0);
+        c->phi = p->phi_deg * (pi / 180.0);
+        c->B2sigemarho = (p->Ha * p->Ha * c->viscosity) / (L * L);
+        c->sinphi = std::sin(c->phi);
+        c->cosphi = std::cos(c->phi);
+    }
     if (!(c->tauf > 0.5)) return LBM_ERR_PARAM;
     return LBM_OK;
 }
@@ -372,6 +388,10 @@ extern "C" int lbm_create(const lbm_params* p, int device, lbm_handle** out) {
     P.geqc = c.thermalGeqCoeff;
     P.use_g = p->use_g ? 1 : 0;
     P.legacy = p->legacy_thermal ? 1 : 0;
+    P.ha = p->side_heated_ha ? 1 : 0;
+    P.B2 = c.B2sigemarho;
+    P.sinphi = c.sinphi;
+    P.cosphi = c.cosphi;
     DiagScalars& D = h->dsc;
     D.Thot = p->Thot;
     D.Tcold = p->Tcold;

@@ -68,8 +68,12 @@ __device__ __forceinline__ void collide_2d(const double* F, double rho, double u
     s[0] = 0.0; s[1] = P.Snu; s[2] = P.Snu; s[3] = 0.0; s[4] = P.Sq;
     s[5] = 0.0; s[6] = P.Sq;  s[7] = P.Snu; s[8] = P.Snu;
 
-    const double Fx = 0.0;
-    const double Fy = rho * P.gBeta * (T - P.Tref);
+    double Fx = 0.0;
+    double Fy = rho * P.gBeta * (T - P.Tref);
+    if (P.ha) {  // SideHeatedHa (2DRB.F90:722-726): buoyancy plus the magnetic force
+        Fx = 0.0 + P.B2 * (v * P.sinphi * P.cosphi - u * P.sinphi * P.sinphi);
+        Fy = rho * P.gBeta * (T - P.Tref) + rho * P.B2 * (u * P.sinphi * P.cosphi - v * P.cosphi * P.cosphi);
+    }
     FxOut = Fx;
     FyOut = Fy;
 
@@ -703,8 +707,9 @@ __global__ void k_materialize(Geo g, PhysC P, ExactArrays A, const double* __res
 // ------------------------------------------------------------------------------------
 // restart reconstruction (reconstruct_macro_from_fg, 2DRB.F90:1144-1200,
 // 3DRB.F90:1392-1463): T = sum g (the macroT call), rho = sum f, u = (mom + F/2)/rho with
-// F = rho gBeta (T - Tref).  The reference iterates that assignment three times; the
-// right-hand side does not depend on u, so one evaluation gives the same value.
+// F = rho gBeta (T - Tref).  The reference iterates that assignment three times; without
+// the magnetic force the right-hand side does not depend on u, so one pass gives the same
+// value.
 // ------------------------------------------------------------------------------------
 template <int D>
 __global__ void k_reconstruct(Geo g, PhysC P, ExactArrays A, unsigned int* bad) {
@@ -727,9 +732,19 @@ __global__ void k_reconstruct(Geo g, PhysC P, ExactArrays A, unsigned int* bad) 
         const double momy = F[2] - F[4] + F[5] + F[6] - F[7] - F[8];
         double u = 0.0, v = 0.0, Fx = 0.0, Fy = 0.0;
         if (rho > 0.0) {
-            Fy = rho * P.gBeta * (T - P.Tref);
-            u = (momx + 0.5 * Fx) / rho;
-            v = (momy + 0.5 * Fy) / rho;
+            u = momx / rho;
+            v = momy / rho;
+            // three fixed-point passes (2DRB.F90:1165-1177); with the magnetic force F depends on u
+            for (int iter = 0; iter < (P.ha ? 3 : 1); ++iter) {
+                Fx = 0.0;
+                Fy = rho * P.gBeta * (T - P.Tref);
+                if (P.ha) {
+                    Fx = P.B2 * (v * P.sinphi * P.cosphi - u * P.sinphi * P.sinphi);
+                    Fy = rho * P.gBeta * (T - P.Tref) + rho * P.B2 * (u * P.sinphi * P.cosphi - v * P.cosphi * P.cosphi);
+                }
+                u = (momx + 0.5 * Fx) / rho;
+                v = (momy + 0.5 * Fy) / rho;
+            }
         } else {
             *bad = 1u;
         }

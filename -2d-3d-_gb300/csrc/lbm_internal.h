@@ -16,6 +16,8 @@ struct PhysC {
     double Qk, Qnu, SG, paraA;          // thermal relaxation, M1G factor, legacy a_T
     double omegaT0, omegaT1, geqc;      // thermal weights and g^eq coefficient
     int use_g, legacy;
+    int ha;                             // SideHeatedHa: magnetic force in the 2D collision
+    double B2, sinphi, cosphi;          // B2sigemarho, sin(phi), cos(phi)
 };
 
 // Inputs of `initial` that depend on host-side math (sin/cos of the RB perturbation).

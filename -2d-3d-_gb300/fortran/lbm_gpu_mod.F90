@@ -45,6 +45,8 @@ module lbm_gpu_mod
     integer(c_int32_t) :: use_g, legacy_thermal, precision, pattern
     integer(c_int64_t) :: seed
     real(c_double)     :: noise_amp
+    integer(c_int32_t) :: side_heated_ha, reserved0   ! #define SideHeatedHa (2D)
+    real(c_double)     :: Ha, phi_deg
   end type lbm_params
 
   type, bind(C) :: lbm_nu_wall

@@ -36,6 +36,7 @@ class LbmParams(C.Structure):
         ("use_g", C.c_int32), ("legacy_thermal", C.c_int32),
         ("precision", C.c_int32), ("pattern", C.c_int32),
         ("seed", C.c_uint64), ("noise_amp", C.c_double),
+        ("side_heated_ha", C.c_int32), ("reserved0", C.c_int32), ("Ha", C.c_double), ("phi_deg", C.c_double),
     ]
 
     def copy(self):
@@ -56,7 +57,8 @@ class LbmConstants(C.Structure):
         "lengthUnit", "Tref", "tauf", "viscosity", "diffusivity", "paraA",
         "gBeta", "timeUnit", "velocityUnit", "heatFluxScale", "velocityScaleCompare",
         "Snu", "Sq", "Se", "Seps", "Spi", "Sm",
-        "taug", "Qk", "Qnu", "SG", "thermalGeqCoeff", "cs2T", "omegaT0", "omegaT1")]
+        "taug", "Qk", "Qnu", "SG", "thermalGeqCoeff", "cs2T", "omegaT0", "omegaT1",
+        "B2sigemarho", "phi", "sinphi", "cosphi")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

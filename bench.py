@@ -35,6 +35,10 @@ METRIC = "coupled MLUPS (D3Q19/D3Q7 MRT-LBM step)"
 UNIT = "MLUPS"
 N_CELL_EDGE = 128
 BYTES_PER_CELL = {"fp64": 416, "fp32": 208, "fp16": 104}  # populations read + written once
+# FP64 work of the plain method per coupled cell update (3D), counted by ncu on the fused
+# kernels (sass thread instructions, flow + thermal): dadd 466, dmul 143, dfma 106.
+FP64_INST_PER_CELL = 466 + 143 + 106
+FP64_FLOP_PER_CELL = 466 + 143 + 2 * 106
 DTYPE = {"fp64": "f64", "fp32": "f32", "fp16": "f16-storage/f32-arith"}
 FALLBACK_HBM_GBS = 6800.0
 
@@ -63,14 +67,37 @@ def measured_hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic():
-    """Per-launch DRAM bytes of each fused kernel from the committed ncu summary, if any."""
+def ncu_traffic(cells):
+    """DRAM bytes per step (flow + thermal launch) of each storage form from the committed ncu
+    capture, scaled to `cells` by the cells it was captured on; None when absent."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(path) as fh:
-            return json.load(fh)
+            data = json.load(fh)
     except Exception:
         return {}
+    return {prec: v["bytes_per_step"] * cells / v["cells"] for prec, v in data.items() if isinstance(v, dict)}
+
+
+def fp64_peak_tflops():
+    """cuBLAS DGEMM (8192^3, best of 3) on this GPU: the FP64 denominator of the plain method."""
+    import torch
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    c = a @ b
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = float("inf")
+    for _ in range(3):
+        e0.record()
+        c = a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b, c
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
 class ClockSampler:
@@ -403,7 +430,7 @@ def run_gpu(args):
     from lbmgpu import build as lbuild
     lbuild.build()
     peak, peak_kind = measured_hbm_peak()
-    traffic = ncu_traffic()
+    traffic = ncu_traffic(args.size ** 3)
     results = {}
     precs = [x for x in args.precisions.split(",") if x]
     with ClockSampler(local) as clk:
@@ -427,6 +454,21 @@ def run_gpu(args):
                 "traffic": t, "peak_kind": peak_kind, "kernel": desc,
                 "algorithmic_bytes_per_cell": BYTES_PER_CELL[prec]}
 
+    def roof_fp64():
+        # the plain method's bound: FP64 issue (DRAM stays below 11% busy)
+        r = results["fp64"]
+        step_s = (r["ms_flow"] + r["ms_thermal"]) / 1e3
+        tflops = FP64_FLOP_PER_CELL * cells / step_s / 1e12
+        pk = fp64_peak_tflops()
+        sm_mhz = clocks.get("sm_mhz") or 2070.0
+        import torch
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        issue_peak = 2.0 * sms * sm_mhz * 1e6  # FP64 pipe: 2 thread instructions per clock per SM
+        return {"bound": "fp64", "achieved": tflops, "peak": pk, "unit": "TFLOP/s", "frac": tflops / pk,
+                "peak_kind": "measured live: cuBLAS DGEMM 8192^3", "flop_per_cell": FP64_FLOP_PER_CELL,
+                "issue_frac": FP64_INST_PER_CELL * cells / step_s / issue_peak,
+                "issue_peak_note": "FP64 pipe 2 thread instructions / clock / SM at the sampled SM clock"}
+
     head = results[precs[0]]
     line = {
         "metric": METRIC, "value": head["mlups"] * world, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -434,6 +476,7 @@ def run_gpu(args):
         "vs_baseline": None, "dtype": DTYPE[precs[0]], "data": "synthetic", "config": workload_config(args.size),
         "parallelism": "replicas" if world > 1 else "single GPU",
         "roofline": roof(precs[0]),
+        "roofline_fp64": roof_fp64() if "fp64" in results else None,
         "e2e": e2e,
         "gpu_launches": 2 * args.steps,
         "clocks": clocks,

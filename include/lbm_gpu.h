@@ -95,6 +95,10 @@ typedef struct lbm_params {
     int32_t pattern;        /* LBM_PATTERN_AB / LBM_PATTERN_AA                              */
     uint64_t seed;          /* seed of the initial temperature noise                        */
     double  noise_amp;      /* T += noise_amp*(2*xi-1), xi = splitmix64(seed ^ cell) in [0,1) */
+    int32_t side_heated_ha; /* SideHeatedHa: magnetic (Lorentz) force, 2D plain FP64 method    */
+    int32_t reserved0;      /* 0                                                            */
+    double  Ha;             /* Hartmann number (2DRB.F90:89, default 20)                     */
+    double  phi_deg;        /* field angle in degrees from +x (2DRB.F90:90, default 0)       */
 } lbm_params;
 
 /* Derived constants, computed exactly as the reference's `parameter` statements
@@ -105,6 +109,8 @@ typedef struct lbm_constants {
     double Snu, Sq, Se, Seps, Spi, Sm;      /* flow MRT rates (2D uses Snu, Sq)         */
     double taug, Qk, Qnu, SG, thermalGeqCoeff, cs2T;
     double omegaT0, omegaT1;                /* thermal weights: rest, moving             */
+    double B2sigemarho, phi, sinphi, cosphi; /* SideHeatedHa (2DRB.F90:88-92); sin/cos of phi
+                                               as the host's libm gives them                 */
 } lbm_constants;
 
 /* Wall Nusselt numbers of RBcalc_Nu_wall_avg (2DRB.F90:2308-2473, 3DRB.F90:2049-2210). */

@@ -141,6 +141,14 @@ static int derive(const lbm_params* p, lbm_constants* c) {
         }
     }
     c->SG = 1.0 - 0.5 * c->Qk;  // collisionT: SG = 1 - 0.5*Qk (2DRB.F90:915, 3DRB.F90:1113)
+    if (p->side_heated_ha) {
+        if (p->dim != 2) return LBM_ERR_PARAM;
+        const double pi = std::acos(-1.0);                             // 2DRB.F90:67
+        c->phi = p->phi_deg * (pi / 180.0);                            // 2DRB.F90:90
+        c->B2sigemarho = (p->Ha * p->Ha * c->viscosity) / (L * L);     // 2DRB.F90:91
+        c->sinphi = std::sin(c->phi);
+        c->cosphi = std::cos(c->phi);
+    }
     if (!(c->tauf > 0.5)) return LBM_ERR_PARAM;
     return LBM_OK;
 }
@@ -536,6 +544,8 @@ static void collision2d(ora_handle* h) {
     const int nx = h->nx, ny = h->ny;
     const lbm_constants& c = h->c;
     const double Snu = c.Snu, Sq = c.Sq, gBeta = c.gBeta, Tref = c.Tref;
+    const bool ha = h->p.side_heated_ha != 0;
+    const double B2 = c.B2sigemarho, sphi = c.sinphi, cphi = c.cosphi;
 #pragma omp parallel for schedule(static)
     for (int j = 1; j <= ny; ++j) {
         double m[9], m_post[9], meq[9], s[9], fSource[9];
@@ -561,6 +571,10 @@ static void collision2d(ora_handle* h) {
 
             double Fx = 0.0;
             double Fy = rho * gBeta * (T - Tref);
+            if (ha) {  // SideHeatedHa (2DRB.F90:722-726)
+                Fx = 0.0 + B2 * (v * sphi * cphi - u * sphi * sphi);
+                Fy = rho * gBeta * (T - Tref) + rho * B2 * (u * sphi * cphi - v * cphi * cphi);
+            }
             h->Fx[ci] = Fx;
             h->Fy[ci] = Fy;
 
@@ -1059,6 +1073,8 @@ extern "C" int ora_reconstruct_macro_from_fg(ora_handle* h) {
     ora_macroT(h);
     const double gBeta = h->c.gBeta, Tref = h->c.Tref;
     const bool useG = h->p.use_g != 0;
+    const bool ha = h->p.side_heated_ha != 0;
+    const double B2 = h->c.B2sigemarho, sphi = h->c.sinphi, cphi = h->c.cosphi;
     int bad = 0;
 #pragma omp parallel for schedule(static) reduction(| : bad)
     for (long long ci = 0; ci < (long long)h->ncell; ++ci) {
@@ -1094,9 +1110,18 @@ extern "C" int ora_reconstruct_macro_from_fg(ora_handle* h) {
             h->rho[ci] = rho;
             double u = 0.0, v = 0.0, Fx = 0.0, Fy = 0.0;
             if (rho > 0.0) {
-                Fy = rho * gBeta * (T - Tref);
-                u = (momx + 0.5 * Fx) / rho;
-                v = (momy + 0.5 * Fy) / rho;
+                u = momx / rho;
+                v = momy / rho;
+                for (int iter = 1; iter <= 3; ++iter) {  // 2DRB.F90:1165-1177
+                    Fx = 0.0;
+                    Fy = rho * gBeta * (T - Tref);
+                    if (ha) {
+                        Fx = B2 * (v * sphi * cphi - u * sphi * sphi);
+                        Fy = rho * gBeta * (T - Tref) + rho * B2 * (u * sphi * cphi - v * cphi * cphi);
+                    }
+                    u = (momx + 0.5 * Fx) / rho;
+                    v = (momy + 0.5 * Fy) / rho;
+                }
             } else {
                 bad = 1;
             }

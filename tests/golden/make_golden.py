@@ -256,6 +256,10 @@ def step_fixture(ref_dir, case):
     src_text = "\n".join(src_lines)
     defines = set(case["defines"])
     over = {"nx": case["nx"], "ny": case["ny"], "Rayleigh": case["Ra"], "Prandtl": case["Pr"], "Mach": case["Mach"]}
+    if "SideHeatedHa" in case["defines"]:
+        # Ha and the field angle (2DRB.F90:89-90); phi = deg*(pi/180) in the reference's order
+        over["Ha"] = case["Ha"]
+        over["phi"] = case["phi_deg"] * (math.acos(-1.0) / 180.0)
     if dim == 3:
         over["nz"] = case["nz"]
     consts = module_constants(src_lines, "commondata3d" if dim == 3 else "commondata", defines, over)
@@ -292,6 +296,8 @@ def step_fixture(ref_dir, case):
     meta = {k: v for k, v in case.items() if k != "defines"}
     meta["defines"] = sorted(defines)
     meta["constants"] = {k: consts[k] for k in ("tauf", "viscosity", "diffusivity", "gBeta", "Qk", "paraA")}
+    if "SideHeatedHa" in defines:
+        meta["constants"]["B2sigemarho"] = consts["B2sigemarho"]
     meta["diagnostics"] = diag
     return out, meta
 
@@ -364,6 +370,9 @@ STEP_CASES = [
     dict(name="rb2d_noslip_nog", dim=2, nx=8, ny=7, Ra=2e4, Pr=7.0, Mach=0.1, steps=2, seed=11,
          defines=["steadyFlow", "HorizontalWallsNoslip", "VerticalWallsNoslip", "RayleighBenardCell",
                   "HorizontalWallsConstT", "VerticalWallsAdiabatic"]),
+    dict(name="side2d_ha", dim=2, nx=8, ny=9, Ra=1e5, Pr=0.71, Mach=0.1, steps=3, seed=12, Ha=15.0, phi_deg=30.0,
+         defines=["steadyFlow", "HorizontalWallsNoslip", "VerticalWallsNoslip", "SideHeatedCell",
+                  "HorizontalWallsAdiabatic", "VerticalWallsConstT", "SideHeatedHa", "EnableUseG"]),
     dict(name="rb3d_noslip", dim=3, nx=6, ny=5, nz=4, Ra=1e6, Pr=0.71, Mach=0.1 * math.sqrt(3.0), steps=3, seed=8,
          defines=["steadyFlow", "HorizontalWallsNoslip", "VerticalWallsNoslip", "SpanwiseWallsNoslip",
                   "RayleighBenardCell", "HorizontalWallsConstT", "VerticalWallsAdiabatic", "SpanwiseWallsAdiabatic",

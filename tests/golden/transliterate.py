@@ -375,6 +375,7 @@ class ReferenceSubroutines:
         self.source[name] = code
         self.args[name] = args
         glb = {"math": math, "np": np, "min": min, "max": max, "mod": lambda a, b: int(math.fmod(a, b)),
+               "sin": math.sin, "cos": math.cos,
                "_minval": lambda a, lo, hi: min(a[lo:hi + 1]), "_maxval": lambda a, lo, hi: max(a[lo:hi + 1]),
                "huge": _huge, "ctime": lambda *a: "", "time": lambda *a: 0, "_call": self._call}
         exec(code, glb)

@@ -33,6 +33,9 @@ def params_for(meta):
     p.bc_thermal[1] = LBM_BCT_CONST if "HorizontalWallsConstT" in d else LBM_BCT_ADIABATIC
     p.bc_thermal[2] = LBM_BCT_PERIODIC if "SpanwiseWallsPeriodicalT" in d else LBM_BCT_ADIABATIC
     p.use_g = 1 if "EnableUseG" in d else 0
+    p.side_heated_ha = 1 if "SideHeatedHa" in d else 0
+    p.Ha = meta.get("Ha", 20.0)
+    p.phi_deg = meta.get("phi_deg", 0.0)
     p.legacy_thermal = 1 if "EnableLegacyThermalScheme" in d else 0
     p.precision = 0
     p.pattern = 0

@@ -54,7 +54,8 @@ def test_params_struct_layout(gpu_lib):
     assert p.use_g == 1 and p.legacy_thermal == 0 and p.seed == 20261203 and p.noise_amp == 0.0
     p3 = lbmgpu.params_default(3)
     assert (p3.nx, p3.ny, p3.nz, p3.Ra) == (120, 120, 120, 1e7)
-    assert C.sizeof(LbmParams) == 120
+    assert C.sizeof(LbmParams) == 144
+    assert (p.side_heated_ha, p.Ha, p.phi_deg) == (0, 20.0, 0.0)
 
 
 @pytest.mark.parametrize("dim,legacy", [(2, False), (3, False), (2, True), (3, True)])
@@ -75,3 +76,26 @@ def test_invalid_parameters_rejected(gpu_lib):
         mutate(p)
         with pytest.raises(lbmgpu.LbmError):
             lbmgpu.derive_constants(p)
+
+
+def test_magnetic_force_only_in_2d_plain_method(gpu_lib, oracle_mod):
+    """SideHeatedHa exists in the 2D program only (2DRB.F90:88-92); the FP32/FP16 lag state
+    carries F_y only, so those forms refuse it.  The constants follow 2DRB.F90:67, 89-91."""
+    import math
+    import lbmgpu
+    p = rb_params(dim=2, nx=40, ny=20, Ra=1e5)
+    p.side_heated_ha, p.Ha, p.phi_deg = 1, 15.0, 30.0
+    c = lbmgpu.derive_constants(p)
+    assert c.B2sigemarho == (15.0 * 15.0 * c.viscosity) / (c.lengthUnit * c.lengthUnit)
+    assert c.phi == 30.0 * (math.acos(-1.0) / 180.0)
+    assert (c.sinphi, c.cosphi) == (math.sin(c.phi), math.cos(c.phi))
+    assert oracle_mod.Oracle(p).constants(LbmConstants).B2sigemarho == c.B2sigemarho
+    for mutate in (lambda q: setattr(q, "precision", 1), lambda q: setattr(q, "precision", 2)):
+        q = p.copy()
+        mutate(q)
+        with pytest.raises(lbmgpu.LbmError):
+            lbmgpu.derive_constants(q)
+    q3 = rb_params(dim=3, n=16)
+    q3.side_heated_ha = 1
+    with pytest.raises(lbmgpu.LbmError):
+        lbmgpu.derive_constants(q3)
