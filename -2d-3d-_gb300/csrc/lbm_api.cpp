@@ -449,6 +449,12 @@ extern "C" const char* lbm_status_string(int s) {
     }
 }
 
+extern "C" int lbm_get_params(const lbm_handle* h, lbm_params* out) {
+    if (!h || !out) return LBM_ERR_PARAM;
+    *out = h->p;
+    return LBM_OK;
+}
+
 extern "C" int lbm_get_constants(const lbm_handle* h, lbm_constants* out) {
     if (!h || !out) return LBM_ERR_PARAM;
     *out = h->c;

@@ -101,6 +101,13 @@ void diag_wall_rows(const Geo& g, const DiagScalars& D, const S* T, double* Tl, 
 template <class S>
 void diag_gather_plane(const Geo& g, const S* f, int axis, int idx, double* out, cudaStream_t s);
 
+// Fine-grid |psi| search of calc_psi_absmax_fine_spline on device arrays: xExt (nx+2),
+// yExt (ny+2), rows (ny x (nx+2)) and their spline second derivatives y2rows; scratch xfine
+// (nFineX x ny); per fine x column k the largest |psi| and the first fine y index holding it.
+int psi_fine_search(int nx, int ny, double xLen, double yLen, int nFineX, int nFineY, const double* xExt,
+                    const double* yExt, const double* rows, const double* y2rows, double* xfine, double* best_val,
+                    int* best_l, cudaStream_t s);
+
 // ---- layout transforms (lbm_reduce.cu) -------------------------------------------------
 // Fortran AoS f(0:q-1, cells) <-> device SoA f[q][cells], FP64.
 void aos_to_soa(const double* aos, double* soa, int q, long long ncell, cudaStream_t s);

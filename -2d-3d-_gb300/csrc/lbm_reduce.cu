@@ -263,6 +263,110 @@ template void diag_wall_rows<float>(const Geo&, const DiagScalars&, const float*
 template void diag_gather_plane<double>(const Geo&, const double*, int, int, double*, cudaStream_t);
 template void diag_gather_plane<float>(const Geo&, const float*, int, int, double*, cudaStream_t);
 
+// ---- fine-grid |psi| search (calc_psi_absmax_fine_spline, 2DRB.F90:2873-2998) ----------
+// The reference interpolates psi on a grid of nFinePerUnit points per unit length with
+// natural cubic splines: first along x on every coarse row, then along y on every fine x
+// column, and keeps the first point of largest |psi| in (x outer, y inner) order.  Here a
+// thread per (fine x, coarse row) evaluates the row splines, and a block per fine x builds
+// its column spline in shared memory and scans the fine y points; ties go to the smallest
+// (k, l), which is the sequential scan's choice.
+__device__ double d_splint(int n, const double* xa, const double* ya, const double* y2a, double x) {
+    int klo = 1, khi = n;
+    while (khi - klo > 1) {
+        const int k = (khi + klo) / 2;
+        if (xa[k - 1] > x) khi = k;
+        else klo = k;
+    }
+    const double h = xa[khi - 1] - xa[klo - 1];
+    if (h == 0.0) return ya[klo - 1];
+    const double a = (xa[khi - 1] - x) / h;
+    const double b = (x - xa[klo - 1]) / h;
+    return a * ya[klo - 1] + b * ya[khi - 1] +
+           ((a * a * a - a) * y2a[klo - 1] + (b * b * b - b) * y2a[khi - 1]) * (h * h) / 6.0;
+}
+
+__device__ void d_spline_natural(int n, const double* x, const double* y, double* y2, double* u) {
+    y2[0] = 0.0;
+    u[0] = 0.0;
+    for (int i = 2; i <= n - 1; ++i) {
+        const double sig = (x[i - 1] - x[i - 2]) / (x[i] - x[i - 2]);
+        const double p = sig * y2[i - 2] + 2.0;
+        y2[i - 1] = (sig - 1.0) / p;
+        u[i - 1] = (6.0 * ((y[i] - y[i - 1]) / (x[i] - x[i - 1]) - (y[i - 1] - y[i - 2]) / (x[i - 1] - x[i - 2])) /
+                        (x[i] - x[i - 2]) - sig * u[i - 2]) / p;
+    }
+    y2[n - 1] = 0.0;
+    for (int k = n - 1; k >= 1; --k) y2[k - 1] = y2[k - 1] * y2[k] + u[k - 1];
+}
+
+// psi_xfine(k, j) for k < nFineX, j < ny: rows[j] = [0, psi(1..nx, j), 0], y2rows[j] its spline
+__global__ void k_psi_rows(int nx, int ny, int nFineX, double xLen, const double* xExt, const double* rows,
+                           const double* y2rows, double* xfine) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)nFineX * ny) return;
+    const int k = (int)(e % nFineX), j = (int)(e / nFineX);
+    const double xq = xLen * (double)k / (double)(nFineX - 1);
+    xfine[(long long)k * ny + j] = d_splint(nx + 2, xExt, rows + (size_t)j * (nx + 2), y2rows + (size_t)j * (nx + 2), xq);
+}
+
+__global__ void k_psi_columns(int ny, int nFineX, int nFineY, double yLen, const double* yExt, const double* xfine,
+                              double* best_val, int* best_l) {
+    extern __shared__ double sh[];
+    const int n = ny + 2;
+    double* col = sh;
+    double* y2 = sh + n;
+    double* uu = sh + 2 * n;
+    __shared__ double red_v[256];
+    __shared__ int red_l[256];
+    const int k = blockIdx.x;
+    if (threadIdx.x == 0) {
+        col[0] = 0.0;
+        col[n - 1] = 0.0;
+        for (int j = 0; j < ny; ++j) col[j + 1] = xfine[(long long)k * ny + j];
+        d_spline_natural(n, yExt, col, y2, uu);
+    }
+    __syncthreads();
+    double bv = -1.0;
+    int bl = 0x7fffffff;
+    for (int l = threadIdx.x; l < nFineY; l += blockDim.x) {
+        const double yq = yLen * (double)l / (double)(nFineY - 1);
+        const double a = fabs(d_splint(n, yExt, col, y2, yq));
+        if (a > bv) {  // the first (smallest l) of this thread's largest values
+            bv = a;
+            bl = l;
+        }
+    }
+    red_v[threadIdx.x] = bv;
+    red_l[threadIdx.x] = bl;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            const double v2 = red_v[threadIdx.x + o];
+            const int l2 = red_l[threadIdx.x + o];
+            if (v2 > red_v[threadIdx.x] || (v2 == red_v[threadIdx.x] && l2 < red_l[threadIdx.x])) {
+                red_v[threadIdx.x] = v2;
+                red_l[threadIdx.x] = l2;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        best_val[k] = red_v[0];
+        best_l[k] = red_l[0];
+    }
+}
+
+int psi_fine_search(int nx, int ny, double xLen, double yLen, int nFineX, int nFineY, const double* xExt,
+                    const double* yExt, const double* rows, const double* y2rows, double* xfine, double* best_val,
+                    int* best_l, cudaStream_t s) {
+    const long long ne = (long long)nFineX * ny;
+    k_psi_rows<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(nx, ny, nFineX, xLen, xExt, rows, y2rows, xfine);
+    const size_t shm = (size_t)3 * (ny + 2) * sizeof(double);
+    if (shm > 48 * 1024) return LBM_ERR_PARAM;
+    k_psi_columns<<<nFineX, 256, shm, s>>>(ny, nFineX, nFineY, yLen, yExt, xfine, best_val, best_l);
+    return cudaGetLastError() == cudaSuccess ? LBM_OK : LBM_ERR_CUDA;
+}
+
 // ---- layout transforms ----------------------------------------------------------------
 __global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict__ soa, int q, long long n) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;

@@ -76,6 +76,21 @@ SIGNATURES = {
     "lbm_RBcalc_umid_max": ([_vp, _vp], _i32),
     "lbm_RBcalc_vmid_max": ([_vp, _vp], _i32),
     "lbm_RBcalc_wmid_max": ([_vp, _vp], _i32),
+    "lbm_get_params": ([_vp, _vp], _i32),
+    "lbm_output_binary": ([_vp, C.c_char_p], _i32),
+    "lbm_output_Tecplot": ([_vp, C.c_char_p, _i64], _i32),
+    "lbm_calc_psi_vort_and_output": ([_vp, C.c_char_p, _i64, _i32, _vp], _i32),
+    "lbm_output_binary_host": ([C.c_char_p, _i32, _i32, _i32, _i32, C.c_double, _dp, _dp, _dp, _dp, _dp], _i32),
+    "lbm_tecplot_fields_2d": ([C.c_char_p, _i32, _i32, C.c_double, C.c_double, _dp, _dp, _dp], _i32),
+    "lbm_tecplot_full_3d": ([C.c_char_p, _i32, _i32, _i32, C.c_double, _dp, _dp, _dp, _dp], _i32),
+    "lbm_tecplot_midplane_3d": ([C.c_char_p, _i32, _i32, _i32, _i32, C.c_double, C.c_double, _dp, _dp, _dp, _dp],
+                                _i32),
+    "lbm_tecplot_midplane_stream_3d": ([C.c_char_p, _i32, _i32, _i32, _i32, C.c_double, C.c_double, _dp, _dp, _dp],
+                                       _i32),
+    "lbm_psi_vort_2d": ([_i32, _i32, C.c_double, C.c_double, _dp, _dp, _dp, _dp], _i32),
+    "lbm_tecplot_psi_vort_2d": ([C.c_char_p, _i32, _i32, C.c_double, _dp, _dp], _i32),
+    "lbm_psi_center_2d": ([_i32, _i32, C.c_double, _dp, _dp], _i32),
+    "lbm_psi_absmax_fine_spline": ([_i32, _i32, C.c_double, _dp, _i32, _dp, _dp, _dp, _dp], _i32),
     "lbm_backupData": ([_vp, C.c_char_p, _i32], _i32),
     "lbm_reload": ([_vp, C.c_char_p, _i32], _i32),
     "lbm_reload_form": ([_vp], _i32),
@@ -297,6 +312,25 @@ class Lattice:
         m = {"reference": LBM_RELOAD_REFERENCE, "continue": LBM_RELOAD_CONTINUE, "auto": LBM_RELOAD_AUTO}[mode]
         self._ck(self.lib.lbm_reload(self._h, os.fsencode(path), m), "reload")
         return "continue" if self.lib.lbm_reload_form(self._h) == 1 else "reference"
+
+    # -- snapshot writers (output_binary, output_Tecplot, calc_psi_vort_and_output) ----
+    def output_binary(self, path):
+        """The reference's output_binary file: records of (L/kappa) u, v[, w], T, rho."""
+        self._ck(self.lib.lbm_output_binary(self._h, os.fsencode(path)), "output_binary")
+
+    def output_Tecplot(self, prefix, number=0):
+        """The reference's Tecplot files <prefix>-...<number, 12 digits>.plt (one in 2D, seven in 3D)."""
+        self._ck(self.lib.lbm_output_Tecplot(self._h, os.fsencode(prefix), int(number)), "output_Tecplot")
+
+    def calc_psi_vort_and_output(self, prefix=None, number=0, fine_per_unit=10000):
+        """2D stream function / vorticity: writes <prefix>-psiVort-<n>.plt (unless prefix is
+        None) and returns the centre value and the fine-grid maximum of |psi|."""
+        from .abi import LbmPsiSummary
+        out = LbmPsiSummary()
+        pre = os.fsencode(prefix) if prefix is not None else None
+        self._ck(self.lib.lbm_calc_psi_vort_and_output(self._h, pre, int(number), int(fine_per_unit), C.byref(out)),
+                 "calc_psi_vort_and_output")
+        return out.as_dict()
 
     # -- state transfer (Fortran layout) ------------------------------------------------
     def get_state(self, field):

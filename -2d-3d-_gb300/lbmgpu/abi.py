@@ -73,6 +73,14 @@ class LbmNuWall(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class LbmPsiSummary(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("psi_center", "psi_center_abs", "psi_abs_max", "x_at_max", "y_at_max",
+                                          "psi_center_abs_fine")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class LbmMidMax(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("value", "pos1", "pos2", "mid")]
 

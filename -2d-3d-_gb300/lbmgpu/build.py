@@ -7,6 +7,7 @@ Translation units and their floating-point flags:
   lbm_fast_tma.cu           : the same step with population rows staged by bulk copies
   lbm_api.cpp               : host code (-ffp-contract=off for the host-side fits)
   lbm_checkpoint.cpp        : Fortran unformatted sequential records (restart files)
+  lbm_output.cpp            : snapshot / Tecplot writers, stream function post-processing
 The units compile in parallel; a full build takes well under two minutes.
 """
 import concurrent.futures as cf
@@ -34,6 +35,7 @@ UNITS = [
     ("lbm_ensemble.cu", ["-fmad=true"]),
     ("lbm_api.cpp", []),
     ("lbm_checkpoint.cpp", []),
+    ("lbm_output.cpp", []),
     ("lbm_noalloc.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
 ]
 

@@ -288,6 +288,52 @@ int lbm_RBcalc_umid_max(lbm_handle* h, lbm_mid_max* out);
 int lbm_RBcalc_vmid_max(lbm_handle* h, lbm_mid_max* out);
 int lbm_RBcalc_wmid_max(lbm_handle* h, lbm_mid_max* out);
 
+/* ---- snapshot writers and stream-function post-processing ------------------------------
+ * output_binary (3DRB.F90:1599-1627, 2DRB.F90:1357-1389): unformatted sequential records
+ *   velocityScaleCompare*u, *v, [*w], T, rho to `path`.
+ * output_Tecplot (2DRB.F90:1443-1570; 3DRB.F90:1676-1700): the reference's Tecplot binary
+ *   files, named as the reference names them from a prefix and a number (12 digits):
+ *   2D  <prefix>-<n>.plt (X, Y, U_nd, V_nd, T);
+ *   3D  <prefix>-fullField-<n>.plt (3DRB.F90:3018-3099), -midX/-midY/-midZ- mid planes
+ *       (2619-2719), -midXpsiVort/-midYpsiVort/-midZpsiVort- stream function and vorticity of
+ *       the mid planes (2721-3016).
+ * calc_psi_vort_and_output (2D, 2DRB.F90:2657-2780): stream function and vorticity, the
+ *   <prefix>-psiVort-<n>.plt file (prefix NULL: no file), psi at the centre by 4x4 Lagrange
+ *   interpolation (output_psi_center_abs, 3085-3165), and the largest |psi| on a fine grid of
+ *   nFinePerUnit points per unit length with natural splines (calc_psi_absmax_fine_spline,
+ *   2873-2998; the reference uses 10000), the fine grid searched on the GPU. */
+typedef struct lbm_psi_summary {
+    double psi_center, psi_center_abs;         /* coarse-grid Lagrange value at the centre */
+    double psi_abs_max, x_at_max, y_at_max;    /* fine-grid maximum of |psi| and position   */
+    double psi_center_abs_fine;                /* |psi| at the centre from the splines      */
+} lbm_psi_summary;
+int lbm_get_params(const lbm_handle* h, lbm_params* out);
+int lbm_output_binary(lbm_handle* h, const char* path);
+int lbm_output_Tecplot(lbm_handle* h, const char* prefix, int64_t number);
+int lbm_calc_psi_vort_and_output(lbm_handle* h, const char* prefix, int64_t number, int nFinePerUnit,
+                                 lbm_psi_summary* out);
+/* The same writers on host arrays in the Fortran layout (no GPU needed, except the fine-grid
+ * search of lbm_psi_absmax_fine_spline, which runs on the current device). */
+int lbm_output_binary_host(const char* path, int dim, int nx, int ny, int nz, double velocityScaleCompare,
+                           const double* u, const double* v, const double* w, const double* T, const double* rho);
+int lbm_tecplot_fields_2d(const char* path, int nx, int ny, double lengthUnit, double velocityScaleCompare,
+                          const double* u, const double* v, const double* T);
+int lbm_tecplot_full_3d(const char* path, int nx, int ny, int nz, double lengthUnit, const double* u,
+                        const double* v, const double* w, const double* T);
+int lbm_tecplot_midplane_3d(const char* path, int axis, int nx, int ny, int nz, double lengthUnit,
+                            double velocityScaleCompare, const double* u, const double* v, const double* w,
+                            const double* T);
+int lbm_tecplot_midplane_stream_3d(const char* path, int axis, int nx, int ny, int nz, double lengthUnit,
+                                   double velocityScaleCompare, const double* u, const double* v, const double* w);
+int lbm_psi_vort_2d(int nx, int ny, double lengthUnit, double velocityScaleCompare, const double* u,
+                    const double* v, double* psi, double* vort);
+int lbm_tecplot_psi_vort_2d(const char* path, int nx, int ny, double lengthUnit, const double* psi,
+                            const double* vort);
+int lbm_psi_center_2d(int nx, int ny, double lengthUnit, const double* psi, double* psi_center);
+int lbm_psi_absmax_fine_spline(int nx, int ny, double lengthUnit, const double* psi, int nFinePerUnit,
+                               double* psi_abs_max, double* x_at_max, double* y_at_max,
+                               double* psi_center_abs_fine);
+
 /* ---- restart files (backupData, 3DRB.F90:1638-1665 / 2DRB.F90:1402-1430; reload,
  *      3DRB.F90:602-623 / 2DRB.F90:621-637; reconstruct_macro_from_fg,
  *      3DRB.F90:1392-1463 / 2DRB.F90:1144-1200) -----------------------------------------

@@ -287,6 +287,9 @@ def step_fixture(ref_dir, case):
     for name in FIELDS_OUT[dim]:
         out["out_" + name] = to_fortran_layout(ns[name], inner, name in ("f", "g", "f_post", "g_post"))
     diag = diagnostics(subs, ns, dim, case)
+    writer_bytes, writer_meta = writers(path, defines, ns, dim, case)
+    out.update(writer_bytes)
+    diag["writers"] = writer_meta
     # restart from the stepped f and g: initial with loadInitField = 1 reads them and calls
     # reconstruct_macro_from_fg, whose first statement (call macroT) the translation drops
     subs.run("macroT", ns)
@@ -299,6 +302,55 @@ def step_fixture(ref_dir, case):
     if "SideHeatedHa" in defines:
         meta["constants"]["B2sigemarho"] = consts["B2sigemarho"]
     meta["diagnostics"] = diag
+    return out, meta
+
+
+FINE_PER_UNIT = 20  # calc_psi_absmax_fine_spline's nFinePerUnit for the fixtures (10000 in the reference)
+
+
+def writers(path, defines, ns0, dim, case):
+    """The reference's Tecplot writers and stream-function post-processing on the stepped
+    state: the bytes each writes (`plt_*` arrays) and the numbers it computes."""
+    import copy
+    from transliterate import ReferenceSubroutines
+    subs = ReferenceSubroutines(path, defines, overrides={"nFinePerUnit": FINE_PER_UNIT})
+    L = ns0["lengthUnit"]
+    base = dict(ns0)
+    base["xp"] = coords(case["nx"], L)
+    base["yp"] = coords(case["ny"], L)
+    if dim == 3:
+        base["zp"] = coords(case["nz"], L)
+    base["itc"] = 0
+
+    def fresh():
+        return {k: (copy.deepcopy(v) if isinstance(v, np.ndarray) else v) for k, v in base.items()}
+
+    files, meta = {}, {}
+    if dim == 2:
+        subs.take_stream()
+        subs.run("output_Tecplot", fresh())
+        files["plt_fields"] = subs.take_stream()
+        ns = fresh()
+        subs.run("calc_psi_vort_and_output", ns)
+        files["plt_psiVort"] = subs.take_stream()
+        subs.module = ns
+        subs._call("output_psi_center_abs", [ns["psi"]])
+        meta["psi"] = {"psi_center": float(subs.last_ns["psi_center"]), "psi_abs_max": float(ns["psi_abs_max"]),
+                       "x_at_max": float(ns["x_at_max"]), "y_at_max": float(ns["y_at_max"]),
+                       "psi_center_abs_fine": float(ns["psi_center_abs_fine"]), "nFinePerUnit": FINE_PER_UNIT}
+        inner = (slice(1, case["nx"] + 1), slice(1, case["ny"] + 1))
+        arrays = {"psi_psi": to_fortran_layout(ns["psi"], inner, False),
+                  "psi_vort": to_fortran_layout(ns["vort"], inner, False)}
+    else:
+        arrays = {}
+        for name in ("write_full_fields_plt", "write_midplane_x", "write_midplane_y", "write_midplane_z",
+                     "write_midplane_stream_x", "write_midplane_stream_y", "write_midplane_stream_z"):
+            subs.module = fresh()
+            subs.take_stream()
+            subs._call(name, ["file.plt"])
+            files["plt_" + name] = subs.take_stream()
+    out = {k: np.frombuffer(v, dtype=np.uint8) for k, v in files.items()}
+    out.update(arrays)
     return out, meta
 
 
