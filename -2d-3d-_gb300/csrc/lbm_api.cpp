@@ -55,6 +55,7 @@ struct lbm_handle {
     double* gbuf[2] = {nullptr, nullptr};
     bool fused_valid = false;  // true: current state is in the fused buffers
     int cur = 0;               // fused buffer index holding f_post_N / g_post_N
+    AAState aa;                // in-place pattern: A.f / A.g are the only population arrays
 
     // FP32 / FP16 storage forms
     FastState F{};
@@ -62,6 +63,7 @@ struct lbm_handle {
     // captured chunk of fused steps
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
+    int graph_key = 0;  // in-place pattern: the layout state the chunk was captured from
 
     // scratch
     double* d_part = nullptr;
@@ -141,7 +143,7 @@ static int validate(const lbm_params* p) {
         if (p->bc_thermal[2] != LBM_BCT_ADIABATIC && p->bc_thermal[2] != LBM_BCT_PERIODIC) return LBM_ERR_PARAM;
     }
     if (p->precision < LBM_FP64 || p->precision > LBM_FP16) return LBM_ERR_PARAM;
-    if (p->pattern != LBM_PATTERN_AB) return LBM_ERR_PARAM;  // the in-place AA pattern is not built yet
+    if (p->pattern != LBM_PATTERN_AB && p->pattern != LBM_PATTERN_AA) return LBM_ERR_PARAM;
     // the magnetic force exists in the 2D program only (2DRB.F90:88-92); the FP32/FP16 forms
     // carry only F_y in their lag state
     if (p->side_heated_ha && (p->dim != 2 || p->precision != LBM_FP64 || !std::isfinite(p->Ha) ||
@@ -283,15 +285,34 @@ static int allocate(lbm_handle* h) {
     do {                                                  \
         if ((st = dalloc(h, &(ptr), (size_t)(cnt))) != LBM_OK) return st; \
     } while (0)
-    if (h->p.precision == LBM_FP64) {
-        AL(h->fbuf[0], h->q * n);
-        AL(h->fbuf[1], h->q * n);
-        AL(h->gbuf[0], h->qt * n);
-        AL(h->gbuf[1], h->qt * n);
+    if (h->p.precision == LBM_FP64 && h->p.pattern == LBM_PATTERN_AA) {
+        // one array per lattice, which is also the module array; no f_post / g_post
         AL(h->A.f, h->q * n);
         AL(h->A.g, h->qt * n);
-        h->A.fpost = h->fbuf[0];
-        h->A.gpost = h->gbuf[0];
+        h->fbuf[0] = h->A.f;
+        h->gbuf[0] = h->A.g;
+        h->A.fpost = nullptr;
+        h->A.gpost = nullptr;
+        for (int ax = 0; ax < 3; ++ax) {
+            double* pf = nullptr;
+            double* pg = nullptr;
+            if (h->geo.bcf[ax] == LBM_BC_PERIODIC) AL(pf, (size_t)h->q * aa_face_cells(h->geo, ax));
+            if (h->geo.bct[ax] == LBM_BCT_PERIODIC) AL(pg, (size_t)h->qt * aa_face_cells(h->geo, ax));
+            h->aa.face_f[ax] = pf;
+            h->aa.face_g[ax] = pg;
+        }
+    }
+    if (h->p.precision == LBM_FP64) {
+        if (h->p.pattern != LBM_PATTERN_AA) {
+            AL(h->fbuf[0], h->q * n);
+            AL(h->fbuf[1], h->q * n);
+            AL(h->gbuf[0], h->qt * n);
+            AL(h->gbuf[1], h->qt * n);
+            AL(h->A.f, h->q * n);
+            AL(h->A.g, h->qt * n);
+            h->A.fpost = h->fbuf[0];
+            h->A.gpost = h->gbuf[0];
+        }
         AL(h->A.rho, n);
         AL(h->A.u, n);
         AL(h->A.v, n);
@@ -517,10 +538,14 @@ extern "C" int lbm_initial(lbm_handle* h) {
         CK(h, cudaStreamSynchronize(h->stream));
     }
     if (h->p.precision == LBM_FP64) {
-        h->A.fpost = h->fbuf[0];
-        h->A.gpost = h->gbuf[0];
+        if (h->p.pattern != LBM_PATTERN_AA) {
+            h->A.fpost = h->fbuf[0];
+            h->A.gpost = h->gbuf[0];
+        }
         h->cur = 0;
         h->fused_valid = false;
+        h->aa.fpar = h->aa.gpar = 0;  // module data in the streamed layout
+        h->aa.graw = false;
         exact_initial(h->geo, h->phys, I, h->A, h->dim, h->stream);
     } else {
         fast_initial(h->F, h->geo, h->phys, I, h->dim, h->stream);
@@ -539,6 +564,12 @@ static int materialize(lbm_handle* h) {
         return LBM_OK;
     }
     if (!h->fused_valid) return LBM_OK;
+    if (h->p.pattern == LBM_PATTERN_AA) {
+        // the arrays are the module populations; the state stays where it is
+        exact_aa_materialize(h->geo, h->phys, h->A, h->dim, h->aa, h->stream);
+        CK_LAUNCH(h, "materialize");
+        return LBM_OK;
+    }
     exact_materialize(h->geo, h->phys, h->A, h->dim, h->fbuf[h->cur], h->gbuf[h->cur], h->stream);
     CK_LAUNCH(h, "materialize");
     h->A.fpost = h->fbuf[h->cur];
@@ -555,6 +586,8 @@ static int stage(lbm_handle* h, int which) {
     if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
     if (h->p.precision != LBM_FP64)
         return fail(h, LBM_ERR_STATE, "stage entry points exist for the FP64 plain method only");
+    if (h->p.pattern == LBM_PATTERN_AA)
+        return fail(h, LBM_ERR_STATE, "stage entry points need the two-buffer pattern (separate f and f_post)");
     CK(h, cudaSetDevice(h->device));
     int st = materialize(h);
     if (st != LBM_OK) return st;
@@ -579,12 +612,18 @@ extern "C" int lbm_macroT(lbm_handle* h) { return stage(h, STAGE_MACROT); }
 // FP32/FP16 handles advance with the single fused kernel (lbm_fused.cu) unless it is
 // switched off or the geometry needs whole tiles it does not have.
 static bool use_single(const lbm_handle* h) {
-    return h->p.precision != LBM_FP64 && h->F.single_kernel && fast_fused_supported(h->geo, h->dim);
+    return h->p.precision != LBM_FP64 && !h->F.aa && h->F.single_kernel && fast_fused_supported(h->geo, h->dim);
 }
+
+static bool in_place(const lbm_handle* h) { return h->p.pattern == LBM_PATTERN_AA; }
+
+static const AAState& aa_state(const lbm_handle* h) { return h->p.precision == LBM_FP64 ? h->aa : h->F.AA; }
 
 static void enqueue_one(lbm_handle* h, bool first) {
     const int nxt = h->cur ^ 1;
-    if (h->p.precision == LBM_FP64) {
+    if (h->p.precision == LBM_FP64 && in_place(h)) {
+        exact_aa_step(h->geo, h->phys, h->A, h->dim, first, h->aa, h->stream);
+    } else if (h->p.precision == LBM_FP64) {
         exact_fused_step(h->geo, h->phys, h->A, h->dim, first, h->fbuf[h->cur], h->gbuf[h->cur], h->fbuf[nxt],
                          h->gbuf[nxt], h->stream);
         h->cur = nxt;
@@ -596,11 +635,28 @@ static void enqueue_one(lbm_handle* h, bool first) {
     }
 }
 
+// In-place pattern: a chunk (an even number of steps) starts and ends with the flow array
+// in the streamed layout; the thermal array's layout and its push flag are part of what
+// was captured, so a chunk replays only from the state it was captured in.
+static int layout_key(const lbm_handle* h) {
+    const AAState& S = aa_state(h);
+    return 1 + S.gpar + 2 * (S.graw ? 1 : 0);
+}
+
 static bool at_graph_origin(const lbm_handle* h) {
+    if (in_place(h)) return aa_state(h).fpar == 0;
     return h->p.precision == LBM_FP64 ? h->cur == 0 : fast_at_origin(h->F);
 }
 
+static void drop_chunk(lbm_handle* h) {
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->graph_exec = nullptr;
+    h->graph = nullptr;
+}
+
 static int capture_chunk(lbm_handle* h) {
+    h->graph_key = in_place(h) ? layout_key(h) : 0;
     CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 0; s < kChunkSteps; ++s) enqueue_one(h, false);
     cudaGraph_t g = nullptr;
@@ -628,12 +684,18 @@ extern "C" int lbm_step(lbm_handle* h, int64_t nsteps) {
     if (use_single(h) && !h->F.ahead && done < nsteps) fast_enter(h->F, h->geo, h->phys, h->dim, h->stream);
     while (done < nsteps) {
         if (at_graph_origin(h) && nsteps - done >= kChunkSteps) {
+            if (h->graph_exec && in_place(h) && h->graph_key != layout_key(h)) {
+                CK(h, cudaStreamSynchronize(h->stream));
+                drop_chunk(h);
+            }
             if (!h->graph_exec) {
                 int st = capture_chunk(h);
                 if (st != LBM_OK) return st;
             }
             CK(h, cudaGraphLaunch(h->graph_exec, h->stream));
             done += kChunkSteps;
+            // a chunk holds odd thermal sweeps: the thermal array's slots are pushed values now
+            if (in_place(h)) (h->p.precision == LBM_FP64 ? h->aa : h->F.AA).graw = true;
         } else {
             enqueue_one(h, false);
             done += 1;
@@ -1135,6 +1197,8 @@ static int state_io(lbm_handle* h, int field, double* dst, const double* src, si
     const int qq = (field == LBM_FIELD_F || field == LBM_FIELD_F_POST) ? h->q : h->qt;
     const size_t want = pop ? (size_t)qq * n : (size_t)n;
     if (count != want) return fail(h, LBM_ERR_PARAM, "count does not match the field size");
+    if (in_place(h) && (field == LBM_FIELD_F_POST || field == LBM_FIELD_G_POST))
+        return fail(h, LBM_ERR_STATE, "the in-place pattern keeps no post-collision array");
     if (h->p.precision != LBM_FP64) {
         if ((st = ensure_stage(h, want)) != LBM_OK) return st;
         if (dst) {
@@ -1152,10 +1216,17 @@ static int state_io(lbm_handle* h, int field, double* dst, const double* src, si
         }
         return LBM_OK;
     }
+    if (src) h->fused_valid = false;  // the module arrays are the state again
     if (pop) {
         double* soa = field == LBM_FIELD_F ? h->A.f : field == LBM_FIELD_G ? h->A.g : field == LBM_FIELD_F_POST ? h->A.fpost : h->A.gpost;
+        const bool th = field == LBM_FIELD_G;
         if ((st = ensure_stage(h, want)) != LBM_OK) return st;
-        if (dst) {
+        if (dst && in_place(h)) {
+            aa_module_view(h->geo, qq, th, LBM_FP64, soa, th ? h->aa.gpar : h->aa.fpar, h->aa.graw, h->d_stage, false,
+                           false, 0.0, 0.0, h->stream);
+            CK_LAUNCH(h, "module view");
+            CK(h, cudaMemcpyAsync(dst, h->d_stage, want * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        } else if (dst) {
             soa_to_aos(soa, h->d_stage, qq, n, h->stream);
             CK_LAUNCH(h, "soa_to_aos");
             CK(h, cudaMemcpyAsync(dst, h->d_stage, want * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1163,6 +1234,12 @@ static int state_io(lbm_handle* h, int field, double* dst, const double* src, si
             CK(h, cudaMemcpyAsync(h->d_stage, src, want * sizeof(double), cudaMemcpyHostToDevice, h->stream));
             aos_to_soa(h->d_stage, soa, qq, n, h->stream);
             CK_LAUNCH(h, "aos_to_soa");
+            if (th) {  // module data in the streamed layout
+                h->aa.gpar = 0;
+                h->aa.graw = false;
+            } else {
+                h->aa.fpar = 0;
+            }
         }
         CK(h, cudaStreamSynchronize(h->stream));
         return LBM_OK;
@@ -1200,6 +1277,8 @@ constexpr size_t kIoChunk = size_t(64) << 20;         // host staging per copy
 constexpr int kFormExact = 0;      // FP64 module arrays (f, g come from the two reference records)
 constexpr int kFormFastFused = 1;  // FP32/FP16 fused buffers F[cur], G[cur], B[cur], L[cur]
 constexpr int kFormFastModule = 2; // FP32/FP16 module arrays fref, gref, rho, u, v, w, T, B, L
+constexpr int kFormFastAA = 3;     // FP32/FP16 in-place arrays as they lie, module scalars, B, L
+                                   // (header words 11-14: flow / thermal layout, push flag, fused)
 
 struct Pinned {
     void* p = nullptr;
@@ -1252,6 +1331,11 @@ static std::vector<ContArray> cont_arrays(lbm_handle* h, int form) {
     const int c = F.cur;
     if (form == kFormFastFused) {
         v = {{F.fbuf[c], (size_t)h->q * n * F.esize}, {F.gbuf[c], (size_t)h->qt * n * F.esize}};
+    } else if (form == kFormFastAA) {
+        v = {{F.fbuf[0], (size_t)h->q * n * F.esize}, {F.gbuf[0], (size_t)h->qt * n * F.esize}, {F.rho, b}, {F.u, b},
+             {F.v, b}};
+        if (d3) v.push_back({F.w, b});
+        v.push_back({F.T, b});
     } else {
         v = {{F.fref, (size_t)h->q * n * F.esize}, {F.gref, (size_t)h->qt * n * F.esize}, {F.rho, b}, {F.u, b},
              {F.v, b}};
@@ -1316,6 +1400,12 @@ static void cont_header(const lbm_handle* h, int form, size_t narrays, int64_t h
     hdr[8] = h->itc;
     hdr[9] = (int64_t)narrays;
     hdr[10] = h->p.precision == LBM_FP64 ? 8 : (int64_t)h->F.esize;
+    if (form == kFormFastAA) {
+        hdr[11] = h->F.AA.fpar;
+        hdr[12] = h->F.AA.gpar;
+        hdr[13] = h->F.AA.graw ? 1 : 0;
+        hdr[14] = h->F.fused_valid ? 1 : 0;
+    }
 }
 
 extern "C" int lbm_backupData(lbm_handle* h, const char* path, int flags) {
@@ -1336,8 +1426,16 @@ extern "C" int lbm_backupData(lbm_handle* h, const char* path, int flags) {
     for (int which = 0; which < 2; ++which) {
         const int qq = which == 0 ? h->q : h->qt;
         const double* src = nullptr;
-        if (fp64) {
+        if (fp64 && !in_place(h)) {
             src = which == 0 ? h->A.f : h->A.g;
+        } else if (fp64) {
+            // the module view of the in-place array
+            if ((st = ensure_stage(h, (size_t)qq * n)) != LBM_OK) return st;
+            aa_module_view(h->geo, qq, which == 1, LBM_FP64, which == 0 ? h->A.f : h->A.g,
+                           which == 0 ? h->aa.fpar : h->aa.gpar, h->aa.graw, h->d_stage, true, false, 0.0, 0.0,
+                           h->stream);
+            CK_LAUNCH(h, "module view");
+            src = h->d_stage;
         } else {
             if ((st = ensure_stage(h, (size_t)qq * n)) != LBM_OK) return st;
             st = fast_export(h->F, h->geo, h->phys, h->dim, which == 0 ? LBM_FIELD_F : LBM_FIELD_G, h->d_stage,
@@ -1349,7 +1447,7 @@ extern "C" int lbm_backupData(lbm_handle* h, const char* path, int flags) {
         if ((st = write_device_record(h, file.fp, src, (size_t)qq * n * sizeof(double), pin)) != LBM_OK) return st;
     }
     if (flags == LBM_BACKUP_CONTINUE) {
-        const int form = fp64 ? kFormExact : (h->F.fused_valid ? kFormFastFused : kFormFastModule);
+        const int form = fp64 ? kFormExact : (h->F.aa ? kFormFastAA : (h->F.fused_valid ? kFormFastFused : kFormFastModule));
         std::vector<ContArray> arrays = cont_arrays(h, form);
         int64_t hdr[kContHeader];
         cont_header(h, form, arrays.size(), hdr);
@@ -1400,8 +1498,11 @@ static std::string cont_mismatch(lbm_handle* h, const RestartScan& s) {
         return "continuation records were written for another lattice size";
     if (H[6] != h->p.precision) return "continuation records were written for another storage precision";
     const bool fp64 = h->p.precision == LBM_FP64;
-    if (fp64 ? H[7] != kFormExact : (H[7] != kFormFastFused && H[7] != kFormFastModule))
-        return "unknown continuation form";
+    if (fp64 ? H[7] != kFormExact
+             : (h->F.aa ? H[7] != kFormFastAA : (H[7] != kFormFastFused && H[7] != kFormFastModule)))
+        return "continuation records were written for another storage form or access pattern";
+    if (H[7] == kFormFastAA && (H[11] < 0 || H[11] > 1 || H[12] < 0 || H[12] > 1 || H[13] < 0 || H[13] > 1))
+        return "continuation header holds an unknown layout state";
     std::vector<ContArray> arrays = cont_arrays(h, (int)H[7]);
     if (arrays.size() != s.lens.size()) return "continuation record count differs";
     for (size_t k = 0; k < arrays.size(); ++k)
@@ -1481,10 +1582,14 @@ extern "C" int lbm_reload(lbm_handle* h, const char* path, int mode) {
             return lost(fail(h, LBM_ERR_IO, "restart file truncated"));
     }
     if (fp64) {
-        h->A.fpost = h->fbuf[0];
-        h->A.gpost = h->gbuf[0];
+        if (!in_place(h)) {
+            h->A.fpost = h->fbuf[0];
+            h->A.gpost = h->gbuf[0];
+        }
         h->cur = 0;
         h->fused_valid = false;
+        h->aa.fpar = h->aa.gpar = 0;  // the records are module data: the streamed layout
+        h->aa.graw = false;
     } else {
         h->F.cur = 0;
         h->F.ahead = false;
@@ -1496,6 +1601,12 @@ extern "C" int lbm_reload(lbm_handle* h, const char* path, int mode) {
         for (const ContArray& a : cont_arrays(h, form))
             if ((st = read_device_record(h, file.fp, a.dptr, a.bytes, pin)) != LBM_OK) return lost(st);
         if (!fp64) h->F.fused_valid = form == kFormFastFused;
+        if (form == kFormFastAA) {
+            h->F.AA.fpar = (int)scan.hdr[11];
+            h->F.AA.gpar = (int)scan.hdr[12];
+            h->F.AA.graw = scan.hdr[13] != 0;
+            h->F.fused_valid = scan.hdr[14] != 0;
+        }
         h->itc = scan.hdr[8];
         h->reload_form = 1;
         h->initialised = true;
@@ -1571,7 +1682,11 @@ extern "C" int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, 
     for (auto& e : ev) CK(h, cudaEventCreate(&e));
     CK(h, cudaEventRecord(ev[0], h->stream));
     for (int64_t k = 0; k < nsteps; ++k) {
-        if (h->p.precision == LBM_FP64) {
+        if (h->p.precision == LBM_FP64 && in_place(h)) {
+            exact_aa_step(h->geo, h->phys, h->A, h->dim, false, h->aa, h->stream, 0);
+            CK(h, cudaEventRecord(ev[2 * k + 1], h->stream));
+            exact_aa_step(h->geo, h->phys, h->A, h->dim, false, h->aa, h->stream, 1);
+        } else if (h->p.precision == LBM_FP64) {
             const int nxt = h->cur ^ 1;
             exact_fused_step(h->geo, h->phys, h->A, h->dim, false, h->fbuf[h->cur], h->gbuf[h->cur], h->fbuf[nxt],
                              h->gbuf[nxt], h->stream, 0);
@@ -1658,14 +1773,23 @@ extern "C" int lbm_footprint(const lbm_params* p, size_t* bytes) {
     const size_t n = (size_t)p->nx * p->ny * (size_t)(p->dim == 3 ? p->nz : 1);
     const size_t q = p->dim == 3 ? 19 : 9, qt = p->dim == 3 ? 7 : 5;
     size_t b = 0;
+    const bool aa = p->pattern == LBM_PATTERN_AA;
+    const size_t es = p->precision == LBM_FP64 ? 8 : (p->precision == LBM_FP16 ? 2 : 4);
     if (p->precision == LBM_FP64) {
-        b += 8 * n * (3 * q + 3 * qt);                       // f_post A/B, g_post A/B, f, g
+        b += 8 * n * (aa ? q + qt : 3 * q + 3 * qt);         // AA: f, g | f_post A/B, g_post A/B, f, g
         b += 8 * n * (p->dim == 3 ? 13 : 11);                // rho u v T Bx By up vp Tp (+w Bz wp Tlag | Fx Fy)
     } else {
-        const size_t es = p->precision == LBM_FP16 ? 2 : 4;
-        b += es * n * (3 * q + 3 * qt);                      // F A/B, G A/B, f, g (module)
-        b += 4 * n * (2 * (p->dim == 3 ? 3 : 2) + 2);        // B_prev A/B, lag A/B
+        const size_t nb = aa ? 1 : 2;
+        b += es * n * (aa ? q + qt : 3 * q + 3 * qt);        // AA: f, g | F A/B, G A/B, f, g (module)
+        b += 4 * n * nb * ((p->dim == 3 ? 3 : 2) + 1);       // B_prev, lag (A/B: two each)
         b += 4 * n * (p->dim == 3 ? 9 : 7);                  // rho u v T up vp Tp (+w wp)
+    }
+    if (aa) {  // face snapshots of the periodic axes
+        const size_t fx = (size_t)p->ny * (p->dim == 3 ? p->nz : 1), fz = (size_t)p->nx * p->ny;
+        if (p->bc_flow[0] == LBM_BC_PERIODIC) b += es * q * fx;
+        if (p->bc_thermal[0] == LBM_BCT_PERIODIC) b += es * qt * fx;
+        if (p->dim == 3 && p->bc_flow[2] == LBM_BC_PERIODIC) b += es * q * fz;
+        if (p->dim == 3 && p->bc_thermal[2] == LBM_BCT_PERIODIC) b += es * qt * fz;
     }
     b += 8 * ((size_t)diag_blocks((long long)n) * DIAG_NSUM + 3 * (size_t)p->nx + (size_t)p->ny);
     *bytes = b;
@@ -1745,6 +1869,7 @@ extern "C" const char* lbm_ensemble_last_error(const lbm_ensemble* e) { return e
 extern "C" int lbm_ensemble_add(lbm_ensemble* e, lbm_handle* h) {
     if (!e || !h) return LBM_ERR_PARAM;
     if (h->p.precision == LBM_FP64) return efail(e, LBM_ERR_STATE, "the batched form takes FP32/FP16 handles");
+    if (h->p.pattern == LBM_PATTERN_AA) return efail(e, LBM_ERR_STATE, "the batched form takes two-buffer handles");
     if (h->device != e->device) return efail(e, LBM_ERR_PARAM, "handle is on another device");
     if (!h->initialised) return efail(e, LBM_ERR_STATE, "lbm_initial has not been called on the handle");
     if (h->ensemble) return efail(e, LBM_ERR_STATE, "handle already belongs to an ensemble");

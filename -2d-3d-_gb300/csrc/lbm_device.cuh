@@ -99,8 +99,8 @@ __host__ __device__ inline long long cell_index(const Geo& g, int i, int j, int 
 //   periodic : f_post(a) of the cell wrapped along that axis only, other indices
 //              unchanged (the reference's same-row copy, 2DRB.F90:821-828).
 // LOAD(dir, cell) returns the stored value converted to the arithmetic type.
-template <int Q, class T, class LOAD>
-__device__ __forceinline__ T pull_flow(const Geo& g, int a, int i, int j, int k, long long c, LOAD load) {
+template <int Q, class T, class LOAD, class WRAP>
+__device__ __forceinline__ T pull_flow_w(const Geo& g, int a, int i, int j, int k, long long c, LOAD load, WRAP wrap) {
     const int si = i - Lat<Q>::ex(a), sj = j - Lat<Q>::ey(a), sk = k - Lat<Q>::ez(a);
     int axis = -1;
     if (Lat<Q>::ex(a) != 0 && (si < 0 || si >= g.nx)) axis = 0;
@@ -111,9 +111,16 @@ __device__ __forceinline__ T pull_flow(const Geo& g, int a, int i, int j, int k,
         return load(a, c + off);
     }
     if (pick3(g.bcf, axis) == LBM_BC_NOSLIP) return load(Lat<Q>::opp(a), c);
-    if (axis == 0) return load(a, cell_index(g, si < 0 ? g.nx - 1 : 0, j, k));
-    if (axis == 1) return load(a, cell_index(g, i, sj < 0 ? g.ny - 1 : 0, k));
-    return load(a, cell_index(g, i, j, sk < 0 ? g.nz - 1 : 0));
+    if (axis == 0) return wrap(0, a, cell_index(g, si < 0 ? g.nx - 1 : 0, j, k));
+    if (axis == 1) return wrap(1, a, cell_index(g, i, sj < 0 ? g.ny - 1 : 0, k));
+    return wrap(2, a, cell_index(g, i, j, sk < 0 ? g.nz - 1 : 0));
+}
+
+// The same with the periodic source read like any other: WRAP(axis, dir, cell) is the hook
+// the in-place (AA) pattern uses to read face values from a snapshot.
+template <int Q, class T, class LOAD>
+__device__ __forceinline__ T pull_flow(const Geo& g, int a, int i, int j, int k, long long c, LOAD load) {
+    return pull_flow_w<Q, T>(g, a, i, j, k, c, load, [&](int, int d, long long cc) { return load(d, cc); });
 }
 
 // Thermal pull (D2Q5 / D3Q7, axis-aligned: at most one axis out of range), with the
@@ -121,8 +128,8 @@ __device__ __forceinline__ T pull_flow(const Geo& g, int a, int i, int j, int k,
 //   constant T : -g_post(opp(a)) + bc term (2*omegaT*Tw, Tw = Thot low face / Tcold high);
 //   adiabatic  :  g_post(opp(a));
 //   periodic   :  g_post(a) of the wrapped cell.
-template <int QT, class T, class LOAD>
-__device__ __forceinline__ T pull_thermal(const Geo& g, int a, int i, int j, int k, long long c, LOAD load) {
+template <int QT, class T, class LOAD, class WRAP>
+__device__ __forceinline__ T pull_thermal_w(const Geo& g, int a, int i, int j, int k, long long c, LOAD load, WRAP wrap) {
     if (a == 0) return load(0, c);
     const int si = i - Lat<QT>::ex(a), sj = j - Lat<QT>::ey(a), sk = k - Lat<QT>::ez(a);
     int axis = -1;
@@ -137,9 +144,97 @@ __device__ __forceinline__ T pull_thermal(const Geo& g, int a, int i, int j, int
     const int bt = pick3(g.bct, axis);
     if (bt == LBM_BCT_CONST) return -load(Lat<QT>::opp(a), c) + (T)(low ? pick3(g.bcT_lo, axis) : pick3(g.bcT_hi, axis));
     if (bt == LBM_BCT_ADIABATIC) return load(Lat<QT>::opp(a), c);
-    if (axis == 0) return load(a, cell_index(g, si < 0 ? g.nx - 1 : 0, j, k));
-    if (axis == 1) return load(a, cell_index(g, i, sj < 0 ? g.ny - 1 : 0, k));
-    return load(a, cell_index(g, i, j, sk < 0 ? g.nz - 1 : 0));
+    if (axis == 0) return wrap(0, a, cell_index(g, si < 0 ? g.nx - 1 : 0, j, k));
+    if (axis == 1) return wrap(1, a, cell_index(g, i, sj < 0 ? g.ny - 1 : 0, k));
+    return wrap(2, a, cell_index(g, i, j, sk < 0 ? g.nz - 1 : 0));
+}
+
+template <int QT, class T, class LOAD>
+__device__ __forceinline__ T pull_thermal(const Geo& g, int a, int i, int j, int k, long long c, LOAD load) {
+    return pull_thermal_w<QT, T>(g, a, i, j, k, c, load, [&](int, int d, long long cc) { return load(d, cc); });
+}
+
+// ------------------------------------------------------------------------------------
+// In-place (AA) access pattern.  One array per lattice; its layout alternates:
+//   parity 0 ("streamed"): slot (a, x) holds the streamed population f_a(x), i.e. what the
+//            pull above returns -- the reference's module array f;
+//   parity 1 ("swapped") : slot (opp(a), x) holds the post-collision f_post_a(x).
+// An even sweep reads a cell's own slots and writes its post-collision values back into
+// the opposite slots of the same cell.  An odd sweep pulls through the swapped layout
+// (dir d of cell s lives in slot (opp(d), s)) and pushes each post-collision value to
+// every slot that the next pull resolves to it, so the array is streamed again.  Every
+// slot an odd sweep writes is read in that sweep only by the cell that writes it, except
+// across a periodic face: those reads come from a snapshot of the face slots taken before
+// the sweep (aa_face_index indexes it).  The boundary rules are the pull's, so the
+// sequence of states equals the two-buffer sequence value for value.
+// ------------------------------------------------------------------------------------
+// Index of cell (i,j,k) in the face plane normal to `axis`.
+__device__ __forceinline__ long long aa_face_index(const Geo& g, int axis, int i, int j, int k) {
+    return axis == 0 ? (long long)j + (long long)g.ny * k
+                     : (axis == 1 ? (long long)i + (long long)g.nx * k : (long long)i + (long long)g.nx * j);
+}
+__host__ __device__ inline long long aa_face_cells(const Geo& g, int axis) {
+    return axis == 0 ? (long long)g.ny * g.nz : (axis == 1 ? (long long)g.nx * g.nz : (long long)g.nx * g.ny);
+}
+
+// Face snapshots of one array (one pointer per axis, null where the axis is not periodic).
+template <class S>
+struct AAFace {
+    const S *p0, *p1, *p2;
+};
+template <class S>
+__device__ __forceinline__ const S* aa_face_ptr(const AAFace<S>& w, int axis) {
+    return axis == 0 ? w.p0 : (axis == 1 ? w.p1 : w.p2);
+}
+
+// Push of the post-collision value v of direction a at cell (i,j,k) (odd sweep).
+// STORE(slot_dir, cell, value) writes the streamed layout.  Values are stored as they
+// leave the collision: a slot filled across a constant-temperature wall holds the raw
+// g_post, and the reader applies -g + 2 w T_w (aa_local_thermal), so the stored number and
+// the arithmetic on it are those of the two-buffer pull.  THERMAL selects the thermal
+// boundary table.
+template <int Q, bool THERMAL, class T, class STORE>
+__device__ __forceinline__ void aa_push(const Geo& g, int a, int i, int j, int k, long long c, T v, STORE store) {
+    const int ex = Lat<Q>::ex(a), ey = Lat<Q>::ey(a), ez = Lat<Q>::ez(a);
+    const int ti = i + ex, tj = j + ey, tk = k + ez;
+    const bool ox = ex != 0 && (ti < 0 || ti >= g.nx);
+    const bool oy = ey != 0 && (tj < 0 || tj >= g.ny);
+    const bool oz = ez != 0 && (tk < 0 || tk >= g.nz);
+    if (!ox && !oy && !oz) {
+        store(a, c + (long long)ex + (long long)g.nx * ((long long)ey + (long long)g.ny * (long long)ez), v);
+        return;
+    }
+    auto periodic = [&](int axis) {
+        return THERMAL ? pick3(g.bct, axis) == LBM_BCT_PERIODIC : pick3(g.bcf, axis) == LBM_BC_PERIODIC;
+    };
+    // the pull of opp(a) into this cell has the target as its source and is resolved on
+    // the last out-of-range axis of the target: a wall returns this value
+    const int ax = oz ? 2 : (oy ? 1 : 0);
+    if (!periodic(ax)) store(Lat<Q>::opp(a), c, v);
+    // the cell wrapped along an out-of-range periodic axis pulls this value when no later
+    // axis of its own source is out of range
+    const bool iy = ey != 0 && (j - ey < 0 || j - ey >= g.ny);
+    const bool iz = ez != 0 && (k - ez < 0 || k - ez >= g.nz);
+    if (ox && periodic(0) && !iy && !iz) store(a, cell_index(g, ti < 0 ? g.nx - 1 : 0, j, k), v);
+    if (oy && periodic(1) && !iz) store(a, cell_index(g, i, tj < 0 ? g.ny - 1 : 0, k), v);
+    if (oz && periodic(2)) store(a, cell_index(g, i, j, tk < 0 ? g.nz - 1 : 0), v);
+}
+
+// Thermal population a of cell (i,j,k) from the streamed layout.  raw: the slot was filled
+// by a push, so a constant-temperature wall's rule is still to be applied (slots written
+// from module data -- initial, a state load -- already hold the module value).
+template <int QT, class T, class LOAD>
+__device__ __forceinline__ T aa_local_thermal(const Geo& g, int a, int i, int j, int k, long long c, bool raw, LOAD load) {
+    const T v = load(a, c);
+    if (a == 0 || !raw) return v;
+    const int si = i - Lat<QT>::ex(a), sj = j - Lat<QT>::ey(a), sk = k - Lat<QT>::ez(a);
+    int axis = -1;
+    bool low = false;
+    if (Lat<QT>::ex(a) != 0 && (si < 0 || si >= g.nx)) { axis = 0; low = si < 0; }
+    if (Lat<QT>::ey(a) != 0 && (sj < 0 || sj >= g.ny)) { axis = 1; low = sj < 0; }
+    if (Lat<QT>::ez(a) != 0 && (sk < 0 || sk >= g.nz)) { axis = 2; low = sk < 0; }
+    if (axis < 0 || pick3(g.bct, axis) != LBM_BCT_CONST) return v;
+    return -v + (T)(low ? pick3(g.bcT_lo, axis) : pick3(g.bcT_hi, axis));
 }
 
 // Decompose a linear thread index into (i,j,k).

@@ -417,10 +417,15 @@ __global__ void k_initial(Geo g, PhysC P, InitC I, ExactArrays A) {
     A.vp[c] = 0.0;
     A.Tp[c] = 0.0;
     if (D == 3) A.wp[c] = 0.0;
+    // the in-place pattern has no post-collision arrays (null pointers)
+    if (A.fpost) {
 #pragma unroll
-    for (int a = 0; a < Q; ++a) A.fpost[a * n + c] = 0.0;
+        for (int a = 0; a < Q; ++a) A.fpost[a * n + c] = 0.0;
+    }
+    if (A.gpost) {
 #pragma unroll
-    for (int a = 0; a < QT; ++a) A.gpost[a * n + c] = 0.0;
+        for (int a = 0; a < QT; ++a) A.gpost[a * n + c] = 0.0;
+    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -705,6 +710,174 @@ __global__ void k_materialize(Geo g, PhysC P, ExactArrays A, const double* __res
 }
 
 // ------------------------------------------------------------------------------------
+// In-place (AA) form of the two fused kernels: one array per lattice, the layout parity
+// of each array selects where a cell reads and writes (lbm_device.cuh).  The arithmetic
+// is k_flow / k_thermal's, on the same values, so each state equals the two-buffer one.
+// ODD: this kernel's own array is in the swapped layout (odd sweep: pull, then push).
+// gpar / fpar: layout of the other array, which the kernel only reads.  graw: the thermal
+// array's streamed slots were filled by pushes.
+// ------------------------------------------------------------------------------------
+template <int D, bool ODD>
+__global__ void __launch_bounds__(128) k_aa_flow(Geo g, PhysC P, ExactArrays A, double* f,
+                                                 const double* __restrict__ gs, AAFace<double> wf, int gpar,
+                                                 int graw, int first) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
+    const long long n = g.ncell;
+    double F[Q], FP[Q], rho, u, v, w = 0.0, T;
+    if (ODD) {
+        auto lf = [&](int b, long long cc) { return f[Lat<Q>::opp(b) * n + cc]; };
+        auto wr = [&](int ax, int b, long long) {
+            return aa_face_ptr(wf, ax)[b * aa_face_cells(g, ax) + aa_face_index(g, ax, i, j, k)];
+        };
+#pragma unroll
+        for (int a = 0; a < Q; ++a) F[a] = pull_flow_w<Q, double>(g, a, i, j, k, c, lf, wr);
+    } else {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) F[a] = f[a * n + c];
+    }
+    if (first) {
+        rho = A.rho[c];
+        u = A.u[c];
+        v = A.v[c];
+        if (D == 3) w = A.w[c];
+        T = A.T[c];
+    } else {
+        double G[QT];
+        if (gpar) {
+            auto lg = [&](int b, long long cc) { return gs[Lat<QT>::opp(b) * n + cc]; };
+#pragma unroll
+            for (int a = 0; a < QT; ++a) G[a] = pull_thermal<QT, double>(g, a, i, j, k, c, lg);
+        } else {
+            auto lg = [&](int b, long long cc) { return gs[b * n + cc]; };
+#pragma unroll
+            for (int a = 0; a < QT; ++a) G[a] = aa_local_thermal<QT, double>(g, a, i, j, k, c, graw != 0, lg);
+        }
+        T = sumT<QT>(G);
+        if (D == 2) macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
+        else macro_3d(F, A.Tlag[c], P, rho, u, v, w);
+    }
+    if (D == 2) {
+        double Fx, Fy;
+        collide_2d(F, rho, u, v, T, P, FP, Fx, Fy);
+        A.Fx[c] = Fx;
+        A.Fy[c] = Fy;
+    } else {
+        collide_3d(F, rho, u, v, w, T, P, FP);
+    }
+    if (ODD) {
+        auto st = [&](int b, long long cc, double val) { f[b * n + cc] = val; };
+#pragma unroll
+        for (int a = 0; a < Q; ++a) aa_push<Q, false, double>(g, a, i, j, k, c, FP[a], st);
+    } else {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) f[Lat<Q>::opp(a) * n + c] = FP[a];
+    }
+}
+
+template <int D, bool ODD>
+__global__ void __launch_bounds__(128) k_aa_thermal(Geo g, PhysC P, ExactArrays A, const double* __restrict__ fs,
+                                                    double* gg, AAFace<double> wg, int fpar, int graw, int first) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
+    const long long n = g.ncell;
+    double F[Q], G[QT], GP[QT];
+    if (fpar) {
+        auto lf = [&](int b, long long cc) { return fs[Lat<Q>::opp(b) * n + cc]; };
+#pragma unroll
+        for (int a = 0; a < Q; ++a) F[a] = pull_flow<Q, double>(g, a, i, j, k, c, lf);
+    } else {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) F[a] = fs[a * n + c];
+    }
+    if (ODD) {
+        auto lg = [&](int b, long long cc) { return gg[Lat<QT>::opp(b) * n + cc]; };
+        auto wr = [&](int ax, int b, long long) {
+            return aa_face_ptr(wg, ax)[b * aa_face_cells(g, ax) + aa_face_index(g, ax, i, j, k)];
+        };
+#pragma unroll
+        for (int a = 0; a < QT; ++a) G[a] = pull_thermal_w<QT, double>(g, a, i, j, k, c, lg, wr);
+    } else {
+        auto lg = [&](int b, long long cc) { return gg[b * n + cc]; };
+#pragma unroll
+        for (int a = 0; a < QT; ++a) G[a] = aa_local_thermal<QT, double>(g, a, i, j, k, c, graw != 0, lg);
+    }
+    const double Tprev = first ? A.T[c] : sumT<QT>(G);
+    if (D == 2) {
+        double rho, u, v, Bx, By;
+        macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
+        collideT_2d(G, u, v, Tprev, A.Bx[c], A.By[c], P, GP, Bx, By);
+        if (P.use_g) {
+            A.Bx[c] = Bx;
+            A.By[c] = By;
+        }
+    } else {
+        double rho, u, v, w, Bx, By, Bz;
+        macro_3d(F, Tprev, P, rho, u, v, w);
+        collideT_3d(G, u, v, w, Tprev, A.Bx[c], A.By[c], A.Bz[c], P, GP, Bx, By, Bz);
+        if (P.use_g) {
+            A.Bx[c] = Bx;
+            A.By[c] = By;
+            A.Bz[c] = Bz;
+        }
+        A.Tlag[c] = Tprev;
+    }
+    if (ODD) {
+        auto st = [&](int b, long long cc, double val) { gg[b * n + cc] = val; };
+#pragma unroll
+        for (int a = 0; a < QT; ++a) aa_push<QT, true, double>(g, a, i, j, k, c, GP[a], st);
+    } else {
+#pragma unroll
+        for (int a = 0; a < QT; ++a) gg[Lat<QT>::opp(a) * n + c] = GP[a];
+    }
+}
+
+// Module scalars of step N from the in-place arrays (k_materialize without the population
+// copies: the arrays already are the module populations, read through their layout).
+template <int D>
+__global__ void k_aa_materialize(Geo g, PhysC P, ExactArrays A, const double* __restrict__ fs,
+                                 const double* __restrict__ gs, int fpar, int gpar, int graw) {
+    long long c;
+    int i, j, k;
+    if (!thread_cell(g, c, i, j, k)) return;
+    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
+    const long long n = g.ncell;
+    double F[Q], G[QT];
+    if (fpar) {
+        auto lf = [&](int b, long long cc) { return fs[Lat<Q>::opp(b) * n + cc]; };
+#pragma unroll
+        for (int a = 0; a < Q; ++a) F[a] = pull_flow<Q, double>(g, a, i, j, k, c, lf);
+    } else {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) F[a] = fs[a * n + c];
+    }
+    if (gpar) {
+        auto lg = [&](int b, long long cc) { return gs[Lat<QT>::opp(b) * n + cc]; };
+#pragma unroll
+        for (int a = 0; a < QT; ++a) G[a] = pull_thermal<QT, double>(g, a, i, j, k, c, lg);
+    } else {
+        auto lg = [&](int b, long long cc) { return gs[b * n + cc]; };
+#pragma unroll
+        for (int a = 0; a < QT; ++a) G[a] = aa_local_thermal<QT, double>(g, a, i, j, k, c, graw != 0, lg);
+    }
+    double rho, u, v, w;
+    if (D == 2) {
+        macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
+    } else {
+        macro_3d(F, A.Tlag[c], P, rho, u, v, w);
+        A.w[c] = w;
+    }
+    A.rho[c] = rho;
+    A.u[c] = u;
+    A.v[c] = v;
+    A.T[c] = sumT<QT>(G);
+}
+
+// ------------------------------------------------------------------------------------
 // restart reconstruction (reconstruct_macro_from_fg, 2DRB.F90:1144-1200,
 // 3DRB.F90:1392-1463): T = sum g (the macroT call), rho = sum f, u = (mom + F/2)/rho with
 // F = rho gBeta (T - Tref).  The reference iterates that assignment three times; without
@@ -848,6 +1021,51 @@ void exact_fused_step(const Geo& g, const PhysC& P, const ExactArrays& A, int di
             if (th) k_thermal<3, false><<<nb, 128, 0, s>>>(g, P, A, fnext, gprev, gnext);
         }
     }
+}
+
+static AAFace<double> aa_faces(void* const face[3]) {
+    return AAFace<double>{(const double*)face[0], (const double*)face[1], (const double*)face[2]};
+}
+
+static bool any_face(void* const face[3]) { return face[0] || face[1] || face[2]; }
+
+void exact_aa_step(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, bool first, AAState& S,
+                   cudaStream_t s, int part) {
+    const unsigned nb = nblocks(g.ncell, 128);
+    const int fi = first ? 1 : 0, raw = S.graw ? 1 : 0;
+    if (part != 1) {
+        if (S.fpar && any_face(S.face_f)) aa_snapshot(g, dim == 3 ? 19 : 9, false, LBM_FP64, A.f, S.face_f, s);
+        const AAFace<double> wf = aa_faces(S.face_f);
+        if (dim == 2) {
+            if (S.fpar) k_aa_flow<2, true><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw, fi);
+            else k_aa_flow<2, false><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw, fi);
+        } else {
+            if (S.fpar) k_aa_flow<3, true><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw, fi);
+            else k_aa_flow<3, false><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw, fi);
+        }
+        S.fpar ^= 1;
+    }
+    if (part != 0) {
+        if (S.gpar && any_face(S.face_g)) aa_snapshot(g, dim == 3 ? 7 : 5, true, LBM_FP64, A.g, S.face_g, s);
+        const AAFace<double> wg = aa_faces(S.face_g);
+        if (dim == 2) {
+            if (S.gpar) k_aa_thermal<2, true><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw, fi);
+            else k_aa_thermal<2, false><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw, fi);
+        } else {
+            if (S.gpar) k_aa_thermal<3, true><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw, fi);
+            else k_aa_thermal<3, false><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw, fi);
+        }
+        if (S.gpar) S.graw = true;
+        S.gpar ^= 1;
+    }
+}
+
+void exact_aa_materialize(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, const AAState& S,
+                          cudaStream_t s) {
+    const unsigned nb = nblocks(g.ncell, 128);
+    const int raw = S.graw ? 1 : 0;
+    if (dim == 2) k_aa_materialize<2><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, S.fpar, S.gpar, raw);
+    else k_aa_materialize<3><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, S.fpar, S.gpar, raw);
 }
 
 void exact_reconstruct(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, unsigned int* bad,

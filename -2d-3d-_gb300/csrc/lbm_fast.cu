@@ -205,8 +205,11 @@ int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn
     F.qt = p.dim == 3 ? 7 : 5;
     F.esize = p.precision == LBM_FP16 ? 2 : 4;
     const long long n = g.ncell;
+    F.aa = p.pattern == LBM_PATTERN_AA;
+    F.AA = AAState{};
     int st;
-    for (int b = 0; b < 2; ++b) {
+    const int nbuf = F.aa ? 1 : 2;
+    for (int b = 0; b < nbuf; ++b) {
         if ((st = alloc(&F.fbuf[b], F.esize * F.q * n)) != LBM_OK) return st;
         if ((st = alloc(&F.gbuf[b], F.esize * F.qt * n)) != LBM_OK) return st;
         for (int c = 0; c < (p.dim == 3 ? 3 : 2); ++c)
@@ -215,8 +218,24 @@ int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn
     }
     if ((st = alloc((void**)&F.err, sizeof(int))) != LBM_OK) return st;
     if (cudaMemset(F.err, 0, sizeof(int)) != cudaSuccess) return LBM_ERR_CUDA;
-    if ((st = alloc(&F.fref, F.esize * F.q * n)) != LBM_OK) return st;
-    if ((st = alloc(&F.gref, F.esize * F.qt * n)) != LBM_OK) return st;
+    if (F.aa) {
+        // one array each, which is also the module array; the lag fields are read and
+        // written by the same thread, so one buffer serves both parities
+        F.fref = F.fbuf[0];
+        F.gref = F.gbuf[0];
+        for (int c = 0; c < 3; ++c) F.B[1][c] = F.B[0][c];
+        F.L[1] = F.L[0];
+        F.tma = false;
+        for (int ax = 0; ax < 3; ++ax) {
+            if (g.bcf[ax] == LBM_BC_PERIODIC && (st = alloc(&F.AA.face_f[ax], F.esize * F.q * aa_face_cells(g, ax))) != LBM_OK)
+                return st;
+            if (g.bct[ax] == LBM_BCT_PERIODIC && (st = alloc(&F.AA.face_g[ax], F.esize * F.qt * aa_face_cells(g, ax))) != LBM_OK)
+                return st;
+        }
+    } else {
+        if ((st = alloc(&F.fref, F.esize * F.q * n)) != LBM_OK) return st;
+        if ((st = alloc(&F.gref, F.esize * F.qt * n)) != LBM_OK) return st;
+    }
     float** scal[] = {&F.rho, &F.u, &F.v, &F.T, &F.up, &F.vp, &F.Tp};
     for (float** s : scal)
         if ((st = alloc((void**)s, sizeof(float) * n)) != LBM_OK) return st;
@@ -247,6 +266,8 @@ void fast_initial(FastState& F, const Geo& g, const PhysC& P, const InitC& I, in
     F.cur = 0;
     F.fused_valid = false;
     F.ahead = false;
+    F.AA.fpar = F.AA.gpar = 0;  // the in-place arrays now hold module data
+    F.AA.graw = false;
     DISPATCH_S(F, {
         FastArgs<S> A = args_for<S>(F, 0, 0, 0, 0);
         if (dim == 2) k_fast_initial<2, S><<<nb(g.ncell, 256), 256, 0, s>>>(g, pf, I, A);
@@ -275,6 +296,15 @@ void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first,
     const PhysF pf = to_physf(P);
     const Geo g = dev_geo(g0, P);
     const int cur = F.cur, nxt = F.cur ^ 1;
+    if (F.aa) {
+        F.ahead = false;
+        fast_step_aa(F, g, pf, dim, first, s, part);
+        if (part != 0) {
+            F.cur = nxt;
+            F.fused_valid = true;
+        }
+        return;
+    }
     const unsigned blocks = nb(g.ncell, 128);
     const bool paired = F.pairs && g.nx % 2 == 0;
     dim3 pgrid, pblock;
@@ -330,6 +360,10 @@ void fast_materialize(FastState& F, const Geo& g0, const PhysC& P, int dim, cuda
     if (!F.fused_valid) return;
     const PhysF pf = to_physf(P);
     const Geo g = dev_geo(g0, P);
+    if (F.aa) {
+        fast_materialize_aa(F, g, pf, dim, s);
+        return;
+    }
     DISPATCH_S(F, {
         const S* fin = (const S*)F.fbuf[F.cur];
         const S* gin = (const S*)F.gbuf[F.cur];
@@ -348,6 +382,14 @@ int fast_export(const FastState& F, const Geo& g, const PhysC& P, int dim, int f
     const long long n = g.ncell;
     const bool d3 = dim == 3;
     const double wt0 = P.omegaT0 * P.Tref, wt1 = P.omegaT1 * P.Tref;
+    if (F.aa && (field == LBM_FIELD_F || field == LBM_FIELD_G)) {
+        // the module view, read through the array's layout
+        const bool th = field == LBM_FIELD_G;
+        aa_module_view(dev_geo(g, P), th ? F.qt : F.q, th, F.precision, th ? F.gbuf[0] : F.fbuf[0],
+                       th ? F.AA.gpar : F.AA.fpar, F.AA.graw, out, soa, true, wt0, wt1, s);
+        return LBM_OK;
+    }
+    if (F.aa && (field == LBM_FIELD_F_POST || field == LBM_FIELD_G_POST)) return LBM_ERR_STATE;
     if (field == LBM_FIELD_F || field == LBM_FIELD_F_POST || field == LBM_FIELD_G || field == LBM_FIELD_G_POST) {
         const bool th = field == LBM_FIELD_G || field == LBM_FIELD_G_POST;
         const void* src = field == LBM_FIELD_F ? F.fref : field == LBM_FIELD_G ? F.gref
@@ -403,6 +445,12 @@ int fast_import(FastState& F, const Geo& g, const PhysC& P, int dim, int field, 
         });
         F.fused_valid = false;
         F.ahead = false;
+        if (th) {
+            F.AA.gpar = 0;  // module data in the streamed layout
+            F.AA.graw = false;
+        } else {
+            F.AA.fpar = 0;
+        }
         return LBM_OK;
     }
     float* dst = nullptr;

@@ -21,6 +21,8 @@
 
 namespace lbm {
 
+struct PhysF;
+
 struct FastState {
     int precision = LBM_FP32;  // LBM_FP32 or LBM_FP16
     int dim = 3, q = 19, qt = 7;
@@ -45,6 +47,10 @@ struct FastState {
     bool pairs = false;
     bool tma = false;
     int* err = nullptr;         // device flag: a bounded wait of a staged kernel gave up
+    // In-place (AA) pattern: fbuf[0] / gbuf[0] are the only population arrays and also the
+    // module arrays (fref, gref alias them); B and L have one buffer each.
+    bool aa = false;
+    AAState AA;
 };
 
 using AllocFn = std::function<int(void**, size_t)>;
@@ -62,8 +68,11 @@ bool fast_fused_supported(const Geo& g, int dim);
 bool fast_tma_supported(const Geo& g, int dim, int precision);
 // Read and clear the device error flag of the staged kernels (synchronises the stream).
 int fast_take_error(FastState& F, cudaStream_t s);
+// In-place pattern step and materialisation (lbm_fast_aa.cu); g is the deviation geometry.
+void fast_step_aa(FastState& F, const Geo& g, const PhysF& pf, int dim, bool first, cudaStream_t s, int part);
+void fast_materialize_aa(FastState& F, const Geo& g, const PhysF& pf, int dim, cudaStream_t s);
 // Rebuild the module arrays (f, g, rho, u, v, w, T) of the current step; leaves the fused
-// buffers valid.
+// buffers valid.  In-place pattern: the module scalars only (the arrays are the populations).
 void fast_materialize(FastState& F, const Geo& g, const PhysC& P, int dim, cudaStream_t s);
 inline bool fast_fused_valid(const FastState& F) { return F.fused_valid; }
 inline bool fast_at_origin(const FastState& F) { return F.cur == 0; }

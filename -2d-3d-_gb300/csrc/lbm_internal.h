@@ -47,6 +47,27 @@ enum Stage {
     STAGE_COLLISIONT, STAGE_STREAMINGT, STAGE_BOUNCEBACKT, STAGE_MACROT
 };
 
+// ---- in-place (AA) access pattern --------------------------------------------------------
+// State of the pattern for one lattice: the layout parity of the flow and thermal arrays
+// (0 streamed, 1 swapped; lbm_device.cuh) and the face snapshots that an odd sweep reads
+// across periodic faces.
+struct AAState {
+    int fpar = 0, gpar = 0;
+    bool graw = false;  // the thermal array's streamed slots were filled by pushes (raw values)
+    void* face_f[3] = {nullptr, nullptr, nullptr};  // per periodic flow axis: q * face cells
+    void* face_g[3] = {nullptr, nullptr, nullptr};
+};
+
+// Storage precision of an array handed to the pattern's helpers (LBM_FP64/FP32/FP16).
+// Snapshot the face slots of every periodic axis of one array before its odd sweep.
+void aa_snapshot(const Geo& g, int q, bool thermal, int precision, const void* arr, void* const face[3],
+                 cudaStream_t s);
+// The module (streamed) view of one array into FP64: AoS (Fortran order) or SoA.  dev:
+// the array stores deviations from the rest state (FP32/FP16 forms; w0/w1 are the thermal
+// rest values) and each value is rounded to the storage type as the module array holds it.
+void aa_module_view(const Geo& g, int q, bool thermal, int precision, const void* arr, int par, bool raw, double* out,
+                    bool soa, bool dev, double w0, double w1, cudaStream_t s);
+
 // ---- exact FP64 kernels (lbm_exact.cu) ------------------------------------------------
 void exact_initial(const Geo& g, const PhysC& P, const InitC& I, const ExactArrays& A, int dim, cudaStream_t s);
 void exact_stage(int stage, const Geo& g, const PhysC& P, const ExactArrays& A, int dim, cudaStream_t s);
@@ -55,6 +76,13 @@ void exact_fused_step(const Geo& g, const PhysC& P, const ExactArrays& A, int di
                       const double* gprev, double* fnext, double* gnext, cudaStream_t s, int part = 2);
 void exact_materialize(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, const double* fcur,
                        const double* gcur, cudaStream_t s);
+
+// In-place pattern: part 0 = flow sweep, 1 = thermal sweep, 2 = both; flips the parities.
+void exact_aa_step(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, bool first, AAState& S,
+                   cudaStream_t s, int part = 2);
+// Module scalars (rho, u, v, w, T) of the current step from the in-place arrays A.f, A.g.
+void exact_aa_materialize(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, const AAState& S,
+                          cudaStream_t s);
 
 // Restart: rebuild T, rho, u, v, w, B_prev and the 2D force from the SoA populations A.f,
 // A.g (reconstruct_macro_from_fg); sets *bad = 1 when some cell has rho <= 0.

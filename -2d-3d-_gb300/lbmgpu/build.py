@@ -5,6 +5,7 @@ Translation units and their floating-point flags:
   lbm_reduce.cu -fmad=false : FP64 diagnostics, per-cell terms rounded as in the reference
   lbm_fast.cu               : FP32 arithmetic on FP32/FP16 storage, FMA contraction allowed
   lbm_fast_tma.cu           : the same step with population rows staged by bulk copies
+  lbm_fast_aa.cu            : the same step in the in-place (AA) access pattern
   lbm_api.cpp               : host code (-ffp-contract=off for the host-side fits)
   lbm_checkpoint.cpp        : Fortran unformatted sequential records (restart files)
   lbm_output.cpp            : snapshot / Tecplot writers, stream function post-processing
@@ -31,6 +32,7 @@ UNITS = [
     ("lbm_reduce.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
     ("lbm_fast.cu", ["-fmad=true"]),
     ("lbm_fast_tma.cu", ["-fmad=true"]),
+    ("lbm_fast_aa.cu", ["-fmad=true"]),
     ("lbm_fused.cu", ["-fmad=true"]),
     ("lbm_ensemble.cu", ["-fmad=true"]),
     ("lbm_api.cpp", []),

@@ -99,3 +99,22 @@ def test_magnetic_force_only_in_2d_plain_method(gpu_lib, oracle_mod):
     q3.side_heated_ha = 1
     with pytest.raises(lbmgpu.LbmError):
         lbmgpu.derive_constants(q3)
+
+
+def test_in_place_pattern_accepted_and_smaller(gpu_lib):
+    """LBM_PATTERN_AA is a valid pattern for every precision; its device footprint holds one
+    population array per lattice (the two-buffer form holds three: A, B and the module
+    array) plus face snapshots for periodic axes."""
+    import lbmgpu
+    for dim in (2, 3):
+        for prec in ("fp64", "fp32", "fp16"):
+            ab = rb_params(dim=dim, n=64, precision=prec)
+            aa = rb_params(dim=dim, n=64, precision=prec, pattern="AA")
+            lbmgpu.derive_constants(aa)
+            n = ab.nx * ab.ny * (ab.nz if dim == 3 else 1)
+            q = 26 if dim == 3 else 14
+            es = {"fp64": 8, "fp32": 4, "fp16": 2}[prec]
+            saved = lbmgpu.footprint(ab) - lbmgpu.footprint(aa)
+            lag = 0 if prec == "fp64" else 4 * n * (4 if dim == 3 else 3)
+            faces = es * (19 + 7 if dim == 3 else 9 + 5) * ab.ny if dim == 2 else 0  # 2D cells are x-periodic
+            assert saved == 2 * es * q * n + lag - faces, (dim, prec)
