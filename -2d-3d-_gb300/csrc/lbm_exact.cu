@@ -715,10 +715,14 @@ __global__ void k_materialize(Geo g, PhysC P, ExactArrays A, const double* __res
 // is k_flow / k_thermal's, on the same values, so each state equals the two-buffer one.
 // ODD: this kernel's own array is in the swapped layout (odd sweep: pull, then push).
 // gpar / fpar: layout of the other array, which the kernel only reads.  graw: the thermal
-// array's streamed slots were filled by pushes.
+// array's streamed slots were filled by pushes.  The own array is read through the
+// read-only path although the sweep writes it: every slot is read only by the cell that
+// owns it and written only by that cell after all of its reads (lbm_fast_aa.cu, ldA).
 // ------------------------------------------------------------------------------------
+// Six blocks per SM as the two-buffer flow kernel gets with its 80 registers (the FP64
+// pipe needs the warps); the in-place flow kernels fit that without spilling.
 template <int D, bool ODD>
-__global__ void __launch_bounds__(128) k_aa_flow(Geo g, PhysC P, ExactArrays A, double* f,
+__global__ void __launch_bounds__(128, 6) k_aa_flow(Geo g, PhysC P, ExactArrays A, double* f,
                                                  const double* __restrict__ gs, AAFace<double> wf, int gpar,
                                                  int graw, int first) {
     long long c;
@@ -728,15 +732,15 @@ __global__ void __launch_bounds__(128) k_aa_flow(Geo g, PhysC P, ExactArrays A, 
     const long long n = g.ncell;
     double F[Q], FP[Q], rho, u, v, w = 0.0, T;
     if (ODD) {
-        auto lf = [&](int b, long long cc) { return f[Lat<Q>::opp(b) * n + cc]; };
+        auto lf = [&](int b, long long cc) { return __ldg(f + Lat<Q>::opp(b) * n + cc); };
         auto wr = [&](int ax, int b, long long) {
-            return aa_face_ptr(wf, ax)[b * aa_face_cells(g, ax) + aa_face_index(g, ax, i, j, k)];
+            return __ldg(aa_face_ptr(wf, ax) + b * aa_face_cells(g, ax) + aa_face_index(g, ax, i, j, k));
         };
 #pragma unroll
         for (int a = 0; a < Q; ++a) F[a] = pull_flow_w<Q, double>(g, a, i, j, k, c, lf, wr);
     } else {
 #pragma unroll
-        for (int a = 0; a < Q; ++a) F[a] = f[a * n + c];
+        for (int a = 0; a < Q; ++a) F[a] = __ldg(f + a * n + c);
     }
     if (first) {
         rho = A.rho[c];
@@ -795,14 +799,14 @@ __global__ void __launch_bounds__(128) k_aa_thermal(Geo g, PhysC P, ExactArrays 
         for (int a = 0; a < Q; ++a) F[a] = fs[a * n + c];
     }
     if (ODD) {
-        auto lg = [&](int b, long long cc) { return gg[Lat<QT>::opp(b) * n + cc]; };
+        auto lg = [&](int b, long long cc) { return __ldg(gg + Lat<QT>::opp(b) * n + cc); };
         auto wr = [&](int ax, int b, long long) {
-            return aa_face_ptr(wg, ax)[b * aa_face_cells(g, ax) + aa_face_index(g, ax, i, j, k)];
+            return __ldg(aa_face_ptr(wg, ax) + b * aa_face_cells(g, ax) + aa_face_index(g, ax, i, j, k));
         };
 #pragma unroll
         for (int a = 0; a < QT; ++a) G[a] = pull_thermal_w<QT, double>(g, a, i, j, k, c, lg, wr);
     } else {
-        auto lg = [&](int b, long long cc) { return gg[b * n + cc]; };
+        auto lg = [&](int b, long long cc) { return __ldg(gg + b * n + cc); };
 #pragma unroll
         for (int a = 0; a < QT; ++a) G[a] = aa_local_thermal<QT, double>(g, a, i, j, k, c, graw != 0, lg);
     }

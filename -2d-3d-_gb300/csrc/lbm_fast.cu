@@ -225,7 +225,6 @@ int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn
         F.gref = F.gbuf[0];
         for (int c = 0; c < 3; ++c) F.B[1][c] = F.B[0][c];
         F.L[1] = F.L[0];
-        F.tma = false;
         for (int ax = 0; ax < 3; ++ax) {
             if (g.bcf[ax] == LBM_BC_PERIODIC && (st = alloc(&F.AA.face_f[ax], F.esize * F.q * aa_face_cells(g, ax))) != LBM_OK)
                 return st;

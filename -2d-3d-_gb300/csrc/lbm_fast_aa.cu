@@ -12,18 +12,9 @@
 #include "lbm_fast.h"
 #include "lbm_fast_cells.cuh"
 #include "lbm_fast_pairs.cuh"
+#include "lbm_fast_aa.cuh"
 
 namespace lbm {
-
-// Coherent loads for the array a kernel also writes (the read-only path may not be used
-// for memory the same kernel stores to).
-template <class S> __device__ __forceinline__ float ldA(const S* p, long long i);
-template <> __device__ __forceinline__ float ldA<float>(const float* p, long long i) { return p[i]; }
-template <> __device__ __forceinline__ float ldA<__half>(const __half* p, long long i) { return __half2float(p[i]); }
-
-// The value the module array of storage type S holds for an arithmetic value x.
-template <class S> __device__ __forceinline__ float roundS(float x) { return x; }
-template <> __device__ __forceinline__ float roundS<__half>(float x) { return __half2float(__float2half_rn(x)); }
 
 // conversions of the generic helpers (S = double for the FP64 plain method)
 template <class S> __device__ __forceinline__ double to_d(S x) { return (double)x; }
@@ -138,57 +129,7 @@ __global__ void __launch_bounds__(128) k_aa_flow_f(Geo g, PhysF P, FastArgs<S> A
     long long c;
     int i, j, k;
     if (!fcell(g, c, i, j, k)) return;
-    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
-    const long long n = g.ncell;
-    float d[Q], dp[Q], dr, rho, u, v, w = 0.0f, T;
-    if (ODD) {
-        auto lf = [&](int b, long long cc) { return ldA(f, Lat<Q>::opp(b) * n + cc); };
-        auto wr = [&](int ax, int b, long long) {
-            return ldA(aa_face_ptr(wf, ax), b * aa_face_cells(g, ax) + aa_face_index(g, ax, i, j, k));
-        };
-#pragma unroll
-        for (int a = 0; a < Q; ++a) d[a] = pull_flow_w<Q, float>(g, a, i, j, k, c, lf, wr);
-    } else {
-#pragma unroll
-        for (int a = 0; a < Q; ++a) d[a] = ldA(f, a * n + c);
-    }
-    if (FIRST) {
-        rho = A.rho[c];
-        dr = rho - 1.0f;
-        u = A.u[c];
-        v = A.v[c];
-        if (D == 3) w = A.w[c];
-        T = A.T[c];
-    } else {
-        float ts = 0.0f;
-        if (gpar) {
-            auto lg = [&](int b, long long cc) { return ldS(gs, Lat<QT>::opp(b) * n + cc); };
-#pragma unroll
-            for (int a = 0; a < QT; ++a) ts += pull_thermal<QT, float>(g, a, i, j, k, c, lg);
-        } else {
-            auto lg = [&](int b, long long cc) { return ldS(gs, b * n + cc); };
-#pragma unroll
-            for (int a = 0; a < QT; ++a) ts += aa_local_thermal<QT, float>(g, a, i, j, k, c, graw != 0, lg);
-        }
-        T = ts + P.Tref;
-        float Fy;
-        fmacro<D>(d, A.lag_in[c], P, dr, rho, u, v, w, Fy);
-    }
-    const float Fy = rho * P.gBeta * (T - P.Tref);
-    if (D == 2) {
-        A.lag_out[c] = Fy;
-        fcollide_2d(d, dr, rho, u, v, Fy, P, dp);
-    } else {
-        fcollide_3d(d, dr, rho, u, v, w, Fy, P, dp);
-    }
-    if (ODD) {
-        auto st = [&](int b, long long cc, float val) { f[b * n + cc] = toS<S>(val); };
-#pragma unroll
-        for (int a = 0; a < Q; ++a) aa_push<Q, false, float>(g, a, i, j, k, c, dp[a], st);
-    } else {
-#pragma unroll
-        for (int a = 0; a < Q; ++a) f[Lat<Q>::opp(a) * n + c] = toS<S>(dp[a]);
-    }
+    aa_flow_cell<D, S, ODD, FIRST>(g, P, A, f, gs, wf, gpar, graw, c, i, j, k);
 }
 
 template <int D, class S, bool ODD, bool FIRST>
@@ -197,68 +138,7 @@ __global__ void __launch_bounds__(128) k_aa_thermal_f(Geo g, PhysF P, FastArgs<S
     long long c;
     int i, j, k;
     if (!fcell(g, c, i, j, k)) return;
-    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
-    const long long n = g.ncell;
-    float d[Q], G[QT], GP[QT];
-    if (fpar) {
-        auto lf = [&](int b, long long cc) { return ldS(fs, Lat<Q>::opp(b) * n + cc); };
-#pragma unroll
-        for (int a = 0; a < Q; ++a) d[a] = pull_flow<Q, float>(g, a, i, j, k, c, lf);
-    } else {
-#pragma unroll
-        for (int a = 0; a < Q; ++a) d[a] = ldS(fs, a * n + c);
-    }
-    float e[QT];
-    if (ODD) {
-        auto lg = [&](int b, long long cc) { return ldA(gg, Lat<QT>::opp(b) * n + cc); };
-        auto wr = [&](int ax, int b, long long) {
-            return ldA(aa_face_ptr(wg, ax), b * aa_face_cells(g, ax) + aa_face_index(g, ax, i, j, k));
-        };
-#pragma unroll
-        for (int a = 0; a < QT; ++a) e[a] = pull_thermal_w<QT, float>(g, a, i, j, k, c, lg, wr);
-    } else {
-        auto lg = [&](int b, long long cc) { return ldA(gg, b * n + cc); };
-#pragma unroll
-        for (int a = 0; a < QT; ++a) e[a] = aa_local_thermal<QT, float>(g, a, i, j, k, c, graw != 0, lg);
-    }
-    float Tprev;
-    if (FIRST) {
-        // the module array holds each value rounded to the storage type
-#pragma unroll
-        for (int a = 0; a < QT; ++a) G[a] = roundS<S>(e[a]) + wT<QT>(P, a) * P.Tref;
-        Tprev = A.T[c];
-    } else {
-        float ts = 0.0f;
-#pragma unroll
-        for (int a = 0; a < QT; ++a) {
-            G[a] = e[a] + wT<QT>(P, a) * P.Tref;
-            ts += G[a];
-        }
-        Tprev = ts;
-    }
-    float dr, rho, u, v, w, Fy;
-    fmacro<D>(d, D == 2 ? A.lag_in[c] : Tprev, P, dr, rho, u, v, w, Fy);
-    if (D == 2) {
-        float Bx = A.Bin0[c], By = A.Bin1[c];
-        fcollideT_2d(G, u, v, Tprev, Bx, By, P, GP);
-        A.Bout0[c] = Bx;
-        A.Bout1[c] = By;
-    } else {
-        float Bx = A.Bin0[c], By = A.Bin1[c], Bz = A.Bin2[c];
-        fcollideT_3d(G, u, v, w, Tprev, Bx, By, Bz, P, GP);
-        A.Bout0[c] = Bx;
-        A.Bout1[c] = By;
-        A.Bout2[c] = Bz;
-        A.lag_out[c] = Tprev;
-    }
-    if (ODD) {
-        auto st = [&](int b, long long cc, float val) { gg[b * n + cc] = toS<S>(val); };
-#pragma unroll
-        for (int a = 0; a < QT; ++a) aa_push<QT, true, float>(g, a, i, j, k, c, GP[a] - wT<QT>(P, a) * P.Tref, st);
-    } else {
-#pragma unroll
-        for (int a = 0; a < QT; ++a) gg[Lat<QT>::opp(a) * n + c] = toS<S>(GP[a] - wT<QT>(P, a) * P.Tref);
-    }
+    aa_thermal_cell<D, S, ODD, FIRST>(g, P, A, fs, gg, wg, fpar, graw, c, i, j, k);
 }
 
 // Module scalars (rho, u, v, w, T) of the current step, populations left in place.
@@ -300,6 +180,266 @@ __global__ void k_aa_materialize_f(Geo g, PhysF P, FastArgs<S> A, const S* __res
 }
 
 // ------------------------------------------------------------------------------------
+// Paired form: cells (i0, j, k) and (i0+1, j, k) per thread (nx even), populations moved as
+// 2-element vectors as in lbm_fast_pairs.cuh; the per-cell arithmetic is flow_pair_2k's and
+// thermal_pair_2k's statement for statement.  Pushes whose target shifts along x, or
+// leaves the lattice, are scalar stores through aa_push.
+// ------------------------------------------------------------------------------------
+// 2-element loads: CO = coherent (an array this kernel writes), otherwise the read-only path
+template <class S, bool CO> __device__ __forceinline__ float2 ld2(const S* p, long long i);
+template <> __device__ __forceinline__ float2 ld2<float, false>(const float* p, long long i) {
+    return __ldg(reinterpret_cast<const float2*>(p + i));
+}
+template <> __device__ __forceinline__ float2 ld2<float, true>(const float* p, long long i) {
+    return __ldg(reinterpret_cast<const float2*>(p + i));  // see ldA
+}
+__device__ __forceinline__ float2 h2f2(unsigned int w) {
+    return __half22float2(__halves2half2(__ushort_as_half((unsigned short)(w & 0xFFFFu)),
+                                         __ushort_as_half((unsigned short)(w >> 16))));
+}
+template <> __device__ __forceinline__ float2 ld2<__half, false>(const __half* p, long long i) {
+    return h2f2(__ldg(reinterpret_cast<const unsigned int*>(p + i)));
+}
+template <> __device__ __forceinline__ float2 ld2<__half, true>(const __half* p, long long i) {
+    return h2f2(__ldg(reinterpret_cast<const unsigned int*>(p + i)));  // see ldA
+}
+
+// Values at x = i0 - ex and i0 + 1 - ex of one row (both inside the lattice in x).
+template <class S, bool CO>
+__device__ __forceinline__ float2 row2(const Geo& g, const S* p, int ex, int i0, long long row) {
+    if (ex == 0) return ld2<S, CO>(p, row + i0);
+    if (ex == 1) {
+        const float2 lo = ld2<S, CO>(p, row + (i0 > 0 ? i0 - 2 : 0));
+        const float2 hi = ld2<S, CO>(p, row + i0);
+        return make_float2(lo.y, hi.x);
+    }
+    const float2 lo = ld2<S, CO>(p, row + i0);
+    const float2 hi = ld2<S, CO>(p, row + (i0 + 2 < g.nx ? i0 + 2 : i0));
+    return make_float2(lo.y, hi.x);
+}
+
+// Pull of direction a into the pair from the swapped layout (dir d of cell s in plane
+// opp(d)); sources outside the lattice take the scalar pull with its boundary rule.
+template <int Q, bool TH, class S, bool CO, class LOAD, class W0, class W1>
+__device__ __forceinline__ float2 swp_pull2(const Geo& g, const S* p, int a, int i0, int j, int k, long long c0,
+                                           long long n, LOAD load, W0 w0, W1 w1) {
+    const int ex = Lat<Q>::ex(a), ey = Lat<Q>::ey(a), ez = Lat<Q>::ez(a);
+    const int sj = j - ey, sk = k - ez;
+    const bool yz = (ey == 0 || (sj >= 0 && sj < g.ny)) && (ez == 0 || (sk >= 0 && sk < g.nz));
+    float2 v = make_float2(0.0f, 0.0f);
+    if (yz)
+        v = row2<S, CO>(g, p, ex, i0, (long long)Lat<Q>::opp(a) * n + (long long)g.nx * ((long long)sj + (long long)g.ny * sk));
+    if (!yz || (ex == 1 && i0 == 0))
+        v.x = TH ? pull_thermal_w<Q, float>(g, a, i0, j, k, c0, load, w0) : pull_flow_w<Q, float>(g, a, i0, j, k, c0, load, w0);
+    if (!yz || (ex == -1 && i0 + 2 >= g.nx))
+        v.y = TH ? pull_thermal_w<Q, float>(g, a, i0 + 1, j, k, c0 + 1, load, w1)
+                 : pull_flow_w<Q, float>(g, a, i0 + 1, j, k, c0 + 1, load, w1);
+    return v;
+}
+
+// Thermal pair from the streamed layout, wall rule applied to pushed slots.
+template <int QT, class S, bool CO>
+__device__ __forceinline__ float2 loc_thermal2(const Geo& g, const S* p, int a, int i0, int j, int k, long long c0,
+                                              long long n, bool raw) {
+    float2 v = ld2<S, CO>(p, (long long)a * n + c0);
+    if (raw && a != 0) {
+        const float x = v.x, y = v.y;
+        v.x = aa_local_thermal<QT, float>(g, a, i0, j, k, c0, true, [&](int, long long) { return x; });
+        v.y = aa_local_thermal<QT, float>(g, a, i0 + 1, j, k, c0 + 1, true, [&](int, long long) { return y; });
+    }
+    return v;
+}
+
+// Push of the pair's post-collision values of direction a (odd sweep).
+template <int Q, bool TH, class S>
+__device__ __forceinline__ void push2(const Geo& g, S* p, int a, int i0, int j, int k, long long c0, long long n, float v0,
+                                      float v1) {
+    const int ex = Lat<Q>::ex(a), ey = Lat<Q>::ey(a), ez = Lat<Q>::ez(a);
+    const int tj = j + ey, tk = k + ez;
+    const bool yz = (ey == 0 || (tj >= 0 && tj < g.ny)) && (ez == 0 || (tk >= 0 && tk < g.nz));
+    if (ex == 0 && yz) {
+        Vec2<S>::st(p, (long long)a * n + c0 + (long long)g.nx * ((long long)ey + (long long)g.ny * ez), v0, v1);
+        return;
+    }
+    auto st = [&](int b, long long cc, float v) { p[(long long)b * n + cc] = toS<S>(v); };
+    aa_push<Q, TH, float>(g, a, i0, j, k, c0, v0, st);
+    aa_push<Q, TH, float>(g, a, i0 + 1, j, k, c0 + 1, v1, st);
+}
+
+__device__ __forceinline__ bool aa_pair_cell(const Geo& g, long long& c0, int& i0, int& j, int& k) {
+    i0 = 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    j = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    k = (int)blockIdx.z;
+    if (i0 >= g.nx || j >= g.ny) return false;
+    c0 = (long long)i0 + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
+    return true;
+}
+
+template <int D, class S, bool ODD>
+__global__ void __launch_bounds__(128) k_aa_flow_p(Geo g, PhysF P, FastArgs<S> A, S* f, const S* __restrict__ gs,
+                                                   AAFace<S> wf, int gpar, int graw) {
+    long long c0;
+    int i0, j, k;
+    if (!aa_pair_cell(g, c0, i0, j, k)) return;
+    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
+    const long long n = g.ncell;
+    float d0[Q], d1[Q];
+    if (ODD) {
+        auto lf = [&](int b, long long cc) { return ldA(f, Lat<Q>::opp(b) * n + cc); };
+        auto w0 = [&](int ax, int b, long long) {
+            return ldA(aa_face_ptr(wf, ax), b * aa_face_cells(g, ax) + aa_face_index(g, ax, i0, j, k));
+        };
+        auto w1 = [&](int ax, int b, long long) {
+            return ldA(aa_face_ptr(wf, ax), b * aa_face_cells(g, ax) + aa_face_index(g, ax, i0 + 1, j, k));
+        };
+#pragma unroll
+        for (int a = 0; a < Q; ++a) {
+            const float2 v = swp_pull2<Q, false, S, true>(g, f, a, i0, j, k, c0, n, lf, w0, w1);
+            d0[a] = v.x;
+            d1[a] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) {
+            const float2 v = ld2<S, true>(f, a * n + c0);
+            d0[a] = v.x;
+            d1[a] = v.y;
+        }
+    }
+    float ts0 = 0.0f, ts1 = 0.0f;
+    if (gpar) {
+        auto lg = [&](int b, long long cc) { return ldS(gs, Lat<QT>::opp(b) * n + cc); };
+        auto wd = [&](int, int b, long long cc) { return lg(b, cc); };
+#pragma unroll
+        for (int a = 0; a < QT; ++a) {
+            const float2 e = swp_pull2<QT, true, S, false>(g, gs, a, i0, j, k, c0, n, lg, wd, wd);
+            ts0 += e.x;
+            ts1 += e.y;
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < QT; ++a) {
+            const float2 e = loc_thermal2<QT, S, false>(g, gs, a, i0, j, k, c0, n, graw != 0);
+            ts0 += e.x;
+            ts1 += e.y;
+        }
+    }
+    const float2 lag = ld2<float, true>(A.lag_in, c0);
+    float dp0[Q], dp1[Q], Fy0, Fy1;
+    {
+        const float T = ts0 + P.Tref;
+        float dr, rho, u, v, w = 0.0f, Fm;
+        fmacro<D>(d0, lag.x, P, dr, rho, u, v, w, Fm);
+        Fy0 = rho * P.gBeta * (T - P.Tref);
+        if (D == 2) fcollide_2d(d0, dr, rho, u, v, Fy0, P, dp0);
+        else fcollide_3d(d0, dr, rho, u, v, w, Fy0, P, dp0);
+    }
+    {
+        const float T = ts1 + P.Tref;
+        float dr, rho, u, v, w = 0.0f, Fm;
+        fmacro<D>(d1, lag.y, P, dr, rho, u, v, w, Fm);
+        Fy1 = rho * P.gBeta * (T - P.Tref);
+        if (D == 2) fcollide_2d(d1, dr, rho, u, v, Fy1, P, dp1);
+        else fcollide_3d(d1, dr, rho, u, v, w, Fy1, P, dp1);
+    }
+    if (D == 2) stf2(A.lag_out, c0, Fy0, Fy1);
+    if (ODD) {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) push2<Q, false, S>(g, f, a, i0, j, k, c0, n, dp0[a], dp1[a]);
+    } else {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) Vec2<S>::st(f, Lat<Q>::opp(a) * n + c0, dp0[a], dp1[a]);
+    }
+}
+
+template <int D, class S, bool ODD>
+__global__ void __launch_bounds__(128) k_aa_thermal_p(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fs, S* gg,
+                                                      AAFace<S> wg, int fpar, int graw) {
+    long long c0;
+    int i0, j, k;
+    if (!aa_pair_cell(g, c0, i0, j, k)) return;
+    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
+    const long long n = g.ncell;
+    float d0[Q], d1[Q], G0[QT], G1[QT];
+    if (fpar) {
+        auto lf = [&](int b, long long cc) { return ldS(fs, Lat<Q>::opp(b) * n + cc); };
+        auto wd = [&](int, int b, long long cc) { return lf(b, cc); };
+#pragma unroll
+        for (int a = 0; a < Q; ++a) {
+            const float2 v = swp_pull2<Q, false, S, false>(g, fs, a, i0, j, k, c0, n, lf, wd, wd);
+            d0[a] = v.x;
+            d1[a] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) {
+            const float2 v = ld2<S, false>(fs, a * n + c0);
+            d0[a] = v.x;
+            d1[a] = v.y;
+        }
+    }
+    float ts0 = 0.0f, ts1 = 0.0f;
+    if (ODD) {
+        auto lg = [&](int b, long long cc) { return ldA(gg, Lat<QT>::opp(b) * n + cc); };
+        auto w0 = [&](int ax, int b, long long) {
+            return ldA(aa_face_ptr(wg, ax), b * aa_face_cells(g, ax) + aa_face_index(g, ax, i0, j, k));
+        };
+        auto w1 = [&](int ax, int b, long long) {
+            return ldA(aa_face_ptr(wg, ax), b * aa_face_cells(g, ax) + aa_face_index(g, ax, i0 + 1, j, k));
+        };
+#pragma unroll
+        for (int a = 0; a < QT; ++a) {
+            const float2 e = swp_pull2<QT, true, S, true>(g, gg, a, i0, j, k, c0, n, lg, w0, w1);
+            G0[a] = e.x + wT<QT>(P, a) * P.Tref;
+            G1[a] = e.y + wT<QT>(P, a) * P.Tref;
+            ts0 += G0[a];
+            ts1 += G1[a];
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < QT; ++a) {
+            const float2 e = loc_thermal2<QT, S, true>(g, gg, a, i0, j, k, c0, n, graw != 0);
+            G0[a] = e.x + wT<QT>(P, a) * P.Tref;
+            G1[a] = e.y + wT<QT>(P, a) * P.Tref;
+            ts0 += G0[a];
+            ts1 += G1[a];
+        }
+    }
+    const float2 bx = ld2<float, true>(A.Bin0, c0), by = ld2<float, true>(A.Bin1, c0);
+    const float2 bz = D == 3 ? ld2<float, true>(A.Bin2, c0) : make_float2(0.0f, 0.0f);
+    const float2 lag = D == 2 ? ld2<float, true>(A.lag_in, c0) : make_float2(0.0f, 0.0f);
+    float GP0[QT], GP1[QT];
+    float Bx0 = bx.x, By0 = by.x, Bz0 = bz.x, Bx1 = bx.y, By1 = by.y, Bz1 = bz.y;
+    {
+        float dr, rho, u, v, w, Fy;
+        fmacro<D>(d0, D == 2 ? lag.x : ts0, P, dr, rho, u, v, w, Fy);
+        if (D == 2) fcollideT_2d(G0, u, v, ts0, Bx0, By0, P, GP0);
+        else fcollideT_3d(G0, u, v, w, ts0, Bx0, By0, Bz0, P, GP0);
+    }
+    {
+        float dr, rho, u, v, w, Fy;
+        fmacro<D>(d1, D == 2 ? lag.y : ts1, P, dr, rho, u, v, w, Fy);
+        if (D == 2) fcollideT_2d(G1, u, v, ts1, Bx1, By1, P, GP1);
+        else fcollideT_3d(G1, u, v, w, ts1, Bx1, By1, Bz1, P, GP1);
+    }
+    stf2(A.Bout0, c0, Bx0, Bx1);
+    stf2(A.Bout1, c0, By0, By1);
+    if (D == 3) {
+        stf2(A.Bout2, c0, Bz0, Bz1);
+        stf2(A.lag_out, c0, ts0, ts1);
+    }
+    if (ODD) {
+#pragma unroll
+        for (int a = 0; a < QT; ++a)
+            push2<QT, true, S>(g, gg, a, i0, j, k, c0, n, GP0[a] - wT<QT>(P, a) * P.Tref, GP1[a] - wT<QT>(P, a) * P.Tref);
+    } else {
+#pragma unroll
+        for (int a = 0; a < QT; ++a)
+            Vec2<S>::st(gg, Lat<QT>::opp(a) * n + c0, GP0[a] - wT<QT>(P, a) * P.Tref, GP1[a] - wT<QT>(P, a) * P.Tref);
+    }
+}
+
+// ------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------
 template <class S>
@@ -322,6 +462,8 @@ static AAFace<S> aa_faces(void* const face[3]) {
 
 static bool any_face(void* const face[3]) { return face[0] || face[1] || face[2]; }
 
+bool fast_aa_tma_sweep(FastState& F, const Geo& g, const PhysF& pf, int dim, const void* A, int part, cudaStream_t s);
+
 template <int D, class S, bool FIRST>
 static void aa_step_launch(FastState& F, const Geo& g, const PhysF& pf, cudaStream_t s, int part) {
     AAState& st = F.AA;
@@ -330,18 +472,40 @@ static void aa_step_launch(FastState& F, const Geo& g, const PhysF& pf, cudaStre
     S* gg = (S*)F.gbuf[0];
     const unsigned nb = (unsigned)((g.ncell + 127) / 128);
     const int raw = st.graw ? 1 : 0;
+    // two cells per thread where the two-buffer form uses them too; the first step (module
+    // arrays) and odd nx take one cell per thread
+    const bool paired = !FIRST && F.pairs && g.nx % 2 == 0;
+    const int pairs = g.nx / 2, bx = pairs > 32 ? 64 : 32, by = 128 / bx;
+    const dim3 pgrid((pairs + bx - 1) / bx, (g.ny + by - 1) / by, g.nz), pblock(bx, by, 1);
     if (part != 1) {
         if (st.fpar && any_face(st.face_f)) aa_snapshot(g, F.q, false, F.precision, f, st.face_f, s);
         const AAFace<S> wf = aa_faces<S>(st.face_f);
-        if (st.fpar) k_aa_flow_f<D, S, true, FIRST><<<nb, 128, 0, s>>>(g, pf, A, f, gg, wf, st.gpar, raw);
-        else k_aa_flow_f<D, S, false, FIRST><<<nb, 128, 0, s>>>(g, pf, A, f, gg, wf, st.gpar, raw);
+        // the even flow sweep touches only the cell's own slots: staging buys nothing there
+        if (!FIRST && F.tma && st.fpar && fast_aa_tma_sweep(F, g, pf, D, &A, 0, s)) {
+            // staged rows (lbm_fast_tma.cu)
+        } else if (paired) {
+            if (st.fpar) k_aa_flow_p<D, S, true><<<pgrid, pblock, 0, s>>>(g, pf, A, f, gg, wf, st.gpar, raw);
+            else k_aa_flow_p<D, S, false><<<pgrid, pblock, 0, s>>>(g, pf, A, f, gg, wf, st.gpar, raw);
+        } else if (st.fpar) {
+            k_aa_flow_f<D, S, true, FIRST><<<nb, 128, 0, s>>>(g, pf, A, f, gg, wf, st.gpar, raw);
+        } else {
+            k_aa_flow_f<D, S, false, FIRST><<<nb, 128, 0, s>>>(g, pf, A, f, gg, wf, st.gpar, raw);
+        }
         st.fpar ^= 1;
     }
     if (part != 0) {
         if (st.gpar && any_face(st.face_g)) aa_snapshot(g, F.qt, true, F.precision, gg, st.face_g, s);
         const AAFace<S> wg = aa_faces<S>(st.face_g);
-        if (st.gpar) k_aa_thermal_f<D, S, true, FIRST><<<nb, 128, 0, s>>>(g, pf, A, f, gg, wg, st.fpar, raw);
-        else k_aa_thermal_f<D, S, false, FIRST><<<nb, 128, 0, s>>>(g, pf, A, f, gg, wg, st.fpar, raw);
+        if (!FIRST && F.tma && fast_aa_tma_sweep(F, g, pf, D, &A, 1, s)) {
+            // staged rows (lbm_fast_tma.cu)
+        } else if (paired) {
+            if (st.gpar) k_aa_thermal_p<D, S, true><<<pgrid, pblock, 0, s>>>(g, pf, A, f, gg, wg, st.fpar, raw);
+            else k_aa_thermal_p<D, S, false><<<pgrid, pblock, 0, s>>>(g, pf, A, f, gg, wg, st.fpar, raw);
+        } else if (st.gpar) {
+            k_aa_thermal_f<D, S, true, FIRST><<<nb, 128, 0, s>>>(g, pf, A, f, gg, wg, st.fpar, raw);
+        } else {
+            k_aa_thermal_f<D, S, false, FIRST><<<nb, 128, 0, s>>>(g, pf, A, f, gg, wg, st.fpar, raw);
+        }
         if (st.gpar) st.graw = true;
         st.gpar ^= 1;
     }

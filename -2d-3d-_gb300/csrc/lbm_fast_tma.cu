@@ -16,6 +16,13 @@
 // arithmetic is the one-cell path's inline functions, so the values are the same bit for
 // bit.
 //
+// The in-place (AA) pattern uses the same kernel with other row sources and stores: an
+// array in the swapped layout is staged from plane opp(a) at the pull's source rows, one in
+// the streamed layout from plane a at the tile's own rows (no shift), and the interior
+// cells store either back into their own opposite slots (even sweep) or at c + e_a (odd
+// sweep: every target of an interior cell lies inside the lattice).  Face cells take the
+// in-place one-cell path (lbm_fast_aa.cuh).
+//
 // Requirements (else the one-cell kernels run): nx a multiple of 8 (16-byte aligned rows
 // for FP16 and FP32), and one row of a tile fitting the stage budget.
 #include <cuda_fp16.h>
@@ -24,6 +31,7 @@
 #include <mutex>
 
 #include "lbm_fast.h"
+#include "lbm_fast_aa.cuh"
 #include "lbm_fast_cells.cuh"
 
 namespace lbm {
@@ -33,7 +41,23 @@ namespace {
 constexpr unsigned kHeader = 128;          // mbarriers at the start of shared memory
 constexpr unsigned kWaitLimit = 1u << 22;  // bounded mbarrier polling
 
+// Where a staged population row comes from, and where a cell's new values go.
+constexpr int kRowPull = 0;   // two buffers: plane a, source rows (j - ey, k - ez), shift ex
+constexpr int kRowSwap = 1;   // in-place swapped layout: plane opp(a), source rows, shift ex
+constexpr int kRowLocal = 2;  // in-place streamed layout: plane a, the tile's own rows, no shift
+constexpr int kStoreOut = 0;  // two buffers: plane a of the output array at the cell
+constexpr int kStorePush = 1; // in-place odd sweep: plane a at c + e_a
+constexpr int kStoreOpp = 2;  // in-place even sweep: plane opp(a) at the cell
+
 }  // namespace
+
+// In-place pattern: what the face cells of a staged sweep need (lbm_fast_aa.cuh).
+template <class S>
+struct AAExtra {
+    AAFace<S> face;  // snapshots of the periodic faces of the swept array
+    int opar;        // layout of the other array
+    int graw;        // the thermal array's streamed slots hold pushed values
+};
 
 // Pipeline shape: threads per block, stages, blocks per SM, stage budget and limit.
 // PipeA: two blocks of 8 warps per SM, 3 x 36 KB each.  A deeper shape (one 16-warp block
@@ -192,7 +216,7 @@ __device__ __forceinline__ void face_cell(const Geo& g, long long f, int& i, int
 // warp, lane l issuing copy l (the Q + QT population rows, then the float rows).  Lane 0
 // announces the byte count of the whole tile on the mbarrier before any copy is issued;
 // the phase completes when every byte has landed.
-template <int D, class S>
+template <int D, class S, int LF, int LG>
 __device__ __forceinline__ void issue_tile(const Geo& g, long long t, int R, int ntj, unsigned char* st, uint64_t* bar,
                                            const S* __restrict__ fsrc, const S* __restrict__ gsrc, const float* fl0,
                                            const float* fl1, const float* fl2, int nfloat) {
@@ -214,9 +238,12 @@ __device__ __forceinline__ void issue_tile(const Geo& g, long long t, int R, int
     if (lane < Q + QT) {
         const bool th = lane >= Q;
         const int b = th ? lane - Q : lane;
-        const int ey = th ? Lat<QT>::ey(b) : Lat<Q>::ey(b), ez = th ? Lat<QT>::ez(b) : Lat<Q>::ez(b);
+        const int mode = th ? LG : LF;
+        const int ey = mode == kRowLocal ? 0 : (th ? Lat<QT>::ey(b) : Lat<Q>::ey(b));
+        const int ez = mode == kRowLocal ? 0 : (th ? Lat<QT>::ez(b) : Lat<Q>::ez(b));
+        const int plane = mode == kRowSwap ? (th ? Lat<QT>::opp(b) : Lat<Q>::opp(b)) : b;
         const long long row0 = (long long)nx * ((long long)(j0 - ey) + (long long)ny * (long long)(k - ez));
-        src = (th ? gsrc : fsrc) + (long long)b * n + row0;
+        src = (th ? gsrc : fsrc) + (long long)plane * n + row0;
         dst = (th ? sg : sf) + (size_t)b * rc;
         bytes = (unsigned)((size_t)rows * nx * sizeof(S));
     } else if (lane < Q + QT + nfloat) {
@@ -234,11 +261,24 @@ __device__ __forceinline__ void issue_tile(const Geo& g, long long t, int R, int
     if (bytes) bulk_load(dst, src, bytes, bar);
 }
 
+// Slot of direction a's new value for interior cell c.
+template <int Q, int ST>
+__device__ __forceinline__ long long store_index(const Geo& g, int a, long long c, long long n) {
+    if (ST == kStoreOpp) return (long long)Lat<Q>::opp(a) * n + c;
+    if (ST == kStorePush)
+        return (long long)a * n + c + (long long)Lat<Q>::ex(a) +
+               (long long)g.nx * ((long long)Lat<Q>::ey(a) + (long long)g.ny * (long long)Lat<Q>::ez(a));
+    return (long long)a * n + c;
+}
+
 // KIND 0: flow collision (flow_cell_2k, not FIRST); KIND 1: thermal (thermal_cell_2k).
-template <int D, class S, int KIND, class PP>
+// LF / LG: row modes of f and g; ST: store mode (kRow* / kStore* above).  In the in-place
+// pattern `out` is the swept array itself (fin for the flow, gin for the thermal kernel):
+// no value a cell loads is stored in the same sweep by another cell (lbm_fast_aa.cuh).
+template <int D, class S, int KIND, class PP, int LF = kRowPull, int LG = kRowPull, int ST = kStoreOut>
 __global__ void __launch_bounds__(PP::threads, PP::blocks)
     k_fast_tma(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin, const S* __restrict__ gin,
-               S* __restrict__ out, int R, int ntj, long long ntiles, unsigned stage_bytes, int* err) {
+               S* __restrict__ out, int R, int ntj, long long ntiles, unsigned stage_bytes, int* err, AAExtra<S> X) {
     constexpr int kThreads = PP::threads, kStages = PP::stages, kWarps = PP::warps;
     constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
     constexpr int NF = KIND == 0 ? 1 : 3;
@@ -264,7 +304,8 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
     if (threadIdx.x < 32) {
         for (int s = 0; s < kStages - 1; ++s) {
             const long long t = blockIdx.x + (long long)s * gridDim.x;
-            if (t < ntiles) issue_tile<D, S>(g, t, R, ntj, buf + (size_t)s * stage_bytes, &bars[s], fin, gin, fl0, fl1, fl2, NF);
+            if (t < ntiles)
+                issue_tile<D, S, LF, LG>(g, t, R, ntj, buf + (size_t)s * stage_bytes, &bars[s], fin, gin, fl0, fl1, fl2, NF);
         }
     }
     long long it = 0;
@@ -277,7 +318,8 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
             if (tn < ntiles) {
                 if (it >= 1 && !mbar_wait(&empty[sn], (unsigned)(((it - 1) / kStages) & 1), err)) return;
                 fence_async_shared();
-                issue_tile<D, S>(g, tn, R, ntj, buf + (size_t)sn * stage_bytes, &bars[sn], fin, gin, fl0, fl1, fl2, NF);
+                issue_tile<D, S, LF, LG>(g, tn, R, ntj, buf + (size_t)sn * stage_bytes, &bars[sn], fin, gin, fl0, fl1, fl2,
+                                         NF);
             }
         }
         if (!mbar_wait(&bars[s], (unsigned)((it / kStages) & 1), err)) return;
@@ -293,11 +335,11 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
             const long long c = (long long)i + (long long)nx * ((long long)j + (long long)ny * k);
             float d[Q];
 #pragma unroll
-            for (int a = 0; a < Q; ++a) d[a] = s2f(sf[a * rc + (size_t)r * nx + (i - Lat<Q>::ex(a))]);
+            for (int a = 0; a < Q; ++a) d[a] = s2f(sf[a * rc + (size_t)r * nx + (i - (LF == kRowLocal ? 0 : Lat<Q>::ex(a)))]);
             if (KIND == 0) {
                 float ts = 0.0f;
 #pragma unroll
-                for (int a = 0; a < QT; ++a) ts += s2f(sg[a * rc + (size_t)r * nx + (i - Lat<QT>::ex(a))]);
+                for (int a = 0; a < QT; ++a) ts += s2f(sg[a * rc + (size_t)r * nx + (i - (LG == kRowLocal ? 0 : Lat<QT>::ex(a)))]);
                 const float T = ts + P.Tref;
                 float dr, rho, u, v, w = 0.0f, Fm;
                 fmacro<D>(d, sfl[(size_t)r * nx + i], P, dr, rho, u, v, w, Fm);
@@ -310,12 +352,12 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
                     fcollide_3d(d, dr, rho, u, v, w, Fy, P, dp);
                 }
 #pragma unroll
-                for (int a = 0; a < Q; ++a) out[a * n + c] = toS<S>(dp[a]);
+                for (int a = 0; a < Q; ++a) out[store_index<Q, ST>(g, a, c, n)] = toS<S>(dp[a]);
             } else {
                 float G[QT], GP[QT], ts = 0.0f;
 #pragma unroll
                 for (int a = 0; a < QT; ++a) {
-                    G[a] = s2f(sg[a * rc + (size_t)r * nx + (i - Lat<QT>::ex(a))]) + wT<QT>(P, a) * P.Tref;
+                    G[a] = s2f(sg[a * rc + (size_t)r * nx + (i - (LG == kRowLocal ? 0 : Lat<QT>::ex(a)))]) + wT<QT>(P, a) * P.Tref;
                     ts += G[a];
                 }
                 const size_t e = (size_t)r * nx + i;
@@ -335,7 +377,7 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
                     A.lag_out[c] = ts;
                 }
 #pragma unroll
-                for (int a = 0; a < QT; ++a) out[a * n + c] = toS<S>(GP[a] - wT<QT>(P, a) * P.Tref);
+                for (int a = 0; a < QT; ++a) out[store_index<QT, ST>(g, a, c, n)] = toS<S>(GP[a] - wT<QT>(P, a) * P.Tref);
             }
         }
         __syncwarp();
@@ -347,14 +389,20 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
         int i, j, k;
         face_cell<D>(g, f, i, j, k);
         const long long c = (long long)i + (long long)nx * ((long long)j + (long long)ny * k);
-        if (KIND == 0) flow_cell_2k<D, false, S>(g, P, A, fin, gin, out, c, i, j, k);
-        else thermal_cell_2k<D, false, S>(g, P, A, fin, gin, out, c, i, j, k);
+        if (ST == kStoreOut) {
+            if (KIND == 0) flow_cell_2k<D, false, S>(g, P, A, fin, gin, out, c, i, j, k);
+            else thermal_cell_2k<D, false, S>(g, P, A, fin, gin, out, c, i, j, k);
+        } else if (KIND == 0) {
+            aa_flow_cell<D, S, ST == kStorePush, false>(g, P, A, out, gin, X.face, X.opar, X.graw, c, i, j, k);
+        } else {
+            aa_thermal_cell<D, S, ST == kStorePush, false>(g, P, A, fin, out, X.face, X.opar, X.graw, c, i, j, k);
+        }
     }
 }
 
-template <int D, class S, int KIND, class PP>
+template <int D, class S, int KIND, class PP, int LF = kRowPull, int LG = kRowPull, int ST = kStoreOut>
 static bool launch_tma(const Geo& g, const PhysF& pf, const FastArgs<S>& A, const S* fin, const S* gin, S* out,
-                       int* err, cudaStream_t s) {
+                       int* err, cudaStream_t s, AAExtra<S> X = AAExtra<S>{}) {
     const TmaPlan p = tma_plan<D, S, PP>(g, KIND == 0 ? 1 : 3);
     if (!p.ok) return false;
     static bool configured = false;
@@ -362,14 +410,14 @@ static bool launch_tma(const Geo& g, const PhysF& pf, const FastArgs<S>& A, cons
     {
         std::lock_guard<std::mutex> lock(mu);
         if (!configured) {
-            if (cudaFuncSetAttribute(k_fast_tma<D, S, KIND, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            if (cudaFuncSetAttribute(k_fast_tma<D, S, KIND, PP, LF, LG, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)(kHeader + PP::stages * PP::max_stage)) != cudaSuccess)
                 return false;
             configured = true;
         }
     }
-    k_fast_tma<D, S, KIND, PP><<<p.grid, PP::threads, p.smem, s>>>(g, pf, A, fin, gin, out, p.R, p.ntj, p.ntiles,
-                                                                   p.stage, err);
+    k_fast_tma<D, S, KIND, PP, LF, LG, ST><<<p.grid, PP::threads, p.smem, s>>>(g, pf, A, fin, gin, out, p.R, p.ntj,
+                                                                                p.ntiles, p.stage, err, X);
     return true;
 }
 
@@ -402,6 +450,35 @@ bool fast_step_tma(FastState& F, const Geo& g, const PhysF& pf, int dim, const v
                                          (const __half*)fin, (const __half*)gin, (__half*)fout, (__half*)gout, s, part);
     return step_tma_s<float, PipeA>(F, g, pf, dim, *(const FastArgs<float>*)Af, *(const FastArgs<float>*)At,
                                     (const float*)fin, (const float*)gin, (float*)fout, (float*)gout, s, part);
+}
+
+// In-place pattern, one sweep of the flow (part 0) or thermal (part 1) array with staged
+// rows, when both arrays have the layouts of an ordinary step (flow sweep: g in the same
+// layout as f; thermal sweep: f one layout ahead of g).  Returns false (nothing launched)
+// otherwise or when the geometry does not qualify.
+template <int D, class S>
+static bool aa_tma_s(FastState& F, const Geo& g, const PhysF& pf, const FastArgs<S>& A, int part, cudaStream_t s) {
+    const AAState& st = F.AA;
+    S* f = (S*)F.fbuf[0];
+    S* gg = (S*)F.gbuf[0];
+    if (part == 0) {
+        if (st.gpar != st.fpar) return false;
+        const AAExtra<S> X{AAFace<S>{(const S*)st.face_f[0], (const S*)st.face_f[1], (const S*)st.face_f[2]}, st.gpar,
+                           st.graw ? 1 : 0};
+        if (st.fpar) return launch_tma<D, S, 0, PipeA, kRowSwap, kRowSwap, kStorePush>(g, pf, A, f, gg, f, F.err, s, X);
+        return launch_tma<D, S, 0, PipeA, kRowLocal, kRowLocal, kStoreOpp>(g, pf, A, f, gg, f, F.err, s, X);
+    }
+    if (st.fpar == st.gpar) return false;
+    const AAExtra<S> X{AAFace<S>{(const S*)st.face_g[0], (const S*)st.face_g[1], (const S*)st.face_g[2]}, st.fpar,
+                       st.graw ? 1 : 0};
+    if (st.gpar) return launch_tma<D, S, 1, PipeA, kRowLocal, kRowSwap, kStorePush>(g, pf, A, f, gg, gg, F.err, s, X);
+    return launch_tma<D, S, 1, PipeA, kRowSwap, kRowLocal, kStoreOpp>(g, pf, A, f, gg, gg, F.err, s, X);
+}
+
+bool fast_aa_tma_sweep(FastState& F, const Geo& g, const PhysF& pf, int dim, const void* A, int part, cudaStream_t s) {
+    if (dim != 3) return false;
+    if (F.precision == LBM_FP16) return aa_tma_s<3, __half>(F, g, pf, *(const FastArgs<__half>*)A, part, s);
+    return aa_tma_s<3, float>(F, g, pf, *(const FastArgs<float>*)A, part, s);
 }
 
 }  // namespace lbm

@@ -423,6 +423,53 @@ def served_run(args, local, plain3d_mlups):
     return summary
 
 
+def at_size_run(args, local, n=384, steps=40):
+    """The 384^3 configuration (Ra 1e9, U 0.07): FP16 / FP32 / FP64 storage in the in-place
+    (AA) pattern beside the two-buffer pattern -- throughput, device footprint, per-sweep
+    kernel times, and the AA state after the same steps against FP64 AA (a short run: the
+    time-averaged Nu of 200,000 steps is not a bench leg)."""
+    import numpy as np
+    import torch
+    import lbmgpu
+    from lbmgpu.abi import rb_params
+    out = {"workload": "3D Rayleigh-Benard cube D3Q19/D3Q7 MRT, %d^3 cells, Ra=1e9, Pr=0.71, U=0.07, no-slip walls, "
+                       "adiabatic sides, T linear + 1e-3 seeded noise" % n, "cells": n ** 3,
+           "steps_each": steps + 6}
+    T = {}
+    for prec in ("fp16", "fp32", "fp64"):
+        out[prec] = {}
+        for pat in ("AB", "AA"):
+            p = rb_params(dim=3, n=n, Ra=1e9, Pr=0.71, U=0.07, noise_amp=1e-3, seed=20261203, precision=prec,
+                          pattern=pat)
+            lat = lbmgpu.Lattice(p, device=local)
+            lat.initial()
+            lat.step(4)
+            lat.sync()
+            stream = torch.cuda.ExternalStream(lat.stream_handle(), device=torch.device("cuda", local))
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            t0.record(stream)
+            lat.step(steps)
+            t1.record(stream)
+            t1.synchronize()
+            ms = t0.elapsed_time(t1)
+            tf, tt = lat.time_kernels(2)  # one even and one odd step
+            nu, re = lat.calNuRe()
+            out[prec][pat] = {"mlups": n ** 3 * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps,
+                              "ms_flow_thermal_mean_of_2": [tf, tt], "footprint_GB": lbmgpu.footprint(p) / 1e9,
+                              "Nu": nu, "Re": re}
+            if pat == "AA":
+                T[prec] = (lat.get_state("T"), nu, re)
+            lat.close()
+    t64, nu64, re64 = T["fp64"]
+    dev = np.linalg.norm(t64 - np.mean(t64))
+    for prec in ("fp16", "fp32"):
+        t, nu, re = T[prec]
+        out[prec]["vs_fp64_AA"] = {"T_L2_rel": float(np.linalg.norm(t - t64) / dev),
+                                   "dNu_rel": abs(nu - nu64) / abs(nu64), "dRe_rel": abs(re - re64) / abs(re64)}
+    return out
+
+
 def run_gpu(args):
     rank, world, local, pg = dist_setup(args)
     import torch
@@ -488,6 +535,8 @@ def run_gpu(args):
         line["batched"] = ensemble_run(args, local)
     if rank == 0 and not args.no_served:
         line["served"] = served_run(args, local, results["fp64"]["mlups"] if "fp64" in results else 700.0)
+    if rank == 0 and not args.no_size:
+        line["at_384"] = at_size_run(args, local)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n=args.size)
     if rank == 0:
@@ -505,6 +554,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-form leg (64 2D instances)")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream leg")
+    ap.add_argument("--no-size", action="store_true", help="skip the 384^3 leg (in-place vs two-buffer pattern)")
     ap.add_argument("--served-full", action="store_true", help="served leg as configured: 600 s, 5000-step window")
     ap.add_argument("--served-seconds", type=float, default=20.0)
     ap.add_argument("--served-drain", type=float, default=40.0)

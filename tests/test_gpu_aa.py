@@ -187,3 +187,75 @@ def test_in_place_refusals():
     ens = Ensemble()
     with pytest.raises(LbmError):
         ens.add(fast)
+
+
+@pytest.mark.parametrize("pairs", [0, 1])
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+@pytest.mark.parametrize("name", ["3d_periodic_xz", "3d_side_heated", "2d_walls", "2d_periodic_x"])
+def test_in_place_forms(name, precision, pairs):
+    """One cell per thread and two cells per thread in the in-place pattern, against the
+    two-buffer default form."""
+    from lbmgpu import LBM_OPT_PAIRS
+    p = cases()[name].copy()
+    p.precision = {"fp32": 1, "fp16": 2}[precision]
+    aa, ab = pair(p)
+    aa.set_option(LBM_OPT_PAIRS, pairs)
+    for lat in (aa, ab):
+        lat.initial()
+        lat.step(69)
+    assert_same(aa, ab, p, "%s %s pairs=%d" % (name, precision, pairs))
+
+
+def staged_cases():
+    """Lattices with nx a multiple of 8 (the staged kernels' rows are 16-byte aligned)."""
+    out = {
+        "noslip": rb_params(dim=3, nx=16, ny=14, nz=12, Ra=1e6, noise_amp=1e-3, seed=41),
+        "periodic_xz": rb_params(dim=3, nx=16, ny=10, nz=8, Ra=1e6, noise_amp=1e-3, seed=42, periodic_x=True),
+        "legacy_periodic_z": rb_params(dim=3, nx=24, ny=10, nz=8, Ra=1e5, U=0.02, noise_amp=1e-3, seed=43,
+                                       legacy_thermal=True),
+    }
+    for name in ("periodic_xz", "legacy_periodic_z"):
+        out[name].bc_flow[2] = LBM_BC_PERIODIC
+        out[name].bc_thermal[2] = LBM_BCT_PERIODIC
+    side = rb_params(dim=3, nx=16, ny=10, nz=6, Ra=1e5, noise_amp=1e-3, seed=44)
+    side.cell = LBM_CELL_SIDE
+    side.bc_thermal[0] = LBM_BCT_CONST
+    side.bc_thermal[1] = LBM_BCT_ADIABATIC
+    out["side_heated"] = side
+    return out
+
+
+@pytest.mark.parametrize("staged", [0, 1])
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+@pytest.mark.parametrize("name", sorted(staged_cases()))
+def test_in_place_staged(name, precision, staged):
+    """Staged rows (bulk copies into shared memory) in the in-place pattern: interior tiles
+    staged from the swapped or the streamed layout, face cells on the one-cell path."""
+    from lbmgpu import LBM_OPT_STAGED
+    p = staged_cases()[name].copy()
+    p.precision = {"fp32": 1, "fp16": 2}[precision]
+    aa, ab = pair(p)
+    aa.set_option(LBM_OPT_STAGED, staged)
+    for lat in (aa, ab):
+        lat.initial()
+    for n in (2, 35, 32, 1):
+        for lat in (aa, ab):
+            lat.step(n)
+        assert_same(aa, ab, p, "%s %s staged=%d" % (name, precision, staged))
+    aa.sync()
+
+
+def test_in_place_staged_mixed_layouts():
+    """After populations are loaded into one array only, the arrays' layouts are out of step
+    and the staged sweeps give way to the one-cell kernels; results stay equal."""
+    p = staged_cases()["periodic_xz"].copy()
+    p.precision = 2
+    aa, ab = pair(p)
+    for lat in (aa, ab):
+        lat.initial()
+        lat.step(3)
+    g = ab.get_state("g")
+    for lat in (aa, ab):
+        lat.set_state("g", g)
+        lat.step(37)
+    assert_same(aa, ab, p, "mixed layouts")
