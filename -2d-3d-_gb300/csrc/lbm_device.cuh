@@ -177,6 +177,16 @@ __host__ __device__ inline long long aa_face_cells(const Geo& g, int axis) {
     return axis == 0 ? (long long)g.ny * g.nz : (axis == 1 ? (long long)g.nx * g.nz : (long long)g.nx * g.ny);
 }
 
+// A cell that touches no face of the lattice: every pull source and push target of it is
+// the neighbour at offset -e_a / +e_a, with no boundary rule.
+__device__ __forceinline__ bool aa_inner(const Geo& g, int i, int j, int k) {
+    return i > 0 && i < g.nx - 1 && j > 0 && j < g.ny - 1 && (g.nz == 1 || (k > 0 && k < g.nz - 1));
+}
+template <int Q>
+__device__ __forceinline__ long long lat_off(const Geo& g, int a) {
+    return (long long)Lat<Q>::ex(a) + (long long)g.nx * ((long long)Lat<Q>::ey(a) + (long long)g.ny * (long long)Lat<Q>::ez(a));
+}
+
 // Face snapshots of one array (one pointer per axis, null where the axis is not periodic).
 template <class S>
 struct AAFace {

@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256) k_ens_flow(const EnsMember<S>* __restrict
         for (long long c = c0 + threadIdx.x; c < ce; c += blockDim.x) {
             int i, j, k;
             cell_coords(g, c, i, j, k);
-            flow_cell_2k<D, false, S>(g, P, A, m.f[cur], m.gp[cur], m.f[nxt], c, i, j, k);
+            flow_cell_2k<D, false, S, false>(g, P, A, m.f[cur], m.gp[cur], m.f[nxt], c, i, j, k);
         }
     }
 }
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(256) k_ens_thermal(const EnsMember<S>* __restr
         for (long long c = c0 + threadIdx.x; c < ce; c += blockDim.x) {
             int i, j, k;
             cell_coords(g, c, i, j, k);
-            thermal_cell_2k<D, false, S>(g, P, A, m.f[nxt], m.gp[cur], m.gp[nxt], c, i, j, k);
+            thermal_cell_2k<D, false, S, false>(g, P, A, m.f[nxt], m.gp[cur], m.gp[nxt], c, i, j, k);
         }
     }
 }

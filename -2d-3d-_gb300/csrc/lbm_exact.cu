@@ -719,12 +719,13 @@ __global__ void k_materialize(Geo g, PhysC P, ExactArrays A, const double* __res
 // read-only path although the sweep writes it: every slot is read only by the cell that
 // owns it and written only by that cell after all of its reads (lbm_fast_aa.cu, ldA).
 // ------------------------------------------------------------------------------------
-// Six blocks per SM as the two-buffer flow kernel gets with its 80 registers (the FP64
-// pipe needs the warps); the in-place flow kernels fit that without spilling.
-template <int D, bool ODD>
-__global__ void __launch_bounds__(128, 6) k_aa_flow(Geo g, PhysC P, ExactArrays A, double* f,
+// FIRST is a template parameter as in k_flow: with rho and u known to come from the macro
+// step, the compiler reuses its sums in the collision's moment transform (a run-time
+// choice repeats 45 additions on the FP64 pipe, 8% of the step on GB300).
+template <int D, bool ODD, bool FIRST>
+__global__ void __launch_bounds__(128) k_aa_flow(Geo g, PhysC P, ExactArrays A, double* f,
                                                  const double* __restrict__ gs, AAFace<double> wf, int gpar,
-                                                 int graw, int first) {
+                                                 int graw) {
     long long c;
     int i, j, k;
     if (!thread_cell(g, c, i, j, k)) return;
@@ -742,7 +743,7 @@ __global__ void __launch_bounds__(128, 6) k_aa_flow(Geo g, PhysC P, ExactArrays 
 #pragma unroll
         for (int a = 0; a < Q; ++a) F[a] = __ldg(f + a * n + c);
     }
-    if (first) {
+    if (FIRST) {
         rho = A.rho[c];
         u = A.u[c];
         v = A.v[c];
@@ -781,9 +782,9 @@ __global__ void __launch_bounds__(128, 6) k_aa_flow(Geo g, PhysC P, ExactArrays 
     }
 }
 
-template <int D, bool ODD>
+template <int D, bool ODD, bool FIRST>
 __global__ void __launch_bounds__(128) k_aa_thermal(Geo g, PhysC P, ExactArrays A, const double* __restrict__ fs,
-                                                    double* gg, AAFace<double> wg, int fpar, int graw, int first) {
+                                                    double* gg, AAFace<double> wg, int fpar, int graw) {
     long long c;
     int i, j, k;
     if (!thread_cell(g, c, i, j, k)) return;
@@ -810,7 +811,7 @@ __global__ void __launch_bounds__(128) k_aa_thermal(Geo g, PhysC P, ExactArrays 
 #pragma unroll
         for (int a = 0; a < QT; ++a) G[a] = aa_local_thermal<QT, double>(g, a, i, j, k, c, graw != 0, lg);
     }
-    const double Tprev = first ? A.T[c] : sumT<QT>(G);
+    const double Tprev = FIRST ? A.T[c] : sumT<QT>(G);
     if (D == 2) {
         double rho, u, v, Bx, By;
         macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
@@ -1033,34 +1034,35 @@ static AAFace<double> aa_faces(void* const face[3]) {
 
 static bool any_face(void* const face[3]) { return face[0] || face[1] || face[2]; }
 
-void exact_aa_step(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, bool first, AAState& S,
-                   cudaStream_t s, int part) {
+template <int D, bool FIRST>
+static void aa_step_d(const Geo& g, const PhysC& P, const ExactArrays& A, AAState& S, cudaStream_t s, int part) {
     const unsigned nb = nblocks(g.ncell, 128);
-    const int fi = first ? 1 : 0, raw = S.graw ? 1 : 0;
+    const int raw = S.graw ? 1 : 0;
     if (part != 1) {
-        if (S.fpar && any_face(S.face_f)) aa_snapshot(g, dim == 3 ? 19 : 9, false, LBM_FP64, A.f, S.face_f, s);
+        if (S.fpar && any_face(S.face_f)) aa_snapshot(g, D == 3 ? 19 : 9, false, LBM_FP64, A.f, S.face_f, s);
         const AAFace<double> wf = aa_faces(S.face_f);
-        if (dim == 2) {
-            if (S.fpar) k_aa_flow<2, true><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw, fi);
-            else k_aa_flow<2, false><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw, fi);
-        } else {
-            if (S.fpar) k_aa_flow<3, true><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw, fi);
-            else k_aa_flow<3, false><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw, fi);
-        }
+        if (S.fpar) k_aa_flow<D, true, FIRST><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw);
+        else k_aa_flow<D, false, FIRST><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw);
         S.fpar ^= 1;
     }
     if (part != 0) {
-        if (S.gpar && any_face(S.face_g)) aa_snapshot(g, dim == 3 ? 7 : 5, true, LBM_FP64, A.g, S.face_g, s);
+        if (S.gpar && any_face(S.face_g)) aa_snapshot(g, D == 3 ? 7 : 5, true, LBM_FP64, A.g, S.face_g, s);
         const AAFace<double> wg = aa_faces(S.face_g);
-        if (dim == 2) {
-            if (S.gpar) k_aa_thermal<2, true><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw, fi);
-            else k_aa_thermal<2, false><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw, fi);
-        } else {
-            if (S.gpar) k_aa_thermal<3, true><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw, fi);
-            else k_aa_thermal<3, false><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw, fi);
-        }
+        if (S.gpar) k_aa_thermal<D, true, FIRST><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw);
+        else k_aa_thermal<D, false, FIRST><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw);
         if (S.gpar) S.graw = true;
         S.gpar ^= 1;
+    }
+}
+
+void exact_aa_step(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, bool first, AAState& S,
+                   cudaStream_t s, int part) {
+    if (dim == 2) {
+        if (first) aa_step_d<2, true>(g, P, A, S, s, part);
+        else aa_step_d<2, false>(g, P, A, S, s, part);
+    } else {
+        if (first) aa_step_d<3, true>(g, P, A, S, s, part);
+        else aa_step_d<3, false>(g, P, A, S, s, part);
     }
 }
 

@@ -195,11 +195,13 @@ static inline unsigned nb(long long n, int bs) { return (unsigned)((n + bs - 1) 
 
 int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn& alloc) {
     F.precision = p.precision;
-    // Measured on GB300 (3D cubes 128^3 and 256^3, 2D 1024 x 512): 3D FP16 is fastest with
-    // staged rows (scalar 2-byte loads leave the one-cell kernel waiting on memory), 3D FP32
-    // with one cell per thread, 2D (lattices that live in L2) with two cells per thread.
-    F.tma = p.dim == 3 && p.precision == LBM_FP16;
-    F.pairs = p.dim == 2 || p.precision == LBM_FP16;
+    // Measured on GB300 (3D cubes 128^3 and 384^3; 2D 256 x 128 to 4096 x 2048): with the
+    // boundary tests confined to the face cells, one cell per thread is the fastest form
+    // for 3D in both storage types (FP16 17.3 G cell updates/s at 384^3 against 13.0 G for
+    // the staged rows) and for 2D FP16; 2D FP32 is fastest with two cells per thread.  The
+    // staged and paired forms stay selectable (LBM_OPT_STAGED, LBM_OPT_PAIRS).
+    F.tma = false;
+    F.pairs = p.dim == 2 && p.precision == LBM_FP32;
     F.dim = p.dim;
     F.q = p.dim == 3 ? 19 : 9;
     F.qt = p.dim == 3 ? 7 : 5;
@@ -223,6 +225,9 @@ int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn
         // written by the same thread, so one buffer serves both parities
         F.fref = F.fbuf[0];
         F.gref = F.gbuf[0];
+        // in-place defaults (lbm_fast_aa.cu): one cell per thread except the even flow sweep
+        F.pairs = false;
+        F.tma = false;
         for (int c = 0; c < 3; ++c) F.B[1][c] = F.B[0][c];
         F.L[1] = F.L[0];
         for (int ax = 0; ax < 3; ++ax) {

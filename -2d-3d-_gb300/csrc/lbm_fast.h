@@ -42,8 +42,8 @@ struct FastState {
     bool single_kernel = false; // one-launch fused step (lbm_fused.cu); off: the two-kernel step is faster today
     int kchunk = 16;            // z planes per block of the fused kernel (3D)
     // Form of the non-first two-kernel step, chosen by fast_allocate from GB300 timings:
-    // staged rows (lbm_fast_tma.cu) for 3D FP16; two cells per thread in 2D and as the 3D
-    // FP16 fallback; one cell per thread for 3D FP32.
+    // one cell per thread, except two cells per thread for 2D FP32; staged rows
+    // (lbm_fast_tma.cu) on request.
     bool pairs = false;
     bool tma = false;
     int* err = nullptr;         // device flag: a bounded wait of a staged kernel gave up

@@ -261,6 +261,11 @@ __device__ __forceinline__ void push2(const Geo& g, S* p, int a, int i0, int j, 
         Vec2<S>::st(p, (long long)a * n + c0 + (long long)g.nx * ((long long)ey + (long long)g.ny * ez), v0, v1);
         return;
     }
+    if (yz && i0 + ex >= 0 && i0 + 1 + ex < g.nx) {  // both targets inside: plain stores
+        p[(long long)a * n + c0 + lat_off<Q>(g, a)] = toS<S>(v0);
+        p[(long long)a * n + c0 + 1 + lat_off<Q>(g, a)] = toS<S>(v1);
+        return;
+    }
     auto st = [&](int b, long long cc, float v) { p[(long long)b * n + cc] = toS<S>(v); };
     aa_push<Q, TH, float>(g, a, i0, j, k, c0, v0, st);
     aa_push<Q, TH, float>(g, a, i0 + 1, j, k, c0 + 1, v1, st);
@@ -472,9 +477,13 @@ static void aa_step_launch(FastState& F, const Geo& g, const PhysF& pf, cudaStre
     S* gg = (S*)F.gbuf[0];
     const unsigned nb = (unsigned)((g.ncell + 127) / 128);
     const int raw = st.graw ? 1 : 0;
-    // two cells per thread where the two-buffer form uses them too; the first step (module
-    // arrays) and odd nx take one cell per thread
+    // Forms measured on GB300 (3D, 128^3 to 384^3): the even flow sweep, whose loads and
+    // stores are all the cell's own slots, is fastest with two cells per thread; every other
+    // sweep with one cell per thread (LBM_OPT_PAIRS / LBM_OPT_STAGED select the paired or
+    // staged form for them).  The first step (module arrays) and odd nx take one cell per
+    // thread.
     const bool paired = !FIRST && F.pairs && g.nx % 2 == 0;
+    const bool paired_even_flow = !FIRST && g.nx % 2 == 0 && st.fpar == 0;
     const int pairs = g.nx / 2, bx = pairs > 32 ? 64 : 32, by = 128 / bx;
     const dim3 pgrid((pairs + bx - 1) / bx, (g.ny + by - 1) / by, g.nz), pblock(bx, by, 1);
     if (part != 1) {
@@ -483,7 +492,7 @@ static void aa_step_launch(FastState& F, const Geo& g, const PhysF& pf, cudaStre
         // the even flow sweep touches only the cell's own slots: staging buys nothing there
         if (!FIRST && F.tma && st.fpar && fast_aa_tma_sweep(F, g, pf, D, &A, 0, s)) {
             // staged rows (lbm_fast_tma.cu)
-        } else if (paired) {
+        } else if (paired || paired_even_flow) {
             if (st.fpar) k_aa_flow_p<D, S, true><<<pgrid, pblock, 0, s>>>(g, pf, A, f, gg, wf, st.gpar, raw);
             else k_aa_flow_p<D, S, false><<<pgrid, pblock, 0, s>>>(g, pf, A, f, gg, wf, st.gpar, raw);
         } else if (st.fpar) {

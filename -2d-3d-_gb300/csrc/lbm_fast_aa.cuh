@@ -30,7 +30,11 @@ __device__ __forceinline__ void aa_flow_cell(const Geo& g, const PhysF& P, const
     constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
     const long long n = g.ncell;
     float d[Q], dp[Q], dr, rho, u, v, w = 0.0f, T;
-    if (ODD) {
+    const bool inner = aa_inner(g, i, j, k);  // no boundary rule on any pull or push
+    if (ODD && inner) {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) d[a] = ldA(f, Lat<Q>::opp(a) * n + c - lat_off<Q>(g, a));
+    } else if (ODD) {
         auto lf = [&](int b, long long cc) { return ldA(f, Lat<Q>::opp(b) * n + cc); };
         auto wr = [&](int ax, int b, long long) {
             return ldA(aa_face_ptr(wf, ax), b * aa_face_cells(g, ax) + aa_face_index(g, ax, i, j, k));
@@ -50,10 +54,16 @@ __device__ __forceinline__ void aa_flow_cell(const Geo& g, const PhysF& P, const
         T = A.T[c];
     } else {
         float ts = 0.0f;
-        if (gpar) {
+        if (gpar && inner) {
+#pragma unroll
+            for (int a = 0; a < QT; ++a) ts += ldS(gs, Lat<QT>::opp(a) * n + c - lat_off<QT>(g, a));
+        } else if (gpar) {
             auto lg = [&](int b, long long cc) { return ldS(gs, Lat<QT>::opp(b) * n + cc); };
 #pragma unroll
             for (int a = 0; a < QT; ++a) ts += pull_thermal<QT, float>(g, a, i, j, k, c, lg);
+        } else if (inner) {
+#pragma unroll
+            for (int a = 0; a < QT; ++a) ts += ldS(gs, a * n + c);
         } else {
             auto lg = [&](int b, long long cc) { return ldS(gs, b * n + cc); };
 #pragma unroll
@@ -70,7 +80,10 @@ __device__ __forceinline__ void aa_flow_cell(const Geo& g, const PhysF& P, const
     } else {
         fcollide_3d(d, dr, rho, u, v, w, Fy, P, dp);
     }
-    if (ODD) {
+    if (ODD && inner) {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) f[a * n + c + lat_off<Q>(g, a)] = toS<S>(dp[a]);
+    } else if (ODD) {
         auto st = [&](int b, long long cc, float val) { f[b * n + cc] = toS<S>(val); };
 #pragma unroll
         for (int a = 0; a < Q; ++a) aa_push<Q, false, float>(g, a, i, j, k, c, dp[a], st);
@@ -88,7 +101,11 @@ __device__ __forceinline__ void aa_thermal_cell(const Geo& g, const PhysF& P, co
     constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
     const long long n = g.ncell;
     float d[Q], G[QT], GP[QT];
-    if (fpar) {
+    const bool inner = aa_inner(g, i, j, k);  // no boundary rule on any pull or push
+    if (fpar && inner) {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) d[a] = ldS(fs, Lat<Q>::opp(a) * n + c - lat_off<Q>(g, a));
+    } else if (fpar) {
         auto lf = [&](int b, long long cc) { return ldS(fs, Lat<Q>::opp(b) * n + cc); };
 #pragma unroll
         for (int a = 0; a < Q; ++a) d[a] = pull_flow<Q, float>(g, a, i, j, k, c, lf);
@@ -97,13 +114,19 @@ __device__ __forceinline__ void aa_thermal_cell(const Geo& g, const PhysF& P, co
         for (int a = 0; a < Q; ++a) d[a] = ldS(fs, a * n + c);
     }
     float e[QT];
-    if (ODD) {
+    if (ODD && inner) {
+#pragma unroll
+        for (int a = 0; a < QT; ++a) e[a] = ldA(gg, Lat<QT>::opp(a) * n + c - lat_off<QT>(g, a));
+    } else if (ODD) {
         auto lg = [&](int b, long long cc) { return ldA(gg, Lat<QT>::opp(b) * n + cc); };
         auto wr = [&](int ax, int b, long long) {
             return ldA(aa_face_ptr(wg, ax), b * aa_face_cells(g, ax) + aa_face_index(g, ax, i, j, k));
         };
 #pragma unroll
         for (int a = 0; a < QT; ++a) e[a] = pull_thermal_w<QT, float>(g, a, i, j, k, c, lg, wr);
+    } else if (inner) {
+#pragma unroll
+        for (int a = 0; a < QT; ++a) e[a] = ldA(gg, a * n + c);
     } else {
         auto lg = [&](int b, long long cc) { return ldA(gg, b * n + cc); };
 #pragma unroll
@@ -139,7 +162,10 @@ __device__ __forceinline__ void aa_thermal_cell(const Geo& g, const PhysF& P, co
         A.Bout2[c] = Bz;
         A.lag_out[c] = Tprev;
     }
-    if (ODD) {
+    if (ODD && inner) {
+#pragma unroll
+        for (int a = 0; a < QT; ++a) gg[a * n + c + lat_off<QT>(g, a)] = toS<S>(GP[a] - wT<QT>(P, a) * P.Tref);
+    } else if (ODD) {
         auto st = [&](int b, long long cc, float val) { gg[b * n + cc] = toS<S>(val); };
 #pragma unroll
         for (int a = 0; a < QT; ++a) aa_push<QT, true, float>(g, a, i, j, k, c, GP[a] - wT<QT>(P, a) * P.Tref, st);

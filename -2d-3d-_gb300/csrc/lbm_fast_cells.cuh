@@ -19,8 +19,10 @@ struct FastArgs {
 };
 
 // Flow collision of step n: f_post_n from f_post_{n-1} (or the module arrays when FIRST).
-// Reads lag_in (3D: T_{n-2}; 2D: F_y,n-1); writes lag_out (2D: F_y,n).
-template <int D, bool FIRST, class S>
+// Reads lag_in (3D: T_{n-2}; 2D: F_y,n-1); writes lag_out (2D: F_y,n).  INNER: cells off
+// the lattice's faces pull at fixed offsets without the boundary tests (the batched kernels
+// leave it off: their persistent loops would carry both paths' registers).
+template <int D, bool FIRST, class S, bool INNER = true>
 __device__ __forceinline__ void flow_cell_2k(const Geo& g, const PhysF& P, const FastArgs<S>& A, const S* __restrict__ fin,
                                              const S* __restrict__ gin, S* __restrict__ fout, long long c, int i, int j,
                                              int k) {
@@ -37,13 +39,22 @@ __device__ __forceinline__ void flow_cell_2k(const Geo& g, const PhysF& P, const
         if (D == 3) w = A.w[c];
         T = A.T[c];
     } else {
-        auto lf = [&](int a, long long cc) { return ldS(fin, a * n + cc); };
-        auto lg = [&](int a, long long cc) { return ldS(gin, a * n + cc); };
-#pragma unroll
-        for (int a = 0; a < Q; ++a) d[a] = pull_flow<Q, float>(g, a, i, j, k, c, lf);
+        // loads only in the branch: the arithmetic after it is one sequence for every cell,
+        // so FMA contraction rounds it as in the paired and staged kernels
         float ts = 0.0f;
+        if (INNER && aa_inner(g, i, j, k)) {  // no pull off the faces needs a boundary rule
 #pragma unroll
-        for (int a = 0; a < QT; ++a) ts += pull_thermal<QT, float>(g, a, i, j, k, c, lg);
+            for (int a = 0; a < Q; ++a) d[a] = ldS(fin, a * n + c - lat_off<Q>(g, a));
+#pragma unroll
+            for (int a = 0; a < QT; ++a) ts += ldS(gin, a * n + c - lat_off<QT>(g, a));
+        } else {
+            auto lf = [&](int a, long long cc) { return ldS(fin, a * n + cc); };
+            auto lg = [&](int a, long long cc) { return ldS(gin, a * n + cc); };
+#pragma unroll
+            for (int a = 0; a < Q; ++a) d[a] = pull_flow<Q, float>(g, a, i, j, k, c, lf);
+#pragma unroll
+            for (int a = 0; a < QT; ++a) ts += pull_thermal<QT, float>(g, a, i, j, k, c, lg);
+        }
         T = ts + P.Tref;  // sum of deviations + Tref * sum(wT)
         float Fy;
         fmacro<D>(d, A.lag_in[c], P, dr, rho, u, v, w, Fy);
@@ -61,21 +72,35 @@ __device__ __forceinline__ void flow_cell_2k(const Geo& g, const PhysF& P, const
 
 // Streaming, boundary and macro of the flow, and thermal collision of step n.
 // 2D reads lag_in = F_y,n; 3D writes lag_out = T_{n-1}.
-template <int D, bool FIRST, class S>
+template <int D, bool FIRST, class S, bool INNER = true>
 __device__ __forceinline__ void thermal_cell_2k(const Geo& g, const PhysF& P, const FastArgs<S>& A, const S* __restrict__ fin,
                                              const S* __restrict__ gin, S* __restrict__ gout, long long c, int i, int j,
                                              int k) {
     constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
     const long long n = g.ncell;
     float d[Q], G[QT], GP[QT];
+    const bool inner = INNER && aa_inner(g, i, j, k);  // no pull needs a boundary rule
     auto lf = [&](int a, long long cc) { return ldS(fin, a * n + cc); };
+    if (inner) {
 #pragma unroll
-    for (int a = 0; a < Q; ++a) d[a] = pull_flow<Q, float>(g, a, i, j, k, c, lf);
+        for (int a = 0; a < Q; ++a) d[a] = ldS(fin, a * n + c - lat_off<Q>(g, a));
+    } else {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) d[a] = pull_flow<Q, float>(g, a, i, j, k, c, lf);
+    }
     float Tprev;
     if (FIRST) {
 #pragma unroll
         for (int a = 0; a < QT; ++a) G[a] = ldS(A.gref, a * n + c) + wT<QT>(P, a) * P.Tref;
         Tprev = A.T[c];
+    } else if (inner) {
+        float ts = 0.0f;
+#pragma unroll
+        for (int a = 0; a < QT; ++a) {
+            G[a] = ldS(gin, a * n + c - lat_off<QT>(g, a)) + wT<QT>(P, a) * P.Tref;
+            ts += G[a];
+        }
+        Tprev = ts;
     } else {
         auto lg = [&](int a, long long cc) { return ldS(gin, a * n + cc); };
         float ts = 0.0f;

@@ -390,8 +390,8 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
         face_cell<D>(g, f, i, j, k);
         const long long c = (long long)i + (long long)nx * ((long long)j + (long long)ny * k);
         if (ST == kStoreOut) {
-            if (KIND == 0) flow_cell_2k<D, false, S>(g, P, A, fin, gin, out, c, i, j, k);
-            else thermal_cell_2k<D, false, S>(g, P, A, fin, gin, out, c, i, j, k);
+            if (KIND == 0) flow_cell_2k<D, false, S, false>(g, P, A, fin, gin, out, c, i, j, k);
+            else thermal_cell_2k<D, false, S, false>(g, P, A, fin, gin, out, c, i, j, k);
         } else if (KIND == 0) {
             aa_flow_cell<D, S, ST == kStorePush, false>(g, P, A, out, gin, X.face, X.opar, X.graw, c, i, j, k);
         } else {

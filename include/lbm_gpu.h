@@ -60,6 +60,11 @@ extern "C" {
 /* ---- streaming pattern ---------------------------------------------------------------- */
 #define LBM_PATTERN_AB 0 /* two population buffers (ping-pong)                              */
 #define LBM_PATTERN_AA 1 /* one buffer, in-place even/odd (AA) access pattern               */
+/* The in-place pattern gives the same values as the two-buffer pattern, bit for bit, in
+ * less than half the device memory (one population array per lattice, which is also the
+ * module array).  It keeps no post-collision arrays: LBM_FIELD_F_POST / LBM_FIELD_G_POST
+ * and the stage entry points (lbm_collision ... lbm_macroT) return LBM_ERR_STATE, and
+ * ensembles take two-buffer handles only. */
 
 /* ---- fields for lbm_get_state / lbm_set_state --------------------------------------- */
 #define LBM_FIELD_F       0  /* f(0:q-1,nx,ny,nz), q = 9 (2D) or 19 (3D)                 */
@@ -212,8 +217,10 @@ int lbm_footprint(const lbm_params* p, size_t* bytes);
  *   over LBM_OPT_PAIRS) or pulls every value from global memory (0).  A staged kernel
  *   whose bounded wait for its copies gives up sets a device flag: the next lbm_sync or
  *   diagnostic returns LBM_ERR_TIMEOUT.
- * All forms give the same values bit for bit.  Defaults (fastest on GB300): 3D FP16
- * staged, 3D FP32 one cell per thread, 2D two cells per thread. */
+ * All forms give the same values bit for bit.  Defaults (fastest on GB300): one cell per
+ * thread, except two cells per thread for 2D FP32; in the in-place pattern (LBM_PATTERN_AA)
+ * the even flow sweep, whose accesses are all the cell's own slots, is always paired when
+ * nx is even, and the options select the paired or staged form for the other sweeps. */
 #define LBM_OPT_SINGLE_KERNEL 1
 #define LBM_OPT_KCHUNK        2
 #define LBM_OPT_PAIRS         3
