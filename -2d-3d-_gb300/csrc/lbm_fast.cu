@@ -67,7 +67,7 @@ __global__ void k_fast_initial(Geo g, PhysF P, InitC I, FastArgs<S> A) {
 
 // Flow collision and thermal kernels of the two-kernel step (bodies in lbm_fast_cells.cuh).
 template <int D, bool FIRST, class S>
-__global__ void __launch_bounds__(128) k_fast_flow(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
+__global__ void __launch_bounds__(128, (OneCellBlocks<S, false>::value)) k_fast_flow(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
                                                    const S* __restrict__ gin, S* __restrict__ fout) {
     long long c;
     int i, j, k;
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(128) k_fast_flow(Geo g, PhysF P, FastArgs<S> A
 }
 
 template <int D, bool FIRST, class S>
-__global__ void __launch_bounds__(128) k_fast_thermal(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
+__global__ void __launch_bounds__(128, (OneCellBlocks<S, true>::value)) k_fast_thermal(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
                                                       const S* __restrict__ gin, S* __restrict__ gout) {
     long long c;
     int i, j, k;

@@ -124,7 +124,7 @@ void aa_module_view(const Geo& g, int q, bool thermal, int precision, const void
 // merged from two paths at run time could be rounded differently downstream.
 // ------------------------------------------------------------------------------------
 template <int D, class S, bool ODD, bool FIRST>
-__global__ void __launch_bounds__(128) k_aa_flow_f(Geo g, PhysF P, FastArgs<S> A, S* f, const S* __restrict__ gs,
+__global__ void __launch_bounds__(128, (OneCellBlocks<S, false>::value)) k_aa_flow_f(Geo g, PhysF P, FastArgs<S> A, S* f, const S* __restrict__ gs,
                                                    AAFace<S> wf, int gpar, int graw) {
     long long c;
     int i, j, k;
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(128) k_aa_flow_f(Geo g, PhysF P, FastArgs<S> A
 }
 
 template <int D, class S, bool ODD, bool FIRST>
-__global__ void __launch_bounds__(128) k_aa_thermal_f(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fs, S* gg,
+__global__ void __launch_bounds__(128, (OneCellBlocks<S, true>::value)) k_aa_thermal_f(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fs, S* gg,
                                                       AAFace<S> wg, int fpar, int graw) {
     long long c;
     int i, j, k;

@@ -7,6 +7,15 @@
 
 namespace lbm {
 
+// Resident blocks per SM requested from the one-cell kernels (128 threads).  Measured on
+// GB300: the FP16 kernels and the FP32 thermal kernels run faster with 10 (48 registers,
+// a few bytes of spill) than with the compiler's own choice (56-64 registers, 8 blocks),
+// which keeps more loads in flight; the FP32 flow kernels run slower with it.
+template <class S, bool THERMAL>
+struct OneCellBlocks {
+    static constexpr int value = (sizeof(S) == 2 || THERMAL) ? 10 : 0;  // 0: no minimum
+};
+
 // Pointers of one launch: module arrays plus the B_prev / lag buffers to read and write.
 template <class S>
 struct FastArgs {
