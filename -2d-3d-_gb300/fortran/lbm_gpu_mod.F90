@@ -34,8 +34,12 @@ module lbm_gpu_mod
   integer(c_int), parameter :: LBM_BC_NOSLIP = 0, LBM_BC_PERIODIC = 1
   integer(c_int), parameter :: LBM_BCT_CONST = 0, LBM_BCT_ADIABATIC = 1, LBM_BCT_PERIODIC = 2
   integer(c_int), parameter :: LBM_FP64 = 0, LBM_FP32 = 1, LBM_FP16 = 2
+  integer(c_int), parameter :: LBM_PATTERN_AB = 0, LBM_PATTERN_AA = 1   ! AA: one in-place array, same values
   integer(c_int), parameter :: LBM_FIELD_F = 0, LBM_FIELD_G = 1, LBM_FIELD_RHO = 2, LBM_FIELD_U = 3
   integer(c_int), parameter :: LBM_FIELD_V = 4, LBM_FIELD_W = 5, LBM_FIELD_T = 6
+  integer(c_int), parameter :: LBM_FIELD_BX_PREV = 7, LBM_FIELD_BY_PREV = 8, LBM_FIELD_BZ_PREV = 9
+  integer(c_int), parameter :: LBM_FIELD_FX = 10, LBM_FIELD_FY = 11, LBM_FIELD_F_POST = 12, LBM_FIELD_G_POST = 13
+  integer(c_int), parameter :: LBM_OPT_SINGLE_KERNEL = 1, LBM_OPT_KCHUNK = 2, LBM_OPT_PAIRS = 3, LBM_OPT_STAGED = 4
 
   type, bind(C) :: lbm_params
     integer(c_int32_t) :: dim, nx, ny, nz
@@ -53,6 +57,16 @@ module lbm_gpu_mod
     real(c_double) :: Nu_hot, Nu_cold, Nu_middle
     real(c_double) :: Nu_hot_max, Nu_hot_max_position, Nu_hot_min, Nu_hot_min_position
   end type lbm_nu_wall
+
+  ! mid-line / mid-plane velocity maximum (SideHeatedcalc_*mid_max, RBcalc_*mid_max)
+  type, bind(C) :: lbm_mid_max
+    real(c_double) :: value, pos1, pos2, mid
+  end type lbm_mid_max
+
+  ! 2D stream-function summary of calc_psi_vort_and_output
+  type, bind(C) :: lbm_psi_summary
+    real(c_double) :: psi_center, psi_center_abs, psi_abs_max, x_at_max, y_at_max, psi_center_abs_fine
+  end type lbm_psi_summary
 
   interface
     integer(c_int) function lbm_params_default(dim, p) bind(C, name="lbm_params_default")
@@ -159,6 +173,100 @@ module lbm_gpu_mod
       type(c_ptr), value :: h
       character(kind=c_char), intent(in) :: path(*)
       integer(c_int), value :: mode
+    end function
+    integer(c_int) function lbm_reload_form(h) bind(C, name="lbm_reload_form")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    ! side-heated cavity (SideHeatedCell) and mid-line / mid-plane diagnostics
+    integer(c_int) function lbm_SideHeatedcalc_Nu_global(h, Nu) bind(C, name="lbm_SideHeatedcalc_Nu_global")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double) :: Nu
+    end function
+    integer(c_int) function lbm_SideHeatedcalc_Nu_wall_avg(h, w) bind(C, name="lbm_SideHeatedcalc_Nu_wall_avg")
+      import :: c_int, c_ptr, lbm_nu_wall
+      type(c_ptr), value :: h
+      type(lbm_nu_wall) :: w
+    end function
+    integer(c_int) function lbm_SideHeatedcalc_umid_max(h, m) bind(C, name="lbm_SideHeatedcalc_umid_max")
+      import :: c_int, c_ptr, lbm_mid_max
+      type(c_ptr), value :: h
+      type(lbm_mid_max) :: m
+    end function
+    integer(c_int) function lbm_SideHeatedcalc_vmid_max(h, m) bind(C, name="lbm_SideHeatedcalc_vmid_max")
+      import :: c_int, c_ptr, lbm_mid_max
+      type(c_ptr), value :: h
+      type(lbm_mid_max) :: m
+    end function
+    integer(c_int) function lbm_SideHeatedcalc_wmid_max(h, m) bind(C, name="lbm_SideHeatedcalc_wmid_max")
+      import :: c_int, c_ptr, lbm_mid_max
+      type(c_ptr), value :: h
+      type(lbm_mid_max) :: m
+    end function
+    integer(c_int) function lbm_RBcalc_umid_max(h, m) bind(C, name="lbm_RBcalc_umid_max")
+      import :: c_int, c_ptr, lbm_mid_max
+      type(c_ptr), value :: h
+      type(lbm_mid_max) :: m
+    end function
+    integer(c_int) function lbm_RBcalc_vmid_max(h, m) bind(C, name="lbm_RBcalc_vmid_max")
+      import :: c_int, c_ptr, lbm_mid_max
+      type(c_ptr), value :: h
+      type(lbm_mid_max) :: m
+    end function
+    integer(c_int) function lbm_RBcalc_wmid_max(h, m) bind(C, name="lbm_RBcalc_wmid_max")
+      import :: c_int, c_ptr, lbm_mid_max
+      type(c_ptr), value :: h
+      type(lbm_mid_max) :: m
+    end function
+    ! snapshot writers: output_binary, output_Tecplot(pltFolderPrefix, itc), calc_psi_vort_and_output
+    integer(c_int) function lbm_output_binary(h, path) bind(C, name="lbm_output_binary")
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: h
+      character(kind=c_char), intent(in) :: path(*)
+    end function
+    integer(c_int) function lbm_output_Tecplot(h, prefix, number) bind(C, name="lbm_output_Tecplot")
+      import :: c_int, c_ptr, c_char, c_int64_t
+      type(c_ptr), value :: h
+      character(kind=c_char), intent(in) :: prefix(*)
+      integer(c_int64_t), value :: number
+    end function
+    ! prefix = c_null_ptr: no file, the summary only
+    integer(c_int) function lbm_calc_psi_vort_and_output(h, prefix, number, nFinePerUnit, summary) &
+        bind(C, name="lbm_calc_psi_vort_and_output")
+      import :: c_int, c_ptr, c_int64_t, lbm_psi_summary
+      type(c_ptr), value :: h, prefix
+      integer(c_int64_t), value :: number
+      integer(c_int), value :: nFinePerUnit
+      type(lbm_psi_summary) :: summary
+    end function
+    ! handle utilities
+    integer(c_int) function lbm_sync(h) bind(C, name="lbm_sync")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int64_t) function lbm_itc(h) bind(C, name="lbm_itc")
+      import :: c_int64_t, c_ptr
+      type(c_ptr), value :: h
+    end function
+    type(c_ptr) function lbm_last_error(h) bind(C, name="lbm_last_error")   ! C string
+      import :: c_ptr
+      type(c_ptr), value :: h
+    end function
+    integer(c_int) function lbm_get_params(h, p) bind(C, name="lbm_get_params")
+      import :: c_int, c_ptr, lbm_params
+      type(c_ptr), value :: h
+      type(lbm_params) :: p
+    end function
+    integer(c_int) function lbm_set_option(h, option, value) bind(C, name="lbm_set_option")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      integer(c_int), value :: option, value
+    end function
+    integer(c_int) function lbm_footprint(p, bytes) bind(C, name="lbm_footprint")
+      import :: c_int, c_size_t, lbm_params
+      type(lbm_params), intent(in) :: p
+      integer(c_size_t) :: bytes
     end function
   end interface
 end module lbm_gpu_mod

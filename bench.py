@@ -423,7 +423,7 @@ def served_run(args, local, plain3d_mlups):
     return summary
 
 
-def at_size_run(args, local, n=384, steps=40):
+def at_size_run(args, local, peak, n=384, steps=40):
     """The 384^3 configuration (Ra 1e9, U 0.07): FP16 / FP32 / FP64 storage in the in-place
     (AA) pattern beside the two-buffer pattern -- throughput, device footprint, per-sweep
     kernel times, and the AA state after the same steps against FP64 AA (a short run: the
@@ -435,6 +435,7 @@ def at_size_run(args, local, n=384, steps=40):
     out = {"workload": "3D Rayleigh-Benard cube D3Q19/D3Q7 MRT, %d^3 cells, Ra=1e9, Pr=0.71, U=0.07, no-slip walls, "
                        "adiabatic sides, T linear + 1e-3 seeded noise" % n, "cells": n ** 3,
            "steps_each": steps + 6}
+    traffic = ncu_traffic(n ** 3)
     T = {}
     for prec in ("fp16", "fp32", "fp64"):
         out[prec] = {}
@@ -455,9 +456,15 @@ def at_size_run(args, local, n=384, steps=40):
             ms = t0.elapsed_time(t1)
             tf, tt = lat.time_kernels(2)  # one even and one odd step
             nu, re = lat.calNuRe()
-            out[prec][pat] = {"mlups": n ** 3 * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps,
+            rate = n ** 3 * steps / (ms / 1e3)  # cell updates / s, graph-replayed steps
+            key = prec if pat == "AB" else prec + "_aa"
+            achieved = BYTES_PER_CELL[prec] * rate / 1e9
+            out[prec][pat] = {"mlups": rate / 1e6, "ms_per_step": ms / steps,
                               "ms_flow_thermal_mean_of_2": [tf, tt], "footprint_GB": lbmgpu.footprint(p) / 1e9,
-                              "Nu": nu, "Re": re}
+                              "Nu": nu, "Re": re,
+                              "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                           "frac": achieved / peak, "traffic": traffic.get(key),
+                                           "algorithmic_bytes_per_cell": BYTES_PER_CELL[prec]}}
             if pat == "AA":
                 T[prec] = (lat.get_state("T"), nu, re)
             lat.close()
@@ -536,7 +543,7 @@ def run_gpu(args):
     if rank == 0 and not args.no_served:
         line["served"] = served_run(args, local, results["fp64"]["mlups"] if "fp64" in results else 700.0)
     if rank == 0 and not args.no_size:
-        line["at_384"] = at_size_run(args, local)
+        line["at_384"] = at_size_run(args, local, peak)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n=args.size)
     if rank == 0:
