@@ -128,7 +128,10 @@ __global__ void __launch_bounds__(128, (OneCellBlocks<S, false>::value)) k_aa_fl
                                                    AAFace<S> wf, int gpar, int graw) {
     long long c;
     int i, j, k;
-    if (!fcell(g, c, i, j, k)) return;
+    // the FP16 odd sweep runs fastest with the x-face cells in warps of their own (its
+    // boundary path, pulls and pushes, is the longest); every other one-cell kernel is
+    // faster with cells in lattice order (row-aligned warps)
+    if (ODD && sizeof(S) == 2 ? !split_cell(g, c, i, j, k) : !fcell(g, c, i, j, k)) return;
     aa_flow_cell<D, S, ODD, FIRST>(g, P, A, f, gs, wf, gpar, graw, c, i, j, k);
 }
 

@@ -287,6 +287,34 @@ __device__ __forceinline__ bool fcell(const Geo& g, long long& c, int& i, int& j
     return true;
 }
 
+// Cell of a thread, x-face cells apart: threads [0, rows*(nx-2)) take the cells with
+// 0 < i < nx-1 row by row, the last 2*rows threads the x-face cells (i = 0, nx-1 of each
+// row).  A warp then holds either x-interior cells, which take the fixed-offset path
+// unless their row lies on a y/z face, or face cells only, where with cells in lattice
+// order every warp that holds an x-face cell runs both the fixed-offset and the boundary
+// path.  The price is warps that no longer start at a row (one more sector per access).
+// The launch is ncell threads, as for fcell.
+__device__ __forceinline__ bool split_cell(const Geo& g, long long& c, int& i, int& j, int& k) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long rows = (long long)g.ny * g.nz;
+    const int nxi = g.nx - 2;
+    const long long nin = rows * nxi;
+    long long r;
+    if (t < nin) {
+        r = t / nxi;
+        i = 1 + (int)(t - r * nxi);
+    } else {
+        const long long f = t - nin;
+        if (f >= 2 * rows) return false;
+        r = f >> 1;
+        i = (f & 1) ? g.nx - 1 : 0;
+    }
+    j = (int)(r % g.ny);
+    k = (int)(r / g.ny);
+    c = (long long)i + (long long)g.nx * r;
+    return true;
+}
+
 template <int QT>
 __device__ __forceinline__ float wT(const PhysF& P, int a) {
     return a == 0 ? P.omegaT0 : P.omegaT1;
