@@ -1406,6 +1406,10 @@ static void cont_header(const lbm_handle* h, int form, size_t narrays, int64_t h
         hdr[13] = h->F.AA.graw ? 1 : 0;
         hdr[14] = h->F.fused_valid ? 1 : 0;
     }
+    if (h->p.precision != LBM_FP64) {  // the step counter that keys FP16 stochastic rounding
+        unsigned long long t = 0;
+        if (cudaMemcpy(&t, h->F.tick, sizeof(t), cudaMemcpyDeviceToHost) == cudaSuccess) hdr[15] = (int64_t)t;
+    }
 }
 
 extern "C" int lbm_backupData(lbm_handle* h, const char* path, int flags) {
@@ -1607,6 +1611,11 @@ extern "C" int lbm_reload(lbm_handle* h, const char* path, int mode) {
             h->F.AA.graw = scan.hdr[13] != 0;
             h->F.fused_valid = scan.hdr[14] != 0;
         }
+        if (!fp64) {
+            const unsigned long long t = (unsigned long long)scan.hdr[15];
+            CK(h, cudaMemcpyAsync(h->F.tick, &t, sizeof(t), cudaMemcpyHostToDevice, h->stream));
+            CK(h, cudaStreamSynchronize(h->stream));
+        }
         h->itc = scan.hdr[8];
         h->reload_form = 1;
         h->initialised = true;
@@ -1640,6 +1649,7 @@ extern "C" int lbm_reload(lbm_handle* h, const char* path, int mode) {
         for (auto& fv : fields)
             if ((st = fast_import(F, h->geo, h->phys, h->dim, fv.first, fv.second, h->stream)) != LBM_OK)
                 return lost(fail(h, st, "field import failed"));
+        CK(h, cudaMemsetAsync(F.tick, 0, sizeof(unsigned long long), h->stream));  // a new start: itc = 0
         CK_LAUNCH(h, "import");
     }
     // initial after a reload: up = vp = wp = Tp = 0 (3DRB.F90:627-632, steadyFlow)
@@ -1749,6 +1759,11 @@ extern "C" int lbm_set_option(lbm_handle* h, int option, int value) {
         case LBM_OPT_STAGED:
             if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the plain FP64 method has no staged form");
             h->F.tma = value != 0;
+            break;
+        case LBM_OPT_FP16_ROUNDING:
+            if (h->p.precision != LBM_FP16) return fail(h, LBM_ERR_STATE, "the rounding option is for FP16 storage");
+            if (h->ensemble) return fail(h, LBM_ERR_STATE, "remove the handle from its ensemble before changing its rounding");
+            h->F.sr = value != 0;
             break;
         default:
             return fail(h, LBM_ERR_PARAM, "unknown option");

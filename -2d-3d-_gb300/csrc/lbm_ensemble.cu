@@ -25,6 +25,7 @@ struct EnsMember {
     S* gp[2];
     float* B[2][3];
     float* L[2];
+    unsigned long long* tick;  // the member's step counter (stochastic rounding of FP16)
     int cur;    // buffer parity when the table was built
 };
 
@@ -47,6 +48,7 @@ __global__ void __launch_bounds__(256, 2) k_ens_flow(const EnsMember<S>* __restr
         FastArgs<S> A{};
         A.lag_in = m.L[cur];
         A.lag_out = m.L[nxt];
+        A.tick = m.tick;
         const long long c0 = (long long)tt.y * tile_cells;
         const long long ce = min(c0 + tile_cells, g.ncell);
         for (long long c = c0 + threadIdx.x; c < ce; c += blockDim.x) {
@@ -72,6 +74,7 @@ __global__ void __launch_bounds__(256, 2) k_ens_thermal(const EnsMember<S>* __re
         A.Bout0 = m.B[nxt][0]; A.Bout1 = m.B[nxt][1]; A.Bout2 = m.B[nxt][2];
         A.lag_in = m.L[nxt];
         A.lag_out = m.L[nxt];
+        A.tick = m.tick;
         const long long c0 = (long long)tt.y * tile_cells;
         const long long ce = min(c0 + tile_cells, g.ncell);
         for (long long c = c0 + threadIdx.x; c < ce; c += blockDim.x) {
@@ -80,6 +83,13 @@ __global__ void __launch_bounds__(256, 2) k_ens_thermal(const EnsMember<S>* __re
             thermal_cell_2k<D, false, S, kEnsInner<D>>(g, P, A, m.f[nxt], m.gp[cur], m.gp[nxt], c, i, j, k);
         }
     }
+}
+
+// Every member's step counter advances by one after a batched step.
+template <class S>
+__global__ void k_ens_tick(const EnsMember<S>* __restrict__ mem, int nmem) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < nmem) *mem[m].tick += 1ULL;
 }
 
 template <class S>
@@ -92,7 +102,8 @@ static cudaError_t build_typed(EnsPlan& plan, const std::vector<EnsMemberHost>& 
             if (mh.dim != dim) continue;
             EnsMember<S> m{};
             m.g = dev_geo(mh.geo, mh.phys);
-            m.P = to_physf(mh.phys);
+            m.P = fast_physf(*mh.F, mh.phys);
+            m.tick = mh.F->tick;
             for (int b = 0; b < 2; ++b) {
                 m.f[b] = (S*)mh.F->fbuf[b];
                 m.gp[b] = (S*)mh.F->gbuf[b];
@@ -156,6 +167,11 @@ static void step_typed(const EnsPlan& plan, int flip, cudaStream_t s) {
                 else k_ens_thermal<3, S><<<grid, blk, 0, s>>>(mem, plan.d_tiles[di], plan.ntiles[di], tc, flip);
             }
         }
+    }
+    for (int di = 0; di < 2; ++di) {
+        if (plan.nmembers[di] == 0) continue;
+        k_ens_tick<S><<<(plan.nmembers[di] + 127) / 128, 128, 0, s>>>((const EnsMember<S>*)plan.d_members[di],
+                                                                      plan.nmembers[di]);
     }
 }
 

@@ -27,6 +27,7 @@ static FastArgs<S> args_for(const FastState& F, int bin, int bout, int lin, int 
     a.Bout0 = F.B[bout][0]; a.Bout1 = F.B[bout][1]; a.Bout2 = F.B[bout][2];
     a.lag_in = F.L[lin];
     a.lag_out = F.L[lout];
+    a.tick = F.tick;
     return a;
 }
 
@@ -188,10 +189,20 @@ __global__ void k_d2f(const double* __restrict__ x, float* __restrict__ y, long 
     if (e < n) y[e] = (float)x[e];
 }
 
+__global__ void k_tick(unsigned long long* t) { *t += 1ULL; }
+
 // ------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------
 static inline unsigned nb(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+PhysF fast_physf(const FastState& F, const PhysC& P) {
+    PhysF pf = to_physf(P);
+    pf.sr = (F.sr && F.precision == LBM_FP16) ? 1 : 0;
+    return pf;
+}
+
+void fast_tick(FastState& F, cudaStream_t s) { k_tick<<<1, 1, 0, s>>>(F.tick); }
 
 int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn& alloc) {
     F.precision = p.precision;
@@ -220,6 +231,9 @@ int fast_allocate(FastState& F, const lbm_params& p, const Geo& g, const AllocFn
     }
     if ((st = alloc((void**)&F.err, sizeof(int))) != LBM_OK) return st;
     if (cudaMemset(F.err, 0, sizeof(int)) != cudaSuccess) return LBM_ERR_CUDA;
+    if ((st = alloc((void**)&F.tick, sizeof(unsigned long long))) != LBM_OK) return st;
+    if (cudaMemset(F.tick, 0, sizeof(unsigned long long)) != cudaSuccess) return LBM_ERR_CUDA;
+    F.sr = p.precision == LBM_FP16;
     if (F.aa) {
         // one array each, which is also the module array; the lag fields are read and
         // written by the same thread, so one buffer serves both parities
@@ -272,6 +286,7 @@ void fast_initial(FastState& F, const Geo& g, const PhysC& P, const InitC& I, in
     F.ahead = false;
     F.AA.fpar = F.AA.gpar = 0;  // the in-place arrays now hold module data
     F.AA.graw = false;
+    cudaMemsetAsync(F.tick, 0, sizeof(unsigned long long), s);
     DISPATCH_S(F, {
         FastArgs<S> A = args_for<S>(F, 0, 0, 0, 0);
         if (dim == 2) k_fast_initial<2, S><<<nb(g.ncell, 256), 256, 0, s>>>(g, pf, I, A);
@@ -297,13 +312,14 @@ int fast_take_error(FastState& F, cudaStream_t s) {
 }
 
 void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first, cudaStream_t s, int part) {
-    const PhysF pf = to_physf(P);
+    const PhysF pf = fast_physf(F, P);
     const Geo g = dev_geo(g0, P);
     const int cur = F.cur, nxt = F.cur ^ 1;
     if (F.aa) {
         F.ahead = false;
         fast_step_aa(F, g, pf, dim, first, s, part);
         if (part != 0) {
+            fast_tick(F, s);
             F.cur = nxt;
             F.fused_valid = true;
         }
@@ -349,6 +365,7 @@ void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first,
         }
     });
     if (part != 0) {
+        fast_tick(F, s);
         F.cur = nxt;
         F.fused_valid = true;
     }

@@ -51,6 +51,11 @@ struct FastState {
     // module arrays (fref, gref alias them); B and L have one buffer each.
     bool aa = false;
     AAState AA;
+    // FP16 storage rounds new populations stochastically (lbm_fast_math.cuh, storeS), with
+    // random bits keyed on this device step counter (steps since initial; continuation
+    // records keep it).
+    bool sr = false;
+    unsigned long long* tick = nullptr;
 };
 
 using AllocFn = std::function<int(void**, size_t)>;
@@ -68,6 +73,10 @@ bool fast_fused_supported(const Geo& g, int dim);
 bool fast_tma_supported(const Geo& g, int dim, int precision);
 // Read and clear the device error flag of the staged kernels (synchronises the stream).
 int fast_take_error(FastState& F, cudaStream_t s);
+// Physics constants of the step kernels of this handle (adds the rounding mode).
+PhysF fast_physf(const FastState& F, const PhysC& P);
+// Advance the step counter by one step (after a step's thermal kernel).
+void fast_tick(FastState& F, cudaStream_t s);
 // In-place pattern step and materialisation (lbm_fast_aa.cu); g is the deviation geometry.
 void fast_step_aa(FastState& F, const Geo& g, const PhysF& pf, int dim, bool first, cudaStream_t s, int part);
 void fast_materialize_aa(FastState& F, const Geo& g, const PhysF& pf, int dim, cudaStream_t s);

@@ -253,25 +253,26 @@ __device__ __forceinline__ float2 loc_thermal2(const Geo& g, const S* p, int a, 
     return v;
 }
 
-// Push of the pair's post-collision values of direction a (odd sweep).
+// Push of the pair's post-collision values of direction a (odd sweep), already rounded to
+// the storage type.
 template <int Q, bool TH, class S>
-__device__ __forceinline__ void push2(const Geo& g, S* p, int a, int i0, int j, int k, long long c0, long long n, float v0,
-                                      float v1) {
+__device__ __forceinline__ void push2(const Geo& g, S* p, int a, int i0, int j, int k, long long c0, long long n, S v0,
+                                      S v1) {
     const int ex = Lat<Q>::ex(a), ey = Lat<Q>::ey(a), ez = Lat<Q>::ez(a);
     const int tj = j + ey, tk = k + ez;
     const bool yz = (ey == 0 || (tj >= 0 && tj < g.ny)) && (ez == 0 || (tk >= 0 && tk < g.nz));
     if (ex == 0 && yz) {
-        Vec2<S>::st(p, (long long)a * n + c0 + (long long)g.nx * ((long long)ey + (long long)g.ny * ez), v0, v1);
+        Vec2<S>::st_raw(p, (long long)a * n + c0 + (long long)g.nx * ((long long)ey + (long long)g.ny * ez), v0, v1);
         return;
     }
     if (yz && i0 + ex >= 0 && i0 + 1 + ex < g.nx) {  // both targets inside: plain stores
-        p[(long long)a * n + c0 + lat_off<Q>(g, a)] = toS<S>(v0);
-        p[(long long)a * n + c0 + 1 + lat_off<Q>(g, a)] = toS<S>(v1);
+        p[(long long)a * n + c0 + lat_off<Q>(g, a)] = v0;
+        p[(long long)a * n + c0 + 1 + lat_off<Q>(g, a)] = v1;
         return;
     }
-    auto st = [&](int b, long long cc, float v) { p[(long long)b * n + cc] = toS<S>(v); };
-    aa_push<Q, TH, float>(g, a, i0, j, k, c0, v0, st);
-    aa_push<Q, TH, float>(g, a, i0 + 1, j, k, c0 + 1, v1, st);
+    auto st = [&](int b, long long cc, S v) { p[(long long)b * n + cc] = v; };
+    aa_push<Q, TH, S>(g, a, i0, j, k, c0, v0, st);
+    aa_push<Q, TH, S>(g, a, i0 + 1, j, k, c0 + 1, v1, st);
 }
 
 __device__ __forceinline__ bool aa_pair_cell(const Geo& g, long long& c0, int& i0, int& j, int& k) {
@@ -351,12 +352,14 @@ __global__ void __launch_bounds__(128) k_aa_flow_p(Geo g, PhysF P, FastArgs<S> A
         else fcollide_3d(d1, dr, rho, u, v, w, Fy1, P, dp1);
     }
     if (D == 2) stf2(A.lag_out, c0, Fy0, Fy1);
+    const unsigned long long r0 = sr_base(*A.tick, c0, 0), r1 = sr_base(*A.tick, c0 + 1, 0);
     if (ODD) {
 #pragma unroll
-        for (int a = 0; a < Q; ++a) push2<Q, false, S>(g, f, a, i0, j, k, c0, n, dp0[a], dp1[a]);
+        for (int a = 0; a < Q; ++a)
+            push2<Q, false, S>(g, f, a, i0, j, k, c0, n, storeS<S>(dp0[a], P.sr, r0, a), storeS<S>(dp1[a], P.sr, r1, a));
     } else {
 #pragma unroll
-        for (int a = 0; a < Q; ++a) Vec2<S>::st(f, Lat<Q>::opp(a) * n + c0, dp0[a], dp1[a]);
+        for (int a = 0; a < Q; ++a) Vec2<S>::st_new(f, Lat<Q>::opp(a) * n + c0, dp0[a], dp1[a], P.sr, r0, r1, a);
     }
 }
 
@@ -436,14 +439,17 @@ __global__ void __launch_bounds__(128) k_aa_thermal_p(Geo g, PhysF P, FastArgs<S
         stf2(A.Bout2, c0, Bz0, Bz1);
         stf2(A.lag_out, c0, ts0, ts1);
     }
+    const unsigned long long r0 = sr_base(*A.tick, c0, 1), r1 = sr_base(*A.tick, c0 + 1, 1);
     if (ODD) {
 #pragma unroll
         for (int a = 0; a < QT; ++a)
-            push2<QT, true, S>(g, gg, a, i0, j, k, c0, n, GP0[a] - wT<QT>(P, a) * P.Tref, GP1[a] - wT<QT>(P, a) * P.Tref);
+            push2<QT, true, S>(g, gg, a, i0, j, k, c0, n, storeS<S>(GP0[a] - wT<QT>(P, a) * P.Tref, P.sr, r0, a),
+                               storeS<S>(GP1[a] - wT<QT>(P, a) * P.Tref, P.sr, r1, a));
     } else {
 #pragma unroll
         for (int a = 0; a < QT; ++a)
-            Vec2<S>::st(gg, Lat<QT>::opp(a) * n + c0, GP0[a] - wT<QT>(P, a) * P.Tref, GP1[a] - wT<QT>(P, a) * P.Tref);
+            Vec2<S>::st_new(gg, Lat<QT>::opp(a) * n + c0, GP0[a] - wT<QT>(P, a) * P.Tref, GP1[a] - wT<QT>(P, a) * P.Tref,
+                            P.sr, r0, r1, a);
     }
 }
 
@@ -460,6 +466,7 @@ static FastArgs<S> aa_args(const FastState& F) {
     a.Bout0 = F.B[0][0]; a.Bout1 = F.B[0][1]; a.Bout2 = F.B[0][2];
     a.lag_in = F.L[0];
     a.lag_out = F.L[0];
+    a.tick = F.tick;
     return a;
 }
 

@@ -80,16 +80,19 @@ __device__ __forceinline__ void aa_flow_cell(const Geo& g, const PhysF& P, const
     } else {
         fcollide_3d(d, dr, rho, u, v, w, Fy, P, dp);
     }
+    // rounded by source cell and direction (the two-buffer kernels' bits); the push only
+    // routes the stored value
+    const unsigned long long rb = sr_base(*A.tick, c, 0);
     if (ODD && inner) {
 #pragma unroll
-        for (int a = 0; a < Q; ++a) f[a * n + c + lat_off<Q>(g, a)] = toS<S>(dp[a]);
+        for (int a = 0; a < Q; ++a) f[a * n + c + lat_off<Q>(g, a)] = storeS<S>(dp[a], P.sr, rb, a);
     } else if (ODD) {
-        auto st = [&](int b, long long cc, float val) { f[b * n + cc] = toS<S>(val); };
+        auto st = [&](int b, long long cc, S val) { f[b * n + cc] = val; };
 #pragma unroll
-        for (int a = 0; a < Q; ++a) aa_push<Q, false, float>(g, a, i, j, k, c, dp[a], st);
+        for (int a = 0; a < Q; ++a) aa_push<Q, false, S>(g, a, i, j, k, c, storeS<S>(dp[a], P.sr, rb, a), st);
     } else {
 #pragma unroll
-        for (int a = 0; a < Q; ++a) f[Lat<Q>::opp(a) * n + c] = toS<S>(dp[a]);
+        for (int a = 0; a < Q; ++a) f[Lat<Q>::opp(a) * n + c] = storeS<S>(dp[a], P.sr, rb, a);
     }
 }
 
@@ -162,16 +165,19 @@ __device__ __forceinline__ void aa_thermal_cell(const Geo& g, const PhysF& P, co
         A.Bout2[c] = Bz;
         A.lag_out[c] = Tprev;
     }
+    const unsigned long long rb = sr_base(*A.tick, c, 1);
     if (ODD && inner) {
 #pragma unroll
-        for (int a = 0; a < QT; ++a) gg[a * n + c + lat_off<QT>(g, a)] = toS<S>(GP[a] - wT<QT>(P, a) * P.Tref);
+        for (int a = 0; a < QT; ++a)
+            gg[a * n + c + lat_off<QT>(g, a)] = storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a);
     } else if (ODD) {
-        auto st = [&](int b, long long cc, float val) { gg[b * n + cc] = toS<S>(val); };
+        auto st = [&](int b, long long cc, S val) { gg[b * n + cc] = val; };
 #pragma unroll
-        for (int a = 0; a < QT; ++a) aa_push<QT, true, float>(g, a, i, j, k, c, GP[a] - wT<QT>(P, a) * P.Tref, st);
+        for (int a = 0; a < QT; ++a)
+            aa_push<QT, true, S>(g, a, i, j, k, c, storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a), st);
     } else {
 #pragma unroll
-        for (int a = 0; a < QT; ++a) gg[Lat<QT>::opp(a) * n + c] = toS<S>(GP[a] - wT<QT>(P, a) * P.Tref);
+        for (int a = 0; a < QT; ++a) gg[Lat<QT>::opp(a) * n + c] = storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a);
     }
 }
 

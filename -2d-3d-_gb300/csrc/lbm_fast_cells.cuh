@@ -25,6 +25,7 @@ struct FastArgs {
     float *Bout0, *Bout1, *Bout2;
     const float* lag_in;
     float* lag_out;
+    const unsigned long long* tick;  // the lattice's step counter (stochastic rounding)
 };
 
 // Flow collision of step n: f_post_n from f_post_{n-1} (or the module arrays when FIRST).
@@ -75,8 +76,9 @@ __device__ __forceinline__ void flow_cell_2k(const Geo& g, const PhysF& P, const
     } else {
         fcollide_3d(d, dr, rho, u, v, w, Fy, P, dp);
     }
+    const unsigned long long rb = sr_base(*A.tick, c, 0);
 #pragma unroll
-    for (int a = 0; a < Q; ++a) fout[a * n + c] = toS<S>(dp[a]);
+    for (int a = 0; a < Q; ++a) fout[a * n + c] = storeS<S>(dp[a], P.sr, rb, a);
 }
 
 // Streaming, boundary and macro of the flow, and thermal collision of step n.
@@ -135,8 +137,9 @@ __device__ __forceinline__ void thermal_cell_2k(const Geo& g, const PhysF& P, co
         A.Bout2[c] = Bz;
         A.lag_out[c] = Tprev;
     }
+    const unsigned long long rb = sr_base(*A.tick, c, 1);
 #pragma unroll
-    for (int a = 0; a < QT; ++a) gout[a * n + c] = toS<S>(GP[a] - wT<QT>(P, a) * P.Tref);
+    for (int a = 0; a < QT; ++a) gout[a * n + c] = storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a);
 }
 
 }  // namespace lbm

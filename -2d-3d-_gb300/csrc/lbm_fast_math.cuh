@@ -24,6 +24,48 @@ template <class S> __device__ __forceinline__ S toS(float x);
 template <> __device__ __forceinline__ float toS<float>(float x) { return x; }
 template <> __device__ __forceinline__ __half toS<__half>(float x) { return __float2half_rn(x); }
 
+// ------------------------------------------------------------------------------------
+// Stochastic rounding of new FP16 populations.  Near the onset of convection a step
+// changes a stored deviation by less than half an FP16 unit in the last place (at 128^3,
+// Ra 1e7, the buoyancy of a 1e-3 temperature seed moves populations by ~1e-8 per step
+// against units of ~1e-6): round-to-nearest drops every such increment and the lattice
+// stays conductive.  Rounding up with probability equal to the dropped fraction keeps the
+// increments in expectation.  The random bits are a hash of (the lattice's step counter,
+// the cell, flow or thermal set, direction), so every kernel form and both access
+// patterns round the same value the same way, and a run is reproducible bit for bit.
+// ------------------------------------------------------------------------------------
+// Per-cell base of the random bits of one set (kind 0 flow, 1 thermal) at step `tick`.
+__device__ __forceinline__ unsigned long long sr_base(unsigned long long tick, long long c, unsigned kind) {
+    unsigned long long z = (unsigned long long)c * 0x9E3779B97F4A7C15ULL ^ ((tick << 1) | kind) * 0xD1B54A32D192ED03ULL;
+    z ^= z >> 31;
+    z *= 0xBF58476D1CE4E5B9ULL;
+    z ^= z >> 29;
+    z *= 0x94D049BB133111EBULL;
+    return z ^ (z >> 32);
+}
+__device__ __forceinline__ unsigned sr_bits(unsigned long long base, int a) {
+    return (unsigned)((base * (0x9E3779B97F4A7C15ULL + 2ULL * (unsigned long long)a)) >> 32);
+}
+// x rounded to FP16 at random: the float's bits below the half's last place (13 for a
+// normal half, more for a subnormal one) plus uniform random bits, then truncated.  The
+// result is a multiple of the half's unit in the last place, so the conversion is exact.
+__device__ __forceinline__ __half half_sr(float x, unsigned r) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned mag = b & 0x7FFFFFFFu;
+    const int e = (int)(mag >> 23);
+    const int k = e >= 113 ? 13 : 126 - e;  // half min-normal exponent is float exponent 113
+    if (k > 24) return __float2half_rn(x);  // below 2^-25: rounds to zero either way
+    const unsigned mask = (1u << k) - 1u;
+    return __float2half_rn(__uint_as_float((b & 0x80000000u) | ((mag + (r & mask)) & ~mask)));
+}
+// New population a of a cell rounded to storage type S: stochastically when `sr` (FP16
+// storage, the default), otherwise to nearest.
+template <class S> __device__ __forceinline__ S storeS(float x, bool sr, unsigned long long base, int a);
+template <> __device__ __forceinline__ float storeS<float>(float x, bool, unsigned long long, int) { return x; }
+template <> __device__ __forceinline__ __half storeS<__half>(float x, bool sr, unsigned long long base, int a) {
+    return sr ? half_sr(x, sr_bits(base, a)) : __float2half_rn(x);
+}
+
 // Rest weights (D2Q9 2DRB.F90:506-512, D3Q19 3DRB.F90:669-671).
 template <int Q>
 __host__ __device__ constexpr double wrest(int a) {
@@ -37,6 +79,7 @@ struct PhysF {
     float Qk, Qnu, SG, paraA;
     float omegaT0, omegaT1, geqc;
     int use_g, legacy;
+    int sr;  // FP16 storage: stochastic rounding of the new populations (storeS)
 };
 
 inline PhysF to_physf(const PhysC& P) {
@@ -47,6 +90,7 @@ inline PhysF to_physf(const PhysC& P) {
     F.Qk = (float)P.Qk; F.Qnu = (float)P.Qnu; F.SG = (float)P.SG; F.paraA = (float)P.paraA;
     F.omegaT0 = (float)P.omegaT0; F.omegaT1 = (float)P.omegaT1; F.geqc = (float)P.geqc;
     F.use_g = P.use_g; F.legacy = P.legacy;
+    F.sr = 0;
     return F;
 }
 

@@ -351,8 +351,9 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
                 } else {
                     fcollide_3d(d, dr, rho, u, v, w, Fy, P, dp);
                 }
+                const unsigned long long rb = sr_base(*A.tick, c, 0);
 #pragma unroll
-                for (int a = 0; a < Q; ++a) out[store_index<Q, ST>(g, a, c, n)] = toS<S>(dp[a]);
+                for (int a = 0; a < Q; ++a) out[store_index<Q, ST>(g, a, c, n)] = storeS<S>(dp[a], P.sr, rb, a);
             } else {
                 float G[QT], GP[QT], ts = 0.0f;
 #pragma unroll
@@ -376,8 +377,10 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
                     A.Bout2[c] = Bz;
                     A.lag_out[c] = ts;
                 }
+                const unsigned long long rb = sr_base(*A.tick, c, 1);
 #pragma unroll
-                for (int a = 0; a < QT; ++a) out[store_index<QT, ST>(g, a, c, n)] = toS<S>(GP[a] - wT<QT>(P, a) * P.Tref);
+                for (int a = 0; a < QT; ++a)
+                    out[store_index<QT, ST>(g, a, c, n)] = storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a);
             }
         }
         __syncwarp();

@@ -37,6 +37,7 @@ struct FusedArgs {
     float *Bout0, *Bout1, *Bout2;
     float* lag_out;  // 3D: T_{n-1} -> L[cur^1]; 2D: F_y,n+1 -> L[cur]
     float bc_lo[3], bc_hi[3];  // anti-bounce-back terms for full g (2 wT Tw)
+    const unsigned long long* tick;  // step counter n: g_post_n rounds with n, f_post_{n+1} with n+1
 };
 
 template <int D>
@@ -83,8 +84,9 @@ __device__ __forceinline__ void thermal_cell(const Geo& g, const PhysF& P, const
         }
     }
     if (owner) {
+        const unsigned long long rb = sr_base(*A.tick, c, 1);
 #pragma unroll
-        for (int a = 0; a < QT; ++a) A.gout[a * n + c] = toS<S>(GP[a] - wT<QT>(P, a) * P.Tref);
+        for (int a = 0; a < QT; ++a) A.gout[a * n + c] = storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a);
     }
 }
 
@@ -171,8 +173,9 @@ __device__ __forceinline__ void flow_cell(const Geo& g, const PhysF& P, const Fu
     } else {
         fcollide_3d(d, m[0], m[1], m[2], m[3], m[4], Fy, P, dp);
     }
+    const unsigned long long rb = sr_base(*A.tick + 1, c, 0);
 #pragma unroll
-    for (int a = 0; a < Q; ++a) A.fout[a * n + c] = toS<S>(dp[a]);
+    for (int a = 0; a < Q; ++a) A.fout[a * n + c] = storeS<S>(dp[a], P.sr, rb, a);
 }
 
 template <int D, class S>
@@ -243,7 +246,7 @@ bool fast_fused_supported(const Geo& g, int dim) {
 }
 
 void fast_fused_step(FastState& F, const Geo& g0, const PhysC& P, int dim, cudaStream_t s) {
-    const PhysF pf = to_physf(P);
+    const PhysF pf = fast_physf(F, P);
     const Geo g = dev_geo(g0, P);
     const int c = F.cur;
     auto launch = [&](auto tag) {
@@ -255,6 +258,7 @@ void fast_fused_step(FastState& F, const Geo& g0, const PhysC& P, int dim, cudaS
         A.fout = (S*)F.fbuf[c];
         A.gout = (S*)F.gbuf[c ^ 1];
         A.Bout0 = F.B[c ^ 1][0]; A.Bout1 = F.B[c ^ 1][1]; A.Bout2 = F.B[c ^ 1][2];
+        A.tick = F.tick;
         if (dim == 2) {
             A.lag_in = F.L[c ^ 1];
             A.lag_out = F.L[c];
@@ -277,6 +281,7 @@ void fast_fused_step(FastState& F, const Geo& g0, const PhysC& P, int dim, cudaS
     };
     if (F.precision == LBM_FP16) launch(__half());
     else launch(float());
+    fast_tick(F, s);
     F.cur ^= 1;
 }
 

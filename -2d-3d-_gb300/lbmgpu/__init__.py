@@ -102,6 +102,7 @@ LBM_OPT_SINGLE_KERNEL = 1
 LBM_OPT_KCHUNK = 2
 LBM_OPT_PAIRS = 3
 LBM_OPT_STAGED = 4
+LBM_OPT_FP16_ROUNDING = 5  # FP16 storage: 1 stochastic rounding (default), 0 nearest
 
 _lib = None
 

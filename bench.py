@@ -477,6 +477,43 @@ def at_size_run(args, local, peak, n=384, steps=40):
     return out
 
 
+def config0_run(args, local, steps=20000, cpu_steps=400):
+    """The 2D reference case (256 x 128, x-periodic, Ra 1e5, Pr 0.71, U 0.1, plain FP64): its
+    full 20,000 steps on the GPU through lbm_step, the wall-averaged Nu and volume Re at the
+    end, and the CPU oracle on a bounded sample of the same lattice."""
+    import torch
+    import lbmgpu
+    from lbmgpu.abi import rb_params
+    from oracle import oracle as ora
+    p = rb_params(dim=2, nx=256, ny=128, Ra=1e5, Pr=0.71, U=0.1, noise_amp=1e-3, seed=20261203)
+    lat = lbmgpu.Lattice(p, device=local)
+    lat.initial()
+    lat.sync()
+    stream = torch.cuda.ExternalStream(lat.stream_handle(), device=torch.device("cuda", local))
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    lat.step(steps)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b)
+    nu, re = lat.calNuRe()
+    wall = lat.RBcalc_Nu_wall_avg()
+    lat.close()
+    threads = ora.set_threads(os.cpu_count() or 1)
+    o = ora.Oracle(p)
+    o.initial()
+    t0 = time.perf_counter()
+    o.step(cpu_steps)
+    dt = time.perf_counter() - t0
+    cells = 256 * 128
+    return {"workload": "2D RB D2Q9/D2Q5, 256 x 128, x periodic, Ra 1e5, Pr 0.71, U 0.1, FP64 plain method, "
+                        "T linear + 1e-3 seeded noise, %d steps" % steps,
+            "gpu_s": ms / 1e3, "mlups": cells * steps / (ms / 1e3) / 1e6, "Nu_volume": nu, "Re": re,
+            "Nu_hot_wall": wall["Nu_hot"], "Nu_cold_wall": wall["Nu_cold"],
+            "cpu_oracle": {"threads": threads, "steps": cpu_steps, "s": dt, "mlups": cells * cpu_steps / dt / 1e6,
+                           "s_for_all_steps": dt * steps / cpu_steps}}
+
+
 def run_gpu(args):
     rank, world, local, pg = dist_setup(args)
     import torch
@@ -544,6 +581,8 @@ def run_gpu(args):
         line["served"] = served_run(args, local, results["fp64"]["mlups"] if "fp64" in results else 700.0)
     if rank == 0 and not args.no_size:
         line["at_384"] = at_size_run(args, local, peak)
+    if rank == 0 and not args.no_config0:
+        line["config0_2d"] = config0_run(args, local)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n=args.size)
     if rank == 0:
@@ -562,6 +601,7 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-form leg (64 2D instances)")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream leg")
     ap.add_argument("--no-size", action="store_true", help="skip the 384^3 leg (in-place vs two-buffer pattern)")
+    ap.add_argument("--no-config0", action="store_true", help="skip the 2D 256 x 128 FP64 leg (20,000 steps)")
     ap.add_argument("--served-full", action="store_true", help="served leg as configured: 600 s, 5000-step window")
     ap.add_argument("--served-seconds", type=float, default=20.0)
     ap.add_argument("--served-drain", type=float, default=40.0)

@@ -220,11 +220,18 @@ int lbm_footprint(const lbm_params* p, size_t* bytes);
  * All forms give the same values bit for bit.  Defaults (fastest on GB300): one cell per
  * thread, except two cells per thread for 2D FP32; in the in-place pattern (LBM_PATTERN_AA)
  * the even flow sweep, whose accesses are all the cell's own slots, is always paired when
- * nx is even, and the options select the paired or staged form for the other sweeps. */
+ * nx is even, and the options select the paired or staged form for the other sweeps.
+ * LBM_OPT_FP16_ROUNDING: how FP16 storage rounds the new populations of a step.  Stochastic
+ *   (1, default): up with probability equal to the dropped fraction, with random bits keyed
+ *   on (step counter, cell, direction), so results are reproducible and the same in every
+ *   kernel form and both patterns.  Nearest (0) drops every change smaller than half a unit
+ *   in the last place: from a small seed (1e-3 in T) at Ra 1e7 the lattice then never leaves
+ *   the conductive state.  Not settable while the handle is in an ensemble. */
 #define LBM_OPT_SINGLE_KERNEL 1
 #define LBM_OPT_KCHUNK        2
 #define LBM_OPT_PAIRS         3
 #define LBM_OPT_STAGED        4
+#define LBM_OPT_FP16_ROUNDING 5 /* FP16 storage: 1 stochastic rounding (default), 0 nearest */
 int lbm_set_option(lbm_handle* h, int option, int value);
 
 /* ---- measurement hooks (no counterpart in the reference, which times its loop with
