@@ -352,14 +352,14 @@ __global__ void __launch_bounds__(128) k_aa_flow_p(Geo g, PhysF P, FastArgs<S> A
         else fcollide_3d(d1, dr, rho, u, v, w, Fy1, P, dp1);
     }
     if (D == 2) stf2(A.lag_out, c0, Fy0, Fy1);
-    const unsigned long long r0 = sr_base(*A.tick, c0, 0), r1 = sr_base(*A.tick, c0 + 1, 0);
+    S h0[Q], h1[Q];
+    round_pair<Q>(dp0, dp1, h0, h1, P.sr != 0, sr_seed(*A.tick, c0, 0), sr_seed(*A.tick, c0 + 1, 0));
     if (ODD) {
 #pragma unroll
-        for (int a = 0; a < Q; ++a)
-            push2<Q, false, S>(g, f, a, i0, j, k, c0, n, storeS<S>(dp0[a], P.sr, r0, a), storeS<S>(dp1[a], P.sr, r1, a));
+        for (int a = 0; a < Q; ++a) push2<Q, false, S>(g, f, a, i0, j, k, c0, n, h0[a], h1[a]);
     } else {
 #pragma unroll
-        for (int a = 0; a < Q; ++a) Vec2<S>::st_new(f, Lat<Q>::opp(a) * n + c0, dp0[a], dp1[a], P.sr, r0, r1, a);
+        for (int a = 0; a < Q; ++a) Vec2<S>::st_raw(f, Lat<Q>::opp(a) * n + c0, h0[a], h1[a]);
     }
 }
 
@@ -439,17 +439,20 @@ __global__ void __launch_bounds__(128) k_aa_thermal_p(Geo g, PhysF P, FastArgs<S
         stf2(A.Bout2, c0, Bz0, Bz1);
         stf2(A.lag_out, c0, ts0, ts1);
     }
-    const unsigned long long r0 = sr_base(*A.tick, c0, 1), r1 = sr_base(*A.tick, c0 + 1, 1);
+    float e0[QT], e1[QT];
+    S h0[QT], h1[QT];
+#pragma unroll
+    for (int a = 0; a < QT; ++a) {
+        e0[a] = GP0[a] - wT<QT>(P, a) * P.Tref;
+        e1[a] = GP1[a] - wT<QT>(P, a) * P.Tref;
+    }
+    round_pair<QT>(e0, e1, h0, h1, P.sr != 0, sr_seed(*A.tick, c0, 1), sr_seed(*A.tick, c0 + 1, 1));
     if (ODD) {
 #pragma unroll
-        for (int a = 0; a < QT; ++a)
-            push2<QT, true, S>(g, gg, a, i0, j, k, c0, n, storeS<S>(GP0[a] - wT<QT>(P, a) * P.Tref, P.sr, r0, a),
-                               storeS<S>(GP1[a] - wT<QT>(P, a) * P.Tref, P.sr, r1, a));
+        for (int a = 0; a < QT; ++a) push2<QT, true, S>(g, gg, a, i0, j, k, c0, n, h0[a], h1[a]);
     } else {
 #pragma unroll
-        for (int a = 0; a < QT; ++a)
-            Vec2<S>::st_new(gg, Lat<QT>::opp(a) * n + c0, GP0[a] - wT<QT>(P, a) * P.Tref, GP1[a] - wT<QT>(P, a) * P.Tref,
-                            P.sr, r0, r1, a);
+        for (int a = 0; a < QT; ++a) Vec2<S>::st_raw(gg, Lat<QT>::opp(a) * n + c0, h0[a], h1[a]);
     }
 }
 

@@ -82,17 +82,18 @@ __device__ __forceinline__ void aa_flow_cell(const Geo& g, const PhysF& P, const
     }
     // rounded by source cell and direction (the two-buffer kernels' bits); the push only
     // routes the stored value
-    const unsigned long long rb = sr_base(*A.tick, c, 0);
+    S hs[Q];
+    round_cell<Q>(dp, hs, P.sr != 0, sr_seed(*A.tick, c, 0));
     if (ODD && inner) {
 #pragma unroll
-        for (int a = 0; a < Q; ++a) f[a * n + c + lat_off<Q>(g, a)] = storeS<S>(dp[a], P.sr, rb, a);
+        for (int a = 0; a < Q; ++a) f[a * n + c + lat_off<Q>(g, a)] = hs[a];
     } else if (ODD) {
         auto st = [&](int b, long long cc, S val) { f[b * n + cc] = val; };
 #pragma unroll
-        for (int a = 0; a < Q; ++a) aa_push<Q, false, S>(g, a, i, j, k, c, storeS<S>(dp[a], P.sr, rb, a), st);
+        for (int a = 0; a < Q; ++a) aa_push<Q, false, S>(g, a, i, j, k, c, hs[a], st);
     } else {
 #pragma unroll
-        for (int a = 0; a < Q; ++a) f[Lat<Q>::opp(a) * n + c] = storeS<S>(dp[a], P.sr, rb, a);
+        for (int a = 0; a < Q; ++a) f[Lat<Q>::opp(a) * n + c] = hs[a];
     }
 }
 
@@ -165,19 +166,21 @@ __device__ __forceinline__ void aa_thermal_cell(const Geo& g, const PhysF& P, co
         A.Bout2[c] = Bz;
         A.lag_out[c] = Tprev;
     }
-    const unsigned long long rb = sr_base(*A.tick, c, 1);
+    float ev[QT];
+    S hs[QT];
+#pragma unroll
+    for (int a = 0; a < QT; ++a) ev[a] = GP[a] - wT<QT>(P, a) * P.Tref;
+    round_cell<QT>(ev, hs, P.sr != 0, sr_seed(*A.tick, c, 1));
     if (ODD && inner) {
 #pragma unroll
-        for (int a = 0; a < QT; ++a)
-            gg[a * n + c + lat_off<QT>(g, a)] = storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a);
+        for (int a = 0; a < QT; ++a) gg[a * n + c + lat_off<QT>(g, a)] = hs[a];
     } else if (ODD) {
         auto st = [&](int b, long long cc, S val) { gg[b * n + cc] = val; };
 #pragma unroll
-        for (int a = 0; a < QT; ++a)
-            aa_push<QT, true, S>(g, a, i, j, k, c, storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a), st);
+        for (int a = 0; a < QT; ++a) aa_push<QT, true, S>(g, a, i, j, k, c, hs[a], st);
     } else {
 #pragma unroll
-        for (int a = 0; a < QT; ++a) gg[Lat<QT>::opp(a) * n + c] = storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a);
+        for (int a = 0; a < QT; ++a) gg[Lat<QT>::opp(a) * n + c] = hs[a];
     }
 }
 

@@ -76,9 +76,10 @@ __device__ __forceinline__ void flow_cell_2k(const Geo& g, const PhysF& P, const
     } else {
         fcollide_3d(d, dr, rho, u, v, w, Fy, P, dp);
     }
-    const unsigned long long rb = sr_base(*A.tick, c, 0);
+    S hs[Q];
+    round_cell<Q>(dp, hs, P.sr != 0, sr_seed(*A.tick, c, 0));
 #pragma unroll
-    for (int a = 0; a < Q; ++a) fout[a * n + c] = storeS<S>(dp[a], P.sr, rb, a);
+    for (int a = 0; a < Q; ++a) fout[a * n + c] = hs[a];
 }
 
 // Streaming, boundary and macro of the flow, and thermal collision of step n.
@@ -137,9 +138,13 @@ __device__ __forceinline__ void thermal_cell_2k(const Geo& g, const PhysF& P, co
         A.Bout2[c] = Bz;
         A.lag_out[c] = Tprev;
     }
-    const unsigned long long rb = sr_base(*A.tick, c, 1);
+    float ev[QT];
+    S hs[QT];
 #pragma unroll
-    for (int a = 0; a < QT; ++a) gout[a * n + c] = storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a);
+    for (int a = 0; a < QT; ++a) ev[a] = GP[a] - wT<QT>(P, a) * P.Tref;
+    round_cell<QT>(ev, hs, P.sr != 0, sr_seed(*A.tick, c, 1));
+#pragma unroll
+    for (int a = 0; a < QT; ++a) gout[a * n + c] = hs[a];
 }
 
 }  // namespace lbm

@@ -30,40 +30,89 @@ template <> __device__ __forceinline__ __half toS<__half>(float x) { return __fl
 // Ra 1e7, the buoyancy of a 1e-3 temperature seed moves populations by ~1e-8 per step
 // against units of ~1e-6): round-to-nearest drops every such increment and the lattice
 // stays conductive.  Rounding up with probability equal to the dropped fraction keeps the
-// increments in expectation.  The random bits are a hash of (the lattice's step counter,
-// the cell, flow or thermal set, direction), so every kernel form and both access
-// patterns round the same value the same way, and a run is reproducible bit for bit.
+// increments in expectation.  GB300 does it in one instruction for two values,
+// cvt.rs.f16x2.f32 d, a, b, rbits: a goes to the upper half of d and takes rbits[31:16],
+// b the lower half and rbits[15:0]; each value rounds up when the low 13 bits of its half
+// plus its 13 dropped mantissa bits carry (measured on GB300).  The random bits of the new
+// population a of cell c are half a&1 of the 32-bit word a>>1 of a hash of (step counter,
+// cell, flow or thermal set), so every kernel form and both access patterns round a value
+// alike whatever value it is paired with, and a run is reproducible bit for bit.
 // ------------------------------------------------------------------------------------
-// Per-cell base of the random bits of one set (kind 0 flow, 1 thermal) at step `tick`.
-__device__ __forceinline__ unsigned long long sr_base(unsigned long long tick, long long c, unsigned kind) {
-    unsigned long long z = (unsigned long long)c * 0x9E3779B97F4A7C15ULL ^ ((tick << 1) | kind) * 0xD1B54A32D192ED03ULL;
-    z ^= z >> 31;
-    z *= 0xBF58476D1CE4E5B9ULL;
-    z ^= z >> 29;
-    z *= 0x94D049BB133111EBULL;
-    return z ^ (z >> 32);
+__device__ __forceinline__ unsigned fmix32(unsigned h) {
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    h *= 0xC2B2AE35u;
+    return h ^ (h >> 16);
 }
-__device__ __forceinline__ unsigned sr_bits(unsigned long long base, int a) {
-    return (unsigned)((base * (0x9E3779B97F4A7C15ULL + 2ULL * (unsigned long long)a)) >> 32);
+// Seed of one cell's random bits for one set (kind 0 flow, 1 thermal) at step `tick`.
+__device__ __forceinline__ unsigned sr_seed(unsigned long long tick, long long c, unsigned kind) {
+    return fmix32((unsigned)c ^ fmix32((((unsigned)tick << 1) | kind) + 0x9E3779B9u));
 }
-// x rounded to FP16 at random: the float's bits below the half's last place (13 for a
-// normal half, more for a subnormal one) plus uniform random bits, then truncated.  The
-// result is a multiple of the half's unit in the last place, so the conversion is exact.
-__device__ __forceinline__ __half half_sr(float x, unsigned r) {
-    const unsigned b = __float_as_uint(x);
-    const unsigned mag = b & 0x7FFFFFFFu;
-    const int e = (int)(mag >> 23);
-    const int k = e >= 113 ? 13 : 126 - e;  // half min-normal exponent is float exponent 113
-    if (k > 24) return __float2half_rn(x);  // below 2^-25: rounds to zero either way
-    const unsigned mask = (1u << k) - 1u;
-    return __float2half_rn(__uint_as_float((b & 0x80000000u) | ((mag + (r & mask)) & ~mask)));
+// Random bits of directions 2j (low half) and 2j+1 (high half).
+__device__ __forceinline__ unsigned sr_word(unsigned seed, int j) {
+    return fmix32(seed ^ (0x9E3779B9u * (unsigned)(j + 1)));
 }
-// New population a of a cell rounded to storage type S: stochastically when `sr` (FP16
-// storage, the default), otherwise to nearest.
-template <class S> __device__ __forceinline__ S storeS(float x, bool sr, unsigned long long base, int a);
-template <> __device__ __forceinline__ float storeS<float>(float x, bool, unsigned long long, int) { return x; }
-template <> __device__ __forceinline__ __half storeS<__half>(float x, bool sr, unsigned long long base, int a) {
-    return sr ? half_sr(x, sr_bits(base, a)) : __float2half_rn(x);
+__device__ __forceinline__ unsigned cvt_rs_f16x2(float hi, float lo, unsigned rbits) {
+    unsigned d;
+    asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+    return d;
+}
+__device__ __forceinline__ __half lo_half(unsigned d) { return __ushort_as_half((unsigned short)(d & 0xFFFFu)); }
+__device__ __forceinline__ __half hi_half(unsigned d) { return __ushort_as_half((unsigned short)(d >> 16)); }
+
+// The Q new populations v of one cell in storage type S (FP16: stochastically when sr,
+// otherwise to nearest).
+template <int Q>
+__device__ __forceinline__ void round_cell(const float* v, float* h, bool, unsigned) {
+#pragma unroll
+    for (int a = 0; a < Q; ++a) h[a] = v[a];
+}
+template <int Q>
+__device__ __forceinline__ void round_cell(const float* v, __half* h, bool sr, unsigned seed) {
+#pragma unroll
+    for (int j = 0; 2 * j < Q; ++j) {
+        const float lo = v[2 * j], hi = 2 * j + 1 < Q ? v[2 * j + 1] : 0.0f;
+        if (sr) {
+            const unsigned d = cvt_rs_f16x2(hi, lo, sr_word(seed, j));
+            h[2 * j] = lo_half(d);
+            if (2 * j + 1 < Q) h[2 * j + 1] = hi_half(d);
+        } else {
+            h[2 * j] = __float2half_rn(lo);
+            if (2 * j + 1 < Q) h[2 * j + 1] = __float2half_rn(hi);
+        }
+    }
+}
+// The same for two cells (paired forms): value a of each cell takes the bits it takes in
+// round_cell.
+template <int Q>
+__device__ __forceinline__ void round_pair(const float* v0, const float* v1, float* h0, float* h1, bool, unsigned,
+                                           unsigned) {
+#pragma unroll
+    for (int a = 0; a < Q; ++a) {
+        h0[a] = v0[a];
+        h1[a] = v1[a];
+    }
+}
+template <int Q>
+__device__ __forceinline__ void round_pair(const float* v0, const float* v1, __half* h0, __half* h1, bool sr,
+                                           unsigned seed0, unsigned seed1) {
+#pragma unroll
+    for (int j = 0; 2 * j < Q; ++j) {
+        const unsigned w0 = sr ? sr_word(seed0, j) : 0u, w1 = sr ? sr_word(seed1, j) : 0u;
+#pragma unroll
+        for (int a = 2 * j; a < 2 * j + 2 && a < Q; ++a) {
+            if (sr) {
+                const unsigned r0 = (a & 1) ? w0 >> 16 : w0 & 0xFFFFu, r1 = (a & 1) ? w1 >> 16 : w1 & 0xFFFFu;
+                const unsigned d = cvt_rs_f16x2(v1[a], v0[a], (r1 << 16) | r0);
+                h0[a] = lo_half(d);
+                h1[a] = hi_half(d);
+            } else {
+                h0[a] = __float2half_rn(v0[a]);
+                h1[a] = __float2half_rn(v1[a]);
+            }
+        }
+    }
 }
 
 // Rest weights (D2Q9 2DRB.F90:506-512, D3Q19 3DRB.F90:669-671).
@@ -79,7 +128,7 @@ struct PhysF {
     float Qk, Qnu, SG, paraA;
     float omegaT0, omegaT1, geqc;
     int use_g, legacy;
-    int sr;  // FP16 storage: stochastic rounding of the new populations (storeS)
+    int sr;  // FP16 storage: stochastic rounding of the new populations (round_cell, round_pair)
 };
 
 inline PhysF to_physf(const PhysC& P) {

@@ -25,11 +25,7 @@ template <> struct Vec2<float> {
     __device__ static __forceinline__ void st(float* p, long long i, float a, float b) {
         *reinterpret_cast<float2*>(p + i) = make_float2(a, b);
     }
-    // new populations of two cells (direction k, random bases r0, r1), rounded as storeS
-    __device__ static __forceinline__ void st_new(float* p, long long i, float a, float b, bool, unsigned long long,
-                                                  unsigned long long, int) {
-        st(p, i, a, b);
-    }
+    // two values already in the storage type
     __device__ static __forceinline__ void st_raw(float* p, long long i, float a, float b) { st(p, i, a, b); }
 };
 template <> struct Vec2<__half> {
@@ -41,12 +37,6 @@ template <> struct Vec2<__half> {
     __device__ static __forceinline__ void st(__half* p, long long i, float a, float b) {
         // each half rounds as __float2half_rn does in the one-cell path
         const unsigned int lo = __half_as_ushort(__float2half_rn(a)), hi = __half_as_ushort(__float2half_rn(b));
-        *reinterpret_cast<unsigned int*>(p + i) = lo | (hi << 16);
-    }
-    __device__ static __forceinline__ void st_new(__half* p, long long i, float a, float b, bool sr,
-                                                  unsigned long long r0, unsigned long long r1, int k) {
-        const unsigned int lo = __half_as_ushort(storeS<__half>(a, sr, r0, k));
-        const unsigned int hi = __half_as_ushort(storeS<__half>(b, sr, r1, k));
         *reinterpret_cast<unsigned int*>(p + i) = lo | (hi << 16);
     }
     // two values already in the storage type
@@ -145,9 +135,10 @@ __device__ __forceinline__ void flow_pair_2k(const Geo& g, const PhysF& P, const
         else fcollide_3d(d1, dr, rho, u, v, w, Fy1, P, dp1);
     }
     if (D == 2) stf2(A.lag_out, c0, Fy0, Fy1);
-    const unsigned long long r0 = sr_base(*A.tick, c0, 0), r1 = sr_base(*A.tick, c0 + 1, 0);
+    S h0[Q], h1[Q];
+    round_pair<Q>(dp0, dp1, h0, h1, P.sr != 0, sr_seed(*A.tick, c0, 0), sr_seed(*A.tick, c0 + 1, 0));
 #pragma unroll
-    for (int a = 0; a < Q; ++a) Vec2<S>::st_new(fout, a * n + c0, dp0[a], dp1[a], P.sr, r0, r1, a);
+    for (int a = 0; a < Q; ++a) Vec2<S>::st_raw(fout, a * n + c0, h0[a], h1[a]);
 }
 
 // thermal_cell_2k (not FIRST) for the cells c0 and c0 + 1.
@@ -198,11 +189,16 @@ __device__ __forceinline__ void thermal_pair_2k(const Geo& g, const PhysF& P, co
         stf2(A.Bout2, c0, Bz0, Bz1);
         stf2(A.lag_out, c0, ts0, ts1);
     }
-    const unsigned long long r0 = sr_base(*A.tick, c0, 1), r1 = sr_base(*A.tick, c0 + 1, 1);
+    float e0[QT], e1[QT];
+    S h0[QT], h1[QT];
 #pragma unroll
-    for (int a = 0; a < QT; ++a)
-        Vec2<S>::st_new(gout, a * n + c0, GP0[a] - wT<QT>(P, a) * P.Tref, GP1[a] - wT<QT>(P, a) * P.Tref, P.sr, r0,
-                        r1, a);
+    for (int a = 0; a < QT; ++a) {
+        e0[a] = GP0[a] - wT<QT>(P, a) * P.Tref;
+        e1[a] = GP1[a] - wT<QT>(P, a) * P.Tref;
+    }
+    round_pair<QT>(e0, e1, h0, h1, P.sr != 0, sr_seed(*A.tick, c0, 1), sr_seed(*A.tick, c0 + 1, 1));
+#pragma unroll
+    for (int a = 0; a < QT; ++a) Vec2<S>::st_raw(gout, a * n + c0, h0[a], h1[a]);
 }
 
 }  // namespace lbm

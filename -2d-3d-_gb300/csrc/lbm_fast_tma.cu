@@ -351,9 +351,10 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
                 } else {
                     fcollide_3d(d, dr, rho, u, v, w, Fy, P, dp);
                 }
-                const unsigned long long rb = sr_base(*A.tick, c, 0);
+                S hs[Q];
+                round_cell<Q>(dp, hs, P.sr != 0, sr_seed(*A.tick, c, 0));
 #pragma unroll
-                for (int a = 0; a < Q; ++a) out[store_index<Q, ST>(g, a, c, n)] = storeS<S>(dp[a], P.sr, rb, a);
+                for (int a = 0; a < Q; ++a) out[store_index<Q, ST>(g, a, c, n)] = hs[a];
             } else {
                 float G[QT], GP[QT], ts = 0.0f;
 #pragma unroll
@@ -377,10 +378,13 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
                     A.Bout2[c] = Bz;
                     A.lag_out[c] = ts;
                 }
-                const unsigned long long rb = sr_base(*A.tick, c, 1);
+                float ev[QT];
+                S hs[QT];
 #pragma unroll
-                for (int a = 0; a < QT; ++a)
-                    out[store_index<QT, ST>(g, a, c, n)] = storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a);
+                for (int a = 0; a < QT; ++a) ev[a] = GP[a] - wT<QT>(P, a) * P.Tref;
+                round_cell<QT>(ev, hs, P.sr != 0, sr_seed(*A.tick, c, 1));
+#pragma unroll
+                for (int a = 0; a < QT; ++a) out[store_index<QT, ST>(g, a, c, n)] = hs[a];
             }
         }
         __syncwarp();

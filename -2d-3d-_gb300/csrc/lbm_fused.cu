@@ -84,9 +84,13 @@ __device__ __forceinline__ void thermal_cell(const Geo& g, const PhysF& P, const
         }
     }
     if (owner) {
-        const unsigned long long rb = sr_base(*A.tick, c, 1);
+        float ev[QT];
+        S hs[QT];
 #pragma unroll
-        for (int a = 0; a < QT; ++a) A.gout[a * n + c] = storeS<S>(GP[a] - wT<QT>(P, a) * P.Tref, P.sr, rb, a);
+        for (int a = 0; a < QT; ++a) ev[a] = GP[a] - wT<QT>(P, a) * P.Tref;
+        round_cell<QT>(ev, hs, P.sr != 0, sr_seed(*A.tick, c, 1));
+#pragma unroll
+        for (int a = 0; a < QT; ++a) A.gout[a * n + c] = hs[a];
     }
 }
 
@@ -173,9 +177,10 @@ __device__ __forceinline__ void flow_cell(const Geo& g, const PhysF& P, const Fu
     } else {
         fcollide_3d(d, m[0], m[1], m[2], m[3], m[4], Fy, P, dp);
     }
-    const unsigned long long rb = sr_base(*A.tick + 1, c, 0);
+    S hs[Q];
+    round_cell<Q>(dp, hs, P.sr != 0, sr_seed(*A.tick + 1, c, 0));
 #pragma unroll
-    for (int a = 0; a < Q; ++a) A.fout[a * n + c] = storeS<S>(dp[a], P.sr, rb, a);
+    for (int a = 0; a < Q; ++a) A.fout[a * n + c] = hs[a];
 }
 
 template <int D, class S>
