@@ -327,10 +327,13 @@ static int allocate(lbm_handle* h) {
             AL(h->A.Bz, n);
             AL(h->A.wp, n);
             AL(h->A.Tlag, n);
+            AL(h->A.jz, n);
         } else {
             AL(h->A.Fx, n);
             AL(h->A.Fy, n);
         }
+        AL(h->A.jx, n);
+        AL(h->A.jy, n);
     } else {
         st = fast_allocate(h->F, h->p, h->geo, [h](void** p, size_t bytes) {
             cudaError_t e = cudaMalloc(p, bytes > 0 ? bytes : 1);
@@ -413,6 +416,14 @@ extern "C" int lbm_create(const lbm_params* p, int device, lbm_handle** out) {
     P.B2 = c.B2sigemarho;
     P.sinphi = c.sinphi;
     P.cosphi = c.cosphi;
+    P.hSe38 = (1.0 - 0.5 * c.Se) * 38.0;
+    P.hSeps11 = (1.0 - 0.5 * c.Seps) * (-11.0);
+    P.hSq23 = (1.0 - 0.5 * c.Sq) * (-2.0 / 3.0);
+    P.hSnu = 1.0 - 0.5 * c.Snu;
+    P.hSpi = 1.0 - 0.5 * c.Spi;
+    P.h6Snu = 6.0 - 3.0 * c.Snu;
+    P.hSq = 1.0 - 0.5 * c.Sq;
+    P.h2Snu = 2.0 - c.Snu;
     DiagScalars& D = h->dsc;
     D.Thot = p->Thot;
     D.Tcold = p->Tcold;
@@ -1792,7 +1803,7 @@ extern "C" int lbm_footprint(const lbm_params* p, size_t* bytes) {
     const size_t es = p->precision == LBM_FP64 ? 8 : (p->precision == LBM_FP16 ? 2 : 4);
     if (p->precision == LBM_FP64) {
         b += 8 * n * (aa ? q + qt : 3 * q + 3 * qt);         // AA: f, g | f_post A/B, g_post A/B, f, g
-        b += 8 * n * (p->dim == 3 ? 13 : 11);                // rho u v T Bx By up vp Tp (+w Bz wp Tlag | Fx Fy)
+        b += 8 * n * (p->dim == 3 ? 16 : 13);                // rho u v T Bx By up vp Tp jx jy (+w Bz wp Tlag jz | Fx Fy)
     } else {
         const size_t nb = aa ? 1 : 2;
         b += es * n * (aa ? q + qt : 3 * q + 3 * qt);        // AA: f, g | F A/B, G A/B, f, g (module)

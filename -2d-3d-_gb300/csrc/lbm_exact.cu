@@ -18,9 +18,15 @@
 #include <cuda_runtime.h>
 
 #include "lbm_device.cuh"
+#include "lbm_fp64_int.cuh"
 #include "lbm_internal.h"
 
 namespace lbm {
+
+// Products with exact powers of two (x*2, x/4, -0.5*x, ...) are exponent adds on the
+// integer pipes (i64f::iscale), the same bits as the FP64 multiply, which on GB300 is the
+// step's bottleneck; IEEE multiplication is sign-symmetric, so -(2^k x) = (-2^k) x.
+using i64f::iscale;
 
 // ------------------------------------------------------------------------------------
 // Per-cell arithmetic, verbatim from the reference.
@@ -42,16 +48,20 @@ __device__ __forceinline__ double divc(double x, double c) {
 }
 
 // collision (2DRB.F90:688-759).  Writes f_post and the stored body force (Fx, Fy).
+// KNOWN: rho, jx, jy are the macro step's sums of these populations (m0, m3, m5 in the
+// same order), passed in instead of summed again.
+template <bool KNOWN = false>
 __device__ __forceinline__ void collide_2d(const double* F, double rho, double u, double v, double T,
-                                           const PhysC& P, double* FP, double& FxOut, double& FyOut) {
+                                           const PhysC& P, double* FP, double& FxOut, double& FyOut,
+                                           double jx = 0.0, double jy = 0.0) {
     double m[9], meq[9], s[9], fSource[9], m_post[9];
-    m[0] = F[0] + F[1] + F[2] + F[3] + F[4] + F[5] + F[6] + F[7] + F[8];
-    m[1] = -4.0 * F[0] - F[1] - F[2] - F[3] - F[4] + 2.0 * (F[5] + F[6] + F[7] + F[8]);
-    m[2] = 4.0 * F[0] - 2.0 * (F[1] + F[2] + F[3] + F[4]) + F[5] + F[6] + F[7] + F[8];
-    m[3] = F[1] - F[3] + F[5] - F[6] - F[7] + F[8];
-    m[4] = -2.0 * F[1] + 2.0 * F[3] + F[5] - F[6] - F[7] + F[8];
-    m[5] = F[2] - F[4] + F[5] + F[6] - F[7] - F[8];
-    m[6] = -2.0 * F[2] + 2.0 * F[4] + F[5] + F[6] - F[7] - F[8];
+    m[0] = KNOWN ? rho : F[0] + F[1] + F[2] + F[3] + F[4] + F[5] + F[6] + F[7] + F[8];
+    m[1] = -iscale<2>(F[0]) - F[1] - F[2] - F[3] - F[4] + iscale<1>(F[5] + F[6] + F[7] + F[8]);
+    m[2] = iscale<2>(F[0]) - iscale<1>(F[1] + F[2] + F[3] + F[4]) + F[5] + F[6] + F[7] + F[8];
+    m[3] = KNOWN ? jx : F[1] - F[3] + F[5] - F[6] - F[7] + F[8];
+    m[4] = -iscale<1>(F[1]) + iscale<1>(F[3]) + F[5] - F[6] - F[7] + F[8];
+    m[5] = KNOWN ? jy : F[2] - F[4] + F[5] + F[6] - F[7] - F[8];
+    m[6] = -iscale<1>(F[2]) + iscale<1>(F[4]) + F[5] + F[6] - F[7] - F[8];
     m[7] = F[1] - F[2] + F[3] - F[4];
     m[8] = F[5] - F[6] + F[7] - F[8];
 
@@ -77,57 +87,64 @@ __device__ __forceinline__ void collide_2d(const double* F, double rho, double u
     FxOut = Fx;
     FyOut = Fy;
 
+    // (6 - 3 s1) = (6 - 3 s2) = h6Snu, (1 - s/2) = 1 for s3, s5 = 0, hSq for s4, s6,
+    // (2 - s7) = h2Snu, (1 - s8/2) = hSnu: the rates' factors rounded once on the host
     fSource[0] = 0.0;
-    fSource[1] = (6.0 - 3.0 * s[1]) * (u * Fx + v * Fy);
-    fSource[2] = -((6.0 - 3.0 * s[2]) * (u * Fx + v * Fy));
-    fSource[3] = (1.0 - 0.5 * s[3]) * Fx;
-    fSource[4] = -((1.0 - 0.5 * s[4]) * Fx);
-    fSource[5] = (1.0 - 0.5 * s[5]) * Fy;
-    fSource[6] = -((1.0 - 0.5 * s[6]) * Fy);
-    fSource[7] = (2.0 - s[7]) * (u * Fx - v * Fy);
-    fSource[8] = (1.0 - 0.5 * s[8]) * (u * Fy + v * Fx);
+    fSource[1] = P.h6Snu * (u * Fx + v * Fy);
+    fSource[2] = -(P.h6Snu * (u * Fx + v * Fy));
+    fSource[3] = Fx;
+    fSource[4] = -(P.hSq * Fx);
+    fSource[5] = Fy;
+    fSource[6] = -(P.hSq * Fy);
+    fSource[7] = P.h2Snu * (u * Fx - v * Fy);
+    fSource[8] = P.hSnu * (u * Fy + v * Fx);
 
 #pragma unroll
     for (int a = 0; a < 9; ++a) m_post[a] = m[a] - s[a] * (m[a] - meq[a]) + fSource[a];
 
+    const double q7 = iscale<-2>(m_post[7]), q8 = iscale<-2>(m_post[8]);  // m/4
     FP[0] = divc(m_post[0], 9.0) - divc(m_post[1], 9.0) + divc(m_post[2], 9.0);
-    FP[1] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) + divc(m_post[3], 6.0) - divc(m_post[4], 6.0) + m_post[7] / 4.0;
-    FP[2] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) + divc(m_post[5], 6.0) - divc(m_post[6], 6.0) - m_post[7] / 4.0;
-    FP[3] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) - divc(m_post[3], 6.0) + divc(m_post[4], 6.0) + m_post[7] / 4.0;
-    FP[4] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) - divc(m_post[5], 6.0) + divc(m_post[6], 6.0) - m_post[7] / 4.0;
+    FP[1] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) + divc(m_post[3], 6.0) - divc(m_post[4], 6.0) + q7;
+    FP[2] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) + divc(m_post[5], 6.0) - divc(m_post[6], 6.0) - q7;
+    FP[3] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) - divc(m_post[3], 6.0) + divc(m_post[4], 6.0) + q7;
+    FP[4] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) - divc(m_post[5], 6.0) + divc(m_post[6], 6.0) - q7;
     FP[5] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) + divc(m_post[3], 6.0) + divc(m_post[4], 12.0)
-            + divc(m_post[5], 6.0) + divc(m_post[6], 12.0) + m_post[8] / 4.0;
+            + divc(m_post[5], 6.0) + divc(m_post[6], 12.0) + q8;
     FP[6] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) - divc(m_post[3], 6.0) - divc(m_post[4], 12.0)
-            + divc(m_post[5], 6.0) + divc(m_post[6], 12.0) - m_post[8] / 4.0;
+            + divc(m_post[5], 6.0) + divc(m_post[6], 12.0) - q8;
     FP[7] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) - divc(m_post[3], 6.0) - divc(m_post[4], 12.0)
-            - divc(m_post[5], 6.0) - divc(m_post[6], 12.0) + m_post[8] / 4.0;
+            - divc(m_post[5], 6.0) - divc(m_post[6], 12.0) + q8;
     FP[8] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) + divc(m_post[3], 6.0) + divc(m_post[4], 12.0)
-            - divc(m_post[5], 6.0) - divc(m_post[6], 12.0) - m_post[8] / 4.0;
+            - divc(m_post[5], 6.0) - divc(m_post[6], 12.0) - q8;
 }
 
-// collision (3DRB.F90:704-943).
+// collision (3DRB.F90:704-943).  KNOWN: rhoLoc, jx, jy, jz are the macro step's sums of
+// these populations (m0, m3, m5, m7 in the same order), passed in instead of summed again.
+template <bool KNOWN = false>
 __device__ __forceinline__ void collide_3d(const double* f, double rhoLoc, double uLoc, double vLoc, double wLoc,
-                                           double Tc, const PhysC& P, double* fp) {
+                                           double Tc, const PhysC& P, double* fp, double jx = 0.0, double jy = 0.0,
+                                           double jz = 0.0) {
     double m[19], meq[19], s[19], fSource[19], mp[19];
     const double u2 = uLoc * uLoc + vLoc * vLoc + wLoc * wLoc;
-    m[0] = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8] + f[9] + f[10] + f[11] + f[12]
-           + f[13] + f[14] + f[15] + f[16] + f[17] + f[18];
+    m[0] = KNOWN ? rhoLoc
+                 : f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13]
+                       + f[14] + f[15] + f[16] + f[17] + f[18];
     m[1] = -30.0 * f[0] - 11.0 * (f[1] + f[2] + f[3] + f[4] + f[5] + f[6])
-           + 8.0 * (f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14] + f[15] + f[16] + f[17] + f[18]);
-    m[2] = 12.0 * f[0] - 4.0 * (f[1] + f[2] + f[3] + f[4] + f[5] + f[6])
+           + iscale<3>(f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14] + f[15] + f[16] + f[17] + f[18]);
+    m[2] = 12.0 * f[0] - iscale<2>(f[1] + f[2] + f[3] + f[4] + f[5] + f[6])
            + (f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14] + f[15] + f[16] + f[17] + f[18]);
-    m[3] = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
-    m[4] = -4.0 * f[1] + 4.0 * f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
-    m[5] = f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
-    m[6] = -4.0 * f[3] + 4.0 * f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
-    m[7] = f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
-    m[8] = -4.0 * f[5] + 4.0 * f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
-    m[9] = 2.0 * (f[1] + f[2]) - (f[3] + f[4] + f[5] + f[6]) + (f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14])
-           - 2.0 * (f[15] + f[16] + f[17] + f[18]);
-    m[10] = -4.0 * (f[1] + f[2]) + 2.0 * (f[3] + f[4] + f[5] + f[6])
-            + (f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14]) - 2.0 * (f[15] + f[16] + f[17] + f[18]);
+    m[3] = KNOWN ? jx : f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+    m[4] = -iscale<2>(f[1]) + iscale<2>(f[2]) + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+    m[5] = KNOWN ? jy : f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
+    m[6] = -iscale<2>(f[3]) + iscale<2>(f[4]) + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
+    m[7] = KNOWN ? jz : f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
+    m[8] = -iscale<2>(f[5]) + iscale<2>(f[6]) + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
+    m[9] = iscale<1>(f[1] + f[2]) - (f[3] + f[4] + f[5] + f[6]) + (f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14])
+           - iscale<1>(f[15] + f[16] + f[17] + f[18]);
+    m[10] = -iscale<2>(f[1] + f[2]) + iscale<1>(f[3] + f[4] + f[5] + f[6])
+            + (f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14]) - iscale<1>(f[15] + f[16] + f[17] + f[18]);
     m[11] = (f[3] + f[4]) - (f[5] + f[6]) + (f[7] + f[8] + f[9] + f[10]) - (f[11] + f[12] + f[13] + f[14]);
-    m[12] = -2.0 * (f[3] + f[4]) + 2.0 * (f[5] + f[6]) + (f[7] + f[8] + f[9] + f[10]) - (f[11] + f[12] + f[13] + f[14]);
+    m[12] = -iscale<1>(f[3] + f[4]) + iscale<1>(f[5] + f[6]) + (f[7] + f[8] + f[9] + f[10]) - (f[11] + f[12] + f[13] + f[14]);
     m[13] = f[7] - f[8] - f[9] + f[10];
     m[14] = f[15] - f[16] - f[17] + f[18];
     m[15] = f[11] - f[12] - f[13] + f[14];
@@ -135,19 +152,20 @@ __device__ __forceinline__ void collide_3d(const double* f, double rhoLoc, doubl
     m[17] = -f[7] - f[8] + f[9] + f[10] + f[15] - f[16] + f[17] - f[18];
     m[18] = f[11] + f[12] - f[13] - f[14] - f[15] - f[16] + f[17] + f[18];
 
+    const double m2rho = -iscale<1>(rhoLoc);  // -2.0 * rhoLoc
     meq[0] = rhoLoc;
     meq[1] = rhoLoc * (-11.0 + 19.0 * u2);
-    meq[2] = rhoLoc * (3.0 - 11.0 * u2 / 2.0);
+    meq[2] = rhoLoc * (3.0 - iscale<-1>(11.0 * u2));
     meq[3] = rhoLoc * uLoc;
-    meq[4] = divc(-2.0 * rhoLoc * uLoc, 3.0);
+    meq[4] = divc(m2rho * uLoc, 3.0);
     meq[5] = rhoLoc * vLoc;
-    meq[6] = divc(-2.0 * rhoLoc * vLoc, 3.0);
+    meq[6] = divc(m2rho * vLoc, 3.0);
     meq[7] = rhoLoc * wLoc;
-    meq[8] = divc(-2.0 * rhoLoc * wLoc, 3.0);
-    meq[9] = rhoLoc * (2.0 * uLoc * uLoc - vLoc * vLoc - wLoc * wLoc);
-    meq[10] = -0.5 * meq[9];
+    meq[8] = divc(m2rho * wLoc, 3.0);
+    meq[9] = rhoLoc * (iscale<1>(uLoc) * uLoc - vLoc * vLoc - wLoc * wLoc);
+    meq[10] = -iscale<-1>(meq[9]);
     meq[11] = rhoLoc * (vLoc * vLoc - wLoc * wLoc);
-    meq[12] = -0.5 * meq[11];
+    meq[12] = -iscale<-1>(meq[11]);
     meq[13] = rhoLoc * uLoc * vLoc;
     meq[14] = rhoLoc * vLoc * wLoc;
     meq[15] = rhoLoc * uLoc * wLoc;
@@ -167,15 +185,18 @@ __device__ __forceinline__ void collide_3d(const double* f, double rhoLoc, doubl
     const double FyLoc = rhoLoc * P.gBeta * (Tc - P.Tref);
     const double uDotF = vLoc * FyLoc;
 
-    fSource[1] = (1.0 - 0.5 * s[1]) * 38.0 * uDotF;
-    fSource[2] = (1.0 - 0.5 * s[2]) * (-11.0) * uDotF;
-    fSource[6] = (1.0 - 0.5 * s[6]) * (-2.0 / 3.0) * FyLoc;
-    fSource[9] = (1.0 - 0.5 * s[9]) * (-(2.0 * vLoc * FyLoc));
-    fSource[10] = (1.0 - 0.5 * s[10]) * (vLoc * FyLoc);
-    fSource[11] = (1.0 - 0.5 * s[11]) * (2.0 * vLoc * FyLoc);
-    fSource[12] = (1.0 - 0.5 * s[12]) * (-(vLoc * FyLoc));
-    fSource[13] = (1.0 - 0.5 * s[13]) * (uLoc * FyLoc);
-    fSource[14] = (1.0 - 0.5 * s[14]) * (wLoc * FyLoc);
+    // (1 - s/2) factors: s1 = Se, s2 = Seps, s6 = Sq, s9 = s11 = s13 = s14 = Snu, s10 = s12 = Spi,
+    // with the constant multiplied in first as the reference's left-to-right order does
+    const double vF2 = iscale<1>(vLoc) * FyLoc;  // 2.0 * vLoc * FyLoc
+    fSource[1] = P.hSe38 * uDotF;
+    fSource[2] = P.hSeps11 * uDotF;
+    fSource[6] = P.hSq23 * FyLoc;
+    fSource[9] = P.hSnu * (-vF2);
+    fSource[10] = P.hSpi * (vLoc * FyLoc);
+    fSource[11] = P.hSnu * vF2;
+    fSource[12] = P.hSpi * (-(vLoc * FyLoc));
+    fSource[13] = P.hSnu * (uLoc * FyLoc);
+    fSource[14] = P.hSnu * (wLoc * FyLoc);
 
     // m_post = m - S(m - meq) + source; conserved moments (s = 0) keep m plus the force.
     mp[0] = m[0];
@@ -193,6 +214,9 @@ __device__ __forceinline__ void collide_3d(const double* f, double rhoLoc, doubl
 #pragma unroll
     for (int a = 16; a <= 18; ++a) mp[a] = m[a] - s[a] * m[a];
 
+    // m/4 and m/8 as exponent adds
+    const double q13 = iscale<-2>(mp[13]), q14 = iscale<-2>(mp[14]), q15 = iscale<-2>(mp[15]);
+    const double q16 = iscale<-3>(mp[16]), q17 = iscale<-3>(mp[17]), q18 = iscale<-3>(mp[18]);
     fp[0] = divc(mp[0], 19.0) - divc(5.0 * mp[1], 399.0) + divc(mp[2], 21.0);
     fp[1] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) + divc(mp[3], 10.0) - divc(mp[4], 10.0) + divc(mp[9], 18.0) - divc(mp[10], 18.0);
     fp[2] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) - divc(mp[3], 10.0) + divc(mp[4], 10.0) + divc(mp[9], 18.0) - divc(mp[10], 18.0);
@@ -205,29 +229,29 @@ __device__ __forceinline__ void collide_3d(const double* f, double rhoLoc, doubl
     fp[6] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) - divc(mp[7], 10.0) + divc(mp[8], 10.0) - divc(mp[9], 36.0) + divc(mp[10], 36.0)
             - divc(mp[11], 12.0) + divc(mp[12], 12.0);
     fp[7] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0)
-            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) + mp[13] / 4.0 + mp[16] / 8.0 - mp[17] / 8.0;
+            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) + q13 + q16 - q17;
     fp[8] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0)
-            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) - mp[13] / 4.0 - mp[16] / 8.0 - mp[17] / 8.0;
+            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) - q13 - q16 - q17;
     fp[9] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0)
-            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) - mp[13] / 4.0 + mp[16] / 8.0 + mp[17] / 8.0;
+            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) - q13 + q16 + q17;
     fp[10] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0)
-             + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) + mp[13] / 4.0 - mp[16] / 8.0 + mp[17] / 8.0;
+             + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) + q13 - q16 + q17;
     fp[11] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
-             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) + mp[15] / 4.0 - mp[16] / 8.0 + mp[18] / 8.0;
+             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) + q15 - q16 + q18;
     fp[12] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
-             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) - mp[15] / 4.0 + mp[16] / 8.0 + mp[18] / 8.0;
+             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) - q15 + q16 + q18;
     fp[13] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
-             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) - mp[15] / 4.0 - mp[16] / 8.0 - mp[18] / 8.0;
+             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) - q15 - q16 - q18;
     fp[14] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
-             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) + mp[15] / 4.0 + mp[16] / 8.0 - mp[18] / 8.0;
+             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) + q15 + q16 - q18;
     fp[15] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
-             - divc(mp[9], 18.0) - divc(mp[10], 36.0) + mp[14] / 4.0 + mp[17] / 8.0 - mp[18] / 8.0;
+             - divc(mp[9], 18.0) - divc(mp[10], 36.0) + q14 + q17 - q18;
     fp[16] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
-             - divc(mp[9], 18.0) - divc(mp[10], 36.0) - mp[14] / 4.0 - mp[17] / 8.0 - mp[18] / 8.0;
+             - divc(mp[9], 18.0) - divc(mp[10], 36.0) - q14 - q17 - q18;
     fp[17] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
-             - divc(mp[9], 18.0) - divc(mp[10], 36.0) - mp[14] / 4.0 + mp[17] / 8.0 + mp[18] / 8.0;
+             - divc(mp[9], 18.0) - divc(mp[10], 36.0) - q14 + q17 + q18;
     fp[18] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
-             - divc(mp[9], 18.0) - divc(mp[10], 36.0) + mp[14] / 4.0 - mp[17] / 8.0 + mp[18] / 8.0;
+             - divc(mp[9], 18.0) - divc(mp[10], 36.0) + q14 - q17 + q18;
 }
 
 // collisionT (2DRB.F90:921-974).  B = (u T, v T); returns g_post and the new B.
@@ -249,7 +273,7 @@ __device__ __forceinline__ void collideT_2d(const double* G, double u, double v,
     n[0] = G[0] + G[1] + G[2] + G[3] + G[4];
     n[1] = G[1] - G[3];
     n[2] = G[2] - G[4];
-    n[3] = -4.0 * G[0] + G[1] + G[2] + G[3] + G[4];
+    n[3] = -iscale<2>(G[0]) + G[1] + G[2] + G[3] + G[4];
     n[4] = G[1] - G[2] + G[3] - G[4];
     neq[0] = T;
     neq[1] = T * u;
@@ -262,11 +286,12 @@ __device__ __forceinline__ void collideT_2d(const double* G, double u, double v,
     n_post[2] = n[2] - q[2] * (n[2] - neq[2]) + P.SG * dBy;
     n_post[3] = n[3] - q[3] * (n[3] - neq[3]);
     n_post[4] = n[4] - q[4] * (n[4] - neq[4]);
+    const double h1 = iscale<-1>(n_post[1]), h2 = iscale<-1>(n_post[2]), q4 = iscale<-2>(n_post[4]);
     GP[0] = 0.2 * n_post[0] - 0.2 * n_post[3];
-    GP[1] = 0.2 * n_post[0] + 0.5 * n_post[1] + 0.05 * n_post[3] + 0.25 * n_post[4];
-    GP[2] = 0.2 * n_post[0] + 0.5 * n_post[2] + 0.05 * n_post[3] - 0.25 * n_post[4];
-    GP[3] = 0.2 * n_post[0] - 0.5 * n_post[1] + 0.05 * n_post[3] + 0.25 * n_post[4];
-    GP[4] = 0.2 * n_post[0] - 0.5 * n_post[2] + 0.05 * n_post[3] - 0.25 * n_post[4];
+    GP[1] = 0.2 * n_post[0] + h1 + 0.05 * n_post[3] + q4;
+    GP[2] = 0.2 * n_post[0] + h2 + 0.05 * n_post[3] - q4;
+    GP[3] = 0.2 * n_post[0] - h1 + 0.05 * n_post[3] + q4;
+    GP[4] = 0.2 * n_post[0] - h2 + 0.05 * n_post[3] - q4;
 }
 
 // collisionT (3DRB.F90:1121-1191).
@@ -293,7 +318,7 @@ __device__ __forceinline__ void collideT_3d(const double* g, double u, double v,
     n[2] = g[3] - g[4];
     n[3] = g[5] - g[6];
     n[4] = -6.0 * g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6];
-    n[5] = 2.0 * g[1] + 2.0 * g[2] - g[3] - g[4] - g[5] - g[6];
+    n[5] = iscale<1>(g[1]) + iscale<1>(g[2]) - g[3] - g[4] - g[5] - g[6];
     n[6] = g[3] + g[4] - g[5] - g[6];
     neq[0] = T;
     neq[1] = Bx;
@@ -310,31 +335,52 @@ __device__ __forceinline__ void collideT_3d(const double* g, double u, double v,
     n_post[4] = n[4] - q[4] * (n[4] - neq[4]);
     n_post[5] = n[5] - q[5] * (n[5] - neq[5]);
     n_post[6] = n[6] - q[6] * (n[6] - neq[6]);
+    const double h1 = iscale<-1>(n_post[1]), h2 = iscale<-1>(n_post[2]), h3 = iscale<-1>(n_post[3]);
+    const double q6 = iscale<-2>(n_post[6]);
     gp[0] = divc(n_post[0], 7.0) - divc(n_post[4], 7.0);
-    gp[1] = divc(n_post[0], 7.0) + n_post[1] / 2.0 + divc(n_post[4], 42.0) + divc(n_post[5], 6.0);
-    gp[2] = divc(n_post[0], 7.0) - n_post[1] / 2.0 + divc(n_post[4], 42.0) + divc(n_post[5], 6.0);
-    gp[3] = divc(n_post[0], 7.0) + n_post[2] / 2.0 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) + n_post[6] / 4.0;
-    gp[4] = divc(n_post[0], 7.0) - n_post[2] / 2.0 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) + n_post[6] / 4.0;
-    gp[5] = divc(n_post[0], 7.0) + n_post[3] / 2.0 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) - n_post[6] / 4.0;
-    gp[6] = divc(n_post[0], 7.0) - n_post[3] / 2.0 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) - n_post[6] / 4.0;
+    gp[1] = divc(n_post[0], 7.0) + h1 + divc(n_post[4], 42.0) + divc(n_post[5], 6.0);
+    gp[2] = divc(n_post[0], 7.0) - h1 + divc(n_post[4], 42.0) + divc(n_post[5], 6.0);
+    gp[3] = divc(n_post[0], 7.0) + h2 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) + q6;
+    gp[4] = divc(n_post[0], 7.0) - h2 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) + q6;
+    gp[5] = divc(n_post[0], 7.0) + h3 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) - q6;
+    gp[6] = divc(n_post[0], 7.0) - h3 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) - q6;
 }
 
 // macro (2DRB.F90:884-889): u = (sum e f + Fx/2)/rho with the force stored by collision.
-__device__ __forceinline__ void macro_2d(const double* F, double Fx, double Fy, double& rho, double& u, double& v) {
+// jx, jy: the momentum sums before the force term (the reference's left-to-right order
+// adds it last).
+__device__ __forceinline__ void macro_2d(const double* F, double Fx, double Fy, double& rho, double& u, double& v,
+                                         double& jx, double& jy) {
     rho = F[0] + F[1] + F[2] + F[3] + F[4] + F[5] + F[6] + F[7] + F[8];
-    u = (F[1] - F[3] + F[5] - F[6] - F[7] + F[8] + 0.5 * Fx) / rho;
-    v = (F[2] - F[4] + F[5] + F[6] - F[7] - F[8] + 0.5 * Fy) / rho;
+    jx = F[1] - F[3] + F[5] - F[6] - F[7] + F[8];
+    jy = F[2] - F[4] + F[5] + F[6] - F[7] - F[8];
+    u = (jx + iscale<-1>(Fx)) / rho;
+    v = (jy + iscale<-1>(Fy)) / rho;
+}
+
+__device__ __forceinline__ void macro_2d(const double* F, double Fx, double Fy, double& rho, double& u, double& v) {
+    double jx, jy;
+    macro_2d(F, Fx, Fy, rho, u, v, jx, jy);
 }
 
 // macro (3DRB.F90:1077-1092): F_y recomputed with the new rho and the lagged T.
 __device__ __forceinline__ void macro_3d(const double* f, double Tlag, const PhysC& P, double& rho, double& u,
-                                         double& v, double& w) {
+                                         double& v, double& w, double& jx, double& jy, double& jz) {
     rho = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14]
           + f[15] + f[16] + f[17] + f[18];
     const double FyLoc = rho * P.gBeta * (Tlag - P.Tref);
-    u = (f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14]) / rho;
-    v = (f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18] + 0.5 * FyLoc) / rho;
-    w = (f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18]) / rho;
+    jx = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+    jy = f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
+    jz = f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
+    u = jx / rho;
+    v = (jy + iscale<-1>(FyLoc)) / rho;
+    w = jz / rho;
+}
+
+__device__ __forceinline__ void macro_3d(const double* f, double Tlag, const PhysC& P, double& rho, double& u,
+                                         double& v, double& w) {
+    double jx, jy, jz;
+    macro_3d(f, Tlag, P, rho, u, v, w, jx, jy, jz);
 }
 
 template <int QT>
@@ -581,6 +627,47 @@ __global__ void k_macroT(Geo g, const double* __restrict__ gg, double* __restric
 // ------------------------------------------------------------------------------------
 // Fused step kernels
 // ------------------------------------------------------------------------------------
+// Macro step of f_n (with the 2D force F_n or the 3D lag T_{n-1}) and the thermal
+// collision of one cell.  The macro results (rho, u and the momentum sums) go to the module
+// arrays: the next flow kernel pulls the same f_n and uses them instead of repeating the
+// macro step (three IEEE divisions and 45 additions per cell in 3D, on GB300's narrow FP64
+// pipe), and the module rho and u are those of step n as the reference's macro leaves them.
+template <int D>
+__device__ __forceinline__ void thermal_cell(const PhysC& P, const ExactArrays& A, long long c, const double* F,
+                                             const double* G, double Tprev, double* GP) {
+    if (D == 2) {
+        double rho, u, v, jx, jy, Bx, By;
+        macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v, jx, jy);
+        collideT_2d(G, u, v, Tprev, A.Bx[c], A.By[c], P, GP, Bx, By);
+        if (P.use_g) {
+            A.Bx[c] = Bx;
+            A.By[c] = By;
+        }
+        A.rho[c] = rho;
+        A.u[c] = u;
+        A.v[c] = v;
+        A.jx[c] = jx;
+        A.jy[c] = jy;
+    } else {
+        double rho, u, v, w, jx, jy, jz, Bx, By, Bz;
+        macro_3d(F, Tprev, P, rho, u, v, w, jx, jy, jz);
+        collideT_3d(G, u, v, w, Tprev, A.Bx[c], A.By[c], A.Bz[c], P, GP, Bx, By, Bz);
+        if (P.use_g) {
+            A.Bx[c] = Bx;
+            A.By[c] = By;
+            A.Bz[c] = Bz;
+        }
+        A.Tlag[c] = Tprev;
+        A.rho[c] = rho;
+        A.u[c] = u;
+        A.v[c] = v;
+        A.w[c] = w;
+        A.jx[c] = jx;
+        A.jy[c] = jy;
+        A.jz[c] = jz;
+    }
+}
+
 // Flow collision of step n (A_n in the reference's order).  FIRST: the inputs are the
 // reference's module arrays after `initial` or after a materialisation; otherwise they
 // are rebuilt from the fused buffers: f_{n-1} = pull(f_post_{n-1}), T_{n-1} =
@@ -594,14 +681,13 @@ __global__ void __launch_bounds__(128) k_flow(Geo g, PhysC P, ExactArrays A, con
     if (!thread_cell(g, c, i, j, k)) return;
     constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
     const long long n = g.ncell;
-    double F[Q], FP[Q], rho, u, v, w = 0.0, T;
+    double F[Q], FP[Q], T, jx = 0.0, jy = 0.0, jz = 0.0;
+    // rho and u: the module arrays after initial / a materialisation, otherwise the thermal
+    // kernel's macro step of the same f_{n-1} (with the same lag), stored with its sums
+    const double rho = A.rho[c], u = A.u[c], v = A.v[c], w = D == 3 ? A.w[c] : 0.0;
     if (FIRST) {
 #pragma unroll
         for (int a = 0; a < Q; ++a) F[a] = A.f[a * n + c];
-        rho = A.rho[c];
-        u = A.u[c];
-        v = A.v[c];
-        if (D == 3) w = A.w[c];
         T = A.T[c];
     } else {
         auto lf = [&](int a, long long cc) { return fin[a * n + cc]; };
@@ -612,16 +698,17 @@ __global__ void __launch_bounds__(128) k_flow(Geo g, PhysC P, ExactArrays A, con
 #pragma unroll
         for (int a = 0; a < QT; ++a) G[a] = pull_thermal<QT, double>(g, a, i, j, k, c, lg);
         T = sumT<QT>(G);
-        if (D == 2) macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
-        else macro_3d(F, A.Tlag[c], P, rho, u, v, w);
+        jx = A.jx[c];
+        jy = A.jy[c];
+        if (D == 3) jz = A.jz[c];
     }
     if (D == 2) {
         double Fx, Fy;
-        collide_2d(F, rho, u, v, T, P, FP, Fx, Fy);
+        collide_2d<!FIRST>(F, rho, u, v, T, P, FP, Fx, Fy, jx, jy);
         A.Fx[c] = Fx;
         A.Fy[c] = Fy;
     } else {
-        collide_3d(F, rho, u, v, w, T, P, FP);
+        collide_3d<!FIRST>(F, rho, u, v, w, T, P, FP, jx, jy, jz);
     }
 #pragma unroll
     for (int a = 0; a < Q; ++a) fout[a * n + c] = FP[a];
@@ -652,25 +739,7 @@ __global__ void __launch_bounds__(128) k_thermal(Geo g, PhysC P, ExactArrays A, 
         for (int a = 0; a < QT; ++a) G[a] = pull_thermal<QT, double>(g, a, i, j, k, c, lg);
         Tprev = sumT<QT>(G);
     }
-    if (D == 2) {
-        double rho, u, v, Bx, By;
-        macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
-        collideT_2d(G, u, v, Tprev, A.Bx[c], A.By[c], P, GP, Bx, By);
-        if (P.use_g) {
-            A.Bx[c] = Bx;
-            A.By[c] = By;
-        }
-    } else {
-        double rho, u, v, w, Bx, By, Bz;
-        macro_3d(F, Tprev, P, rho, u, v, w);
-        collideT_3d(G, u, v, w, Tprev, A.Bx[c], A.By[c], A.Bz[c], P, GP, Bx, By, Bz);
-        if (P.use_g) {
-            A.Bx[c] = Bx;
-            A.By[c] = By;
-            A.Bz[c] = Bz;
-        }
-        A.Tlag[c] = Tprev;
-    }
+    thermal_cell<D>(P, A, c, F, G, Tprev, GP);
 #pragma unroll
     for (int a = 0; a < QT; ++a) gout[a * n + c] = GP[a];
 }
@@ -743,11 +812,12 @@ __global__ void __launch_bounds__(128) k_aa_flow(Geo g, PhysC P, ExactArrays A, 
 #pragma unroll
         for (int a = 0; a < Q; ++a) F[a] = __ldg(f + a * n + c);
     }
+    double jx = 0.0, jy = 0.0, jz = 0.0;
+    rho = A.rho[c];  // the module arrays, or the thermal kernel's macro step of the same f
+    u = A.u[c];
+    v = A.v[c];
+    if (D == 3) w = A.w[c];
     if (FIRST) {
-        rho = A.rho[c];
-        u = A.u[c];
-        v = A.v[c];
-        if (D == 3) w = A.w[c];
         T = A.T[c];
     } else {
         double G[QT];
@@ -761,16 +831,17 @@ __global__ void __launch_bounds__(128) k_aa_flow(Geo g, PhysC P, ExactArrays A, 
             for (int a = 0; a < QT; ++a) G[a] = aa_local_thermal<QT, double>(g, a, i, j, k, c, graw != 0, lg);
         }
         T = sumT<QT>(G);
-        if (D == 2) macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
-        else macro_3d(F, A.Tlag[c], P, rho, u, v, w);
+        jx = A.jx[c];
+        jy = A.jy[c];
+        if (D == 3) jz = A.jz[c];
     }
     if (D == 2) {
         double Fx, Fy;
-        collide_2d(F, rho, u, v, T, P, FP, Fx, Fy);
+        collide_2d<!FIRST>(F, rho, u, v, T, P, FP, Fx, Fy, jx, jy);
         A.Fx[c] = Fx;
         A.Fy[c] = Fy;
     } else {
-        collide_3d(F, rho, u, v, w, T, P, FP);
+        collide_3d<!FIRST>(F, rho, u, v, w, T, P, FP, jx, jy, jz);
     }
     if (ODD) {
         auto st = [&](int b, long long cc, double val) { f[b * n + cc] = val; };
@@ -812,25 +883,7 @@ __global__ void __launch_bounds__(128) k_aa_thermal(Geo g, PhysC P, ExactArrays 
         for (int a = 0; a < QT; ++a) G[a] = aa_local_thermal<QT, double>(g, a, i, j, k, c, graw != 0, lg);
     }
     const double Tprev = FIRST ? A.T[c] : sumT<QT>(G);
-    if (D == 2) {
-        double rho, u, v, Bx, By;
-        macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v);
-        collideT_2d(G, u, v, Tprev, A.Bx[c], A.By[c], P, GP, Bx, By);
-        if (P.use_g) {
-            A.Bx[c] = Bx;
-            A.By[c] = By;
-        }
-    } else {
-        double rho, u, v, w, Bx, By, Bz;
-        macro_3d(F, Tprev, P, rho, u, v, w);
-        collideT_3d(G, u, v, w, Tprev, A.Bx[c], A.By[c], A.Bz[c], P, GP, Bx, By, Bz);
-        if (P.use_g) {
-            A.Bx[c] = Bx;
-            A.By[c] = By;
-            A.Bz[c] = Bz;
-        }
-        A.Tlag[c] = Tprev;
-    }
+    thermal_cell<D>(P, A, c, F, G, Tprev, GP);
     if (ODD) {
         auto st = [&](int b, long long cc, double val) { gg[b * n + cc] = val; };
 #pragma unroll
@@ -1127,6 +1180,74 @@ __global__ void k_selftest_divc(long long n, uint64_t seed, unsigned long long* 
 }
 
 }  // namespace lbm
+
+// ------------------------------------------------------------------------------------
+// self-test of the integer-pipe binary64 operations against the FP64 pipe
+// ------------------------------------------------------------------------------------
+namespace lbm {
+
+__device__ __forceinline__ uint64_t st_mix(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ bool same_bits(double a, double b) {
+    return (a != a && b != b) || __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+// Sample i: a random bit pattern, paired with (by i mod 4) a random pattern, one within 32
+// binades, one sharing leading significand bits (cancellation), or two values near the
+// bottom of the normal range (subnormal results).
+__global__ void k_selftest_int(long long n, uint64_t seed, unsigned long long* mismatches) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t a = st_mix(seed ^ (2 * (uint64_t)i)), b = st_mix(seed ^ (2 * (uint64_t)i + 1));
+    const int mode = (int)(i & 3);
+    if (mode >= 1) {
+        const long long ea = (long long)((a >> 52) & 0x7FF);
+        long long eb = ea + (long long)((b >> 58) & 63) - 32;
+        eb = eb < 0 ? 0 : (eb > 2046 ? 2046 : eb);
+        b = (b & ~(0x7FFULL << 52)) | ((uint64_t)eb << 52);
+    }
+    if (mode == 2) {
+        const uint64_t keep = st_mix(a) % 53;
+        b = (b & ~i64f::kMant) | ((a & i64f::kMant) ^ (st_mix(b) & ((1ULL << keep) - 1)));
+    }
+    if (mode == 3) {
+        a = (a & ~(0x7F0ULL << 52)) | (0x010ULL << 52);
+        b = (b & ~(0x7F0ULL << 52)) | (0x010ULL << 52);
+    }
+    const double x = __longlong_as_double((long long)a), y = __longlong_as_double((long long)b);
+    unsigned long long bad = 0;
+    bad += !same_bits(i64f::iadd(x, y), __dadd_rn(x, y));
+    bad += !same_bits(i64f::isub(x, y), __dsub_rn(x, y));
+    bad += !same_bits(iscale<1>(x), __dmul_rn(x, 2.0));
+    bad += !same_bits(iscale<2>(y), __dmul_rn(y, 4.0));
+    bad += !same_bits(iscale<3>(x), __dmul_rn(x, 8.0));
+    bad += !same_bits(iscale<-1>(y), __dmul_rn(y, 0.5));
+    bad += !same_bits(iscale<-2>(x), __dmul_rn(x, 0.25));
+    bad += !same_bits(iscale<-3>(y), __dmul_rn(y, 0.125));
+    if (bad) atomicAdd(mismatches, bad);
+}
+
+}  // namespace lbm
+
+extern "C" int lbm_selftest_int_arith(int64_t n, uint64_t seed, int64_t* mismatches) {
+    if (n <= 0 || !mismatches) return LBM_ERR_PARAM;
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, sizeof(*d)) != cudaSuccess) return LBM_ERR_OOM;
+    cudaMemset(d, 0, sizeof(*d));
+    lbm::k_selftest_int<<<(unsigned)((n + 255) / 256), 256>>>((long long)n, seed, d);
+    unsigned long long h = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return LBM_ERR_CUDA;
+    *mismatches = (int64_t)h;
+    return LBM_OK;
+}
 
 extern "C" int lbm_selftest_const_division(int64_t n, uint64_t seed, int64_t* mismatches) {
     if (n <= 0 || !mismatches) return LBM_ERR_PARAM;

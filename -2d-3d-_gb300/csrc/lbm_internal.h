@@ -18,6 +18,11 @@ struct PhysC {
     int use_g, legacy;
     int ha;                             // SideHeatedHa: magnetic force in the 2D collision
     double B2, sinphi, cosphi;          // B2sigemarho, sin(phi), cos(phi)
+    // Factors of the Guo source that depend on the rates only, rounded once on the host in
+    // the reference's order instead of once per cell: 3D (1 - Se/2)*38, (1 - Seps/2)*(-11),
+    // (1 - Sq/2)*(-2/3), 1 - Snu/2, 1 - Spi/2; 2D 6 - 3 Snu, 1 - Sq/2, 2 - Snu (and 1 - Snu/2).
+    double hSe38, hSeps11, hSq23, hSnu, hSpi;
+    double h6Snu, hSq, h2Snu;
 };
 
 // Inputs of `initial` that depend on host-side math (sin/cos of the RB perturbation).
@@ -39,6 +44,10 @@ struct ExactArrays {
     double *Bx, *By, *Bz;
     double *Fx, *Fy;   // 2D: force stored by collision
     double *Tlag;      // 3D fused: T of the previous step
+    // fused: the momentum sums sum_a e_a f_a of the last macro step (no force term), written
+    // by the thermal kernel of step n and read by the flow kernel of step n+1, which pulls
+    // the same f_n: they are its moments m3, m5, m7 (and rho its m0), bit for bit
+    double *jx, *jy, *jz;
     double *up, *vp, *wp, *Tp;
 };
 

@@ -246,6 +246,12 @@ int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, double* ms_
  * compares it bitwise with CUDA's IEEE division on n random normal doubles for each of the
  * 19 constants and returns the number of mismatches (expected 0). */
 int lbm_selftest_const_division(int64_t n, uint64_t seed, int64_t* mismatches);
+/* Self-test (no counterpart in the reference): the plain method computes its products with
+ * exact powers of two (2x, x/4, -0.5x, ...) as exponent adds on the integer pipes; this
+ * compares those, and an integer-pipe binary64 addition, bitwise with the FP64 pipe's
+ * results on n generated operand pairs (random, close exponents, cancellation, subnormal
+ * results) and returns the number of mismatches (expected 0). */
+int lbm_selftest_int_arith(int64_t n, uint64_t seed, int64_t* mismatches);
 
 /* ---- allocation-free diagnostic (no counterpart in the reference) -----------------------
  * For callers that cannot let a library call cudaMalloc: programs whose device memory is
