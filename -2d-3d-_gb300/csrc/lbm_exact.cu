@@ -102,20 +102,23 @@ __device__ __forceinline__ void collide_2d(const double* F, double rho, double u
 #pragma unroll
     for (int a = 0; a < 9; ++a) m_post[a] = m[a] - s[a] * (m[a] - meq[a]) + fSource[a];
 
-    const double q7 = iscale<-2>(m_post[7]), q8 = iscale<-2>(m_post[8]);  // m/4
-    FP[0] = divc(m_post[0], 9.0) - divc(m_post[1], 9.0) + divc(m_post[2], 9.0);
-    FP[1] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) + divc(m_post[3], 6.0) - divc(m_post[4], 6.0) + q7;
-    FP[2] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) + divc(m_post[5], 6.0) - divc(m_post[6], 6.0) - q7;
-    FP[3] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) - divc(m_post[3], 6.0) + divc(m_post[4], 6.0) + q7;
-    FP[4] = divc(m_post[0], 9.0) - divc(m_post[1], 36.0) - divc(m_post[2], 18.0) - divc(m_post[5], 6.0) + divc(m_post[6], 6.0) - q7;
-    FP[5] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) + divc(m_post[3], 6.0) + divc(m_post[4], 12.0)
-            + divc(m_post[5], 6.0) + divc(m_post[6], 12.0) + q8;
-    FP[6] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) - divc(m_post[3], 6.0) - divc(m_post[4], 12.0)
-            + divc(m_post[5], 6.0) + divc(m_post[6], 12.0) - q8;
-    FP[7] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) - divc(m_post[3], 6.0) - divc(m_post[4], 12.0)
-            - divc(m_post[5], 6.0) - divc(m_post[6], 12.0) + q8;
-    FP[8] = divc(m_post[0], 9.0) + divc(m_post[1], 18.0) + divc(m_post[2], 36.0) + divc(m_post[3], 6.0) + divc(m_post[4], 12.0)
-            - divc(m_post[5], 6.0) - divc(m_post[6], 12.0) - q8;
+    // m/4 as exponent adds; x/(c 2^k) = RN(x/c) 2^-k, one exact multiply, for a normal quotient
+    const double q7 = iscale<-2>(m_post[7]), q8 = iscale<-2>(m_post[8]);
+    const double e1 = divc(m_post[1], 9.0), e2 = divc(m_post[2], 9.0), e4 = divc(m_post[4], 6.0),
+                 e6 = divc(m_post[6], 6.0);
+    FP[0] = divc(m_post[0], 9.0) - e1 + e2;
+    FP[1] = divc(m_post[0], 9.0) - __dmul_rn(e1, 0.25) - __dmul_rn(e2, 0.5) + divc(m_post[3], 6.0) - e4 + q7;
+    FP[2] = divc(m_post[0], 9.0) - __dmul_rn(e1, 0.25) - __dmul_rn(e2, 0.5) + divc(m_post[5], 6.0) - e6 - q7;
+    FP[3] = divc(m_post[0], 9.0) - __dmul_rn(e1, 0.25) - __dmul_rn(e2, 0.5) - divc(m_post[3], 6.0) + e4 + q7;
+    FP[4] = divc(m_post[0], 9.0) - __dmul_rn(e1, 0.25) - __dmul_rn(e2, 0.5) - divc(m_post[5], 6.0) + e6 - q7;
+    FP[5] = divc(m_post[0], 9.0) + __dmul_rn(e1, 0.5) + __dmul_rn(e2, 0.25) + divc(m_post[3], 6.0) + __dmul_rn(e4, 0.5)
+            + divc(m_post[5], 6.0) + __dmul_rn(e6, 0.5) + q8;
+    FP[6] = divc(m_post[0], 9.0) + __dmul_rn(e1, 0.5) + __dmul_rn(e2, 0.25) - divc(m_post[3], 6.0) - __dmul_rn(e4, 0.5)
+            + divc(m_post[5], 6.0) + __dmul_rn(e6, 0.5) - q8;
+    FP[7] = divc(m_post[0], 9.0) + __dmul_rn(e1, 0.5) + __dmul_rn(e2, 0.25) - divc(m_post[3], 6.0) - __dmul_rn(e4, 0.5)
+            - divc(m_post[5], 6.0) - __dmul_rn(e6, 0.5) + q8;
+    FP[8] = divc(m_post[0], 9.0) + __dmul_rn(e1, 0.5) + __dmul_rn(e2, 0.25) + divc(m_post[3], 6.0) + __dmul_rn(e4, 0.5)
+            - divc(m_post[5], 6.0) - __dmul_rn(e6, 0.5) - q8;
 }
 
 // collision (3DRB.F90:704-943).  KNOWN: rhoLoc, jx, jy, jz are the macro step's sums of
@@ -214,44 +217,51 @@ __device__ __forceinline__ void collide_3d(const double* f, double rhoLoc, doubl
 #pragma unroll
     for (int a = 16; a <= 18; ++a) mp[a] = m[a] - s[a] * m[a];
 
-    // m/4 and m/8 as exponent adds
+    // m/4 and m/8 as exponent adds.  A moment divided by c and by c 2^k shares the division:
+    // RN(x / (c 2^k)) = RN(x / c) 2^-k whenever the quotient is normal (as divc itself
+    // assumes), so the second quotient is one exact FP64 multiply instead of three
+    // operations.  (An exponent add there measured slower: its rare-case branch sits
+    // between two FP64 operations of every reconstruction sum.)
+    const double d2 = divc(mp[2], 63.0), d4 = divc(mp[4], 10.0), d6 = divc(mp[6], 10.0), d8 = divc(mp[8], 10.0);
+    const double d9 = divc(mp[9], 18.0), d10 = divc(mp[10], 18.0), d12 = divc(mp[12], 12.0);
+    const double d1b = divc(iscale<2>(mp[1]), 1197.0);  // (4 mp1) / 1197
     const double q13 = iscale<-2>(mp[13]), q14 = iscale<-2>(mp[14]), q15 = iscale<-2>(mp[15]);
     const double q16 = iscale<-3>(mp[16]), q17 = iscale<-3>(mp[17]), q18 = iscale<-3>(mp[18]);
     fp[0] = divc(mp[0], 19.0) - divc(5.0 * mp[1], 399.0) + divc(mp[2], 21.0);
-    fp[1] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) + divc(mp[3], 10.0) - divc(mp[4], 10.0) + divc(mp[9], 18.0) - divc(mp[10], 18.0);
-    fp[2] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) - divc(mp[3], 10.0) + divc(mp[4], 10.0) + divc(mp[9], 18.0) - divc(mp[10], 18.0);
-    fp[3] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) + divc(mp[5], 10.0) - divc(mp[6], 10.0) - divc(mp[9], 36.0) + divc(mp[10], 36.0)
-            + divc(mp[11], 12.0) - divc(mp[12], 12.0);
-    fp[4] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) - divc(mp[5], 10.0) + divc(mp[6], 10.0) - divc(mp[9], 36.0) + divc(mp[10], 36.0)
-            + divc(mp[11], 12.0) - divc(mp[12], 12.0);
-    fp[5] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) + divc(mp[7], 10.0) - divc(mp[8], 10.0) - divc(mp[9], 36.0) + divc(mp[10], 36.0)
-            - divc(mp[11], 12.0) + divc(mp[12], 12.0);
-    fp[6] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - divc(mp[2], 63.0) - divc(mp[7], 10.0) + divc(mp[8], 10.0) - divc(mp[9], 36.0) + divc(mp[10], 36.0)
-            - divc(mp[11], 12.0) + divc(mp[12], 12.0);
-    fp[7] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0)
-            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) + q13 + q16 - q17;
-    fp[8] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0)
-            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) - q13 - q16 - q17;
-    fp[9] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0)
-            + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) - q13 + q16 + q17;
-    fp[10] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0)
-             + divc(mp[9], 36.0) + divc(mp[10], 72.0) + divc(mp[11], 12.0) + divc(mp[12], 24.0) + q13 - q16 + q17;
-    fp[11] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
-             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) + q15 - q16 + q18;
-    fp[12] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
-             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) - q15 + q16 + q18;
-    fp[13] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[3], 10.0) + divc(mp[4], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
-             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) - q15 - q16 - q18;
-    fp[14] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[3], 10.0) - divc(mp[4], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
-             + divc(mp[9], 36.0) + divc(mp[10], 72.0) - divc(mp[11], 12.0) - divc(mp[12], 24.0) + q15 + q16 - q18;
-    fp[15] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
-             - divc(mp[9], 18.0) - divc(mp[10], 36.0) + q14 + q17 - q18;
-    fp[16] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0) + divc(mp[7], 10.0) + divc(mp[8], 40.0)
-             - divc(mp[9], 18.0) - divc(mp[10], 36.0) - q14 - q17 - q18;
-    fp[17] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) + divc(mp[5], 10.0) + divc(mp[6], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
-             - divc(mp[9], 18.0) - divc(mp[10], 36.0) - q14 + q17 + q18;
-    fp[18] = divc(mp[0], 19.0) + divc(4.0 * mp[1], 1197.0) + divc(mp[2], 252.0) - divc(mp[5], 10.0) - divc(mp[6], 40.0) - divc(mp[7], 10.0) - divc(mp[8], 40.0)
-             - divc(mp[9], 18.0) - divc(mp[10], 36.0) + q14 - q17 + q18;
+    fp[1] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - d2 + divc(mp[3], 10.0) - d4 + d9 - d10;
+    fp[2] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - d2 - divc(mp[3], 10.0) + d4 + d9 - d10;
+    fp[3] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - d2 + divc(mp[5], 10.0) - d6 - __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.5)
+            + divc(mp[11], 12.0) - d12;
+    fp[4] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - d2 - divc(mp[5], 10.0) + d6 - __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.5)
+            + divc(mp[11], 12.0) - d12;
+    fp[5] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - d2 + divc(mp[7], 10.0) - d8 - __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.5)
+            - divc(mp[11], 12.0) + d12;
+    fp[6] = divc(mp[0], 19.0) - divc(11.0 * mp[1], 2394.0) - d2 - divc(mp[7], 10.0) + d8 - __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.5)
+            - divc(mp[11], 12.0) + d12;
+    fp[7] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) + divc(mp[3], 10.0) + __dmul_rn(d4, 0.25) + divc(mp[5], 10.0) + __dmul_rn(d6, 0.25)
+            + __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.25) + divc(mp[11], 12.0) + __dmul_rn(d12, 0.5) + q13 + q16 - q17;
+    fp[8] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) - divc(mp[3], 10.0) - __dmul_rn(d4, 0.25) + divc(mp[5], 10.0) + __dmul_rn(d6, 0.25)
+            + __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.25) + divc(mp[11], 12.0) + __dmul_rn(d12, 0.5) - q13 - q16 - q17;
+    fp[9] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) + divc(mp[3], 10.0) + __dmul_rn(d4, 0.25) - divc(mp[5], 10.0) - __dmul_rn(d6, 0.25)
+            + __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.25) + divc(mp[11], 12.0) + __dmul_rn(d12, 0.5) - q13 + q16 + q17;
+    fp[10] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) - divc(mp[3], 10.0) - __dmul_rn(d4, 0.25) - divc(mp[5], 10.0) - __dmul_rn(d6, 0.25)
+             + __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.25) + divc(mp[11], 12.0) + __dmul_rn(d12, 0.5) + q13 - q16 + q17;
+    fp[11] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) + divc(mp[3], 10.0) + __dmul_rn(d4, 0.25) + divc(mp[7], 10.0) + __dmul_rn(d8, 0.25)
+             + __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.25) - divc(mp[11], 12.0) - __dmul_rn(d12, 0.5) + q15 - q16 + q18;
+    fp[12] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) - divc(mp[3], 10.0) - __dmul_rn(d4, 0.25) + divc(mp[7], 10.0) + __dmul_rn(d8, 0.25)
+             + __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.25) - divc(mp[11], 12.0) - __dmul_rn(d12, 0.5) - q15 + q16 + q18;
+    fp[13] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) + divc(mp[3], 10.0) + __dmul_rn(d4, 0.25) - divc(mp[7], 10.0) - __dmul_rn(d8, 0.25)
+             + __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.25) - divc(mp[11], 12.0) - __dmul_rn(d12, 0.5) - q15 - q16 - q18;
+    fp[14] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) - divc(mp[3], 10.0) - __dmul_rn(d4, 0.25) - divc(mp[7], 10.0) - __dmul_rn(d8, 0.25)
+             + __dmul_rn(d9, 0.5) + __dmul_rn(d10, 0.25) - divc(mp[11], 12.0) - __dmul_rn(d12, 0.5) + q15 + q16 - q18;
+    fp[15] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) + divc(mp[5], 10.0) + __dmul_rn(d6, 0.25) + divc(mp[7], 10.0) + __dmul_rn(d8, 0.25)
+             - d9 - __dmul_rn(d10, 0.5) + q14 + q17 - q18;
+    fp[16] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) - divc(mp[5], 10.0) - __dmul_rn(d6, 0.25) + divc(mp[7], 10.0) + __dmul_rn(d8, 0.25)
+             - d9 - __dmul_rn(d10, 0.5) - q14 - q17 - q18;
+    fp[17] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) + divc(mp[5], 10.0) + __dmul_rn(d6, 0.25) - divc(mp[7], 10.0) - __dmul_rn(d8, 0.25)
+             - d9 - __dmul_rn(d10, 0.5) - q14 + q17 + q18;
+    fp[18] = divc(mp[0], 19.0) + d1b + __dmul_rn(d2, 0.25) - divc(mp[5], 10.0) - __dmul_rn(d6, 0.25) - divc(mp[7], 10.0) - __dmul_rn(d8, 0.25)
+             - d9 - __dmul_rn(d10, 0.5) + q14 - q17 + q18;
 }
 
 // collisionT (2DRB.F90:921-974).  B = (u T, v T); returns g_post and the new B.
@@ -336,14 +346,14 @@ __device__ __forceinline__ void collideT_3d(const double* g, double u, double v,
     n_post[5] = n[5] - q[5] * (n[5] - neq[5]);
     n_post[6] = n[6] - q[6] * (n[6] - neq[6]);
     const double h1 = iscale<-1>(n_post[1]), h2 = iscale<-1>(n_post[2]), h3 = iscale<-1>(n_post[3]);
-    const double q6 = iscale<-2>(n_post[6]);
+    const double q6 = iscale<-2>(n_post[6]), s5 = divc(n_post[5], 6.0);  // x/12 = RN(x/6) * 0.5
     gp[0] = divc(n_post[0], 7.0) - divc(n_post[4], 7.0);
-    gp[1] = divc(n_post[0], 7.0) + h1 + divc(n_post[4], 42.0) + divc(n_post[5], 6.0);
-    gp[2] = divc(n_post[0], 7.0) - h1 + divc(n_post[4], 42.0) + divc(n_post[5], 6.0);
-    gp[3] = divc(n_post[0], 7.0) + h2 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) + q6;
-    gp[4] = divc(n_post[0], 7.0) - h2 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) + q6;
-    gp[5] = divc(n_post[0], 7.0) + h3 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) - q6;
-    gp[6] = divc(n_post[0], 7.0) - h3 + divc(n_post[4], 42.0) - divc(n_post[5], 12.0) - q6;
+    gp[1] = divc(n_post[0], 7.0) + h1 + divc(n_post[4], 42.0) + s5;
+    gp[2] = divc(n_post[0], 7.0) - h1 + divc(n_post[4], 42.0) + s5;
+    gp[3] = divc(n_post[0], 7.0) + h2 + divc(n_post[4], 42.0) - __dmul_rn(s5, 0.5) + q6;
+    gp[4] = divc(n_post[0], 7.0) - h2 + divc(n_post[4], 42.0) - __dmul_rn(s5, 0.5) + q6;
+    gp[5] = divc(n_post[0], 7.0) + h3 + divc(n_post[4], 42.0) - __dmul_rn(s5, 0.5) - q6;
+    gp[6] = divc(n_post[0], 7.0) - h3 + divc(n_post[4], 42.0) - __dmul_rn(s5, 0.5) - q6;
 }
 
 // macro (2DRB.F90:884-889): u = (sum e f + Fx/2)/rho with the force stored by collision.
@@ -1229,6 +1239,19 @@ __global__ void k_selftest_int(long long n, uint64_t seed, unsigned long long* m
     bad += !same_bits(iscale<-1>(y), __dmul_rn(y, 0.5));
     bad += !same_bits(iscale<-2>(x), __dmul_rn(x, 0.25));
     bad += !same_bits(iscale<-3>(y), __dmul_rn(y, 0.125));
+    // a quotient by c 2^k as the quotient by c scaled (normal quotients): the divisor pairs
+    // of the collisions' inverse transforms
+    const unsigned ex = (unsigned)((a >> 52) & 0x7FF);
+    if (ex >= 64 && ex <= 1984) {
+        bad += !same_bits(iscale<-2>(__ddiv_rn(x, 10.0)), __ddiv_rn(x, 40.0));
+        bad += !same_bits(iscale<-1>(__ddiv_rn(x, 18.0)), __ddiv_rn(x, 36.0));
+        bad += !same_bits(iscale<-2>(__ddiv_rn(x, 18.0)), __ddiv_rn(x, 72.0));
+        bad += !same_bits(iscale<-1>(__ddiv_rn(x, 12.0)), __ddiv_rn(x, 24.0));
+        bad += !same_bits(iscale<-2>(__ddiv_rn(x, 63.0)), __ddiv_rn(x, 252.0));
+        bad += !same_bits(iscale<-1>(__ddiv_rn(x, 6.0)), __ddiv_rn(x, 12.0));
+        bad += !same_bits(iscale<-1>(__ddiv_rn(x, 9.0)), __ddiv_rn(x, 18.0));
+        bad += !same_bits(iscale<-2>(__ddiv_rn(x, 9.0)), __ddiv_rn(x, 36.0));
+    }
     if (bad) atomicAdd(mismatches, bad);
 }
 
