@@ -47,6 +47,20 @@ __device__ __forceinline__ double divc(double x, double c) {
     return __fma_rn(r, rc, q);
 }
 
+// x / b from y = RN(1/b) (CUDA's correctly rounded reciprocal) by Markstein's correction:
+// q = RN(x y), r = x - b q in one fma, RN(q + r y) is the correctly rounded x / b for every
+// normal quotient (Markstein 1990; checked exhaustively for 5- to 11-bit significands with
+// the remainder rounded as the fma rounds it, and against CUDA's division by
+// lbm_selftest_int_arith).  A zero numerator keeps q = RN(x y), which has the IEEE sign.
+// Several quotients by one b share the reciprocal: 3 FP64 operations each instead of a
+// full division.
+__device__ __forceinline__ double div_rcp(double x, double b, double y) {
+    const double q = __dmul_rn(x, y);
+    const double r = __fma_rn(-q, b, x);
+    const double qc = __fma_rn(r, y, q);
+    return (i64f::bits(x) & i64f::kAbs) == 0 ? q : qc;
+}
+
 // collision (2DRB.F90:688-759).  Writes f_post and the stored body force (Fx, Fy).
 // KNOWN: rho, jx, jy are the macro step's sums of these populations (m0, m3, m5 in the
 // same order), passed in instead of summed again.
@@ -364,8 +378,9 @@ __device__ __forceinline__ void macro_2d(const double* F, double Fx, double Fy, 
     rho = F[0] + F[1] + F[2] + F[3] + F[4] + F[5] + F[6] + F[7] + F[8];
     jx = F[1] - F[3] + F[5] - F[6] - F[7] + F[8];
     jy = F[2] - F[4] + F[5] + F[6] - F[7] - F[8];
-    u = (jx + iscale<-1>(Fx)) / rho;
-    v = (jy + iscale<-1>(Fy)) / rho;
+    const double y = __drcp_rn(rho);
+    u = div_rcp(jx + iscale<-1>(Fx), rho, y);
+    v = div_rcp(jy + iscale<-1>(Fy), rho, y);
 }
 
 __device__ __forceinline__ void macro_2d(const double* F, double Fx, double Fy, double& rho, double& u, double& v) {
@@ -382,9 +397,10 @@ __device__ __forceinline__ void macro_3d(const double* f, double Tlag, const Phy
     jx = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
     jy = f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
     jz = f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
-    u = jx / rho;
-    v = (jy + iscale<-1>(FyLoc)) / rho;
-    w = jz / rho;
+    const double y = __drcp_rn(rho);
+    u = div_rcp(jx, rho, y);
+    v = div_rcp(jy + iscale<-1>(FyLoc), rho, y);
+    w = div_rcp(jz, rho, y);
 }
 
 __device__ __forceinline__ void macro_3d(const double* f, double Tlag, const PhysC& P, double& rho, double& u,
@@ -1251,6 +1267,19 @@ __global__ void k_selftest_int(long long n, uint64_t seed, unsigned long long* m
         bad += !same_bits(iscale<-1>(__ddiv_rn(x, 6.0)), __ddiv_rn(x, 12.0));
         bad += !same_bits(iscale<-1>(__ddiv_rn(x, 9.0)), __ddiv_rn(x, 18.0));
         bad += !same_bits(iscale<-2>(__ddiv_rn(x, 9.0)), __ddiv_rn(x, 36.0));
+    }
+    // quotients through a shared correctly rounded reciprocal (div_rcp) against IEEE
+    // division: divisors across the whole normal range and near 1 (densities), numerators
+    // within 40 binades of them
+    {
+        const uint64_t bb = st_mix(a ^ 0x5555ULL);
+        const uint64_t ebits = (i & 1) ? (1021ULL + ((bb >> 60) & 3)) : (64 + (bb >> 52) % 1900);
+        const double den = __longlong_as_double((long long)((ebits << 52) | (bb & i64f::kMant)));  // positive
+        const uint64_t en = ebits + ((b >> 56) % 80) - 40;
+        const double num = __longlong_as_double((long long)((b & i64f::kSign) | (en << 52) | (a & i64f::kMant)));
+        const double yr = __drcp_rn(den);
+        bad += !same_bits(div_rcp(num, den, yr), __ddiv_rn(num, den));
+        bad += !same_bits(div_rcp(-0.0, den, yr), __ddiv_rn(-0.0, den));
     }
     if (bad) atomicAdd(mismatches, bad);
 }

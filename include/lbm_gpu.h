@@ -251,8 +251,9 @@ int lbm_selftest_const_division(int64_t n, uint64_t seed, int64_t* mismatches);
  * compares those, and an integer-pipe binary64 addition, bitwise with the FP64 pipe's
  * results on n generated operand pairs (random, close exponents, cancellation, subnormal
  * results), together with the identity x/(c 2^k) = (x/c) 2^-k for the divisor pairs of the
- * collisions (10/40, 18/36, 18/72, 12/24, 63/252, 6/12, 9/18, 9/36) on normal quotients,
- * and returns the number of mismatches (expected 0). */
+ * collisions (10/40, 18/36, 18/72, 12/24, 63/252, 6/12, 9/18, 9/36) on normal quotients and
+ * the macro step's quotients through one shared correctly rounded reciprocal (x/rho, y/rho,
+ * ...) against IEEE division, and returns the number of mismatches (expected 0). */
 int lbm_selftest_int_arith(int64_t n, uint64_t seed, int64_t* mismatches);
 
 /* ---- allocation-free diagnostic (no counterpart in the reference) -----------------------
