@@ -278,7 +278,9 @@ __device__ __forceinline__ void collide_3d(const double* f, double rhoLoc, doubl
              - d9 - __dmul_rn(d10, 0.5) + q14 - q17 + q18;
 }
 
-// collisionT (2DRB.F90:921-974).  B = (u T, v T); returns g_post and the new B.
+// collisionT (2DRB.F90:921-974).  B = (u T, v T); returns g_post and the new B.  KNOWN: T is
+// the sum of these populations in the same order (n0), passed in instead of summed again.
+template <bool KNOWN = false>
 __device__ __forceinline__ void collideT_2d(const double* G, double u, double v, double T, double Bxp, double Byp,
                                             const PhysC& P, double* GP, double& BxOut, double& ByOut) {
     double n[5], neq[5], q[5], n_post[5];
@@ -294,7 +296,7 @@ __device__ __forceinline__ void collideT_2d(const double* G, double u, double v,
     }
     BxOut = Bx;
     ByOut = By;
-    n[0] = G[0] + G[1] + G[2] + G[3] + G[4];
+    n[0] = KNOWN ? T : G[0] + G[1] + G[2] + G[3] + G[4];
     n[1] = G[1] - G[3];
     n[2] = G[2] - G[4];
     n[3] = -iscale<2>(G[0]) + G[1] + G[2] + G[3] + G[4];
@@ -318,7 +320,8 @@ __device__ __forceinline__ void collideT_2d(const double* G, double u, double v,
     GP[4] = 0.2 * n_post[0] - h2 + 0.05 * n_post[3] - q4;
 }
 
-// collisionT (3DRB.F90:1121-1191).
+// collisionT (3DRB.F90:1121-1191).  KNOWN as in collideT_2d.
+template <bool KNOWN = false>
 __device__ __forceinline__ void collideT_3d(const double* g, double u, double v, double w, double T, double Bxp,
                                             double Byp, double Bzp, const PhysC& P, double* gp, double& BxOut,
                                             double& ByOut, double& BzOut) {
@@ -337,7 +340,7 @@ __device__ __forceinline__ void collideT_3d(const double* g, double u, double v,
     BxOut = Bx;
     ByOut = By;
     BzOut = Bz;
-    n[0] = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6];
+    n[0] = KNOWN ? T : g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6];
     n[1] = g[1] - g[2];
     n[2] = g[3] - g[4];
     n[3] = g[5] - g[6];
@@ -658,13 +661,13 @@ __global__ void k_macroT(Geo g, const double* __restrict__ gg, double* __restric
 // arrays: the next flow kernel pulls the same f_n and uses them instead of repeating the
 // macro step (three IEEE divisions and 45 additions per cell in 3D, on GB300's narrow FP64
 // pipe), and the module rho and u are those of step n as the reference's macro leaves them.
-template <int D>
+template <int D, bool KNOWN>
 __device__ __forceinline__ void thermal_cell(const PhysC& P, const ExactArrays& A, long long c, const double* F,
                                              const double* G, double Tprev, double* GP) {
     if (D == 2) {
         double rho, u, v, jx, jy, Bx, By;
         macro_2d(F, A.Fx[c], A.Fy[c], rho, u, v, jx, jy);
-        collideT_2d(G, u, v, Tprev, A.Bx[c], A.By[c], P, GP, Bx, By);
+        collideT_2d<KNOWN>(G, u, v, Tprev, A.Bx[c], A.By[c], P, GP, Bx, By);
         if (P.use_g) {
             A.Bx[c] = Bx;
             A.By[c] = By;
@@ -677,7 +680,7 @@ __device__ __forceinline__ void thermal_cell(const PhysC& P, const ExactArrays& 
     } else {
         double rho, u, v, w, jx, jy, jz, Bx, By, Bz;
         macro_3d(F, Tprev, P, rho, u, v, w, jx, jy, jz);
-        collideT_3d(G, u, v, w, Tprev, A.Bx[c], A.By[c], A.Bz[c], P, GP, Bx, By, Bz);
+        collideT_3d<KNOWN>(G, u, v, w, Tprev, A.Bx[c], A.By[c], A.Bz[c], P, GP, Bx, By, Bz);
         if (P.use_g) {
             A.Bx[c] = Bx;
             A.By[c] = By;
@@ -724,6 +727,7 @@ __global__ void __launch_bounds__(128) k_flow(Geo g, PhysC P, ExactArrays A, con
 #pragma unroll
         for (int a = 0; a < QT; ++a) G[a] = pull_thermal<QT, double>(g, a, i, j, k, c, lg);
         T = sumT<QT>(G);
+        A.T[c] = T;  // T_{n-1}, the thermal kernel's n0 of the same pulled populations
         jx = A.jx[c];
         jy = A.jy[c];
         if (D == 3) jz = A.jz[c];
@@ -754,18 +758,17 @@ __global__ void __launch_bounds__(128) k_thermal(Geo g, PhysC P, ExactArrays A, 
     auto lf = [&](int a, long long cc) { return fin[a * n + cc]; };
 #pragma unroll
     for (int a = 0; a < Q; ++a) F[a] = pull_flow<Q, double>(g, a, i, j, k, c, lf);
-    double Tprev;
+    // T_{n-1}: the module T, or the flow kernel's sum of the same pulled g_{n-1}
+    const double Tprev = A.T[c];
     if (FIRST) {
 #pragma unroll
         for (int a = 0; a < QT; ++a) G[a] = A.g[a * n + c];
-        Tprev = A.T[c];
     } else {
         auto lg = [&](int a, long long cc) { return gin[a * n + cc]; };
 #pragma unroll
         for (int a = 0; a < QT; ++a) G[a] = pull_thermal<QT, double>(g, a, i, j, k, c, lg);
-        Tprev = sumT<QT>(G);
     }
-    thermal_cell<D>(P, A, c, F, G, Tprev, GP);
+    thermal_cell<D, !FIRST>(P, A, c, F, G, Tprev, GP);
 #pragma unroll
     for (int a = 0; a < QT; ++a) gout[a * n + c] = GP[a];
 }
@@ -857,6 +860,7 @@ __global__ void __launch_bounds__(128) k_aa_flow(Geo g, PhysC P, ExactArrays A, 
             for (int a = 0; a < QT; ++a) G[a] = aa_local_thermal<QT, double>(g, a, i, j, k, c, graw != 0, lg);
         }
         T = sumT<QT>(G);
+        A.T[c] = T;  // T_{n-1}, the thermal sweep's n0 of the same populations
         jx = A.jx[c];
         jy = A.jy[c];
         if (D == 3) jz = A.jz[c];
@@ -908,8 +912,8 @@ __global__ void __launch_bounds__(128) k_aa_thermal(Geo g, PhysC P, ExactArrays 
 #pragma unroll
         for (int a = 0; a < QT; ++a) G[a] = aa_local_thermal<QT, double>(g, a, i, j, k, c, graw != 0, lg);
     }
-    const double Tprev = FIRST ? A.T[c] : sumT<QT>(G);
-    thermal_cell<D>(P, A, c, F, G, Tprev, GP);
+    const double Tprev = A.T[c];  // the module T, or the flow sweep's sum of the same g_{n-1}
+    thermal_cell<D, !FIRST>(P, A, c, F, G, Tprev, GP);
     if (ODD) {
         auto st = [&](int b, long long cc, double val) { gg[b * n + cc] = val; };
 #pragma unroll
