@@ -1,28 +1,17 @@
-// lbm_fp64_int.cuh - binary64 addition and power-of-two scaling on the integer pipes.
+// lbm_fp64_int.cuh - binary64 products with exact powers of two on the integer pipes.
 //
-// GB300's FP64 vector pipe retires 2 thread instructions per clock per SM, while its
-// integer and logic pipes retire 64 or more per clock and sit idle in the plain method's
-// kernels (FP64-issue bound).  These functions compute IEEE-754 binary64 results, rounded to
-// nearest-even, with integer instructions only, so a kernel can move part of its additions
-// off the FP64 pipe and still return the same bits.
+// GB300's FP64 vector pipe retires 2 thread instructions per clock per SM and bounds the
+// plain method's kernels, while the integer pipes sit mostly idle beside it.  A product
+// with an exact power of two, x * 2^K, is an add to the exponent field whenever input and
+// result are normal numbers: the same bits as the FP64 multiply, a handful of integer
+// instructions that overlap with the FP64 work.
 //
-//   iadd(a, b)       a + b   correctly rounded for every finite input (normal, subnormal,
-//                            signed zeros, exact cancellation to +0), overflow to +-inf;
-//                            inf/NaN inputs give inf/NaN (NaN payloads are not specified).
-//   isub(a, b)       a - b = a + (-b) (a sign flip, as IEEE defines subtraction).
-//   iscale<K>(x)     x * 2^K, exact whenever the result is normal (an exponent add); a
-//                    subnormal or overflowing result takes a rounded slow path.
+//   iscale<K>(x)     x * 2^K rounded to nearest-even for every input: the exponent add for
+//                    normal results, zero unchanged, and a rounded slow path (a real branch,
+//                    taken only by subnormal inputs or results, overflow, inf and NaN).
 //
-// Method (the textbook alignment / guard-round-sticky addition): order the operands by
-// magnitude, place both significands with the hidden bit at bit 62 (10 guard bits below
-// the last place), shift the smaller right by the exponent difference with every bit
-// shifted out ORed into bit 0, add or subtract, move the leading one to bit 63 (but not
-// below the smallest normal exponent: such results are exact subnormals), and round the
-// 11 bits below the last place to nearest-even.  A sticky bit kept in bit 0 decides every
-// rounding the same way as the exact sum: the jammed value is odd, every rounding boundary
-// is even, and the exact value lies strictly between the same two even integers.  The
-// round-up carry of the 53-bit significand ripples into the exponent field by plain
-// integer addition of the packed word.
+// (An IEEE addition in integer arithmetic was measured as well: exact, but on GB300 it
+// competes with the FP64 pipe instead of adding to it, so additions stay on the FP64 pipe.)
 //
 // The functions are host-callable too; the host build is checked bit for bit against the
 // CPU's own binary64 arithmetic.
@@ -76,55 +65,6 @@ LBM_I64F_HD unsigned clz64(uint64_t x) {
     return x ? (unsigned)__builtin_clzll(x) : 64u;
 #endif
 }
-
-// x << n for n in [0, 64] (64 gives 0, as the PTX shift defines it).
-LBM_I64F_HD uint64_t shl64(uint64_t x, unsigned n) {
-#if defined(__CUDA_ARCH__)
-    uint64_t r;
-    asm("shl.b64 %0, %1, %2;" : "=l"(r) : "l"(x), "r"(n));
-    return r;
-#else
-    return n >= 64 ? 0 : x << n;
-#endif
-}
-
-// The sum of two binary64 bit patterns, rounded to nearest-even.
-LBM_I64F_HD uint64_t add_bits(uint64_t ua, uint64_t ub) {
-    const uint64_t ma = ua & kAbs, mb = ub & kAbs;
-    const bool swap = ma < mb;
-    const uint64_t x = swap ? ub : ua;  // the operand of larger magnitude carries the sign
-    const uint64_t mx = swap ? mb : ma;
-    const uint64_t my = swap ? ma : mb;
-    const unsigned ex = (unsigned)(mx >> 52), ey = (unsigned)(my >> 52);
-    const bool sub = (int64_t)(ua ^ ub) < 0;
-    // significands, hidden bit at bit 62; a subnormal has no hidden bit and exponent 1
-    const uint64_t fx = ((mx & kMant) | ((uint64_t)(ex != 0) << 52)) << 10;
-    const uint64_t fy = ((my & kMant) | ((uint64_t)(ey != 0) << 52)) << 10;
-    const unsigned exn = ex + (ex == 0), eyn = ey + (ey == 0);
-    unsigned d = exn - eyn;
-    d = d < 63 ? d : 63;  // fy < 2^63: a shift by 63 leaves only the sticky bit
-    const uint64_t lost = fy & ((1ull << d) - 1);
-    const uint64_t ya = (fy >> d) | (uint64_t)(lost != 0);
-    const uint64_t r = sub ? fx - ya : fx + ya;
-    const unsigned lz = clz64(r);
-    const unsigned sh = lz < exn ? lz : exn;  // stop at the subnormal range (exact there)
-    const uint64_t n = shl64(r, sh);
-    const uint64_t lsb = (n >> 11) & 1;
-    const uint64_t up = ((n & 0x7FF) + 0x3FF + lsb) >> 11;
-    uint64_t res = (((uint64_t)(exn - sh)) << 52) + (n >> 11) + up;
-    res |= x & kSign;
-    if (r == 0) res = ua & ub & kSign;  // x - x = +0; (-0) + (-0) = -0
-    if (ex >= 2046) {                     // overflow, infinities and NaNs
-        if (ex == 2047)
-            res = mx > kInf ? (x | kQuiet) : ((sub && my == kInf) ? (kInf | kQuiet) : x);
-        else if ((res & kAbs) >= kInf)
-            res = (x & kSign) | kInf;
-    }
-    return res;
-}
-
-LBM_I64F_HD double iadd(double a, double b) { return dbl(add_bits(bits(a), bits(b))); }
-LBM_I64F_HD double isub(double a, double b) { return dbl(add_bits(bits(a), bits(b) ^ kSign)); }
 
 // x * 2^k when the result is not normal (or x is subnormal): normalise, then round the
 // significand shifted into the subnormal range to nearest-even.

@@ -248,9 +248,8 @@ int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, double* ms_
 int lbm_selftest_const_division(int64_t n, uint64_t seed, int64_t* mismatches);
 /* Self-test (no counterpart in the reference): the plain method computes its products with
  * exact powers of two (2x, x/4, -0.5x, ...) as exponent adds on the integer pipes; this
- * compares those, and an integer-pipe binary64 addition, bitwise with the FP64 pipe's
- * results on n generated operand pairs (random, close exponents, cancellation, subnormal
- * results), together with the identity x/(c 2^k) = (x/c) 2^-k for the divisor pairs of the
+ * compares those bitwise with the FP64 pipe's products on n generated operands (random,
+ * subnormal results included), together with the identity x/(c 2^k) = (x/c) 2^-k for the divisor pairs of the
  * collisions (10/40, 18/36, 18/72, 12/24, 63/252, 6/12, 9/18, 9/36) on normal quotients and
  * the macro step's quotients through one shared correctly rounded reciprocal (x/rho, y/rho,
  * ...) against IEEE division, and returns the number of mismatches (expected 0). */

@@ -1,8 +1,8 @@
-"""Integer-pipe binary64 arithmetic, checked on the host: the exponent-add scaling that the
-plain method uses for its products with exact powers of two, and the integer addition
-(csrc/lbm_fp64_int.cuh), compiled as C++ and compared bit for bit with the CPU's IEEE-754
-arithmetic on about 23 M cases (fp64_int_check.cpp).  The device build is compared with the
-FP64 pipe by test_gpu_parity.py::test_integer_pipe_arithmetic_matches_fp64."""
+"""Integer-pipe binary64 scaling, checked on the host: the exponent add that the plain
+method uses for its products with exact powers of two (csrc/lbm_fp64_int.cuh), compiled as
+C++ and compared bit for bit with the CPU's IEEE-754 multiplication on 7 M operands plus
+the special values (fp64_int_check.cpp).  The device build is compared with the FP64 pipe
+by test_gpu_parity.py::test_integer_pipe_arithmetic_matches_fp64."""
 import os
 import shutil
 import subprocess
@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 
 
-def test_integer_binary64_matches_cpu(tmp_path):
+def test_power_of_two_scaling_matches_cpu(tmp_path):
     cxx = shutil.which("g++") or shutil.which("c++")
     if not cxx:
         pytest.skip("no C++ compiler")

@@ -234,9 +234,10 @@ def test_const_division_matches_ieee(gpu_lib):
 
 
 def test_integer_pipe_arithmetic_matches_fp64(gpu_lib):
-    """Products with exact powers of two (exponent adds on the integer pipes) and the
-    integer-pipe binary64 addition agree bit for bit with the FP64 pipe (2 x 16.7 M
-    operand pairs, including cancellation and subnormal results)."""
+    """Products with exact powers of two (exponent adds on the integer pipes), quotients by
+    c 2^k as scaled quotients by c, and quotients through a shared correctly rounded
+    reciprocal agree bit for bit with the FP64 pipe and IEEE division (2 x 16.7 M samples,
+    subnormal results of the scalings included)."""
     import ctypes as C
     fn = gpu_lib.lbm_selftest_int_arith
     fn.argtypes = [C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]
