@@ -49,9 +49,14 @@ __device__ __forceinline__ unsigned fmix32(unsigned h) {
 __device__ __forceinline__ unsigned sr_seed(unsigned long long tick, long long c, unsigned kind) {
     return fmix32((unsigned)c ^ fmix32((((unsigned)tick << 1) | kind) + 0x9E3779B9u));
 }
-// Random bits of directions 2j (low half) and 2j+1 (high half).
+// Random bits of directions 2j (low half) and 2j+1 (high half).  The seed is already a full
+// avalanche hash of (step, cell, set), uniform over 32 bits, so each word only needs to be a
+// distinct bijection of it: an offset, one multiply by an odd constant and an xorshift that
+// folds the well-mixed high product bits into the low ones (3 instructions, against 9 for
+// another full hash per word; the FP16 kernels are issue-bound at large lattices).
 __device__ __forceinline__ unsigned sr_word(unsigned seed, int j) {
-    return fmix32(seed ^ (0x9E3779B9u * (unsigned)(j + 1)));
+    const unsigned h = (seed + 0x9E3779B9u * (unsigned)(j + 1)) * 0x85EBCA6Bu;
+    return h ^ (h >> 15);
 }
 __device__ __forceinline__ unsigned cvt_rs_f16x2(float hi, float lo, unsigned rbits) {
     unsigned d;
