@@ -7,10 +7,13 @@
 //  * Stage kernels: one per reference subroutine (collision .. macroT), operating on the
 //    reference's module arrays (f, f_post, rho, u, v, w, T, ...), for stage-by-stage parity.
 //  * Fused step: two kernels per time step over SoA population buffers:
-//      k_flow    : pull f_post_{n-1} + boundary rule -> f_{n-1}; macro with the lagged
-//                  temperature; pull g_post_{n-1} -> T_{n-1}; MRT collision -> f_post_n.
-//      k_thermal : pull f_post_n -> f_n, rho_n, u_n; pull g_post_{n-1} -> g_{n-1}, T_{n-1};
-//                  thermal MRT collision with the M1G term -> g_post_n, B_prev, T lag.
+//      k_flow    : pull f_post_{n-1} + boundary rule -> f_{n-1}; pull g_post_{n-1} ->
+//                  T_{n-1}; MRT collision -> f_post_n, with rho, u and the momentum sums
+//                  of f_{n-1} from the previous thermal kernel's macro step (same values,
+//                  not recomputed).
+//      k_thermal : pull f_post_n -> f_n, macro -> rho_n, u_n (stored with the sums);
+//                  pull g_post_{n-1} -> g_{n-1} (T_{n-1} from the flow kernel); thermal MRT
+//                  collision with the M1G term -> g_post_n, B_prev, T lag.
 //    The reference's step order (collision, streaming, bounceback, macro, collisionT,
 //    streamingT, bouncebackT, macroT, 3DRB.F90:227-241) couples flow step n+1 to the
 //    thermal streaming of step n (a dependency cone of radius 2), so one pass per step
@@ -700,8 +703,9 @@ __device__ __forceinline__ void thermal_cell(const PhysC& P, const ExactArrays& 
 // Flow collision of step n (A_n in the reference's order).  FIRST: the inputs are the
 // reference's module arrays after `initial` or after a materialisation; otherwise they
 // are rebuilt from the fused buffers: f_{n-1} = pull(f_post_{n-1}), T_{n-1} =
-// sum pull(g_post_{n-1}), and u_{n-1} from f_{n-1} with the lag (3D: T_{n-2}; 2D: the
-// force F_{n-1} stored by the previous flow collision).
+// sum pull(g_post_{n-1}) (stored for the thermal kernel), and rho, u_{n-1} and the momentum
+// sums from the previous thermal kernel, which computed them from the same f_{n-1} with the
+// lag (3D: T_{n-2}; 2D: the force F_{n-1} stored by the previous flow collision).
 template <int D, bool FIRST>
 __global__ void __launch_bounds__(128) k_flow(Geo g, PhysC P, ExactArrays A, const double* __restrict__ fin,
                                               const double* __restrict__ gin, double* __restrict__ fout) {
@@ -745,7 +749,8 @@ __global__ void __launch_bounds__(128) k_flow(Geo g, PhysC P, ExactArrays A, con
 }
 
 // Streaming + boundary + macro of the flow and thermal collision of step n
-// (B_n .. D_n).  FIRST: g_{n-1} and T_{n-1} are the module arrays.
+// (B_n .. D_n).  FIRST: g_{n-1} and T_{n-1} are the module arrays; otherwise T_{n-1} is the
+// flow kernel's sum of the same pulled g_{n-1}.
 template <int D, bool FIRST>
 __global__ void __launch_bounds__(128) k_thermal(Geo g, PhysC P, ExactArrays A, const double* __restrict__ fin,
                                                  const double* __restrict__ gin, double* __restrict__ gout) {
