@@ -1093,25 +1093,31 @@ void exact_stage(int stage, const Geo& g, const PhysC& P, const ExactArrays& A, 
     }
 }
 
+// Threads per block of the fused step kernels: 128, or 32 on lattices below 65,536 cells,
+// where 128-thread blocks leave a few blocks per SM and the step waits for the SMs that
+// hold one block more than the others (the FP64 kernels are bound by each SM's FP64 pipe).
+static inline int step_block(const Geo& g) { return g.ncell < 65536 ? 32 : 128; }
+
 void exact_fused_step(const Geo& g, const PhysC& P, const ExactArrays& A, int dim, bool first, const double* fprev,
                       const double* gprev, double* fnext, double* gnext, cudaStream_t s, int part) {
-    const unsigned nb = nblocks(g.ncell, 128);
+    const int bs = step_block(g);
+    const unsigned nb = nblocks(g.ncell, bs);
     const bool fl = part != 1, th = part != 0;
     if (dim == 2) {
         if (first) {
-            if (fl) k_flow<2, true><<<nb, 128, 0, s>>>(g, P, A, fprev, gprev, fnext);
-            if (th) k_thermal<2, true><<<nb, 128, 0, s>>>(g, P, A, fnext, gprev, gnext);
+            if (fl) k_flow<2, true><<<nb, bs, 0, s>>>(g, P, A, fprev, gprev, fnext);
+            if (th) k_thermal<2, true><<<nb, bs, 0, s>>>(g, P, A, fnext, gprev, gnext);
         } else {
-            if (fl) k_flow<2, false><<<nb, 128, 0, s>>>(g, P, A, fprev, gprev, fnext);
-            if (th) k_thermal<2, false><<<nb, 128, 0, s>>>(g, P, A, fnext, gprev, gnext);
+            if (fl) k_flow<2, false><<<nb, bs, 0, s>>>(g, P, A, fprev, gprev, fnext);
+            if (th) k_thermal<2, false><<<nb, bs, 0, s>>>(g, P, A, fnext, gprev, gnext);
         }
     } else {
         if (first) {
-            if (fl) k_flow<3, true><<<nb, 128, 0, s>>>(g, P, A, fprev, gprev, fnext);
-            if (th) k_thermal<3, true><<<nb, 128, 0, s>>>(g, P, A, fnext, gprev, gnext);
+            if (fl) k_flow<3, true><<<nb, bs, 0, s>>>(g, P, A, fprev, gprev, fnext);
+            if (th) k_thermal<3, true><<<nb, bs, 0, s>>>(g, P, A, fnext, gprev, gnext);
         } else {
-            if (fl) k_flow<3, false><<<nb, 128, 0, s>>>(g, P, A, fprev, gprev, fnext);
-            if (th) k_thermal<3, false><<<nb, 128, 0, s>>>(g, P, A, fnext, gprev, gnext);
+            if (fl) k_flow<3, false><<<nb, bs, 0, s>>>(g, P, A, fprev, gprev, fnext);
+            if (th) k_thermal<3, false><<<nb, bs, 0, s>>>(g, P, A, fnext, gprev, gnext);
         }
     }
 }
@@ -1124,20 +1130,21 @@ static bool any_face(void* const face[3]) { return face[0] || face[1] || face[2]
 
 template <int D, bool FIRST>
 static void aa_step_d(const Geo& g, const PhysC& P, const ExactArrays& A, AAState& S, cudaStream_t s, int part) {
-    const unsigned nb = nblocks(g.ncell, 128);
+    const int bs = step_block(g);
+    const unsigned nb = nblocks(g.ncell, bs);
     const int raw = S.graw ? 1 : 0;
     if (part != 1) {
         if (S.fpar && any_face(S.face_f)) aa_snapshot(g, D == 3 ? 19 : 9, false, LBM_FP64, A.f, S.face_f, s);
         const AAFace<double> wf = aa_faces(S.face_f);
-        if (S.fpar) k_aa_flow<D, true, FIRST><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw);
-        else k_aa_flow<D, false, FIRST><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw);
+        if (S.fpar) k_aa_flow<D, true, FIRST><<<nb, bs, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw);
+        else k_aa_flow<D, false, FIRST><<<nb, bs, 0, s>>>(g, P, A, A.f, A.g, wf, S.gpar, raw);
         S.fpar ^= 1;
     }
     if (part != 0) {
         if (S.gpar && any_face(S.face_g)) aa_snapshot(g, D == 3 ? 7 : 5, true, LBM_FP64, A.g, S.face_g, s);
         const AAFace<double> wg = aa_faces(S.face_g);
-        if (S.gpar) k_aa_thermal<D, true, FIRST><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw);
-        else k_aa_thermal<D, false, FIRST><<<nb, 128, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw);
+        if (S.gpar) k_aa_thermal<D, true, FIRST><<<nb, bs, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw);
+        else k_aa_thermal<D, false, FIRST><<<nb, bs, 0, s>>>(g, P, A, A.f, A.g, wg, S.fpar, raw);
         if (S.gpar) S.graw = true;
         S.gpar ^= 1;
     }
