@@ -32,7 +32,11 @@ namespace lbm {
 using i64f::iscale;
 
 // ------------------------------------------------------------------------------------
-// Per-cell arithmetic, verbatim from the reference.
+// Per-cell arithmetic in the reference's expression order.  Every rounded operation of the
+// reference happens once, on the same operands; only operations that give the same bits by
+// another route take it (exact power-of-two products on the integer pipes, rate-only
+// factors rounded on the host, shared divisions and reciprocals, macro sums handed between
+// the kernels).
 // ------------------------------------------------------------------------------------
 
 // Division by one of the reference's integer constants c (all below 2^12), as the
