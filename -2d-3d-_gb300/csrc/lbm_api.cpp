@@ -48,6 +48,8 @@ struct lbm_handle {
     std::string err;
     int64_t itc = 0;
     bool initialised = false;
+    // convergence history: the reference's once-per-run flags (first_write, zone_started)
+    bool conv_started = false, conv_zone_started = false;
 
     // FP64 plain method
     ExactArrays A{};
@@ -764,6 +766,66 @@ extern "C" int lbm_check(lbm_handle* h, double* errU, double* errT) {
     if (s[4] != 0.0 || !std::isfinite(s[0]) || !std::isfinite(s[2]))
         return fail(h, LBM_ERR_DIVERGED, "non-finite field or rho <= 0 in " + std::to_string((long long)s[4]) + " cells");
     return LBM_OK;
+}
+
+// caseTag of check: '("Ra=",ES10.3E2,",nx=",I0,",ny=",I0[,",nz=",I0],",useG=",L1,",old=",L1)'
+// (2DRB.F90:1252-1253, 3DRB.F90:1523-1524).
+extern "C" int lbm_case_tag(const lbm_handle* h, char* buf, size_t len) {
+    if (!h || !buf) return LBM_ERR_PARAM;
+    char ra[32];
+    int st = lbm_format_fortran_es(h->p.Ra, 10, 3, 2, ra, sizeof(ra));
+    if (st != LBM_OK) return st;
+    std::string t = std::string("Ra=") + ra + ",nx=" + std::to_string(h->p.nx) + ",ny=" + std::to_string(h->p.ny);
+    if (h->dim == 3) t += ",nz=" + std::to_string(h->p.nz);
+    t += std::string(",useG=") + (h->p.use_g ? "T" : "F") + ",old=" + (h->p.legacy_thermal ? "T" : "F");
+    if (t.size() + 1 > len) return LBM_ERR_PARAM;
+    std::memcpy(buf, t.c_str(), t.size() + 1);
+    return LBM_OK;
+}
+
+extern "C" int lbm_append_convergence_tecplot(lbm_handle* h, const char* filename, int64_t itc, double errorU,
+                                              double errorT) {
+    if (!h || !filename) return LBM_ERR_PARAM;
+    const int st = lbm_append_convergence_tecplot_host(filename, h->conv_started ? 0 : 1, h->dim, itc, errorU, errorT);
+    h->conv_started = true;
+    return st == LBM_OK ? LBM_OK : fail(h, st, std::string("cannot write ") + filename);
+}
+
+extern "C" int lbm_append_convergence_master_tecplot(lbm_handle* h, const char* filename, const char* zone, int64_t itc,
+                                                     double errorU, double errorT) {
+    if (!h || !filename || !zone) return LBM_ERR_PARAM;
+    const int st = lbm_append_convergence_master_tecplot_host(filename, h->conv_zone_started ? 0 : 1, h->dim, zone, itc,
+                                                              errorU, errorT);
+    h->conv_zone_started = true;
+    return st == LBM_OK ? LBM_OK : fail(h, st, std::string("cannot write ") + filename);
+}
+
+// check as the reference's subroutine does it: the errors, then the record appended to the
+// run's file and (under the case tag) to the master file, then echoed to standard output
+// (2DRB.F90:1244-1258, 3DRB.F90:1511-1526).  A diverged field is still logged (its errors
+// are NaN) and reported as LBM_ERR_DIVERGED.
+extern "C" int lbm_check_log(lbm_handle* h, const char* dir, int echo, double* errU, double* errT) {
+    if (!h || !errU || !errT) return LBM_ERR_PARAM;
+    const int chk = lbm_check(h, errU, errT);
+    if (chk != LBM_OK && chk != LBM_ERR_DIVERGED) return chk;
+    const std::string d = (dir && *dir) ? std::string(dir) + "/" : std::string();
+    const bool d3 = h->dim == 3;
+    int st = lbm_append_convergence_tecplot(h, (d + (d3 ? "convergence3D.plt" : "convergence.plt")).c_str(), h->itc,
+                                            *errU, *errT);
+    if (st != LBM_OK) return st;
+    char tag[256];
+    if ((st = lbm_case_tag(h, tag, sizeof(tag))) != LBM_OK) return fail(h, st, "case tag");
+    st = lbm_append_convergence_master_tecplot(h, (d + (d3 ? "convergence_all_3D.plt" : "convergence_all.plt")).c_str(),
+                                               tag, h->itc, *errU, *errT);
+    if (st != LBM_OK) return st;
+    if (echo) {
+        char line[128];
+        if (lbm_convergence_line(h->itc, *errU, *errT, line, sizeof(line)) == LBM_OK) {
+            std::fputs(line, stdout);
+            std::fflush(stdout);
+        }
+    }
+    return chk;
 }
 
 extern "C" int lbm_calNuRe(lbm_handle* h, double* Nu, double* Re) {

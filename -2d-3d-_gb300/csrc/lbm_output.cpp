@@ -9,6 +9,8 @@
 //   calc_psi_vort_and_output   2DRB.F90:2657-2780, output_Tecplot_psi_vort 2DRB.F90:2782-2871
 //   output_psi_center_abs      2DRB.F90:3085-3165 (4-point Lagrange interpolation)
 //   spline_natural / splint    2DRB.F90:3000-3083 (the fine-grid |psi| search runs on the GPU)
+//   append_convergence_tecplot, append_convergence_master_tecplot  2DRB.F90:1269-1343,
+//     3DRB.F90:1533-1591 (formatted text: the convergence history that check appends)
 //
 // The Tecplot files are the reference's stream-access binary: "#!TDV101", int32 control
 // words, strings as one int32 per character and a 0, float32 zone / end-of-header markers,
@@ -576,6 +578,67 @@ int fetch(lbm_handle* h, Fields& F, bool with_T, bool with_rho) {
     return LBM_OK;
 }
 
+// ------------------------------------------------------------------------------------
+// Fortran formatted output of the convergence records.  ESw.d[Ee]: a minus sign for negative
+// values, one nonzero digit (0 for zero), '.', d digits, then the exponent: 'E', sign and two
+// digits; without Ee a three-digit exponent takes the place of the letter ("-100"); with Ee
+// exactly e digits.  NaN and Infinity are spelled out.  Iw right-justifies an integer in w
+// columns, I0 writes it in as few as it needs.  A value that does not fit its field is
+// written as w asterisks.  The decimal digits are the correctly rounded ones, as gfortran
+// and the C library both produce.
+// ------------------------------------------------------------------------------------
+std::string fit(const std::string& s, int w) {
+    if (w <= 0) return s;
+    if ((int)s.size() > w) return std::string((size_t)w, '*');
+    return std::string((size_t)(w - (int)s.size()), ' ') + s;
+}
+
+std::string fortran_es(double x, int w, int d, int e) {
+    if (std::isnan(x)) return fit("NaN", w);
+    if (std::isinf(x)) return fit(x < 0 ? "-Infinity" : "Infinity", w);
+    char buf[64];
+    std::snprintf(buf, sizeof(buf), "%.*E", d, x);
+    const std::string c(buf);
+    const size_t at = c.find('E');
+    const std::string mant = c.substr(0, at);
+    const char sign = c[at + 1];
+    std::string digits = c.substr(at + 2);
+    while (digits.size() > 2 && digits[0] == '0') digits.erase(0, 1);
+    std::string out;
+    if (e > 0) {
+        if ((int)digits.size() > e) return std::string((size_t)w, '*');
+        while ((int)digits.size() < e) digits.insert(0, "0");
+        out = mant + "E" + sign + digits;
+    } else {
+        out = digits.size() <= 2 ? mant + "E" + sign + digits : mant + sign + digits;
+    }
+    return fit(out, w);
+}
+
+std::string fortran_i(long long v, int w) { return fit(std::to_string(v), w); }
+
+// write(u,'(I12,1X,ES24.16,1X,ES24.16)') itc, errorU, errorT
+std::string convergence_line(long long itc, double errU, double errT) {
+    return fortran_i(itc, 12) + " " + fortran_es(errU, 24, 16, 0) + " " + fortran_es(errT, 24, 16, 0) + "\n";
+}
+
+bool file_exists(const char* path) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return false;
+    std::fclose(f);
+    return true;
+}
+
+// Write `text` to `path`: replacing the file (status='replace') or appending to an existing
+// one (status='old', position='append': a missing file is an error, as in the reference).
+int write_text(const char* path, const std::string& text, bool replace) {
+    if (!replace && !file_exists(path)) return LBM_ERR_IO;
+    FILE* f = std::fopen(path, replace ? "wb" : "ab");
+    if (!f) return LBM_ERR_IO;
+    const bool ok = std::fwrite(text.data(), 1, text.size(), f) == text.size();
+    return (std::fclose(f) == 0 && ok) ? LBM_OK : LBM_ERR_IO;
+}
+
 std::string numbered(const char* prefix, const char* tag, long long number, const char* ext) {
     char num[32];
     std::snprintf(num, sizeof(num), "%012lld", number);  // write(filename,'(i12.12)')
@@ -583,6 +646,51 @@ std::string numbered(const char* prefix, const char* tag, long long number, cons
 }
 
 }  // namespace
+
+extern "C" int lbm_format_fortran_es(double x, int w, int d, int e, char* buf, size_t len) {
+    if (!buf || len == 0 || w <= 0 || d < 0 || e < 0) return LBM_ERR_PARAM;
+    const std::string s = fortran_es(x, w, d, e);
+    if (s.size() + 1 > len) return LBM_ERR_PARAM;
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+    return LBM_OK;
+}
+
+extern "C" int lbm_append_convergence_tecplot_host(const char* filename, int first, int dim, int64_t itc, double errorU,
+                                                   double errorT) {
+    if (!filename || (dim != 2 && dim != 3)) return LBM_ERR_PARAM;
+    const std::string line = convergence_line((long long)itc, errorU, errorT);
+    if (first) {  // the run's first record replaces the file (2DRB.F90:1283-1290, 3DRB.F90:1543-1549)
+        const std::string head = std::string("VARIABLES = \"itc\" \"errorU\" \"errorT\"\n") + "ZONE T=\"" +
+                                 (dim == 3 ? "conv3d" : "conv") + "\", F=POINT\n";
+        return write_text(filename, head + line, true);
+    }
+    return write_text(filename, line, false);
+}
+
+extern "C" int lbm_append_convergence_master_tecplot_host(const char* filename, int first, int dim, const char* zone,
+                                                          int64_t itc, double errorU, double errorT) {
+    if (!filename || !zone || (dim != 2 && dim != 3)) return LBM_ERR_PARAM;
+    int st;
+    if (first) {  // a title the first time the file is made, a new zone for every run (2DRB.F90:1322-1337)
+        if (!file_exists(filename)) {
+            const std::string head = std::string("TITLE = \"Convergence comparison") + (dim == 3 ? " 3D" : "") +
+                                     "\"\nVARIABLES = \"itc\" \"errorU\" \"errorT\"\n";
+            if ((st = write_text(filename, head, true)) != LBM_OK) return st;
+        }
+        std::string z(zone);
+        while (!z.empty() && z.back() == ' ') z.pop_back();  // trim(zoneName)
+        if ((st = write_text(filename, "ZONE T=\"" + z + "\", F=POINT\n", false)) != LBM_OK) return st;
+    }
+    return write_text(filename, convergence_line((long long)itc, errorU, errorT), false);
+}
+
+extern "C" int lbm_convergence_line(int64_t itc, double errorU, double errorT, char* buf, size_t len) {
+    if (!buf) return LBM_ERR_PARAM;
+    const std::string s = convergence_line((long long)itc, errorU, errorT);
+    if (s.size() + 1 > len) return LBM_ERR_PARAM;
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+    return LBM_OK;
+}
 
 extern "C" int lbm_output_binary(lbm_handle* h, const char* path) {
     if (!h || !path) return LBM_ERR_PARAM;

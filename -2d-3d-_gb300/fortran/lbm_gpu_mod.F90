@@ -131,6 +131,38 @@ module lbm_gpu_mod
       type(c_ptr), value :: h
       real(c_double) :: errU, errT
     end function
+    ! check as the reference's subroutine does it: convergence[3D].plt and
+    ! convergence_all[_3D].plt appended in dir (C string; '' = working directory), the line
+    ! echoed when echo /= 0
+    integer(c_int) function lbm_check_log(h, dir, echo, errU, errT) bind(C, name="lbm_check_log")
+      import :: c_int, c_ptr, c_char, c_double
+      type(c_ptr), value :: h
+      character(kind=c_char), intent(in) :: dir(*)
+      integer(c_int), value :: echo
+      real(c_double) :: errU, errT
+    end function
+    integer(c_int) function lbm_append_convergence_tecplot(h, filename, itc, errorU, errorT) &
+        bind(C, name="lbm_append_convergence_tecplot")
+      import :: c_int, c_ptr, c_char, c_int64_t, c_double
+      type(c_ptr), value :: h
+      character(kind=c_char), intent(in) :: filename(*)
+      integer(c_int64_t), value :: itc
+      real(c_double), value :: errorU, errorT
+    end function
+    integer(c_int) function lbm_append_convergence_master_tecplot(h, filename, zone, itc, errorU, errorT) &
+        bind(C, name="lbm_append_convergence_master_tecplot")
+      import :: c_int, c_ptr, c_char, c_int64_t, c_double
+      type(c_ptr), value :: h
+      character(kind=c_char), intent(in) :: filename(*), zone(*)
+      integer(c_int64_t), value :: itc
+      real(c_double), value :: errorU, errorT
+    end function
+    integer(c_int) function lbm_case_tag(h, buf, len) bind(C, name="lbm_case_tag")
+      import :: c_int, c_ptr, c_char, c_size_t
+      type(c_ptr), value :: h
+      character(kind=c_char) :: buf(*)
+      integer(c_size_t), value :: len
+    end function
     integer(c_int) function lbm_calNuRe(h, Nu, Re) bind(C, name="lbm_calNuRe")
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: h

@@ -49,6 +49,15 @@ SIGNATURES = {
     "lbm_macroT": ([_vp], _i32),
     "lbm_step": ([_vp, _i64], _i32),
     "lbm_check": ([_vp, _dp, _dp], _i32),
+    "lbm_check_log": ([_vp, C.c_char_p, _i32, _dp, _dp], _i32),
+    "lbm_append_convergence_tecplot": ([_vp, C.c_char_p, _i64, C.c_double, C.c_double], _i32),
+    "lbm_append_convergence_master_tecplot": ([_vp, C.c_char_p, C.c_char_p, _i64, C.c_double, C.c_double], _i32),
+    "lbm_case_tag": ([_vp, C.c_char_p, _sz], _i32),
+    "lbm_append_convergence_tecplot_host": ([C.c_char_p, _i32, _i32, _i64, C.c_double, C.c_double], _i32),
+    "lbm_append_convergence_master_tecplot_host": ([C.c_char_p, _i32, _i32, C.c_char_p, _i64, C.c_double, C.c_double],
+                                                   _i32),
+    "lbm_convergence_line": ([_i64, C.c_double, C.c_double, C.c_char_p, _sz], _i32),
+    "lbm_format_fortran_es": ([C.c_double, _i32, _i32, _i32, C.c_char_p, _sz], _i32),
     "lbm_calNuRe": ([_vp, _dp, _dp], _i32),
     "lbm_RBcalc_Nu_global": ([_vp, _dp], _i32),
     "lbm_RBcalc_Nu_wall_avg": ([_vp, _vp], _i32),
@@ -244,6 +253,20 @@ class Lattice:
         a, b = C.c_double(), C.c_double()
         self._ck(self.lib.lbm_check(self._h, C.byref(a), C.byref(b)), "check")
         return a.value, b.value
+
+    def check_log(self, directory=".", echo=False):
+        """check as the reference runs it: the errors, appended to convergence[3D].plt and
+        (under case_tag()) convergence_all[_3D].plt in `directory`, echoed when echo."""
+        a, b = C.c_double(), C.c_double()
+        self._ck(self.lib.lbm_check_log(self._h, os.fsencode(directory), 1 if echo else 0, C.byref(a), C.byref(b)),
+                 "check_log")
+        return a.value, b.value
+
+    def case_tag(self):
+        """The reference's caseTag string of this lattice (Ra, sizes, useG, legacy switch)."""
+        buf = C.create_string_buffer(256)
+        self._ck(self.lib.lbm_case_tag(self._h, buf, 256), "case_tag")
+        return buf.value.decode()
 
     def calNuRe(self):
         a, b = C.c_double(), C.c_double()

@@ -168,6 +168,27 @@ int lbm_step(lbm_handle* h, int64_t nsteps);
 /* subroutine check: errU = ||u-up||_2/||u||_2, errT = ||T-Tp||_1/||T||_1, then up <- u
  * (2DRB.F90:1213-1260, 3DRB.F90:1475-1528).  Returns LBM_ERR_DIVERGED on a non-finite field. */
 int lbm_check(lbm_handle* h, double* errU, double* errT);
+/* check with the reference's convergence history (2DRB.F90:1249-1258, 3DRB.F90:1522-1526):
+ * lbm_check, then the record (itc, errorU, errorT) appended to <dir>/convergence.plt
+ * (3D: convergence3D.plt) and, under the zone lbm_case_tag, to <dir>/convergence_all.plt
+ * (3D: convergence_all_3D.plt), then echoed to standard output when echo != 0 (the
+ * reference always echoes).  dir NULL or "" = the working directory.  A diverged field is
+ * logged and reported as LBM_ERR_DIVERGED. */
+int lbm_check_log(lbm_handle* h, const char* dir, int echo, double* errU, double* errT);
+/* subroutine append_convergence_tecplot (2DRB.F90:1273-1298, 3DRB.F90:1536-1557): the first
+ * call on a handle replaces the file with the header VARIABLES = "itc" "errorU" "errorT",
+ * ZONE T="conv" (3D "conv3d"), F=POINT and the record; later calls append the record
+ * write(u,'(I12,1X,ES24.16,1X,ES24.16)') (the file must exist, LBM_ERR_IO otherwise). */
+int lbm_append_convergence_tecplot(lbm_handle* h, const char* filename, int64_t itc, double errorU, double errorT);
+/* subroutine append_convergence_master_tecplot (2DRB.F90:1310-1343, 3DRB.F90:1564-1591): the
+ * first call on a handle writes TITLE = "Convergence comparison" (3D: "... 3D") and the
+ * VARIABLES line if the file does not exist, then ZONE T="<zone, trailing blanks trimmed>",
+ * F=POINT; every call appends the record. */
+int lbm_append_convergence_master_tecplot(lbm_handle* h, const char* filename, const char* zone, int64_t itc,
+                                          double errorU, double errorT);
+/* The caseTag of check: "Ra=<ES10.3E2>,nx=<I0>,ny=<I0>[,nz=<I0>],useG=<T|F>,old=<T|F>"
+ * (2DRB.F90:1252-1253, 3DRB.F90:1523-1524). */
+int lbm_case_tag(const lbm_handle* h, char* buf, size_t len);
 /* subroutine calNuRe: volume Nu = 1 + <v T> L/kappa (RB) or <u T> (side heated) and
  * Re = sqrt(<|u|^2>) L/nu (2DRB.F90:1610-1675, 3DRB.F90:1712-1778). */
 int lbm_calNuRe(lbm_handle* h, double* Nu, double* Re);
@@ -334,6 +355,7 @@ int lbm_output_binary(lbm_handle* h, const char* path);
 int lbm_output_Tecplot(lbm_handle* h, const char* prefix, int64_t number);
 int lbm_calc_psi_vort_and_output(lbm_handle* h, const char* prefix, int64_t number, int nFinePerUnit,
                                  lbm_psi_summary* out);
+
 /* The same writers on host arrays in the Fortran layout (no GPU needed, except the fine-grid
  * search of lbm_psi_absmax_fine_spline, which runs on the current device). */
 int lbm_output_binary_host(const char* path, int dim, int nx, int ny, int nz, double velocityScaleCompare,
@@ -355,6 +377,19 @@ int lbm_psi_center_2d(int nx, int ny, double lengthUnit, const double* psi, doub
 int lbm_psi_absmax_fine_spline(int nx, int ny, double lengthUnit, const double* psi, int nFinePerUnit,
                                double* psi_abs_max, double* x_at_max, double* y_at_max,
                                double* psi_center_abs_fine);
+
+/* Host forms of the convergence-history appenders (no handle, no GPU): `first` stands for
+ * the reference's once-per-run flag; dim 2 or 3 picks the zone and title spelling. */
+int lbm_append_convergence_tecplot_host(const char* filename, int first, int dim, int64_t itc, double errorU,
+                                        double errorT);
+int lbm_append_convergence_master_tecplot_host(const char* filename, int first, int dim, const char* zone, int64_t itc,
+                                               double errorU, double errorT);
+/* One convergence record as the reference writes it, write(u,'(I12,1X,ES24.16,1X,ES24.16)')
+ * itc, errorU, errorT, with its newline, into buf (len >= 64). */
+int lbm_convergence_line(int64_t itc, double errorU, double errorT, char* buf, size_t len);
+/* x in the Fortran edit descriptor ESw.d (e = 0) or ESw.dEe, right-justified in w columns
+ * (w asterisks when it does not fit), into buf (len > w). */
+int lbm_format_fortran_es(double x, int w, int d, int e, char* buf, size_t len);
 
 /* ---- restart files (backupData, 3DRB.F90:1638-1665 / 2DRB.F90:1402-1430; reload,
  *      3DRB.F90:602-623 / 2DRB.F90:621-637; reconstruct_macro_from_fg,
