@@ -478,13 +478,15 @@ def at_size_run(args, local, peak, n=384, steps=40):
     return out
 
 
-def config0_run(args, local, steps=20000, cpu_steps=400):
+def config0_run(args, local, steps=20000, cpu_steps=20000):
     """The 2D reference case (256 x 128, x-periodic, Ra 1e5, Pr 0.71, U 0.1, plain FP64): its
     full 20,000 steps on the GPU through lbm_step, the wall-averaged Nu and volume Re at the
-    end, and the CPU oracle on a bounded sample of the same lattice."""
+    end, and the same 20,000 steps of the CPU oracle (about 2.5 s on 16 host threads), with
+    the final temperature field compared bit for bit and Nu, Re (reductions) to 1e-12."""
+    import numpy as np
     import torch
     import lbmgpu
-    from lbmgpu.abi import rb_params
+    from lbmgpu.abi import FIELDS, field_shape, rb_params
     from oracle import oracle as ora
     p = rb_params(dim=2, nx=256, ny=128, Ra=1e5, Pr=0.71, U=0.1, noise_amp=1e-3, seed=20261203)
     lat = lbmgpu.Lattice(p, device=local)
@@ -499,6 +501,7 @@ def config0_run(args, local, steps=20000, cpu_steps=400):
     ms = a.elapsed_time(b)
     nu, re = lat.calNuRe()
     wall = lat.RBcalc_Nu_wall_avg()
+    t_gpu = lat.get_state("T") if cpu_steps == steps else None
     lat.close()
     threads = ora.set_threads(os.cpu_count() or 1)
     o = ora.Oracle(p)
@@ -507,12 +510,18 @@ def config0_run(args, local, steps=20000, cpu_steps=400):
     o.step(cpu_steps)
     dt = time.perf_counter() - t0
     cells = 256 * 128
+    cpu = {"threads": threads, "steps": cpu_steps, "s": dt, "mlups": cells * cpu_steps / dt / 1e6,
+           "s_for_all_steps": dt * steps / cpu_steps}
+    if t_gpu is not None:
+        # the fields bit for bit; Nu and Re are sums that the GPU reduces in another order
+        nu_o, re_o, _ = o.calNuRe()
+        cpu["T_bitwise_equal_to_gpu"] = bool(np.array_equal(t_gpu, o.get(FIELDS["T"], field_shape(p, "T"))))
+        cpu["Nu_Re_rel_diff_to_gpu"] = max(abs(nu - nu_o) / abs(nu_o), abs(re - re_o) / abs(re_o))
+    o.close()
     return {"workload": "2D RB D2Q9/D2Q5, 256 x 128, x periodic, Ra 1e5, Pr 0.71, U 0.1, FP64 plain method, "
                         "T linear + 1e-3 seeded noise, %d steps" % steps,
             "gpu_s": ms / 1e3, "mlups": cells * steps / (ms / 1e3) / 1e6, "Nu_volume": nu, "Re": re,
-            "Nu_hot_wall": wall["Nu_hot"], "Nu_cold_wall": wall["Nu_cold"],
-            "cpu_oracle": {"threads": threads, "steps": cpu_steps, "s": dt, "mlups": cells * cpu_steps / dt / 1e6,
-                           "s_for_all_steps": dt * steps / cpu_steps}}
+            "Nu_hot_wall": wall["Nu_hot"], "Nu_cold_wall": wall["Nu_cold"], "cpu_oracle": cpu}
 
 
 def run_gpu(args):
