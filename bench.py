@@ -176,11 +176,14 @@ def max_over_ranks(pg, x):
     return float(t.item())
 
 
-def cpu_baseline(steps=None, budget_s=12.0, n=N_CELL_EDGE):
-    """C++ restatement of the reference's 8-pass OpenMP CPU step, all host cores, bounded sample."""
+def cpu_baseline(steps=None, budget_s=12.0, n=N_CELL_EDGE, device=None):
+    """C++ restatement of the reference's 8-pass OpenMP CPU step, all host cores, bounded sample.
+    With a device: the GPU plain method then runs the same steps from the same initial state
+    and the final temperature fields are compared bit for bit."""
     from oracle import oracle as ora
     threads = ora.set_threads(os.cpu_count() or 1)
-    o = ora.Oracle(workload_params("fp64", n))
+    p = workload_params("fp64", n)
+    o = ora.Oracle(p)
     o.initial()
     o.step(1)
     t0 = time.perf_counter()
@@ -194,9 +197,22 @@ def cpu_baseline(steps=None, budget_s=12.0, n=N_CELL_EDGE):
             done += 2
     dt = time.perf_counter() - t0
     cells = n ** 3
-    return {"value": cells * done / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d steps of the %d^3 workload (%.1f s), C++ restatement of the reference's OpenMP "
-                      "8-pass step (-O3 -fopenmp), %d threads" % (done, n, dt, threads)}
+    out = {"value": cells * done / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": "%d steps of the %d^3 workload (%.1f s), C++ restatement of the reference's OpenMP "
+                     "8-pass step (-O3 -fopenmp), %d threads" % (done, n, dt, threads)}
+    if device is not None:
+        import numpy as np
+        import lbmgpu
+        from lbmgpu.abi import FIELDS, field_shape
+        lat = lbmgpu.Lattice(p, device=device)
+        lat.initial()
+        lat.step(1 + done)
+        t_gpu = lat.get_state("T")
+        lat.close()
+        out["gpu_check"] = {"steps": 1 + done,
+                            "T_bitwise_equal": bool(np.array_equal(t_gpu, o.get(FIELDS["T"], field_shape(p, "T"))))}
+    o.close()
+    return out
 
 
 def run_reference(args):
@@ -594,7 +610,7 @@ def run_gpu(args):
     if rank == 0 and not args.no_config0:
         line["config0_2d"] = config0_run(args, local)
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(n=args.size)
+        line["cpu_baseline"] = cpu_baseline(n=args.size, device=local)
     if rank == 0:
         print(json.dumps(line))
     return 0
