@@ -11,7 +11,8 @@ Headline `value`: the plain method (FP64, the reference's arithmetic) through th
 kernels, inputs resident in HBM.  The FP32 / FP16 storage forms of the same workload are
 reported beside it.  `e2e` is the same metric through the C ABI with host buffers in the
 reference's Fortran layout (state in, steps, T field and Nu/Re out).  `cpu_baseline` is
-the C++ restatement of the reference's OpenMP CPU path timed on this host's cores.
+the C++ restatement of the reference's OpenMP CPU path timed on this host's cores; the GPU
+then runs the same steps and the two temperature fields are compared bit for bit.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
