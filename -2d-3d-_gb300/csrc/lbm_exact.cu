@@ -120,8 +120,18 @@ __device__ __forceinline__ void collide_2d(const double* F, double rho, double u
     fSource[7] = P.h2Snu * (u * Fx - v * Fy);
     fSource[8] = P.hSnu * (u * Fy + v * Fx);
 
-#pragma unroll
-    for (int a = 0; a < 9; ++a) m_post[a] = m[a] - s[a] * (m[a] - meq[a]) + fSource[a];
+    // conserved moments (zero rates s0, s3, s5): m - 0*(m - meq) + source is m + source for
+    // every finite m but -0 (a zero rate only subtracts a zero; m0 = rho, and a sum of
+    // populations is never -0), as in collide_3d; fSource[0] = 0
+    m_post[0] = m[0];
+    m_post[3] = m[3] + fSource[3];
+    m_post[5] = m[5] + fSource[5];
+    m_post[1] = m[1] - s[1] * (m[1] - meq[1]) + fSource[1];
+    m_post[2] = m[2] - s[2] * (m[2] - meq[2]) + fSource[2];
+    m_post[4] = m[4] - s[4] * (m[4] - meq[4]) + fSource[4];
+    m_post[6] = m[6] - s[6] * (m[6] - meq[6]) + fSource[6];
+    m_post[7] = m[7] - s[7] * (m[7] - meq[7]) + fSource[7];
+    m_post[8] = m[8] - s[8] * (m[8] - meq[8]) + fSource[8];
 
     // m/4 as exponent adds; x/(c 2^k) = RN(x/c) 2^-k, one exact multiply, for a normal quotient
     const double q7 = iscale<-2>(m_post[7]), q8 = iscale<-2>(m_post[8]);
@@ -314,7 +324,7 @@ __device__ __forceinline__ void collideT_2d(const double* G, double u, double v,
     neq[3] = P.legacy ? T * P.paraA : T * (-2.0 / 3.0);
     neq[4] = 0.0;
     q[0] = 0.0; q[1] = P.Qk; q[2] = P.Qk; q[3] = P.Qnu; q[4] = P.Qnu;
-    n_post[0] = n[0] - q[0] * (n[0] - neq[0]);
+    n_post[0] = n[0];  // zero rate q0: n0 - 0*(n0 - T) is n0 (never -0, a sum of populations)
     n_post[1] = n[1] - q[1] * (n[1] - neq[1]) + P.SG * dBx;
     n_post[2] = n[2] - q[2] * (n[2] - neq[2]) + P.SG * dBy;
     n_post[3] = n[3] - q[3] * (n[3] - neq[3]);
@@ -362,7 +372,7 @@ __device__ __forceinline__ void collideT_3d(const double* g, double u, double v,
     neq[5] = 0.0;
     neq[6] = 0.0;
     q[0] = 0.0; q[1] = P.Qk; q[2] = P.Qk; q[3] = P.Qk; q[4] = P.Qnu; q[5] = P.Qnu; q[6] = P.Qnu;
-    n_post[0] = n[0] - q[0] * (n[0] - neq[0]);
+    n_post[0] = n[0];  // zero rate q0: n0 - 0*(n0 - T) is n0 (never -0, a sum of populations)
     n_post[1] = n[1] - q[1] * (n[1] - neq[1]) + P.SG * dBx;
     n_post[2] = n[2] - q[2] * (n[2] - neq[2]) + P.SG * dBy;
     n_post[3] = n[3] - q[3] * (n[3] - neq[3]) + P.SG * dBz;
