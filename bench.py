@@ -37,10 +37,10 @@ UNIT = "MLUPS"
 N_CELL_EDGE = 128
 BYTES_PER_CELL = {"fp64": 416, "fp32": 208, "fp16": 104}  # populations read + written once
 # FP64 work of the plain method per coupled cell update (3D), counted by ncu on the fused
-# kernels (sass thread instructions, flow + thermal): dadd 400, dmul 104, dfma 57.  Products
+# kernels (sass thread instructions, flow + thermal): dadd 398, dmul 103, dfma 57.  Products
 # with exact powers of two run on the integer pipes and are not counted.
-FP64_INST_PER_CELL = 400 + 104 + 57
-FP64_FLOP_PER_CELL = 400 + 104 + 2 * 57
+FP64_INST_PER_CELL = 398 + 103 + 57
+FP64_FLOP_PER_CELL = 398 + 103 + 2 * 57
 DTYPE = {"fp64": "f64", "fp32": "f32", "fp16": "f16-storage/f32-arith"}
 FALLBACK_HBM_GBS = 6800.0
 
