@@ -396,36 +396,7 @@ extern "C" int lbm_create(const lbm_params* p, int device, lbm_handle** out) {
             g.bcT_hi[a] = 2.0 * c.omegaT1 * p->Tcold;
         }
     }
-    PhysC& P = h->phys;
-    P.gBeta = c.gBeta;
-    P.Tref = c.Tref;
-    P.Snu = c.Snu;
-    P.Sq = c.Sq;
-    P.Se = c.Se;
-    P.Seps = c.Seps;
-    P.Spi = c.Spi;
-    P.Sm = c.Sm;
-    P.Qk = c.Qk;
-    P.Qnu = c.Qnu;
-    P.SG = c.SG;
-    P.paraA = c.paraA;
-    P.omegaT0 = c.omegaT0;
-    P.omegaT1 = c.omegaT1;
-    P.geqc = c.thermalGeqCoeff;
-    P.use_g = p->use_g ? 1 : 0;
-    P.legacy = p->legacy_thermal ? 1 : 0;
-    P.ha = p->side_heated_ha ? 1 : 0;
-    P.B2 = c.B2sigemarho;
-    P.sinphi = c.sinphi;
-    P.cosphi = c.cosphi;
-    P.hSe38 = (1.0 - 0.5 * c.Se) * 38.0;
-    P.hSeps11 = (1.0 - 0.5 * c.Seps) * (-11.0);
-    P.hSq23 = (1.0 - 0.5 * c.Sq) * (-2.0 / 3.0);
-    P.hSnu = 1.0 - 0.5 * c.Snu;
-    P.hSpi = 1.0 - 0.5 * c.Spi;
-    P.h6Snu = 6.0 - 3.0 * c.Snu;
-    P.hSq = 1.0 - 0.5 * c.Sq;
-    P.h2Snu = 2.0 - c.Snu;
+    h->phys = make_physc(*p, c);
     DiagScalars& D = h->dsc;
     D.Thot = p->Thot;
     D.Tcold = p->Tcold;
