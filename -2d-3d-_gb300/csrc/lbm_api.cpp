@@ -24,6 +24,7 @@
 #include "../../include/lbm_gpu.h"
 #include "lbm_ensemble.h"
 #include "lbm_fast.h"
+#include "lbm_fixed.h"
 #include "lbm_internal.h"
 #include "lbm_records.h"
 
@@ -58,6 +59,13 @@ struct lbm_handle {
     bool fused_valid = false;  // true: current state is in the fused buffers
     int cur = 0;               // fused buffer index holding f_post_N / g_post_N
     AAState aa;                // in-place pattern: A.f / A.g are the only population arrays
+    // fixed arithmetic (arith = LBM_ARITH_FIXED): fbuf / gbuf hold q60 deviations
+    // (lbm_fixed_cell.cuh); the lag state lives in xb0..xb2 (B_prev) and xlag (3D T lag,
+    // 2D stored force), q60 as well
+    bool fixed = false;
+    PhysX px{};
+    Geo xgeo{};  // geometry with the thermal wall terms of deviations
+    long long *xb0 = nullptr, *xb1 = nullptr, *xb2 = nullptr, *xlag = nullptr;
 
     // FP32 / FP16 storage forms
     FastState F{};
@@ -146,6 +154,11 @@ static int validate(const lbm_params* p) {
     }
     if (p->precision < LBM_FP64 || p->precision > LBM_FP16) return LBM_ERR_PARAM;
     if (p->pattern != LBM_PATTERN_AB && p->pattern != LBM_PATTERN_AA) return LBM_ERR_PARAM;
+    // the fixed arithmetic: FP64 handles, two-buffer pattern, without the magnetic force
+    if (p->arith != LBM_ARITH_REFERENCE && p->arith != LBM_ARITH_FIXED) return LBM_ERR_PARAM;
+    if (p->arith == LBM_ARITH_FIXED &&
+        (p->precision != LBM_FP64 || p->pattern != LBM_PATTERN_AB || p->side_heated_ha))
+        return LBM_ERR_PARAM;
     // the magnetic force exists in the 2D program only (2DRB.F90:88-92); the FP32/FP16 forms
     // carry only F_y in their lag state
     if (p->side_heated_ha && (p->dim != 2 || p->precision != LBM_FP64 || !std::isfinite(p->Ha) ||
@@ -336,6 +349,12 @@ static int allocate(lbm_handle* h) {
         }
         AL(h->A.jx, n);
         AL(h->A.jy, n);
+        if (h->fixed) {
+            AL(h->xb0, n);
+            AL(h->xb1, n);
+            if (d3) AL(h->xb2, n);
+            AL(h->xlag, n);
+        }
     } else {
         st = fast_allocate(h->F, h->p, h->geo, [h](void** p, size_t bytes) {
             cudaError_t e = cudaMalloc(p, bytes > 0 ? bytes : 1);
@@ -374,29 +393,16 @@ extern "C" int lbm_create(const lbm_params* p, int device, lbm_handle** out) {
     h->device = device;
     const lbm_constants& c = h->c;
 
-    Geo& g = h->geo;
-    g.nx = p->nx;
-    g.ny = p->ny;
-    g.nz = p->dim == 3 ? p->nz : 1;
-    g.ncell = (long long)g.nx * g.ny * g.nz;
-    for (int a = 0; a < 3; ++a) {
-        g.bcf[a] = p->bc_flow[a];
-        g.bct[a] = p->bc_thermal[a];
-        if (p->dim == 2 && a == 2) {
-            g.bcf[a] = LBM_BC_NOSLIP;
-            g.bct[a] = LBM_BCT_ADIABATIC;
-        }
-        // anti-bounce-back source (2DRB.F90:1052-1059, 1094-1101; 3DRB.F90:1265-1271, 1309-1315)
-        if (p->legacy_thermal) {
-            const double cc = p->dim == 2 ? (4.0 + c.paraA) / 10.0 : (6.0 + c.paraA) / 21.0;
-            g.bcT_lo[a] = cc * p->Thot;
-            g.bcT_hi[a] = cc * p->Tcold;
-        } else {
-            g.bcT_lo[a] = 2.0 * c.omegaT1 * p->Thot;
-            g.bcT_hi[a] = 2.0 * c.omegaT1 * p->Tcold;
+    h->geo = make_geo(*p, c);
+    h->phys = make_physc(*p, c);
+    if (p->arith == LBM_ARITH_FIXED) {
+        h->fixed = true;
+        h->xgeo = deviation_geo(h->geo, c);
+        if (!make_physx(*p, c, h->px)) {  // a relaxation constant out of the q60 range
+            delete h;
+            return LBM_ERR_PARAM;
         }
     }
-    h->phys = make_physc(*p, c);
     DiagScalars& D = h->dsc;
     D.Thot = p->Thot;
     D.Tcold = p->Tcold;
@@ -540,7 +546,33 @@ extern "C" int lbm_initial(lbm_handle* h) {
     return LBM_OK;
 }
 
-// Rebuild the module arrays from the fused buffers (no-op when already there).
+// The arrays the fixed-arithmetic kernels read and write.
+static FixedArrays fixed_arrays(const lbm_handle* h) {
+    const ExactArrays& A = h->A;
+    FixedArrays X{};
+    X.f = A.f;
+    X.g = A.g;
+    X.rho = A.rho;
+    X.u = A.u;
+    X.v = A.v;
+    X.w = A.w;
+    X.T = A.T;
+    X.Bx = A.Bx;
+    X.By = A.By;
+    X.Bz = A.Bz;
+    X.Tlag = A.Tlag;
+    X.Fx = A.Fx;
+    X.Fy = A.Fy;
+    X.xb0 = h->xb0;
+    X.xb1 = h->xb1;
+    X.xb2 = h->xb2;
+    X.xlag = h->xlag;
+    return X;
+}
+
+// Rebuild the module arrays from the fused buffers (no-op when already there).  The fixed
+// arithmetic keeps its q60 buffers as the state: the module arrays are a rounded FP64 copy,
+// so how often a caller reads diagnostics does not change the run.
 static int materialize(lbm_handle* h) {
     if (h->p.precision != LBM_FP64) {
         fast_materialize(h->F, h->geo, h->phys, h->dim, h->stream);
@@ -548,6 +580,12 @@ static int materialize(lbm_handle* h) {
         return LBM_OK;
     }
     if (!h->fused_valid) return LBM_OK;
+    if (h->fixed) {
+        fixed_materialize(h->xgeo, h->px, fixed_arrays(h), h->dim, (const long long*)h->fbuf[h->cur],
+                          (const long long*)h->gbuf[h->cur], h->stream);
+        CK_LAUNCH(h, "materialize");
+        return LBM_OK;
+    }
     if (h->p.pattern == LBM_PATTERN_AA) {
         // the arrays are the module populations; the state stays where it is
         exact_aa_materialize(h->geo, h->phys, h->A, h->dim, h->aa, h->stream);
@@ -556,6 +594,22 @@ static int materialize(lbm_handle* h) {
     }
     exact_materialize(h->geo, h->phys, h->A, h->dim, h->fbuf[h->cur], h->gbuf[h->cur], h->stream);
     CK_LAUNCH(h, "materialize");
+    h->A.fpost = h->fbuf[h->cur];
+    h->A.gpost = h->gbuf[h->cur];
+    h->fused_valid = false;
+    return LBM_OK;
+}
+
+// Fixed arithmetic: make the FP64 module arrays the state again (before a stage kernel or a
+// state load): materialise, turn the q60 fused buffers into the FP64 post-collision arrays
+// the stage kernels read, and start the next fused step from the module arrays.
+static int release_fixed(lbm_handle* h) {
+    if (!h->fixed || !h->fused_valid) return LBM_OK;
+    int st = materialize(h);
+    if (st != LBM_OK) return st;
+    fixed_post_to_double(h->px, (long long*)h->fbuf[h->cur], (long long*)h->gbuf[h->cur], h->geo.ncell, h->q, h->qt,
+                         h->stream);
+    CK_LAUNCH(h, "post-collision conversion");
     h->A.fpost = h->fbuf[h->cur];
     h->A.gpost = h->gbuf[h->cur];
     h->fused_valid = false;
@@ -573,7 +627,7 @@ static int stage(lbm_handle* h, int which) {
     if (h->p.pattern == LBM_PATTERN_AA)
         return fail(h, LBM_ERR_STATE, "stage entry points need the two-buffer pattern (separate f and f_post)");
     CK(h, cudaSetDevice(h->device));
-    int st = materialize(h);
+    int st = h->fixed ? release_fixed(h) : materialize(h);
     if (st != LBM_OK) return st;
     if (which == STAGE_COLLISION) h->itc += 1;
     exact_stage(which, h->geo, h->phys, h->A, h->dim, h->stream);
@@ -607,6 +661,11 @@ static void enqueue_one(lbm_handle* h, bool first) {
     const int nxt = h->cur ^ 1;
     if (h->p.precision == LBM_FP64 && in_place(h)) {
         exact_aa_step(h->geo, h->phys, h->A, h->dim, first, h->aa, h->stream);
+    } else if (h->p.precision == LBM_FP64 && h->fixed) {
+        fixed_fused_step(h->xgeo, h->px, fixed_arrays(h), h->dim, first, (const long long*)h->fbuf[h->cur],
+                         (const long long*)h->gbuf[h->cur], (long long*)h->fbuf[nxt], (long long*)h->gbuf[nxt],
+                         h->stream);
+        h->cur = nxt;
     } else if (h->p.precision == LBM_FP64) {
         exact_fused_step(h->geo, h->phys, h->A, h->dim, first, h->fbuf[h->cur], h->gbuf[h->cur], h->fbuf[nxt],
                          h->gbuf[nxt], h->stream);
@@ -1234,7 +1293,10 @@ static int state_io(lbm_handle* h, int field, double* dst, const double* src, si
     if (!h || (!dst && !src)) return LBM_ERR_PARAM;
     if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
     CK(h, cudaSetDevice(h->device));
-    int st = materialize(h);
+    // fixed arithmetic: a load makes the module arrays the state; the post-collision arrays
+    // exist only in FP64 form
+    const bool post = field == LBM_FIELD_F_POST || field == LBM_FIELD_G_POST;
+    int st = (h->fixed && (src || post)) ? release_fixed(h) : materialize(h);
     if (st != LBM_OK) return st;
     const long long n = h->geo.ncell;
     const bool pop = field == LBM_FIELD_F || field == LBM_FIELD_G || field == LBM_FIELD_F_POST || field == LBM_FIELD_G_POST;
@@ -1740,6 +1802,15 @@ extern "C" int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, 
             exact_aa_step(h->geo, h->phys, h->A, h->dim, false, h->aa, h->stream, 0);
             CK(h, cudaEventRecord(ev[2 * k + 1], h->stream));
             exact_aa_step(h->geo, h->phys, h->A, h->dim, false, h->aa, h->stream, 1);
+        } else if (h->p.precision == LBM_FP64 && h->fixed) {
+            const int nxt = h->cur ^ 1;
+            const FixedArrays X = fixed_arrays(h);
+            const long long *fc = (const long long*)h->fbuf[h->cur], *gc = (const long long*)h->gbuf[h->cur];
+            long long *fn = (long long*)h->fbuf[nxt], *gn = (long long*)h->gbuf[nxt];
+            fixed_fused_step(h->xgeo, h->px, X, h->dim, false, fc, gc, fn, gn, h->stream, 0);
+            CK(h, cudaEventRecord(ev[2 * k + 1], h->stream));
+            fixed_fused_step(h->xgeo, h->px, X, h->dim, false, fc, gc, fn, gn, h->stream, 1);
+            h->cur = nxt;
         } else if (h->p.precision == LBM_FP64) {
             const int nxt = h->cur ^ 1;
             exact_fused_step(h->geo, h->phys, h->A, h->dim, false, h->fbuf[h->cur], h->gbuf[h->cur], h->fbuf[nxt],
@@ -1837,6 +1908,7 @@ extern "C" int lbm_footprint(const lbm_params* p, size_t* bytes) {
     if (p->precision == LBM_FP64) {
         b += 8 * n * (aa ? q + qt : 3 * q + 3 * qt);         // AA: f, g | f_post A/B, g_post A/B, f, g
         b += 8 * n * (p->dim == 3 ? 16 : 13);                // rho u v T Bx By up vp Tp jx jy (+w Bz wp Tlag jz | Fx Fy)
+        if (p->arith == LBM_ARITH_FIXED) b += 8 * n * (p->dim == 3 ? 4 : 3);  // q60 B_prev and lag
     } else {
         const size_t nb = aa ? 1 : 2;
         b += es * n * (aa ? q + qt : 3 * q + 3 * qt);        // AA: f, g | F A/B, G A/B, f, g (module)

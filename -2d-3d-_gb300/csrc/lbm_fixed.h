@@ -1,0 +1,22 @@
+// lbm_fixed.h - launchers of the fixed arithmetic of FP64 handles (lbm_fixed.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "lbm_fixed_cell.cuh"
+
+namespace lbm {
+
+// One fused step (part 0: flow kernel, 1: thermal kernel, 2: both) on q60 fused buffers.
+// first: the inputs are the FP64 module arrays.  g: deviation geometry (deviation_geo).
+void fixed_fused_step(const Geo& g, const PhysX& X, const FixedArrays& A, int dim, bool first, const long long* fprev,
+                      const long long* gprev, long long* fnext, long long* gnext, cudaStream_t s, int part = 2);
+// The FP64 module arrays of the current step from the q60 fused buffers and the lag.
+void fixed_materialize(const Geo& g, const PhysX& X, const FixedArrays& A, int dim, const long long* fcur,
+                       const long long* gcur, cudaStream_t s);
+// Convert the q60 fused buffers in place to the FP64 post-collision populations of the
+// plain method's layout (the handle then continues from its module arrays).
+void fixed_post_to_double(const PhysX& X, long long* fbuf, long long* gbuf, long long n, int q, int qt,
+                          cudaStream_t s);
+
+}  // namespace lbm

@@ -62,6 +62,45 @@ inline PhysC make_physc(const lbm_params& p, const lbm_constants& c) {
     return P;
 }
 
+// Geometry and boundary switches of one run (host code).  The anti-bounce-back source of a
+// constant-temperature wall is 2 wT Tw (2DRB.F90:1052-1059, 1094-1101; 3DRB.F90:1265-1271,
+// 1309-1315), written in the legacy scheme as (4 + a_T)/10 Tw (2D) or (6 + a_T)/21 Tw (3D).
+inline Geo make_geo(const lbm_params& p, const lbm_constants& c) {
+    Geo g{};
+    g.nx = p.nx;
+    g.ny = p.ny;
+    g.nz = p.dim == 3 ? p.nz : 1;
+    g.ncell = (long long)g.nx * g.ny * g.nz;
+    for (int a = 0; a < 3; ++a) {
+        g.bcf[a] = p.bc_flow[a];
+        g.bct[a] = p.bc_thermal[a];
+        if (p.dim == 2 && a == 2) {
+            g.bcf[a] = LBM_BC_NOSLIP;
+            g.bct[a] = LBM_BCT_ADIABATIC;
+        }
+        if (p.legacy_thermal) {
+            const double cc = p.dim == 2 ? (4.0 + c.paraA) / 10.0 : (6.0 + c.paraA) / 21.0;
+            g.bcT_lo[a] = cc * p.Thot;
+            g.bcT_hi[a] = cc * p.Tcold;
+        } else {
+            g.bcT_lo[a] = 2.0 * c.omegaT1 * p.Thot;
+            g.bcT_hi[a] = 2.0 * c.omegaT1 * p.Tcold;
+        }
+    }
+    return g;
+}
+
+// The same geometry with the thermal wall terms of populations stored as deviations from the
+// rest state (e = g - wT Tref): the wall term minus 2 wT Tref.
+inline Geo deviation_geo(const Geo& g, const lbm_constants& c) {
+    Geo d = g;
+    for (int a = 0; a < 3; ++a) {
+        d.bcT_lo[a] = g.bcT_lo[a] - 2.0 * c.omegaT1 * c.Tref;
+        d.bcT_hi[a] = g.bcT_hi[a] - 2.0 * c.omegaT1 * c.Tref;
+    }
+    return d;
+}
+
 // Inputs of `initial` that depend on host-side math (sin/cos of the RB perturbation).
 struct InitC {
     double L, Thot, Tcold;

@@ -34,6 +34,7 @@ module lbm_gpu_mod
   integer(c_int), parameter :: LBM_BC_NOSLIP = 0, LBM_BC_PERIODIC = 1
   integer(c_int), parameter :: LBM_BCT_CONST = 0, LBM_BCT_ADIABATIC = 1, LBM_BCT_PERIODIC = 2
   integer(c_int), parameter :: LBM_FP64 = 0, LBM_FP32 = 1, LBM_FP16 = 2
+  integer(c_int), parameter :: LBM_ARITH_REFERENCE = 0, LBM_ARITH_FIXED = 1  ! FP64: bitwise | integer pipes
   integer(c_int), parameter :: LBM_PATTERN_AB = 0, LBM_PATTERN_AA = 1   ! AA: one in-place array, same values
   integer(c_int), parameter :: LBM_FIELD_F = 0, LBM_FIELD_G = 1, LBM_FIELD_RHO = 2, LBM_FIELD_U = 3
   integer(c_int), parameter :: LBM_FIELD_V = 4, LBM_FIELD_W = 5, LBM_FIELD_T = 6
@@ -50,7 +51,7 @@ module lbm_gpu_mod
     integer(c_int32_t) :: use_g, legacy_thermal, precision, pattern
     integer(c_int64_t) :: seed
     real(c_double)     :: noise_amp
-    integer(c_int32_t) :: side_heated_ha, reserved0   ! #define SideHeatedHa (2D)
+    integer(c_int32_t) :: side_heated_ha, arith       ! #define SideHeatedHa (2D); FP64 arithmetic
     real(c_double)     :: Ha, phi_deg
   end type lbm_params
 

@@ -19,12 +19,16 @@ LBM_BC_NOSLIP, LBM_BC_PERIODIC = 0, 1
 LBM_BCT_CONST, LBM_BCT_ADIABATIC, LBM_BCT_PERIODIC = 0, 1, 2
 LBM_FP64, LBM_FP32, LBM_FP16 = 0, 1, 2
 LBM_PATTERN_AB, LBM_PATTERN_AA = 0, 1
+LBM_ARITH_REFERENCE, LBM_ARITH_FIXED = 0, 1
 
 FIELDS = {
     "f": 0, "g": 1, "rho": 2, "u": 3, "v": 4, "w": 5, "T": 6,
     "Bx_prev": 7, "By_prev": 8, "Bz_prev": 9, "Fx": 10, "Fy": 11, "f_post": 12, "g_post": 13,
 }
 PRECISIONS = {"fp64": LBM_FP64, "fp32": LBM_FP32, "fp16": LBM_FP16}
+# "fp64x": FP64 handle with the fixed arithmetic (FP64 accuracy on the integer pipes)
+PRECISION_NAMES = {"fp64": (LBM_FP64, LBM_ARITH_REFERENCE), "fp64x": (LBM_FP64, LBM_ARITH_FIXED),
+                   "fp32": (LBM_FP32, LBM_ARITH_REFERENCE), "fp16": (LBM_FP16, LBM_ARITH_REFERENCE)}
 
 
 class LbmParams(C.Structure):
@@ -36,7 +40,7 @@ class LbmParams(C.Structure):
         ("use_g", C.c_int32), ("legacy_thermal", C.c_int32),
         ("precision", C.c_int32), ("pattern", C.c_int32),
         ("seed", C.c_uint64), ("noise_amp", C.c_double),
-        ("side_heated_ha", C.c_int32), ("reserved0", C.c_int32), ("Ha", C.c_double), ("phi_deg", C.c_double),
+        ("side_heated_ha", C.c_int32), ("arith", C.c_int32), ("Ha", C.c_double), ("phi_deg", C.c_double),
     ]
 
     def copy(self):
@@ -47,7 +51,8 @@ class LbmParams(C.Structure):
     def describe(self):
         return {
             "dim": self.dim, "nx": self.nx, "ny": self.ny, "nz": self.nz, "Ra": self.Ra, "Pr": self.Pr,
-            "Mach": self.Mach, "precision": {v: k for k, v in PRECISIONS.items()}[self.precision],
+            "Mach": self.Mach,
+            "precision": "fp64x" if self.arith == LBM_ARITH_FIXED else {v: k for k, v in PRECISIONS.items()}[self.precision],
             "pattern": "AA" if self.pattern == LBM_PATTERN_AA else "AB",
         }
 
@@ -123,7 +128,10 @@ def rb_params(dim=3, n=None, nx=None, ny=None, nz=None, Ra=1e7, Pr=0.71, U=0.1, 
     p.bc_thermal[2] = LBM_BCT_ADIABATIC
     p.use_g = 1 if use_g else 0
     p.legacy_thermal = 1 if legacy_thermal else 0
-    p.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    if isinstance(precision, str):
+        p.precision, p.arith = PRECISION_NAMES[precision]
+    else:
+        p.precision, p.arith = int(precision), LBM_ARITH_REFERENCE
     p.pattern = LBM_PATTERN_AA if str(pattern).upper() == "AA" else LBM_PATTERN_AB
     p.seed = int(seed)
     p.noise_amp = float(noise_amp)

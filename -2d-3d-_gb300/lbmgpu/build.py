@@ -6,6 +6,7 @@ Translation units and their floating-point flags:
   lbm_fast.cu               : FP32 arithmetic on FP32/FP16 storage, FMA contraction allowed
   lbm_fast_tma.cu           : the same step with population rows staged by bulk copies
   lbm_fast_aa.cu            : the same step in the in-place (AA) access pattern
+  lbm_fixed.cu              : the fixed arithmetic of FP64 handles (integer pipes, FP64 accuracy)
   lbm_api.cpp               : host code (-ffp-contract=off for the host-side fits)
   lbm_checkpoint.cpp        : Fortran unformatted sequential records (restart files)
   lbm_output.cpp            : snapshot / Tecplot writers, stream function post-processing
@@ -39,6 +40,7 @@ UNITS = [
     ("lbm_checkpoint.cpp", []),
     ("lbm_output.cpp", []),
     ("lbm_noalloc.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
+    ("lbm_fixed.cu", ["-fmad=false"]),
 ]
 
 

@@ -2,20 +2,28 @@
 
 Requests (a Rayleigh-Benard solve each: 2D or 3D, size, Ra, Pr, seed) arrive over time.
 The server keeps every admitted lattice resident in HBM and advances all of them together
-with one flow and one thermal launch per step (lbm_ensemble_step).  A request is admitted
-as soon as its device footprint (lbm_footprint) fits under the HBM budget, so requests
-that arrive while others are running join the running batch at the next chunk boundary.
-Each solve runs until its volume Nusselt number (calNuRe, 2DRB.F90:1610-1675) changes by
-less than `rel_tol` over `check_every` steps, or until `max_steps`.  Per-solve arithmetic
-does not depend on which other lattices share the launches, so a result is the same alone
-and in the mix.
+with one flow and one thermal launch per step (lbm_ensemble_step).  Requests that arrive
+while others run are admitted as soon as their device footprint (lbm_footprint) fits under
+the HBM budget, and join the running batch at the next chunk boundary.
+
+Admission walks the queue in arrival order and admits every request that fits, so a large
+request that does not fit yet does not hold back smaller ones behind it.  The bypass is
+bounded: once the oldest waiting request has been passed over `max_bypass` times, nothing
+behind it is admitted until it fits, so it cannot starve.
+
+Each solve samples its volume Nusselt number (calNuRe, 2DRB.F90:1610-1675) every chunk and
+stops when the mean of the last `window` steps differs from the mean of the `window` steps
+before by less than `rel_tol` (the windowed steady-Nu criterion; the reference's own
+stopping test compares fields 2000 steps apart, 3DRB.F90:225, 245-247), at `max_steps`
+(capped, reported apart from converged solves), or when a diagnostic reports divergence.
+A request whose lattice cannot be created (device memory, parameters) ends as rejected
+without stopping the others.  Per-solve arithmetic does not depend on which other lattices
+share the launches, so a result is the same alone and in the mix.
 """
-import heapq
 import math
 import time
 from dataclasses import dataclass, field
 
-from . import Ensemble, Lattice, LbmDiverged, footprint
 from .abi import rb_params
 
 
@@ -30,12 +38,13 @@ class Request:
     arrival: float = 0.0   # seconds after the start of the run
     precision: str = "fp32"
 
-    def params(self):
+    def params(self, precision=None):
+        prec = precision or self.precision
         if self.dim == 2:
             return rb_params(dim=2, ny=self.n, nx=2 * self.n, Ra=self.Ra, Pr=self.Pr, U=0.1, noise_amp=1e-3,
-                             seed=self.seed, precision=self.precision)
+                             seed=self.seed, precision=prec)
         return rb_params(dim=3, n=self.n, Ra=self.Ra, Pr=self.Pr, U=0.1, noise_amp=1e-3, seed=self.seed,
-                         precision=self.precision)
+                         precision=prec)
 
     @property
     def cells(self):
@@ -55,10 +64,15 @@ class Result:
     cells: int
     nu_history: list = field(default_factory=list)
     diverged: bool = False
+    rejected: str = ""     # why the request was not run ("" when it ran)
 
     @property
     def time_to_solution(self):
         return self.finished - self.arrival
+
+    @property
+    def capped(self):
+        return self.steps > 0 and not self.converged and not self.diverged
 
 
 def poisson_requests(rate, duration, seed=20261203, sizes_2d=(64, 96, 128, 192, 256, 384, 512),
@@ -79,67 +93,132 @@ def poisson_requests(rate, duration, seed=20261203, sizes_2d=(64, 96, 128, 192, 
     return out
 
 
+def windowed_steady(history, window, rel_tol):
+    """history: [(step, Nu)] sampled at a fixed stride.  True when the mean Nu of the last
+    `window` steps differs from the mean of the `window` steps before it by less than
+    rel_tol (relative to the latter)."""
+    if len(history) < 2:
+        return False
+    stride = history[-1][0] - history[-2][0]
+    if stride <= 0:
+        return False
+    k = max(1, window // stride)
+    if len(history) < 2 * k:
+        return False
+    last = [nu for _, nu in history[-k:]]
+    prev = [nu for _, nu in history[-2 * k:-k]]
+    m1, m0 = sum(last) / k, sum(prev) / k
+    return abs(m1 - m0) <= rel_tol * abs(m0)
+
+
 class SolveServer:
-    def __init__(self, device=0, hbm_budget_bytes=None, budget_fraction=0.8, chunk_steps=500, check_every=5000,
-                 rel_tol=1e-3, max_steps=50000, autotune=False):
-        if check_every % chunk_steps:
-            raise ValueError("check_every must be a multiple of chunk_steps")
+    """lattice_factory(params) -> a Lattice-like object (initial, calNuRe, itc, close);
+    ensemble: an Ensemble-like object (add, remove, step, sync, autotune, close);
+    footprint_fn(params) -> bytes.  The defaults are the library's own; tests pass fakes."""
+
+    def __init__(self, device=0, hbm_budget_bytes=None, budget_fraction=0.8, chunk_steps=500, window=5000,
+                 rel_tol=1e-3, max_steps=50000, autotune=False, max_bypass=8, precision="fp32",
+                 lattice_factory=None, ensemble=None, footprint_fn=None, check_every=None):
+        if check_every is not None:  # older name of the window
+            window = check_every
+        if window % chunk_steps:
+            raise ValueError("window must be a multiple of chunk_steps")
+        if max_steps % chunk_steps:
+            raise ValueError("max_steps must be a multiple of chunk_steps (the cap is checked between chunks)")
         self.device = device
-        self.ens = Ensemble(device)
+        if lattice_factory is None or ensemble is None or footprint_fn is None:
+            from . import Ensemble, Lattice, footprint
+            lattice_factory = lattice_factory or (lambda p: Lattice(p, device=device))
+            ensemble = ensemble if ensemble is not None else Ensemble(device)
+            footprint_fn = footprint_fn or footprint
+        self.make_lattice = lattice_factory
+        self.ens = ensemble
+        self.footprint = footprint_fn
         if hbm_budget_bytes is None:
             import torch
             free, total = torch.cuda.mem_get_info(device)
-            hbm_budget_bytes = int(total * budget_fraction)
+            # a fraction of the GPU, but never more than is free now (other users' memory)
+            hbm_budget_bytes = int(min(total * budget_fraction, free * 0.95))
         self.budget = int(hbm_budget_bytes)
+        self.precision = precision
         self.chunk = int(chunk_steps)
-        self.check_every = int(check_every)
+        self.window = int(window)
         self.rel_tol = float(rel_tol)
         self.max_steps = int(max_steps)
         self.autotune = autotune
+        self.max_bypass = int(max_bypass)
         self.used = 0
-        self.active = {}   # rid -> (request, lattice, bytes, admitted_t, last_check_nu, history)
-        self.queue = []    # FIFO of waiting requests
+        self.active = {}   # rid -> [request, lattice, bytes, admitted_t, history]
+        self.queue = []    # waiting requests in arrival order
+        self.bypassed = {}  # rid -> times a later request was admitted ahead of it
         self.results = []
         self.peak_active = 0
         self.peak_queue = 0
 
-    def _admit(self, now):
-        admitted = False
-        while self.queue:
-            req = self.queue[0]
-            need = footprint(req.params())
-            if need > self.budget:
-                self.queue.pop(0)  # can never fit: reject
-                self.results.append(Result(req.rid, float("nan"), float("nan"), 0, False, req.arrival, now, now,
-                                           req.cells))
-                continue
-            if self.used + need > self.budget:
-                break
-            self.queue.pop(0)
-            lat = Lattice(req.params(), device=self.device)
+    def _reject(self, req, now, why):
+        self.results.append(Result(req.rid, float("nan"), float("nan"), 0, False, req.arrival, now, now, req.cells,
+                                   rejected=why))
+
+    def _start(self, req, now, need):
+        """Create, initialise and add one lattice; False (and a rejected result) on failure."""
+        lat = None
+        try:
+            lat = self.make_lattice(req.params(self.precision))
             lat.initial()
             self.ens.add(lat)
-            self.used += need
-            self.active[req.rid] = [req, lat, need, now, None, []]
-            admitted = True
+        except Exception as e:  # device memory, parameters, ensemble refusal: this request only
+            if lat is not None:
+                try:
+                    lat.close()
+                except Exception:
+                    pass
+            self._reject(req, now, "%s: %s" % (type(e).__name__, e))
+            return False
+        self.used += need
+        self.active[req.rid] = [req, lat, need, now, []]
+        return True
+
+    def _admit(self, now):
+        admitted = False
+        keep = []
+        blocked = False  # the oldest waiting request has been bypassed max_bypass times
+        for req in self.queue:
+            try:
+                need = self.footprint(req.params(self.precision))
+            except Exception as e:
+                self._reject(req, now, "parameters: %s" % e)
+                continue
+            if need > self.budget:
+                self._reject(req, now, "footprint %d B exceeds the budget %d B" % (need, self.budget))
+                continue
+            if blocked or self.used + need > self.budget:
+                keep.append(req)
+                if not blocked and self.bypassed.get(req.rid, 0) >= self.max_bypass:
+                    blocked = True
+                continue
+            if self._start(req, now, need):
+                admitted = True
+                for w in keep:  # everyone still waiting ahead of it was bypassed once more
+                    self.bypassed[w.rid] = self.bypassed.get(w.rid, 0) + 1
+                    if self.bypassed[w.rid] >= self.max_bypass:
+                        blocked = True
+        self.queue = keep
         self.peak_active = max(self.peak_active, len(self.active))
         return admitted
 
     def _finish(self, rid, now, converged, nu, re, diverged=False):
-        req, lat, need, adm, _, hist = self.active.pop(rid)
-        self.results.append(Result(rid, nu, re, lat.itc, converged, req.arrival, adm, now, req.cells, hist,
-                                   diverged))
+        req, lat, need, adm, hist = self.active.pop(rid)
+        self.results.append(Result(rid, nu, re, lat.itc, converged, req.arrival, adm, now, req.cells, hist, diverged))
         self.ens.remove(lat)
         lat.close()
         self.used -= need
+        self.bypassed.pop(rid, None)
 
     def _check(self, now):
+        from . import LbmDiverged
         for rid in list(self.active):
-            req, lat, need, adm, last, hist = self.active[rid]
+            req, lat, need, adm, hist = self.active[rid]
             steps = lat.itc
-            due = steps >= (len(hist) + 1) * self.check_every
-            if not due and steps < self.max_steps:
-                continue
             try:
                 nu, re = lat.calNuRe()
             except LbmDiverged:
@@ -147,14 +226,12 @@ class SolveServer:
                 self._finish(rid, now, False, float("nan"), float("nan"), diverged=True)
                 continue
             hist.append((steps, nu))
-            if last is not None and abs(nu - last) <= self.rel_tol * abs(last):
+            if windowed_steady(hist, self.window, self.rel_tol):
                 self._finish(rid, now, True, nu, re)
             elif steps >= self.max_steps:
                 self._finish(rid, now, False, nu, re)
-            else:
-                self.active[rid][4] = nu
 
-    def run(self, requests, time_limit=None, clock=time.perf_counter):
+    def run(self, requests, time_limit=None, clock=time.perf_counter, sleep=time.sleep):
         """Serve `requests` (arrival times relative to the start); returns the results."""
         pending = sorted(requests, key=lambda r: r.arrival)
         t0 = clock()
@@ -165,13 +242,19 @@ class SolveServer:
             if time_limit is not None and now > time_limit:
                 break
             while i < len(pending) and pending[i].arrival <= now:
-                self.queue.append(pending[i])
+                if pending[i].precision != self.precision and pending[i].precision is not None:
+                    self._reject(pending[i], now, "precision %s: this server batches %s" %
+                                 (pending[i].precision, self.precision))
+                else:
+                    self.queue.append(pending[i])
                 i += 1
             self.peak_queue = max(self.peak_queue, len(self.queue))
             self._admit(now)
             if not self.active:
                 if i < len(pending):
-                    time.sleep(max(0.0, min(0.05, pending[i].arrival - now)))
+                    sleep(max(0.0, min(0.05, pending[i].arrival - now)))
+                elif self.queue:
+                    break  # nothing running and nothing that fits: cannot happen with rejections above
                 continue
             if self.autotune and not tuned and len(self.active) > 1:
                 self.ens.autotune(2)
@@ -183,30 +266,36 @@ class SolveServer:
 
     def close(self):
         for rid in list(self.active):
-            req, lat, need, adm, last, hist = self.active.pop(rid)
+            req, lat, need, adm, hist = self.active.pop(rid)
             self.ens.remove(lat)
             lat.close()
         self.ens.close()
 
 
 def summarize(results, wall_seconds):
-    done = [r for r in results if r.steps > 0]
-    tts = sorted(r.time_to_solution for r in done)
+    ran = [r for r in results if r.steps > 0]
+    conv = [r for r in ran if r.converged]
+    tts = sorted(r.time_to_solution for r in conv)
 
-    def pct(p):
-        if not tts:
+    def pct(xs, p):
+        if not xs:
             return None
-        k = min(len(tts) - 1, max(0, int(math.ceil(p / 100.0 * len(tts))) - 1))
-        return tts[k]
+        k = min(len(xs) - 1, max(0, int(math.ceil(p / 100.0 * len(xs))) - 1))
+        return xs[k]
 
-    cells_steps = sum(r.cells * r.steps for r in done)
+    tts_all = sorted(r.time_to_solution for r in ran)
+    cells_steps = sum(r.cells * r.steps for r in ran)
     return {
-        "completed": len(done),
-        "converged": sum(1 for r in done if r.converged),
-        "capped": sum(1 for r in done if not r.converged and not r.diverged),
-        "diverged": sum(1 for r in done if r.diverged),
-        "solves_per_hour": 3600.0 * len(done) / wall_seconds if wall_seconds > 0 else None,
-        "p50_s": pct(50),
-        "p99_s": pct(99),
+        "completed": len(ran),
+        "converged": len(conv),
+        "capped": sum(1 for r in ran if r.capped),
+        "diverged": sum(1 for r in ran if r.diverged),
+        "rejected": sum(1 for r in results if r.rejected),
+        "converged_solves_per_hour": 3600.0 * len(conv) / wall_seconds if wall_seconds > 0 else None,
+        "completed_solves_per_hour": 3600.0 * len(ran) / wall_seconds if wall_seconds > 0 else None,
+        "p50_s": pct(tts, 50),
+        "p99_s": pct(tts, 99),
+        "p50_s_all_completed": pct(tts_all, 50),
+        "p99_s_all_completed": pct(tts_all, 99),
         "aggregate_mlups": cells_steps / wall_seconds / 1e6 if wall_seconds > 0 else None,
     }

@@ -1,18 +1,21 @@
 #!/usr/bin/env python3
 """Benchmark of the coupled thermal MRT-LBM time step on GB300.
 
-Workload: 3D Rayleigh-Benard cube, D3Q19 MRT flow + D3Q7 MRT temperature, 128^3 cells,
+Workload: 3D Rayleigh-Benard cube, D3Q19 MRT flow + D3Q7 MRT temperature, 256^3 cells,
 no-slip walls, adiabatic side walls, hot bottom (+0.5) / cold top (-0.5), Ra = 1e7,
 Pr = 0.71, free-fall velocity U = 0.1, linear T + seeded 1e-3 noise.  A "step" is one
 coupled (flow + thermal) time step over the whole lattice; MLUPS counts one coupled cell
 update as one, as the reference's runtime print does (3DRB.F90:303-305).
 
-Headline `value`: the plain method (FP64, the reference's arithmetic) through the fused
-kernels, inputs resident in HBM.  The FP32 / FP16 storage forms of the same workload are
-reported beside it.  `e2e` is the same metric through the C ABI with host buffers in the
-reference's Fortran layout (state in, steps, T field and Nu/Re out).  `cpu_baseline` is
-the C++ restatement of the reference's OpenMP CPU path timed on this host's cores; the GPU
-then runs the same steps and the two temperature fields are compared bit for bit.
+Headline `value`: the plain method to FP64 accuracy, through the fused kernels of the fixed
+arithmetic (q60 integers on the integer pipes; within 1e-12 of the reference's populations
+after 1000 steps, within 1e-10 in Nu), inputs resident in HBM.  Beside it: the plain method
+in the reference's own FP64 operations (bit for bit the reference), and the FP32 / FP16
+storage forms.  `e2e` is the headline metric through the C ABI with host buffers in the
+reference's Fortran layout (state in, steps, T field and Nu/Re out).  `cpu_baseline` is the
+C++ restatement of the reference's OpenMP CPU path timed on this host's cores; the GPU then
+runs the same steps with the reference's arithmetic and the two temperature fields are
+compared bit for bit.  The 128^3 configuration is a secondary leg (`config1_128`).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
@@ -34,14 +37,15 @@ for _p in (ROOT, PKG_ROOT):
 
 METRIC = "coupled MLUPS (D3Q19/D3Q7 MRT-LBM step)"
 UNIT = "MLUPS"
-N_CELL_EDGE = 128
-BYTES_PER_CELL = {"fp64": 416, "fp32": 208, "fp16": 104}  # populations read + written once
+N_CELL_EDGE = 256
+BYTES_PER_CELL = {"fp64": 416, "fp64x": 416, "fp32": 208, "fp16": 104}  # populations read + written once
 # FP64 work of the plain method per coupled cell update (3D), counted by ncu on the fused
 # kernels (sass thread instructions, flow + thermal): dadd 398, dmul 103, dfma 57.  Products
 # with exact powers of two run on the integer pipes and are not counted.
 FP64_INST_PER_CELL = 398 + 103 + 57
 FP64_FLOP_PER_CELL = 398 + 103 + 2 * 57
-DTYPE = {"fp64": "f64", "fp32": "f32", "fp16": "f16-storage/f32-arith"}
+DTYPE = {"fp64": "f64", "fp64x": "i64 fixed-point 2^-60 (FP64 accuracy)", "fp32": "f32",
+         "fp16": "f16-storage/f32-arith"}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -55,7 +59,8 @@ def workload_config(n=N_CELL_EDGE):
         "workload": "3D Rayleigh-Benard cube D3Q19/D3Q7 MRT, %d^3 cells, Ra=1e7, Pr=0.71, U=0.1, no-slip walls, "
                     "adiabatic sides, T linear + 1e-3 seeded noise (seed 20261203)" % n,
         "cells": n ** 3,
-        "l2": "inputs larger than L2 (FP64 populations 872 MB, FP32 436 MB, FP16 218 MB per step)",
+        "l2": "inputs larger than L2 (populations per step: FP64 %.0f MB, FP32 %.0f MB, FP16 %.0f MB; L2 129 MB)"
+              % (416 * n ** 3 / 1e6, 208 * n ** 3 / 1e6, 104 * n ** 3 / 1e6),
         "step": "one coupled flow+thermal time step over the whole lattice",
     }
 
@@ -245,10 +250,10 @@ def run_reference(args):
     return 0
 
 
-def time_precision(prec, args, pg, local):
+def time_precision(prec, args, pg, local, size=None):
     import torch
     import lbmgpu
-    p = workload_params(prec, args.size)
+    p = workload_params(prec, size or args.size)
     lat = lbmgpu.Lattice(p, device=local)
     lat.initial()
     lat.step(args.warmup)
@@ -318,11 +323,47 @@ def plain_rate_2d(local, ny=128):
     return 2 * ny * ny * 3200 / dt / 1e6
 
 
-def ensemble_run(args, local, steps_total=13000):
+def run_sampled(p, local, steps, every):
+    """One lattice run alone for `steps` steps, calNuRe sampled every `every` steps; returns
+    (seconds on the device stream, [(step, Nu)], diverged)."""
+    import torch
+    import lbmgpu
+    lat = lbmgpu.Lattice(p, device=local)
+    lat.initial()
+    stream = torch.cuda.ExternalStream(lat.stream_handle(), device=torch.device("cuda", local))
+    hist, diverged = [], False
+    t_dev = 0.0
+    done = 0
+    while done < steps:
+        k = min(every, steps - done)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        lat.step(k)
+        b.record(stream)
+        b.synchronize()
+        t_dev += a.elapsed_time(b) / 1e3
+        done += k
+        try:
+            hist.append((done, lat.calNuRe()[0]))
+        except lbmgpu.LbmDiverged:
+            diverged = True
+            break
+    lat.close()
+    return t_dev, hist, diverged
+
+
+def tail_mean(hist, from_step):
+    xs = [nu for s, nu in hist if s > from_step]
+    return sum(xs) / len(xs) if xs else None
+
+
+def ensemble_run(args, local, steps_total=13000, every=500):
     """Batched form (BASELINE config 3): 64 D2Q9/D2Q5 RB instances, aspect 2, ny drawn from
     {64,...,512}, Ra log-uniform in [1e4, 1e8], Pr in {0.71, 7}, U = 0.1, FP32 storage, one
-    launch per stage over a packed tile table, graph replay, autotuned tiles.  |dNu| is
-    measured against FP64 plain solves of the four smallest instances."""
+    launch per stage over a packed tile table, graph replay, autotuned tiles.  Every member's
+    Nu is sampled every `every` steps; each member is then run alone at FP64 accuracy (the
+    fixed arithmetic, which stays within 1e-12 of the plain method's populations) and the
+    time-averaged Nu of the second half of the run is compared member by member."""
     import random
     import torch
     import lbmgpu
@@ -354,90 +395,136 @@ def ensemble_run(args, local, steps_total=13000):
     b.synchronize()
     ms = a.elapsed_time(b)
     mlups = cells * k / (ms / 1e3) / 1e6
-    # run on to a developed flow and compare the four smallest instances with FP64 solves
-    done = lats[0].itc
-    if steps_total > done:
-        ens.step(steps_total - done)
-    ens.sync()
-    diverged = []
-    nus = {}
-    for m, lat in enumerate(lats):
-        try:
-            nus[m] = lat.calNuRe()[0]
-        except lbmgpu.LbmDiverged:
-            diverged.append({"ny": specs[m]["ny"], "Ra": specs[m]["Ra"], "Pr": specs[m]["Pr"],
-                             "tauf": lat.constants()["tauf"]})
-    small = sorted(nus, key=lambda m: (specs[m]["ny"], m))[:4]
-    dnu = []
-    for m in small:
-        nu32 = nus[m]
-        ref = lbmgpu.Lattice(rb_params(precision="fp64", **specs[m]), device=local)
-        ref.initial()
-        ref.step(lats[m].itc)
-        nu64, _ = ref.calNuRe()
-        ref.close()
-        dnu.append({"ny": specs[m]["ny"], "Ra": specs[m]["Ra"], "Pr": specs[m]["Pr"], "steps": lats[m].itc,
-                    "Nu_fp32_batched": nu32, "Nu_fp64_plain": nu64, "rel_dNu": abs(nu32 - nu64) / abs(nu64)})
+    # run every member on to steps_total, sampling Nu at multiples of `every`
+    hist = {m: [] for m in range(64)}
+    diverged = {}
+    while lats[0].itc < steps_total:
+        done = lats[0].itc
+        nxt = min(steps_total, (done // every + 1) * every)
+        ens.step(nxt - done)
+        ens.sync()
+        for m, lat in enumerate(lats):
+            if m in diverged:
+                continue
+            try:
+                hist[m].append((lat.itc, lat.calNuRe()[0]))
+            except lbmgpu.LbmDiverged:
+                diverged[m] = lat.itc
     ens.close()
     for lat in lats:
         lat.close()
+    half = steps_total // 2
+    members = []
+    for m, sp in enumerate(specs):
+        rec = {"member": m, "ny": sp["ny"], "Ra": sp["Ra"], "Pr": sp["Pr"]}
+        if m in diverged:
+            rec["diverged_fp32_at"] = diverged[m]
+            members.append(rec)
+            continue
+        _, h64, div64 = run_sampled(rb_params(precision="fp64x", **sp), local, steps_total, every)
+        rec["Nu_fp32_batched"] = tail_mean(hist[m], half)
+        rec["Nu_fp64"] = tail_mean(h64, half) if not div64 else None
+        if rec["Nu_fp64"] is not None and rec["Nu_fp32_batched"] is not None:
+            rec["rel_dNu"] = abs(rec["Nu_fp32_batched"] - rec["Nu_fp64"]) / abs(rec["Nu_fp64"])
+        members.append(rec)
+    good = [r["rel_dNu"] for r in members if "rel_dNu" in r and r["Nu_fp64"] >= 1.0]
+    unphys = [r["member"] for r in members if r.get("Nu_fp64") is not None and r["Nu_fp64"] < 1.0]
+    good.sort()
     return {"workload": "64 D2Q9/D2Q5 RB instances, aspect 2, ny in {64..512}, Ra log-uniform 1e4..1e8, "
                         "Pr in {0.71,7}, FP32 storage, %d cells" % cells,
             "aggregate_mlups": mlups, "ms_per_step": ms / k, "steps_timed": k, "autotuned": cfg,
-            "launches_per_step": 2, "dNu_vs_fp64": dnu,
-            "diverged": {"count": len(diverged), "cases": diverged,
-                         "note": "under-resolved draws (tau_f close to 1/2) reported as LBM_ERR_DIVERGED"}}
+            "launches_per_step": 2,
+            "dNu_vs_fp64": {
+                "compared": len(good), "median": good[len(good) // 2] if good else None,
+                "max": good[-1] if good else None, "within_1pct": sum(1 for x in good if x <= 0.01),
+                "excluded_unphysical_fp64_Nu_below_1": unphys,
+                "how": "time-averaged Nu over steps %d..%d sampled every %d steps; FP64 reference: each member "
+                       "alone with the fixed arithmetic (FP64 accuracy)" % (half, steps_total, every)},
+            "members": members,
+            "diverged": {"count": len(diverged), "note": "under-resolved draws (tau_f close to 1/2) reported as "
+                                                         "LBM_ERR_DIVERGED"}}
 
 
-def served_run(args, local, plain3d_mlups):
+def served_run(args, local):
     """Served form (BASELINE config 4): Poisson arrivals at 2/s, half 2D (ny 64..512, aspect 2)
     half 3D (n 64..192), Ra log-uniform 1e4..1e8, Pr in {0.71, 7}, FP32, admission by an 80%
-    HBM budget, each solve run until Nu changes by < 0.1% over a window of steps or a step cap.
-    The default run is scaled to fit a bench (20 s of arrivals, 1000-step window, 4000-step
-    cap); --served-full runs the configuration as stated (600 s, 5000-step window)."""
+    HBM budget, each solve run until its windowed-mean Nu changes by < 0.1% between
+    consecutive windows, or a step cap.  The default run is scaled to fit a bench (20 s of
+    arrivals, 1000-step window, 4000-step cap); --served-full runs the configuration as stated
+    (600 s, 5000-step window).  A seeded random sample of the served requests is then run one
+    at a time with the plain FP64 method and with the FP64-accuracy fixed arithmetic for the
+    same steps: their measured solves/h, and |dNu| of the windowed means."""
+    import random
     import lbmgpu
     from lbmgpu import server as srv
     duration, drain = args.served_seconds, args.served_drain
     window, cap = args.served_window, args.served_cap
+    chunk = 500
     reqs = srv.poisson_requests(2.0, duration)
-    s = srv.SolveServer(device=local, chunk_steps=500, check_every=window, rel_tol=1e-3, max_steps=cap,
+    s = srv.SolveServer(device=local, chunk_steps=chunk, window=window, rel_tol=1e-3, max_steps=cap,
                         autotune=False)
     t0 = time.perf_counter()
     results = s.run(reqs, time_limit=duration + drain)
     wall = time.perf_counter() - t0
-    unfinished = len(s.active) + len(s.queue) + (len(reqs) - len(results) - len(s.active) - len(s.queue))
+    finished = {r.rid for r in results}
+    unfinished = len(reqs) - len(finished)
     summary = srv.summarize(results, wall)
     peak = (s.peak_active, s.peak_queue)
     s.close()
-    # plain FP64 method, one solve at a time, on the same completed work
-    plain2d = plain_rate_2d(local)
     by_id = {r.rid: r for r in reqs}
-    done = [r for r in results if r.steps > 0]
-    plain_s = sum(r.cells * r.steps / ((plain2d if by_id[r.rid].dim == 2 else plain3d_mlups) * 1e6) for r in done)
-    # |dNu| of the two smallest completed solves against FP64 plain solves of the same length
+    ran = [r for r in results if r.steps > 0 and not r.diverged]
+    rng = random.Random(7)
+    sample = rng.sample(ran, min(len(ran), args.served_sample))
+    plain = {"fp64": [0.0, 0], "fp64x": [0.0, 0]}
     dnu = []
-    for r in sorted([r for r in done if not r.diverged], key=lambda r: r.cells)[:2]:
+    t_budget = time.perf_counter() + args.served_plain_budget
+    for r in sample:
+        if time.perf_counter() > t_budget:
+            break
         q = by_id[r.rid]
-        p64 = q.params()
-        p64.precision = 0
-        ref = lbmgpu.Lattice(p64, device=local)
-        ref.initial()
-        ref.step(r.steps)
-        nu64, _ = ref.calNuRe()
-        ref.close()
-        dnu.append({"rid": r.rid, "dim": q.dim, "n": q.n, "Ra": q.Ra, "steps": r.steps, "Nu_fp32_served": r.Nu,
-                    "Nu_fp64_plain": nu64, "rel_dNu": abs(r.Nu - nu64) / abs(nu64)})
+        rec = {"rid": r.rid, "dim": q.dim, "n": q.n, "Ra": q.Ra, "Pr": q.Pr, "steps": r.steps,
+               "converged": r.converged}
+        last = [nu for st, nu in r.nu_history if st > r.steps - window]
+        rec["Nu_fp32_served"] = sum(last) / len(last) if last else None
+        for prec in ("fp64x", "fp64"):
+            t, h, div = run_sampled(q.params(prec), local, r.steps, chunk)
+            plain[prec][0] += t
+            plain[prec][1] += 1
+            rec["s_" + prec] = t
+            if prec == "fp64x" and not div:
+                rec["Nu_fp64"] = tail_mean(h, r.steps - window)
+        if rec.get("Nu_fp64") and rec["Nu_fp32_served"] is not None:
+            rec["rel_dNu"] = abs(rec["Nu_fp32_served"] - rec["Nu_fp64"]) / abs(rec["Nu_fp64"])
+        dnu.append(rec)
+    rel = sorted(x["rel_dNu"] for x in dnu if "rel_dNu" in x)
     summary.update({
         "workload": "Poisson arrivals 2/s for %.0f s, 50/50 2D (ny 64..512, aspect 2) / 3D (n 64..192), Ra "
-                    "log-uniform 1e4..1e8, Pr {0.71,7}, FP32, 80%% HBM budget, stop at |dNu|<0.1%% over %d steps or "
-                    "at %d steps; drain limit %.0f s%s" % (duration, window, cap, drain,
-                    "" if args.served_full else " (scaled from 600 s / 5000-step window: the stated stream "
-                    "oversubscribes one GPU several times)"),
+                    "log-uniform 1e4..1e8, Pr {0.71,7}, FP32, 80%% HBM budget, stop when the %d-step windowed mean "
+                    "of Nu changes < 0.1%% or at %d steps; drain limit %.0f s%s" % (duration, window, cap, drain,
+                    "" if args.served_full else " (scaled from 600 s / 5000-step window)"),
         "arrived": len(reqs), "unfinished_at_limit": unfinished, "wall_s": wall,
         "peak_active": peak[0], "peak_queue": peak[1],
-        "plain_fp64_solves_per_hour_same_work": 3600.0 * len(done) / plain_s if plain_s > 0 else None,
-        "dNu_vs_fp64": dnu,
+        "one_at_a_time_sample": {
+            "requests": len(dnu), "of": len(ran),
+            "plain_fp64_solves_per_hour": 3600.0 * plain["fp64"][1] / plain["fp64"][0] if plain["fp64"][0] else None,
+            "fixed_fp64_solves_per_hour": 3600.0 * plain["fp64x"][1] / plain["fp64x"][0] if plain["fp64x"][0]
+            else None,
+            "note": "each sampled request run alone for the steps it ran served, device time only (no queueing); "
+                    "served solves/h are whole-run wall-clock rates of a different mix, so compare rates per "
+                    "solve of the same sample via served_vs_plain below"},
+        "dNu_vs_fp64": {"compared": len(rel), "median": rel[len(rel) // 2] if rel else None,
+                        "max": rel[-1] if rel else None, "within_1pct": sum(1 for x in rel if x <= 0.01),
+                        "solves": dnu,
+                        "how": "windowed mean of Nu over the solve's last window: served FP32 vs the same request "
+                               "alone at FP64 accuracy (fixed arithmetic) for the same steps"},
     })
+    # throughput of the same sampled work: served aggregate cell updates/s against one at a time
+    if plain["fp64"][0] and dnu:
+        work = sum(by_id[x["rid"]].cells * x["steps"] for x in dnu)
+        summary["served_vs_plain"] = {
+            "served_aggregate_mlups": summary["aggregate_mlups"],
+            "plain_fp64_mlups_one_at_a_time": work / plain["fp64"][0] / 1e6,
+            "fixed_fp64_mlups_one_at_a_time": work / plain["fp64x"][0] / 1e6 if plain["fp64x"][0] else None}
     return summary
 
 
@@ -493,6 +580,102 @@ def at_size_run(args, local, peak, n=384, steps=40):
         out[prec]["vs_fp64_AA"] = {"T_L2_rel": float(np.linalg.norm(t - t64) / dev),
                                    "dNu_rel": abs(nu - nu64) / abs(nu64), "dRe_rel": abs(re - re64) / abs(re64)}
     return out
+
+
+def mean_and_se(xs, batches=10):
+    """Mean of a time series and its standard error from batch means (consecutive blocks),
+    which accounts for the correlation of neighbouring samples of a chaotic flow."""
+    import numpy as np
+    x = np.asarray(xs, dtype=np.float64)
+    if x.size == 0:
+        return None, None
+    nb = min(batches, x.size)
+    blocks = np.array_split(x, nb)
+    means = np.array([b.mean() for b in blocks])
+    se = float(means.std(ddof=1) / math.sqrt(nb)) if nb > 1 else None
+    return float(x.mean()), se
+
+
+def time_series_run(p, local, steps, every, tail_frac):
+    """Advance one lattice `steps` steps, sampling the calNuRe volume Nu and Re every `every`
+    steps (as the reference appends NuVolAvg(t) on every call, 3DRB.F90:1753-1770); returns
+    the series and the mean and standard error over the last `tail_frac` of the samples."""
+    import lbmgpu
+    lat = lbmgpu.Lattice(p, device=local)
+    lat.initial()
+    series = []
+    t0 = time.perf_counter()
+    diverged = None
+    for s in range(every, steps + 1, every):
+        lat.step(every)
+        try:
+            nu, re = lat.calNuRe()
+        except lbmgpu.LbmDiverged as e:
+            diverged = {"step": s, "error": str(e)}
+            break
+        series.append((s, nu, re))
+    lat.sync()
+    wall = time.perf_counter() - t0
+    lat.close()
+    tail = series[int(len(series) * (1.0 - tail_frac)):]
+    nu_m, nu_se = mean_and_se([x[1] for x in tail])
+    re_m, re_se = mean_and_se([x[2] for x in tail])
+    return {"steps": series[-1][0] if series else 0, "wall_s": wall, "samples_averaged": len(tail),
+            "Nu_mean": nu_m, "Nu_se": nu_se, "Re_mean": re_m, "Re_se": re_se, "diverged": diverged,
+            "series": series}
+
+
+def accuracy_run(args, local):
+    """Time-averaged Nu and Re of the storage forms against FP64 on one configuration.
+
+    config1: the 128^3 cube at Ra 1e7 (U 0.1); config2: the 384^3 cube at Ra 1e9 (U 0.07,
+    in-place pattern).  Each run samples calNuRe every `every` steps and averages the last
+    `tail` fraction; the standard error comes from batch means.  Two seeds per storage form
+    give the spread of the time average that the chaotic flow itself produces, against which
+    |dNu| between storage forms is read."""
+    from lbmgpu.abi import rb_params
+    cfg = args.accuracy
+    if cfg == "config1":
+        base = dict(dim=3, n=128, Ra=1e7, Pr=0.71, U=0.1, noise_amp=1e-3, pattern="AB")
+        default_steps, tail = 150000, 0.5
+    else:
+        base = dict(dim=3, n=384, Ra=1e9, Pr=0.71, U=0.07, noise_amp=1e-3, pattern="AA")
+        default_steps, tail = 200000, 0.2
+    steps = args.accuracy_steps or default_steps
+    every = args.accuracy_every
+    runs = {}
+    for item in args.accuracy_forms.split(","):
+        prec, _, seed_tag = item.partition(":")
+        seed = 20261203 + (int(seed_tag) if seed_tag else 0)
+        p = rb_params(precision=prec, seed=seed, **base)
+        key = "%s:seed%d" % (prec, seed)
+        runs[key] = time_series_run(p, local, steps, every, tail)
+        runs[key]["precision"] = prec
+        runs[key]["seed"] = seed
+        print(json.dumps({"accuracy_run": key, "Nu_mean": runs[key]["Nu_mean"], "Nu_se": runs[key]["Nu_se"],
+                          "Re_mean": runs[key]["Re_mean"], "wall_s": runs[key]["wall_s"]}), file=sys.stderr,
+              flush=True)
+    ref_key = next((k for k in runs if runs[k]["precision"] == args.accuracy_ref), None)
+    cmp = {}
+    if ref_key is not None and runs[ref_key]["Nu_mean"]:
+        r = runs[ref_key]
+        for k, x in runs.items():
+            if k == ref_key or x["Nu_mean"] is None:
+                continue
+            cmp[k] = {
+                "dNu_rel": abs(x["Nu_mean"] - r["Nu_mean"]) / abs(r["Nu_mean"]),
+                "dNu_rel_se": math.hypot(x["Nu_se"] or 0.0, r["Nu_se"] or 0.0) / abs(r["Nu_mean"]),
+                "dRe_rel": abs(x["Re_mean"] - r["Re_mean"]) / abs(r["Re_mean"]),
+                "dRe_rel_se": math.hypot(x["Re_se"] or 0.0, r["Re_se"] or 0.0) / abs(r["Re_mean"]),
+            }
+    out = {"accuracy": cfg, "workload": base, "steps": steps, "sample_every": every, "tail_fraction": tail,
+           "reference_run": ref_key, "vs_reference": cmp,
+           "runs": {k: {kk: vv for kk, vv in v.items() if kk != "series"} for k, v in runs.items()}}
+    if args.accuracy_series:
+        with open(args.accuracy_series, "w") as fh:
+            json.dump({k: v["series"] for k, v in runs.items()}, fh)
+    print(json.dumps(out))
+    return 0
 
 
 def config0_run(args, local, steps=20000, cpu_steps=20000):
@@ -602,10 +785,21 @@ def run_gpu(args):
                          "dtype": DTYPE[prec], "roofline": roof(prec), "Nu": results[prec]["Nu"],
                          "Re": results[prec]["Re"]} for prec in results},
     }
+    if rank == 0 and not args.no_128 and args.size != 128:
+        leg = {}
+        for prec in precs:
+            r = time_precision(prec, args, None, local, size=128)
+            leg[prec] = {"mlups": r["mlups"], "ms_per_step": r["ms_per_step"], "ms_flow": r["ms_flow"],
+                         "ms_thermal": r["ms_thermal"], "Nu": r["Nu"], "Re": r["Re"],
+                         "hbm_frac": BYTES_PER_CELL[prec] * 128 ** 3 / ((r["ms_flow"] + r["ms_thermal"]) / 1e3) / 1e9
+                         / peak}
+        line["config1_128"] = {"workload": workload_config(128)["workload"], "forms": leg,
+                               "note": "hbm_frac: algorithmic bytes over the flow + thermal kernel time per step, "
+                                       "of the measured HBM peak"}
     if rank == 0 and not args.no_ensemble:
         line["batched"] = ensemble_run(args, local)
     if rank == 0 and not args.no_served:
-        line["served"] = served_run(args, local, results["fp64"]["mlups"] if "fp64" in results else 700.0)
+        line["served"] = served_run(args, local)
     if rank == 0 and not args.no_size:
         line["at_384"] = at_size_run(args, local, peak)
     if rank == 0 and not args.no_config0:
@@ -634,16 +828,35 @@ def main():
     ap.add_argument("--served-drain", type=float, default=40.0)
     ap.add_argument("--served-window", type=int, default=1000)
     ap.add_argument("--served-cap", type=int, default=4000)
-    ap.add_argument("--size", type=int, default=N_CELL_EDGE, help="cube edge (cells); 128 is the benchmark")
-    ap.add_argument("--precisions", default="fp64,fp32,fp16",
-                    help="comma list; the first is the headline form")
+    ap.add_argument("--served-sample", type=int, default=10, help="served requests re-run one at a time in FP64")
+    ap.add_argument("--served-plain-budget", type=float, default=90.0,
+                    help="seconds for the one-at-a-time FP64 re-runs of the served sample")
+    ap.add_argument("--size", type=int, default=N_CELL_EDGE, help="cube edge (cells); 256 is the benchmark")
+    ap.add_argument("--precisions", default="fp64x,fp64,fp32,fp16",
+                    help="comma list; the first is the headline form (fp64x: FP64 handle, fixed arithmetic)")
+    ap.add_argument("--no-128", action="store_true", help="skip the 128^3 secondary leg")
+    ap.add_argument("--accuracy", choices=["config1", "config2"], default=None,
+                    help="instead of the benchmark: time-averaged Nu/Re of the storage forms against FP64")
+    ap.add_argument("--accuracy-forms", default="fp64,fp64:1,fp32,fp32:1,fp16,fp16:1",
+                    help="comma list of precision[:seed offset] runs of the accuracy leg")
+    ap.add_argument("--accuracy-ref", default="fp64", help="precision of the run the others are compared with")
+    ap.add_argument("--accuracy-steps", type=int, default=0, help="steps per run (0: the configuration's own)")
+    ap.add_argument("--accuracy-every", type=int, default=500, help="steps between calNuRe samples")
+    ap.add_argument("--accuracy-series", default=None, help="write the sampled (step, Nu, Re) series to this file")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.served_full:
-        args.served_seconds, args.served_drain, args.served_window, args.served_cap = 600.0, 1200.0, 5000, 50000
+        args.served_seconds, args.served_drain, args.served_window, args.served_cap = 600.0, 600.0, 5000, 50000
+        args.served_plain_budget = max(args.served_plain_budget, 300.0)
     if args.impl == "reference":
         return run_reference(args)
+    if args.accuracy:
+        import torch
+        torch.cuda.set_device(0)
+        from lbmgpu import build as lbuild
+        lbuild.build()
+        return accuracy_run(args, 0)
     return run_gpu(args)
 
 

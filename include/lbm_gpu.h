@@ -57,6 +57,22 @@ extern "C" {
 #define LBM_FP32 1 /* FP32 storage of deviations from rest weights, FP32 arithmetic          */
 #define LBM_FP16 2 /* FP16 storage of deviations from rest weights, FP32 arithmetic          */
 
+/* ---- arithmetic of FP64 handles (lbm_params.arith) ------------------------------------- */
+/* LBM_ARITH_REFERENCE: the plain method, the reference's FP64 operations in its expression
+ *   order, bit for bit equal to the reference's CPU build (bound by GB300's FP64 pipe).
+ * LBM_ARITH_FIXED: the same step to FP64 accuracy on the integer pipes (no counterpart in the
+ *   reference).  The fused buffers hold populations as 64-bit fixed-point deviations from
+ *   the rest state (units of 2^-60); the moment transforms are exact integer sums and the
+ *   relaxation, equilibria, force and 1/rho are 128-bit integer products, each rounded once
+ *   below 2^-60.  Results match the reference to rounding (tested: <= 1e-12 relative in the
+ *   populations after 1000 steps, <= 1e-10 in Nu, except where the flow amplifies rounding,
+ *   where it stays within the distance of the reference's own FMA-contracted build).  The
+ *   module arrays, diagnostics, state transfer and restart files are the FP64 handle's; a
+ *   restart continues from the FP64 module state.  Two-buffer pattern only; not with
+ *   SideHeatedHa. */
+#define LBM_ARITH_REFERENCE 0
+#define LBM_ARITH_FIXED     1
+
 /* ---- streaming pattern ---------------------------------------------------------------- */
 #define LBM_PATTERN_AB 0 /* two population buffers (ping-pong)                              */
 #define LBM_PATTERN_AA 1 /* one buffer, in-place even/odd (AA) access pattern               */
@@ -101,7 +117,7 @@ typedef struct lbm_params {
     uint64_t seed;          /* seed of the initial temperature noise                        */
     double  noise_amp;      /* T += noise_amp*(2*xi-1), xi = splitmix64(seed ^ cell) in [0,1) */
     int32_t side_heated_ha; /* SideHeatedHa: magnetic (Lorentz) force, 2D plain FP64 method    */
-    int32_t reserved0;      /* 0                                                            */
+    int32_t arith;          /* FP64 handles: LBM_ARITH_REFERENCE (0) or LBM_ARITH_FIXED (1)  */
     double  Ha;             /* Hartmann number (2DRB.F90:89, default 20)                     */
     double  phi_deg;        /* field angle in degrees from +x (2DRB.F90:90, default 0)       */
 } lbm_params;
