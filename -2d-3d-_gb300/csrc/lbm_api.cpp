@@ -11,6 +11,7 @@
 // rebuilds them with one materialisation pass (bit-identical to what the reference
 // holds after iteration N, so stepping resumes on the same trajectory).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -98,6 +99,16 @@ struct lbm_handle {
 // ------------------------------------------------------------------------------------
 // helpers
 // ------------------------------------------------------------------------------------
+// NVTX range around an entry point (stepping, diagnostics, state transfer, restart files),
+// so a timeline from a profiler shows where the host-side calls begin and end.  The
+// header-only NVTX API costs a branch when no tool is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 static int fail(lbm_handle* h, int status, const std::string& msg) {
     if (h) h->err = msg;
     return status;
@@ -483,6 +494,15 @@ static int take_device_error(lbm_handle* h) {
     return LBM_OK;
 }
 
+extern "C" int lbm_selftest_wait_timeout(lbm_handle* h, int64_t polls) {
+    if (!h || polls <= 0 || polls > (1LL << 24)) return LBM_ERR_PARAM;
+    if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the staged kernels exist for FP32/FP16 handles");
+    CK(h, cudaSetDevice(h->device));
+    fast_wait_selftest(h->F, (unsigned)polls, h->stream);
+    CK_LAUNCH(h, "wait self-test");
+    return LBM_OK;
+}
+
 extern "C" int lbm_sync(lbm_handle* h) {
     if (!h) return LBM_ERR_PARAM;
     CK(h, cudaSetDevice(h->device));
@@ -711,6 +731,7 @@ static int capture_chunk(lbm_handle* h) {
 }
 
 extern "C" int lbm_step(lbm_handle* h, int64_t nsteps) {
+    NvtxRange range_("lbm_step");
     if (!h) return LBM_ERR_PARAM;
     if (nsteps < 0) return fail(h, LBM_ERR_PARAM, "nsteps < 0");
     if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
@@ -753,6 +774,7 @@ extern "C" int lbm_step(lbm_handle* h, int64_t nsteps) {
 // diagnostics
 // ------------------------------------------------------------------------------------
 static int run_reduce(lbm_handle* h, DiagOp op, double sums[DIAG_NSUM]) {
+    NvtxRange range_("diagnostic reduction");
     const int nb = diag_blocks(op == DIAG_NU_COLD_MID ? (long long)h->geo.nx * h->geo.nz : h->geo.ncell);
     if (h->p.precision == LBM_FP64) {
         DiagFields<double> F{h->A.u, h->A.v, h->A.w, h->A.T, h->A.rho, h->A.up, h->A.vp, h->A.wp, h->A.Tp};
@@ -1290,6 +1312,7 @@ static double* scalar_ptr(lbm_handle* h, int field) {
 }
 
 static int state_io(lbm_handle* h, int field, double* dst, const double* src, size_t count) {
+    NvtxRange range_("state transfer");
     if (!h || (!dst && !src)) return LBM_ERR_PARAM;
     if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
     CK(h, cudaSetDevice(h->device));
@@ -1519,6 +1542,7 @@ static void cont_header(const lbm_handle* h, int form, size_t narrays, int64_t h
 }
 
 extern "C" int lbm_backupData(lbm_handle* h, const char* path, int flags) {
+    NvtxRange range_("lbm_backupData");
     if (!h || !path) return LBM_ERR_PARAM;
     if (flags != LBM_BACKUP_REFERENCE && flags != LBM_BACKUP_CONTINUE) return fail(h, LBM_ERR_PARAM, "unknown flags");
     if (!h->initialised) return fail(h, LBM_ERR_STATE, "lbm_initial has not been called");
@@ -1621,6 +1645,7 @@ static std::string cont_mismatch(lbm_handle* h, const RestartScan& s) {
 }
 
 extern "C" int lbm_reload(lbm_handle* h, const char* path, int mode) {
+    NvtxRange range_("lbm_reload");
     if (!h || !path) return LBM_ERR_PARAM;
     if (mode != LBM_RELOAD_REFERENCE && mode != LBM_RELOAD_CONTINUE && mode != LBM_RELOAD_AUTO)
         return fail(h, LBM_ERR_PARAM, "unknown reload mode");
@@ -2051,6 +2076,7 @@ static int ens_rebuild(lbm_ensemble* e) {
 }
 
 extern "C" int lbm_ensemble_step(lbm_ensemble* e, int64_t nsteps) {
+    NvtxRange range_("lbm_ensemble_step");
     if (!e || nsteps < 0) return LBM_ERR_PARAM;
     if (e->members.empty() || nsteps == 0) return LBM_OK;
     ECK(e, cudaSetDevice(e->device));

@@ -87,6 +87,18 @@ __host__ __device__ inline long long cell_index(const Geo& g, int i, int j, int 
     return (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
 }
 
+// Index checks of the CPU builds of the shared cell code (compiled with -DLBM_CHECK by the
+// host tests, together with the address and undefined-behaviour sanitizers); nothing in a
+// GPU build.
+#if defined(LBM_CHECK) && !defined(__CUDA_ARCH__)
+}  // namespace lbm
+#include <cassert>
+namespace lbm {
+#define LBM_CHECK_CELL(g, cc) assert((cc) >= 0 && (cc) < (g).ncell)
+#else
+#define LBM_CHECK_CELL(g, cc) ((void)0)
+#endif
+
 // Pull of direction `a` into cell (i,j,k) from a post-collision array, with the
 // reference's boundary handling folded in.
 //
@@ -108,6 +120,7 @@ __device__ __forceinline__ T pull_flow_w(const Geo& g, int a, int i, int j, int 
     if (Lat<Q>::ez(a) != 0 && (sk < 0 || sk >= g.nz)) axis = 2;
     if (axis < 0) {
         const long long off = (long long)(-Lat<Q>::ex(a)) + (long long)g.nx * ((long long)(-Lat<Q>::ey(a)) + (long long)g.ny * (long long)(-Lat<Q>::ez(a)));
+        LBM_CHECK_CELL(g, c + off);
         return load(a, c + off);
     }
     if (pick3(g.bcf, axis) == LBM_BC_NOSLIP) return load(Lat<Q>::opp(a), c);
@@ -139,6 +152,7 @@ __device__ __forceinline__ T pull_thermal_w(const Geo& g, int a, int i, int j, i
     if (Lat<QT>::ez(a) != 0 && (sk < 0 || sk >= g.nz)) { axis = 2; low = sk < 0; }
     if (axis < 0) {
         const long long off = (long long)(-Lat<QT>::ex(a)) + (long long)g.nx * ((long long)(-Lat<QT>::ey(a)) + (long long)g.ny * (long long)(-Lat<QT>::ez(a)));
+        LBM_CHECK_CELL(g, c + off);
         return load(a, c + off);
     }
     const int bt = pick3(g.bct, axis);

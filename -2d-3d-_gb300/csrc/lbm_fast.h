@@ -73,6 +73,9 @@ bool fast_fused_supported(const Geo& g, int dim);
 bool fast_tma_supported(const Geo& g, int dim, int precision);
 // Read and clear the device error flag of the staged kernels (synchronises the stream).
 int fast_take_error(FastState& F, cudaStream_t s);
+// Run the bounded mbarrier wait of the staged kernels on a barrier that never completes,
+// with `limit` polls: it gives up and sets the error flag (lbm_selftest_wait_timeout).
+void fast_wait_selftest(FastState& F, unsigned limit, cudaStream_t s);
 // Physics constants of the step kernels of this handle (adds the rounding mode).
 PhysF fast_physf(const FastState& F, const PhysC& P);
 // Advance the step counter by one step (after a step's thermal kernel).

@@ -108,11 +108,18 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
 __device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // Bounded wait for phase `parity` of `bar`; false (and the error flag set) on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* err) {
-    for (unsigned it = 0; it < kWaitLimit; ++it)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* err, unsigned limit = kWaitLimit) {
+    for (unsigned it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     atomicExch(err, 1);
     return false;
+}
+
+// After a timed-out wait for a stage's copies: wait once more, again bounded, so that copies
+// still in flight land before the block exits and its shared memory is released.
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, unsigned parity) {
+    for (unsigned it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return;
 }
 
 __device__ __forceinline__ float s2f(float x) { return x; }
@@ -322,7 +329,10 @@ __global__ void __launch_bounds__(PP::threads, PP::blocks)
                                          NF);
             }
         }
-        if (!mbar_wait(&bars[s], (unsigned)((it / kStages) & 1), err)) return;
+        if (!mbar_wait(&bars[s], (unsigned)((it / kStages) & 1), err)) {
+            mbar_drain(&bars[s], (unsigned)((it / kStages) & 1));
+            return;
+        }
         const unsigned char* st = buf + (size_t)s * stage_bytes;
         const S* sf = reinterpret_cast<const S*>(st);
         const S* sg = sf + Q * rc;
@@ -487,5 +497,23 @@ bool fast_aa_tma_sweep(FastState& F, const Geo& g, const PhysF& pf, int dim, con
     if (F.precision == LBM_FP16) return aa_tma_s<3, __half>(F, g, pf, *(const FastArgs<__half>*)A, part, s);
     return aa_tma_s<3, float>(F, g, pf, *(const FastArgs<float>*)A, part, s);
 }
+
+// Self-test of the bounded wait and its error report: one warp arms an mbarrier for 128
+// bytes that no copy will deliver (no copy is issued, so nothing is in flight when the block
+// exits), waits with the given iteration limit, and sets the error flag of the handle's
+// staged kernels, which the next lbm_sync reports as LBM_ERR_TIMEOUT.
+__global__ void k_wait_selftest(int* err, unsigned limit) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_arrive_expect(&bar, 128u);
+    __syncthreads();
+    mbar_wait(&bar, 0u, err, limit);
+}
+
+void fast_wait_selftest(FastState& F, unsigned limit, cudaStream_t s) { k_wait_selftest<<<1, 32, 0, s>>>(F.err, limit); }
 
 }  // namespace lbm

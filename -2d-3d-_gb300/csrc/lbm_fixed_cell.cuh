@@ -495,7 +495,10 @@ __device__ __forceinline__ void flow_cell(const Geo& g, const PhysX& X, const Fi
         q60 ts = Qb(0);
         if (aa_inner(g, i, j, k)) {  // no pull off the faces needs a boundary rule
 #pragma unroll
-            for (int a = 0; a < Q; ++a) d[a] = ldq(fin, a * n + c - lat_off<Q>(g, a));
+            for (int a = 0; a < Q; ++a) {
+                LBM_CHECK_CELL(g, c - lat_off<Q>(g, a));
+                d[a] = ldq(fin, a * n + c - lat_off<Q>(g, a));
+            }
 #pragma unroll
             for (int a = 0; a < QT; ++a) ts = ts + ldq(gin, a * n + c - lat_off<QT>(g, a));
         } else {

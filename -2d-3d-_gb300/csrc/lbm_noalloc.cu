@@ -19,8 +19,14 @@
 //
 // Host code cannot use the array's name as a device address (it names a host-side
 // shadow).  The first call on each device looks the address up with
-// cudaGetSymbolAddress while that device is current and caches it; make that first call
-// outside any stream capture.
+// cudaGetSymbolAddress while that device is current and caches it, with the device's
+// multiprocessor count; make that first call outside any stream capture.  The cached
+// address belongs to the device's primary context (the one the runtime API uses): the entry
+// point is for callers on that context, and not valid after cudaDeviceReset.
+//
+// Grid: min(LBM_NOALLOC_MAX_BLOCKS, 4 x multiprocessors) blocks stride over the lattice, so
+// every SM of the device takes part whatever the lattice size; the partials are added in
+// block order, so a call is reproducible on a given device.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -32,12 +38,12 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kMaxBlocks = LBM_NOALLOC_MAX_BLOCKS;
-constexpr long long kCellsPerBlock = LBM_NOALLOC_CELLS_PER_BLOCK;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_nu_re_scratch[3 * kMaxBlocks + 3];
 
 double* g_scratch_addr[kMaxDevices] = {};
+int g_sms[kMaxDevices] = {};
 std::mutex g_setup_mutex;
 
 __device__ __forceinline__ double warp_sum(double x) {
@@ -46,16 +52,14 @@ __device__ __forceinline__ double warp_sum(double x) {
     return x;
 }
 
-// Block b sums the calNuRe terms (2DRB.F90:1631-1663, 3DRB.F90:1731-1768) over its slice
-// [b*kCellsPerBlock, (b+1)*kCellsPerBlock) and writes 3 partials to the scratch.
+// Block b sums the calNuRe terms (2DRB.F90:1631-1663, 3DRB.F90:1731-1768) over the cells
+// b*kThreads + t + k*gridDim.x*kThreads and writes 3 partials to the scratch.
 __global__ void __launch_bounds__(kThreads) k_nu_re_partials(const double* __restrict__ u, const double* __restrict__ v,
                                                              const double* __restrict__ w, const double* __restrict__ T,
                                                              long long ncell, int side, double* scratch) {
-    const long long lo = (long long)blockIdx.x * kCellsPerBlock;
-    long long hi = lo + kCellsPerBlock;
-    if (hi > ncell) hi = ncell;
+    const long long stride = (long long)gridDim.x * kThreads;
     double s_flux = 0.0, s_u2 = 0.0, s_bad = 0.0;
-    for (long long c = lo + threadIdx.x; c < hi; c += kThreads) {
+    for (long long c = (long long)blockIdx.x * kThreads + threadIdx.x; c < ncell; c += stride) {
         const double uc = u[c], vc = v[c], Tc = T[c];
         double r = uc * uc + vc * vc;
         double wc = 0.0;
@@ -109,17 +113,26 @@ extern "C" int lbm_calNuRe_noalloc(const double* u, const double* v, const doubl
     if (cudaGetDevice(&dev) != cudaSuccess) return LBM_ERR_CUDA;
     if (dev < 0 || dev >= kMaxDevices) return LBM_ERR_PARAM;
     double* scratch = nullptr;
+    int sms = 0;
     {
         std::lock_guard<std::mutex> lock(g_setup_mutex);
         if (!g_scratch_addr[dev]) {
             void* p = nullptr;
             if (cudaGetSymbolAddress(&p, g_nu_re_scratch) != cudaSuccess || !p) return LBM_ERR_CUDA;
+            int count = 0;
+            if (cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || count <= 0)
+                return LBM_ERR_CUDA;
+            g_sms[dev] = count;
             g_scratch_addr[dev] = (double*)p;
         }
         scratch = g_scratch_addr[dev];
+        sms = g_sms[dev];
     }
     cudaStream_t s = (cudaStream_t)stream;
-    const int nblocks = (int)((ncell + kCellsPerBlock - 1) / kCellsPerBlock);
+    long long want = (ncell + kThreads - 1) / kThreads;
+    if (want > 4LL * sms) want = 4LL * sms;
+    if (want > kMaxBlocks) want = kMaxBlocks;
+    const int nblocks = (int)want;
     k_nu_re_partials<<<nblocks, kThreads, 0, s>>>(u, v, w, T, (long long)ncell, side_heated ? 1 : 0, scratch);
     k_nu_re_total<<<1, 32, 0, s>>>(scratch, nblocks);
     if (cudaGetLastError() != cudaSuccess) return LBM_ERR_CUDA;

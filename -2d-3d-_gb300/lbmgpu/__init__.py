@@ -65,6 +65,7 @@ SIGNATURES = {
     "lbm_set_state": ([_vp, _i32, _dp, _sz], _i32),
     "lbm_get_stream": ([_vp, C.POINTER(_vp)], _i32),
     "lbm_time_kernels": ([_vp, _i64, _dp, _dp], _i32),
+    "lbm_selftest_wait_timeout": ([_vp, _i64], _i32),
     "lbm_set_option": ([_vp, _i32, _i32], _i32),
     "lbm_footprint": ([_vp, C.POINTER(_sz)], _i32),
     "lbm_ensemble_create": ([_i32, C.POINTER(_vp)], _i32),

@@ -291,6 +291,13 @@ int lbm_selftest_const_division(int64_t n, uint64_t seed, int64_t* mismatches);
  * the macro step's quotients through one shared correctly rounded reciprocal (x/rho, y/rho,
  * ...) against IEEE division, and returns the number of mismatches (expected 0). */
 int lbm_selftest_int_arith(int64_t n, uint64_t seed, int64_t* mismatches);
+/* Self-test of failure detection (no counterpart in the reference, which stops the process,
+ * 3DRB.F90:1457-1460): on an FP32/FP16 handle, runs the staged kernels' bounded mbarrier
+ * wait on a barrier that is armed for bytes no copy delivers (none is issued, so nothing is
+ * in flight), for `polls` polls (1 .. 2^24).  The wait gives up and sets the handle's device
+ * error flag: the next lbm_sync or diagnostic returns LBM_ERR_TIMEOUT and clears it, and the
+ * handle stays usable.  Asynchronous. */
+int lbm_selftest_wait_timeout(lbm_handle* h, int64_t polls);
 
 /* ---- allocation-free diagnostic (no counterpart in the reference) -----------------------
  * For callers that cannot let a library call cudaMalloc: programs whose device memory is
@@ -308,12 +315,15 @@ int lbm_selftest_int_arith(int64_t n, uint64_t seed, int64_t* mismatches);
  * held until the process exits).  Lattices larger than LBM_NOALLOC_MAX_CELLS cells are
  * rejected with LBM_ERR_TOO_LARGE before anything is launched.  The first call on each
  * device looks up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call outside any stream capture.  All calls share the array:
- * calls that overlap on the GPU race and must be serialised by the caller.  A non-finite
- * field value gives LBM_ERR_DIVERGED. */
+ * current; make that first call outside any stream capture.  That address belongs to the
+ * device's primary context: call from that context (the runtime API's), and not after a
+ * cudaDeviceReset.  All calls share the array: calls that overlap on the GPU race and must
+ * be serialised by the caller.  w = NULL means a 2D field (Re from u and v only); a 3D caller
+ * that passes NULL gets Re without the w^2 term and no error.  A non-finite field value
+ * gives LBM_ERR_DIVERGED. */
 #define LBM_ERR_TOO_LARGE            7
-#define LBM_NOALLOC_MAX_BLOCKS       1216
-#define LBM_NOALLOC_CELLS_PER_BLOCK  65536
+#define LBM_NOALLOC_MAX_BLOCKS       1216  /* partial-sum slots; a call uses min(1216, 4 x SMs) */
+#define LBM_NOALLOC_CELLS_PER_BLOCK  65536 /* capacity unit: MAX_CELLS = MAX_BLOCKS x this     */
 #define LBM_NOALLOC_MAX_CELLS        (1216LL * 65536LL) /* 79,691,776 cells, e.g. 430^3 */
 int lbm_calNuRe_noalloc(const double* u, const double* v, const double* w, const double* T, int64_t ncell,
                         int side_heated, double lengthUnit, double diffusivity, double viscosity,

@@ -1,9 +1,11 @@
 #!/usr/bin/env python3
 """Generate the golden fixtures under tests/golden/ from the reference's source text.
 
-Run in a container where the reference is mounted (default /root/reference):
+Run where the reference's sources are readable, naming their 2DRB directory:
 
-    python tests/golden/make_golden.py [--ref /root/reference/2DRB]
+    python tests/golden/make_golden.py --ref <reference checkout>/2DRB
+
+(or set LBM_REFERENCE_2DRB to that directory).
 
 reference_matrices.json: the moment transforms as the reference states them.  The hand-
 expanded statements `m(k) = ...`, `f_post(a,...) = ...` (2DRB.F90:688-696, 743-759;
@@ -77,8 +79,11 @@ def find(lines, pattern, after=0):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference/2DRB")
+    ap.add_argument("--ref", default=os.environ.get("LBM_REFERENCE_2DRB"),
+                    help="the reference's 2DRB directory (default: $LBM_REFERENCE_2DRB)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("name the reference's 2DRB directory with --ref or LBM_REFERENCE_2DRB")
     r2 = open(os.path.join(args.ref, "2DRB.F90"), encoding="utf-8-sig").read().splitlines()
     r3 = open(os.path.join(args.ref, "3DRB.F90"), encoding="utf-8-sig").read().splitlines()
     chai = open(os.path.join(args.ref, "ChaiPRE2020.F90"), encoding="utf-8-sig").read().splitlines()

@@ -223,3 +223,36 @@ def test_fixed_parameters(stepper, oracle_mod):
     c = o.constants(LbmConstants)
     assert stepper.fixed_constants_ok(C.byref(p), C.byref(c)) == 0
     o.close()
+
+
+def test_fixed_stepper_is_clean_under_sanitizers(tmp_path):
+    """The shared cell code (pull with boundary rules, the fixed-arithmetic bodies) built for
+    the CPU with -DLBM_CHECK (index asserts on every computed source cell) and the address and
+    undefined-behaviour sanitizers, run over every switch set: no out-of-range access, no
+    assert, no undefined operation.  This stands in for a device-side bounds check."""
+    import sys
+    cxx, cuda_inc = _cxx()
+    asan = subprocess.run([cxx, "-print-file-name=libasan.so"], capture_output=True, text=True).stdout.strip()
+    if not asan or not os.path.isabs(asan) or not os.path.exists(asan):
+        pytest.skip("no AddressSanitizer runtime")
+    so = str(tmp_path / "libfixed_san.so")
+    cmd = [cxx, "-std=c++17", "-O1", "-g", "-DLBM_CHECK", "-fsanitize=address,undefined",
+           "-fno-sanitize-recover=undefined", "-shared", "-fPIC", "-I", os.path.join(ROOT, "-2d-3d-_gb300", "csrc"),
+           "-I", os.path.join(ROOT, "include"), "-I", cuda_inc, "-o", so, os.path.join(HERE, "fixed_cell_check.cpp")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    script = (
+        "import sys, ctypes as C\n"
+        "sys.path[:0] = [%r, %r, %r]\n"
+        "import test_cpu_fixed as T\n"
+        "from lbmgpu.abi import LbmConstants\n"
+        "from oracle import oracle as ora\n"
+        "lib = C.CDLL(%r); lib.fixed_run.restype = C.c_int\n"
+        "for name, p in T.cases().items():\n"
+        "    o = ora.Oracle(p); o.initial(); c = o.constants(LbmConstants)\n"
+        "    T.run_fixed(lib, p, c, T.state_arrays(o, p), 12)\n"
+        "    o.close()\n"
+        "print('clean')\n" % (ROOT, os.path.join(ROOT, "-2d-3d-_gb300"), HERE, so))
+    env = dict(os.environ, LD_PRELOAD=asan, ASAN_OPTIONS="detect_leaks=0")
+    r = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0 and "clean" in r.stdout, r.stdout[-2000:] + r.stderr[-4000:]

@@ -123,3 +123,27 @@ def test_server_result_same_alone_and_in_mix():
         m = mixed[req.rid]
         assert r.steps == m.steps and r.converged == m.converged
         assert r.Nu == m.Nu and r.Re == m.Re, (req.rid, r.Nu, m.Nu)
+
+
+def test_bounded_wait_timeout_is_reported_and_the_handle_stays_usable():
+    """Failure detection without a GPU fault: the staged kernels' bounded mbarrier wait, run
+    on a barrier armed for bytes that no copy delivers (nothing in flight), gives up after a
+    few thousand polls; the next sync reports LBM_ERR_TIMEOUT, clears the flag, and the
+    handle keeps stepping."""
+    import math
+    from lbmgpu import LbmError, load_library
+    from lbmgpu.abi import LBM_ERR_TIMEOUT
+    p = rb_params(dim=3, n=16, Ra=1e6, noise_amp=1e-3, precision="fp32")
+    lat = Lattice(p)
+    lat.initial()
+    lat.step(4)
+    lat.sync()
+    assert load_library().lbm_selftest_wait_timeout(lat._h, 1 << 12) == 0
+    with pytest.raises(LbmError) as e:
+        lat.sync()
+    assert e.value.status == LBM_ERR_TIMEOUT
+    lat.sync()  # the flag was cleared by the report
+    lat.step(8)
+    nu, re = lat.calNuRe()
+    assert math.isfinite(nu) and math.isfinite(re)
+    lat.close()

@@ -29,13 +29,26 @@ def _bind(lib):
     return fn
 
 
-@pytest.mark.parametrize("dim", [3, 2])
-def test_noalloc_nu_re_matches_calNuRe(gpu_lib, dim):
+def _lattice(case):
+    from lbmgpu.abi import LBM_BCT_ADIABATIC, LBM_BCT_CONST, LBM_CELL_SIDE, rb_params
+    if case == "3d_128":  # a multi-block lattice: every block strides over many cells
+        return rb_params(dim=3, n=128, Ra=1e7, noise_amp=1e-3), 0
+    if case == "2d_20":
+        return rb_params(dim=2, ny=20, Ra=1e6, noise_amp=1e-3), 0
+    p = rb_params(dim=3, nx=24, ny=20, nz=12, Ra=1e5, noise_amp=1e-3, seed=8)  # side-heated: Nu from <u T>
+    p.cell = LBM_CELL_SIDE
+    p.bc_thermal[0] = LBM_BCT_CONST
+    p.bc_thermal[1] = LBM_BCT_ADIABATIC
+    return p, 1
+
+
+@pytest.mark.parametrize("case", ["3d_128", "2d_20", "3d_side"])
+def test_noalloc_nu_re_matches_calNuRe(gpu_lib, case):
     import torch
     from lbmgpu import Lattice
-    from lbmgpu.abi import rb_params
     fn = _bind(gpu_lib)
-    p = rb_params(dim=dim, n=20, ny=20, Ra=1e6, noise_amp=1e-3)
+    p, side = _lattice(case)
+    dim = p.dim
     lat = Lattice(p)
     lat.initial()
     lat.step(150)
@@ -48,14 +61,14 @@ def test_noalloc_nu_re_matches_calNuRe(gpu_lib, dim):
     wptr = dev["w"].data_ptr() if dim == 3 else None
     for _ in range(2):
         nu, re = C.c_double(), C.c_double()
-        st = fn(dev["u"].data_ptr(), dev["v"].data_ptr(), wptr, dev["T"].data_ptr(), ncell, 0,
+        st = fn(dev["u"].data_ptr(), dev["v"].data_ptr(), wptr, dev["T"].data_ptr(), ncell, side,
                 c["lengthUnit"], c["diffusivity"], c["viscosity"], None, C.byref(nu), C.byref(re))
         assert st == 0
         assert nu.value == pytest.approx(nu_ref, rel=NU_RTOL)
         assert re.value == pytest.approx(re_ref, rel=NU_RTOL)
     # a lattice beyond the fixed scratch capacity is rejected before anything is launched
     nu, re = C.c_double(), C.c_double()
-    st = fn(dev["u"].data_ptr(), dev["v"].data_ptr(), wptr, dev["T"].data_ptr(), LBM_NOALLOC_MAX_CELLS + 1, 0,
+    st = fn(dev["u"].data_ptr(), dev["v"].data_ptr(), wptr, dev["T"].data_ptr(), LBM_NOALLOC_MAX_CELLS + 1, side,
             c["lengthUnit"], c["diffusivity"], c["viscosity"], None, C.byref(nu), C.byref(re))
     assert st == LBM_ERR_TOO_LARGE
     lat.close()
