@@ -13,6 +13,12 @@ namespace lbm {
 
 using namespace fxa;
 
+// Resident blocks per SM asked of the interior flow kernel: 4 (128 registers, no spill) ran
+// faster on GB300 than 5 (96 registers and a spill) or 6, at 128^3, 256^3 and 384^3.
+#ifndef LBM_XFLOW_MIN_BLOCKS
+#define LBM_XFLOW_MIN_BLOCKS 4
+#endif
+
 __device__ __forceinline__ bool fixed_cell_of_thread(const Geo& g, long long& c, int& i, int& j, int& k) {
     c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncell) return false;
@@ -38,6 +44,89 @@ __global__ void __launch_bounds__(128) k_xthermal(Geo g, PhysX X, FixedArrays A,
     thermal_cell<D, FIRST>(g, X, A, fin, gin, gout, c, i, j, k);
 }
 
+// Interior cells (no pull needs a boundary rule) of the steady-state step: block (bx, j, k)
+// holds cells i = bx*128 + t of the interior row (j, k), so warps start at row starts (rows
+// are 2 KB-aligned when nx is a multiple of 32); threads on the x faces (i = 0, nx-1) do
+// nothing, the face kernels take every face cell.  Keeping the boundary code out of these
+// kernels keeps them small (instruction fetch) and in fewer registers.
+__device__ __forceinline__ bool fixed_interior_cell(const Geo& g, long long& c, int& i, int& j, int& k) {
+    i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    j = (int)blockIdx.y + 1;
+    k = g.nz > 1 ? (int)blockIdx.z + 1 : 0;
+    if (i < 1 || i >= g.nx - 1) return false;
+    c = (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
+    return true;
+}
+
+// Face cells: x faces (i = 0, nx-1; all j, k), then y faces (j = 0, ny-1; 0 < i < nx-1; all
+// k), then in 3D the z faces (k = 0, nz-1; 0 < i < nx-1; 0 < j < ny-1).
+__host__ __device__ __forceinline__ long long fixed_face_count(const Geo& g) {
+    const long long nx = g.nx, ny = g.ny, nz = g.nz;
+    long long f = 2 * ny * nz + 2 * (nx - 2) * nz;
+    if (nz > 1) f += 2 * (nx - 2) * (ny - 2);
+    return f;
+}
+__device__ __forceinline__ bool fixed_face_cell(const Geo& g, long long& c, int& i, int& j, int& k) {
+    long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= fixed_face_count(g)) return false;
+    const long long nx = g.nx, ny = g.ny, nz = g.nz;
+    const long long nxf = 2 * ny * nz, nyf = 2 * (nx - 2) * nz;
+    if (f < nxf) {
+        i = (f & 1) ? g.nx - 1 : 0;
+        j = (int)((f >> 1) % ny);
+        k = (int)((f >> 1) / ny);
+    } else if ((f -= nxf) < nyf) {
+        j = (f & 1) ? g.ny - 1 : 0;
+        i = 1 + (int)((f >> 1) % (nx - 2));
+        k = (int)((f >> 1) / (nx - 2));
+    } else {
+        f -= nyf;
+        k = (f & 1) ? g.nz - 1 : 0;
+        i = 1 + (int)((f >> 1) % (nx - 2));
+        j = 1 + (int)((f >> 1) / (nx - 2));
+    }
+    c = (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
+    return true;
+}
+
+template <int D>
+__global__ void __launch_bounds__(128, LBM_XFLOW_MIN_BLOCKS) k_xflow_in(Geo g, PhysX X, FixedArrays A, const long long* __restrict__ fin,
+                                                     const long long* __restrict__ gin, long long* __restrict__ fout) {
+    long long c;
+    int i, j, k;
+    if (!fixed_interior_cell(g, c, i, j, k)) return;
+    flow_cell<D, false, 1>(g, X, A, fin, gin, fout, c, i, j, k);
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_xflow_face(Geo g, PhysX X, FixedArrays A, const long long* __restrict__ fin,
+                                                    const long long* __restrict__ gin, long long* __restrict__ fout) {
+    long long c;
+    int i, j, k;
+    if (!fixed_face_cell(g, c, i, j, k)) return;
+    flow_cell<D, false, 2>(g, X, A, fin, gin, fout, c, i, j, k);
+}
+
+template <int D>
+__global__ void __launch_bounds__(128, 6) k_xthermal_in(Geo g, PhysX X, FixedArrays A,
+                                                        const long long* __restrict__ fin,
+                                                        const long long* __restrict__ gin, long long* __restrict__ gout) {
+    long long c;
+    int i, j, k;
+    if (!fixed_interior_cell(g, c, i, j, k)) return;
+    thermal_cell<D, false, 1>(g, X, A, fin, gin, gout, c, i, j, k);
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_xthermal_face(Geo g, PhysX X, FixedArrays A,
+                                                       const long long* __restrict__ fin,
+                                                       const long long* __restrict__ gin, long long* __restrict__ gout) {
+    long long c;
+    int i, j, k;
+    if (!fixed_face_cell(g, c, i, j, k)) return;
+    thermal_cell<D, false, 2>(g, X, A, fin, gin, gout, c, i, j, k);
+}
+
 template <int D>
 __global__ void k_xmaterialize(Geo g, PhysX X, FixedArrays A, const long long* __restrict__ fin,
                                const long long* __restrict__ gin) {
@@ -59,6 +148,22 @@ __global__ void k_xpost_to_double(long long* buf, long long n, int q, PhysX X, i
 
 static inline unsigned xblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// Steady-state step of one dimension: interior kernel and face kernel for each half.
+template <int D>
+static void steady_step(const Geo& g, const PhysX& X, const FixedArrays& A, const long long* fprev,
+                        const long long* gprev, long long* fnext, long long* gnext, cudaStream_t s, bool fl, bool th) {
+    const dim3 bin(128), gin_grid((unsigned)((g.nx + 127) / 128), (unsigned)(g.ny - 2), D == 3 ? (unsigned)(g.nz - 2) : 1u);
+    const unsigned nf = xblocks(fixed_face_count(g), 128);
+    if (fl) {
+        k_xflow_in<D><<<gin_grid, bin, 0, s>>>(g, X, A, fprev, gprev, fnext);
+        k_xflow_face<D><<<nf, 128, 0, s>>>(g, X, A, fprev, gprev, fnext);
+    }
+    if (th) {
+        k_xthermal_in<D><<<gin_grid, bin, 0, s>>>(g, X, A, fnext, gprev, gnext);
+        k_xthermal_face<D><<<nf, 128, 0, s>>>(g, X, A, fnext, gprev, gnext);
+    }
+}
+
 void fixed_fused_step(const Geo& g, const PhysX& X, const FixedArrays& A, int dim, bool first, const long long* fprev,
                       const long long* gprev, long long* fnext, long long* gnext, cudaStream_t s, int part) {
     const int bs = 128;
@@ -69,16 +174,14 @@ void fixed_fused_step(const Geo& g, const PhysX& X, const FixedArrays& A, int di
             if (fl) k_xflow<2, true><<<nb, bs, 0, s>>>(g, X, A, fprev, gprev, fnext);
             if (th) k_xthermal<2, true><<<nb, bs, 0, s>>>(g, X, A, fnext, gprev, gnext);
         } else {
-            if (fl) k_xflow<2, false><<<nb, bs, 0, s>>>(g, X, A, fprev, gprev, fnext);
-            if (th) k_xthermal<2, false><<<nb, bs, 0, s>>>(g, X, A, fnext, gprev, gnext);
+            steady_step<2>(g, X, A, fprev, gprev, fnext, gnext, s, fl, th);
         }
     } else {
         if (first) {
             if (fl) k_xflow<3, true><<<nb, bs, 0, s>>>(g, X, A, fprev, gprev, fnext);
             if (th) k_xthermal<3, true><<<nb, bs, 0, s>>>(g, X, A, fnext, gprev, gnext);
         } else {
-            if (fl) k_xflow<3, false><<<nb, bs, 0, s>>>(g, X, A, fprev, gprev, fnext);
-            if (th) k_xthermal<3, false><<<nb, bs, 0, s>>>(g, X, A, fnext, gprev, gnext);
+            steady_step<3>(g, X, A, fprev, gprev, fnext, gnext, s, fl, th);
         }
     }
 }

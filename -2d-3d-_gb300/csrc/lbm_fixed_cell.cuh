@@ -88,14 +88,29 @@ __device__ __forceinline__ double to_double(q60 a) {
 
 constexpr long long kOne = 1LL << kFrac;
 
-// Product of two q60 numbers, rounded down to q60.
+// Product of two q60 numbers, rounded down to q60: bits 60..123 of the 128-bit product.  On
+// the GPU the high word is one signed 64 x 64 high multiply (mul.hi.s64) and the low word a
+// 64-bit multiply; the host uses a 128-bit integer.  Both give the same bits.
 __device__ __forceinline__ q60 mul(q60 a, q60 b) {
+#ifdef __CUDA_ARCH__
+    const unsigned long long hi = (unsigned long long)__mul64hi(a.s(), b.s());
+    const unsigned long long lo = a.u * b.u;
+    return Qb((long long)((hi << (64 - kFrac)) | (lo >> kFrac)));
+#else
     return Qb((long long)(((__int128)a.s() * (__int128)b.s()) >> kFrac));
+#endif
 }
 // Product with a constant k given as K = round(k * 2^(64-S)) (|k| < 2^(S-1)), rounded down.
 template <int S>
 __device__ __forceinline__ q60 mulk(q60 a, long long K) {
+#ifdef __CUDA_ARCH__
+    const unsigned long long hi = (unsigned long long)__mul64hi(a.s(), K);
+    if (S == 0) return Qb((long long)hi);
+    const unsigned long long lo = a.u * (unsigned long long)K;
+    return Qb((long long)((hi << S) | (lo >> (64 - S))));
+#else
     return Qb((long long)(((__int128)a.s() * (__int128)K) >> (64 - S)));
+#endif
 }
 
 // 1/rho for rho in (1/2, 4): an FP32 reciprocal of the leading bits (24 correct bits), then
@@ -475,7 +490,9 @@ namespace fxa {
 // u, T); otherwise f_{n-1} = pull(f_post_{n-1}), T_{n-1} = sum pull(g_post_{n-1}), and rho,
 // u of the macro step of f_{n-1} with the lag.  2D stores the force F_y,n in the lag.
 // g: geometry whose thermal wall terms are deviations (wall term - 2 wT Tref).
-template <int D, bool FIRST>
+// PATH: 0 = any cell (the boundary rule where a pull leaves the lattice), 1 = a cell known to
+// touch no face (fixed-offset pulls only), 2 = a face cell (boundary path only).
+template <int D, bool FIRST, int PATH = 0>
 __device__ __forceinline__ void flow_cell(const Geo& g, const PhysX& X, const FixedArrays& A, const long long* fin,
                                           const long long* gin, long long* fout, long long c, int i, int j, int k) {
     constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
@@ -493,7 +510,7 @@ __device__ __forceinline__ void flow_cell(const Geo& g, const PhysX& X, const Fi
         tdev = q60(A.T[c]) - Qb(X.tref);
     } else {
         q60 ts = Qb(0);
-        if (aa_inner(g, i, j, k)) {  // no pull off the faces needs a boundary rule
+        if (PATH == 1 || (PATH == 0 && aa_inner(g, i, j, k))) {  // no pull needs a boundary rule
 #pragma unroll
             for (int a = 0; a < Q; ++a) {
                 LBM_CHECK_CELL(g, c - lat_off<Q>(g, a));
@@ -523,13 +540,13 @@ __device__ __forceinline__ void flow_cell(const Geo& g, const PhysX& X, const Fi
 }
 
 // Streaming, boundary and macro of the flow, and thermal collision of step n (k_thermal).
-template <int D, bool FIRST>
+template <int D, bool FIRST, int PATH = 0>
 __device__ __forceinline__ void thermal_cell(const Geo& g, const PhysX& X, const FixedArrays& A, const long long* fin,
                                              const long long* gin, long long* gout, long long c, int i, int j, int k) {
     constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
     const long long n = g.ncell;
     q60 d[Q], e[QT], ep[QT], rho, P[3], U[3], B[3], tdev;
-    const bool inner = aa_inner(g, i, j, k);
+    const bool inner = PATH == 1 || (PATH == 0 && aa_inner(g, i, j, k));
     auto lf = [&](int a, long long cc) { return ldq(fin, a * n + cc); };
     if (inner) {
 #pragma unroll

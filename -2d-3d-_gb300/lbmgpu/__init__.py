@@ -122,11 +122,12 @@ def library_path():
 
 
 def load_library(path=None):
-    """Load liblbmgpu.so from the package directory (built in-tree by lbmgpu.build)."""
+    """Load liblbmgpu.so from the package directory (built in-tree by lbmgpu.build), or from
+    the path in the environment variable LBMGPU_LIBRARY when it is set."""
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = path or library_path()
+    p = path or os.environ.get("LBMGPU_LIBRARY") or library_path()
     if not os.path.exists(p):
         raise RuntimeError("%s is not built; run lbmgpu.build.build() (nvcc, sm_103a)" % p)
     lib = C.CDLL(p)
