@@ -14,6 +14,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <utility>
 #include <cmath>
 #include <cstdio>
 #include <limits>
@@ -67,6 +68,17 @@ struct lbm_handle {
     PhysX px{};
     Geo xgeo{};  // geometry with the thermal wall terms of deviations
     long long *xb0 = nullptr, *xb1 = nullptr, *xb2 = nullptr, *xlag = nullptr;
+    // fused passes (lbm_fixed.cu k_xfused): B_prev double-buffered, the graph of a chunk of
+    // passes and the state it was captured from
+    // LBM_OPT_SINGLE_KERNEL on a fixed handle.  Off by default: on GB300 the fused pass reads
+    // a third less DRAM but executes about 1.4x the integer instructions (the thermal halo is
+    // recomputed with 64-bit products) and runs at half the two-kernel rate (256^3: 4.08 ms
+    // against 2.14 ms per step).
+    bool xfused = false;
+    long long *xb0b = nullptr, *xb1b = nullptr, *xb2b = nullptr;
+    cudaGraph_t xgraph = nullptr;
+    cudaGraphExec_t xgraph_exec = nullptr;
+    int xgraph_key = -1;
 
     // FP32 / FP16 storage forms
     FastState F{};
@@ -297,6 +309,8 @@ static void release(lbm_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     if (h->graph) cudaGraphDestroy(h->graph);
+    if (h->xgraph_exec) cudaGraphExecDestroy(h->xgraph_exec);
+    if (h->xgraph) cudaGraphDestroy(h->xgraph);
     for (void* p : h->allocs) cudaFree(p);
     h->allocs.clear();
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -365,6 +379,11 @@ static int allocate(lbm_handle* h) {
             AL(h->xb1, n);
             if (d3) AL(h->xb2, n);
             AL(h->xlag, n);
+            if (d3 && fixed_fused_supported(h->geo, h->dim)) {
+                AL(h->xb0b, n);
+                AL(h->xb1b, n);
+                AL(h->xb2b, n);
+            }
         }
     } else {
         st = fast_allocate(h->F, h->p, h->geo, [h](void** p, size_t bytes) {
@@ -730,6 +749,74 @@ static int capture_chunk(lbm_handle* h) {
     return LBM_OK;
 }
 
+// ---- fused passes of the fixed arithmetic (3D) --------------------------------------------
+// Between lbm_step calls the handle is in the two-kernel state (f_post_N, g_post_N).  A run of
+// steps enters the fused state (f_post_{N+1}, g_post_N) with the flow half of one step, runs
+// one fused pass per further step, and leaves with the thermal half of the last step.
+static bool use_xfused(const lbm_handle* h) {
+    return h->fixed && h->xfused && h->xb0b && fixed_fused_supported(h->geo, h->dim);
+}
+
+static void x_enter(lbm_handle* h) {
+    const int nxt = h->cur ^ 1;
+    fixed_fused_step(h->xgeo, h->px, fixed_arrays(h), h->dim, false, (const long long*)h->fbuf[h->cur],
+                     (const long long*)h->gbuf[h->cur], (long long*)h->fbuf[nxt], nullptr, h->stream, 0);
+    h->cur = nxt;  // f is one step ahead: fbuf[cur] = f_post_{N+1}, gbuf[cur ^ 1] = g_post_N
+}
+
+static void x_pass(lbm_handle* h) {
+    const int c = h->cur, o = c ^ 1;
+    const long long* bin[3] = {h->xb0, h->xb1, h->xb2};
+    long long* const bout[3] = {h->xb0b, h->xb1b, h->xb2b};
+    fixed_fused_pass(h->xgeo, h->px, (const long long*)h->fbuf[c], (const long long*)h->gbuf[o], (long long*)h->fbuf[o],
+                     (long long*)h->gbuf[c], bin, bout, h->stream);
+    h->cur = o;
+    std::swap(h->xb0, h->xb0b);
+    std::swap(h->xb1, h->xb1b);
+    std::swap(h->xb2, h->xb2b);
+}
+
+static void x_exit(lbm_handle* h) {
+    const int c = h->cur;
+    fixed_fused_step(h->xgeo, h->px, fixed_arrays(h), h->dim, false, nullptr, (const long long*)h->gbuf[c ^ 1],
+                     (long long*)h->fbuf[c], (long long*)h->gbuf[c], h->stream, 1);
+}
+
+// Capture key of a chunk of fused passes: the buffer parity and which B_prev set is current.
+static int x_key(const lbm_handle* h) { return h->cur + 2 * (h->xb0 < h->xb0b ? 1 : 0); }
+
+static int x_run(lbm_handle* h, int64_t passes) {
+    while (passes > 0) {
+        if (passes >= kChunkSteps) {
+            if (h->xgraph_exec && h->xgraph_key != x_key(h)) {
+                CK(h, cudaStreamSynchronize(h->stream));
+                cudaGraphExecDestroy(h->xgraph_exec);
+                cudaGraphDestroy(h->xgraph);
+                h->xgraph_exec = nullptr;
+                h->xgraph = nullptr;
+            }
+            if (!h->xgraph_exec) {
+                h->xgraph_key = x_key(h);
+                CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+                for (int s = 0; s < kChunkSteps; ++s) x_pass(h);
+                cudaGraph_t g = nullptr;
+                cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+                if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+                h->xgraph = g;
+                CK(h, cudaGraphInstantiate(&h->xgraph_exec, g, 0));
+            }
+            // a chunk holds an even number of passes: the buffer parity and the current B_prev
+            // set after it are those before it
+            CK(h, cudaGraphLaunch(h->xgraph_exec, h->stream));
+            passes -= kChunkSteps;
+        } else {
+            x_pass(h);
+            passes -= 1;
+        }
+    }
+    return LBM_OK;
+}
+
 extern "C" int lbm_step(lbm_handle* h, int64_t nsteps) {
     NvtxRange range_("lbm_step");
     if (!h) return LBM_ERR_PARAM;
@@ -746,6 +833,13 @@ extern "C" int lbm_step(lbm_handle* h, int64_t nsteps) {
     }
     // enter the single-kernel phase outside any captured graph
     if (use_single(h) && !h->F.ahead && done < nsteps) fast_enter(h->F, h->geo, h->phys, h->dim, h->stream);
+    if (use_xfused(h) && nsteps - done >= 2) {
+        x_enter(h);
+        int st = x_run(h, nsteps - done - 1);
+        if (st != LBM_OK) return st;
+        x_exit(h);
+        done = nsteps;
+    }
     while (done < nsteps) {
         if (at_graph_origin(h) && nsteps - done >= kChunkSteps) {
             if (h->graph_exec && in_place(h) && h->graph_key != layout_key(h)) {
@@ -1827,6 +1921,16 @@ extern "C" int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, 
             exact_aa_step(h->geo, h->phys, h->A, h->dim, false, h->aa, h->stream, 0);
             CK(h, cudaEventRecord(ev[2 * k + 1], h->stream));
             exact_aa_step(h->geo, h->phys, h->A, h->dim, false, h->aa, h->stream, 1);
+        } else if (use_xfused(h)) {
+            // one fused pass per step: its time goes to the first slot, the second is empty
+            if (k == 0) x_enter(h);
+            CK(h, cudaEventRecord(ev[2 * k + 1], h->stream));
+            x_pass(h);
+            if (k == nsteps - 1) {
+                CK(h, cudaEventRecord(ev[2 * k + 2], h->stream));
+                x_exit(h);
+                continue;
+            }
         } else if (h->p.precision == LBM_FP64 && h->fixed) {
             const int nxt = h->cur ^ 1;
             const FixedArrays X = fixed_arrays(h);
@@ -1863,7 +1967,7 @@ extern "C" int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, 
         float a = 0.f, b = 0.f;
         CK(h, cudaEventElapsedTime(&a, ev[2 * k], ev[2 * k + 1]));
         CK(h, cudaEventElapsedTime(&b, ev[2 * k + 1], ev[2 * k + 2]));
-        if (use_single(h)) {
+        if (use_single(h) || use_xfused(h)) {
             tf += b;  // the fused kernel sits between the middle and the last event
         } else {
             tf += a;
@@ -1881,6 +1985,10 @@ extern "C" int lbm_set_option(lbm_handle* h, int option, int value) {
     if (!h) return LBM_ERR_PARAM;
     switch (option) {
         case LBM_OPT_SINGLE_KERNEL:
+            if (h->fixed) {  // fused passes of the fixed arithmetic (3D), or its two-kernel step
+                h->xfused = value != 0;
+                break;
+            }
             if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the plain FP64 method has no single-kernel form");
             if (h->F.single_kernel != (value != 0)) {
                 // leave the one-ahead phase and drop the graph captured for the other form

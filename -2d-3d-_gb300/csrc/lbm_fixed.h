@@ -19,4 +19,11 @@ void fixed_materialize(const Geo& g, const PhysX& X, const FixedArrays& A, int d
 void fixed_post_to_double(const PhysX& X, long long* fbuf, long long* gbuf, long long n, int q, int qt,
                           cudaStream_t s);
 
+// Fused step (3D, nx <= 512): thermal collision of step s and flow collision of step s+1 in
+// one launch.  In: f_post_s, g_post_{s-1}, B_prev (bin); out: f_post_{s+1}, g_post_s, B_prev
+// (bout, a second set of buffers).
+bool fixed_fused_supported(const Geo& g, int dim);
+void fixed_fused_pass(const Geo& g, const PhysX& X, const long long* fin, const long long* gin, long long* fout,
+                      long long* gout, const long long* const bin[3], long long* const bout[3], cudaStream_t s);
+
 }  // namespace lbm

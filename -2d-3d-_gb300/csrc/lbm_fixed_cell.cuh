@@ -105,9 +105,12 @@ template <int S>
 __device__ __forceinline__ q60 mulk(q60 a, long long K) {
 #ifdef __CUDA_ARCH__
     const unsigned long long hi = (unsigned long long)__mul64hi(a.s(), K);
-    if (S == 0) return Qb((long long)hi);
-    const unsigned long long lo = a.u * (unsigned long long)K;
-    return Qb((long long)((hi << S) | (lo >> (64 - S))));
+    if constexpr (S == 0) {
+        return Qb((long long)hi);
+    } else {
+        const unsigned long long lo = a.u * (unsigned long long)K;
+        return Qb((long long)((hi << S) | (lo >> (64 - S))));
+    }
 #else
     return Qb((long long)(((__int128)a.s() * (__int128)K) >> (64 - S)));
 #endif
@@ -181,6 +184,7 @@ struct PhysX {
     long long sg2;             // SG/2
     long long t_n, t_a;        // -Qnu/norm and Qnu a_T/norm of the a_T T moment
     long long t5_n, t6_n;      // 3D: -Qnu/12, -Qnu/4; 2D: t5_n = -Qnu/4
+    long long bc_lo[3], bc_hi[3];  // constant-T wall terms of deviations (q60), per axis
     int use_g;
 };
 
@@ -239,6 +243,12 @@ inline bool make_physx(const lbm_params& p, const lbm_constants& c, PhysX& X) {
     ok = ok && fx_const(-Qnu / nrm, 0, X.t_n) && fx_const(Qnu * aT / nrm, 0, X.t_a);
     ok = ok && fx_const(d3 ? -Qnu / 12 : -Qnu / 4, 0, X.t5_n) && fx_const(-Qnu / 4, 0, X.t6_n);
     X.use_g = p.use_g ? 1 : 0;
+    const Geo dg = deviation_geo(make_geo(p, c), c);
+    for (int a = 0; a < 3; ++a) {
+        // round(x 2^60) ties to even, as the device conversion q60(double) rounds
+        X.bc_lo[a] = (long long)std::llrint(dg.bcT_lo[a] * 0x1p60);
+        X.bc_hi[a] = (long long)std::llrint(dg.bcT_hi[a] * 0x1p60);
+    }
     return ok;
 }
 

@@ -245,7 +245,11 @@ int lbm_footprint(const lbm_params* p, size_t* bytes);
 
 /* ---- execution options (no counterpart in the reference) --------------------------------
  * LBM_OPT_SINGLE_KERNEL: FP32/FP16 handles advance with one fused kernel per step (1) or
- *   with the two-kernel form (0, default).  Both give the same arithmetic.
+ *   with the two-kernel form (0, default).  Both give the same arithmetic.  On a 3D FP64
+ *   handle with the fixed arithmetic (nx <= 512) it selects the fused pass, which runs the
+ *   thermal collision of one step and the flow collision of the next in one launch and sums
+ *   each cell's T from pushed values in shared memory (1), or the two-kernel step (0,
+ *   default, faster on GB300); both give the same values bit for bit.
  * LBM_OPT_KCHUNK: z planes marched by one block of the fused 3D kernel (default 16).
  * LBM_OPT_PAIRS: the two-kernel FP32/FP16 step moves populations as 2-cell vectors, two
  *   x-adjacent cells per thread (1; used when nx is even) or one cell per thread (0).
