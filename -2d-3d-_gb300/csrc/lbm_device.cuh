@@ -168,6 +168,33 @@ __device__ __forceinline__ T pull_thermal(const Geo& g, int a, int i, int j, int
     return pull_thermal_w<QT, T>(g, a, i, j, k, c, load, [&](int, int d, long long cc) { return load(d, cc); });
 }
 
+// Pulls of a cell whose row is interior (0 < j < ny-1 and, in 3D, 0 < k < nz-1): only the x
+// axis can take a source outside the lattice, at i = 0 or nx-1.  The rule is pull_flow's /
+// pull_thermal's for that case, written with selects so that every lane of a warp runs the
+// same instructions (x-face lanes share warps with interior ones).
+template <int Q, class T, class LOAD>
+__device__ __forceinline__ T pull_flow_xrow(const Geo& g, int a, int i, long long c, LOAD load) {
+    const long long off = (long long)Lat<Q>::ex(a) + (long long)g.nx * ((long long)Lat<Q>::ey(a) + (long long)g.ny * (long long)Lat<Q>::ez(a));
+    if (Lat<Q>::ex(a) == 0) return load(a, c - off);
+    const int si = i - Lat<Q>::ex(a);
+    const bool out = si < 0 || si >= g.nx;
+    if (g.bcf[0] == LBM_BC_NOSLIP) return out ? load(Lat<Q>::opp(a), c) : load(a, c - off);
+    // periodic: the same-row copy from the other end of the row
+    return load(a, c - off + (out ? (long long)Lat<Q>::ex(a) * g.nx : 0LL));
+}
+template <int QT, class T, class LOAD>
+__device__ __forceinline__ T pull_thermal_xrow(const Geo& g, int a, int i, long long c, LOAD load) {
+    const long long off = (long long)Lat<QT>::ex(a) + (long long)g.nx * ((long long)Lat<QT>::ey(a) + (long long)g.ny * (long long)Lat<QT>::ez(a));
+    if (Lat<QT>::ex(a) == 0) return load(a, c - off);
+    const int si = i - Lat<QT>::ex(a);
+    const bool out = si < 0 || si >= g.nx;
+    const int bt = g.bct[0];
+    if (bt == LBM_BCT_PERIODIC) return load(a, c - off + (out ? (long long)Lat<QT>::ex(a) * g.nx : 0LL));
+    const T v = out ? load(Lat<QT>::opp(a), c) : load(a, c - off);
+    if (bt == LBM_BCT_CONST && out) return -v + (T)(si < 0 ? g.bcT_lo[0] : g.bcT_hi[0]);
+    return v;
+}
+
 // ------------------------------------------------------------------------------------
 // In-place (AA) access pattern.  One array per lattice; its layout alternates:
 //   parity 0 ("streamed"): slot (a, x) holds the streamed population f_a(x), i.e. what the

@@ -44,46 +44,36 @@ __global__ void __launch_bounds__(128) k_xthermal(Geo g, PhysX X, FixedArrays A,
     thermal_cell<D, FIRST>(g, X, A, fin, gin, gout, c, i, j, k);
 }
 
-// Interior cells (no pull needs a boundary rule) of the steady-state step: block (bx, j, k)
-// holds cells i = bx*128 + t of the interior row (j, k), so warps start at row starts (rows
-// are 2 KB-aligned when nx is a multiple of 32); threads on the x faces (i = 0, nx-1) do
-// nothing, the face kernels take every face cell.  Keeping the boundary code out of these
-// kernels keeps them small (instruction fetch) and in fewer registers.
+// Cells of interior rows (0 < j < ny-1, and 0 < k < nz-1 in 3D) in the steady-state step:
+// block (bx, j, k) holds cells i = bx*128 + t of the row, so warps start at row starts (rows
+// are 2 KB-aligned when nx is a multiple of 32) and every access of a warp is one contiguous
+// run.  Only x can take a pull source outside the lattice there, which the row pulls handle
+// with selects; the face kernels take the y- and z-face rows.
 __device__ __forceinline__ bool fixed_interior_cell(const Geo& g, long long& c, int& i, int& j, int& k) {
     i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     j = (int)blockIdx.y + 1;
     k = g.nz > 1 ? (int)blockIdx.z + 1 : 0;
-    if (i < 1 || i >= g.nx - 1) return false;
+    if (i >= g.nx) return false;
     c = (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
     return true;
 }
 
-// Face cells: x faces (i = 0, nx-1; all j, k), then y faces (j = 0, ny-1; 0 < i < nx-1; all
-// k), then in 3D the z faces (k = 0, nz-1; 0 < i < nx-1; 0 < j < ny-1).
-__host__ __device__ __forceinline__ long long fixed_face_count(const Geo& g) {
-    const long long nx = g.nx, ny = g.ny, nz = g.nz;
-    long long f = 2 * ny * nz + 2 * (nx - 2) * nz;
-    if (nz > 1) f += 2 * (nx - 2) * (ny - 2);
-    return f;
+// Face rows: the y faces (j = 0, ny-1; every k), then in 3D the z faces (k = 0, nz-1;
+// 0 < j < ny-1); block (bx, r) holds cells i = bx*128 + t of face row r.
+__host__ __device__ __forceinline__ long long fixed_face_rows(const Geo& g) {
+    return 2LL * g.nz + (g.nz > 1 ? 2LL * (g.ny - 2) : 0LL);
 }
 __device__ __forceinline__ bool fixed_face_cell(const Geo& g, long long& c, int& i, int& j, int& k) {
-    long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= fixed_face_count(g)) return false;
-    const long long nx = g.nx, ny = g.ny, nz = g.nz;
-    const long long nxf = 2 * ny * nz, nyf = 2 * (nx - 2) * nz;
-    if (f < nxf) {
-        i = (f & 1) ? g.nx - 1 : 0;
-        j = (int)((f >> 1) % ny);
-        k = (int)((f >> 1) / ny);
-    } else if ((f -= nxf) < nyf) {
-        j = (f & 1) ? g.ny - 1 : 0;
-        i = 1 + (int)((f >> 1) % (nx - 2));
-        k = (int)((f >> 1) / (nx - 2));
+    i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= g.nx) return false;
+    const int r = (int)blockIdx.y;
+    if (r < 2 * g.nz) {
+        j = (r & 1) ? g.ny - 1 : 0;
+        k = r >> 1;
     } else {
-        f -= nyf;
-        k = (f & 1) ? g.nz - 1 : 0;
-        i = 1 + (int)((f >> 1) % (nx - 2));
-        j = 1 + (int)((f >> 1) / (nx - 2));
+        const int s = r - 2 * g.nz;
+        k = (s & 1) ? g.nz - 1 : 0;
+        j = 1 + (s >> 1);
     }
     c = (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
     return true;
@@ -95,7 +85,7 @@ __global__ void __launch_bounds__(128, LBM_XFLOW_MIN_BLOCKS) k_xflow_in(Geo g, P
     long long c;
     int i, j, k;
     if (!fixed_interior_cell(g, c, i, j, k)) return;
-    flow_cell<D, false, 1>(g, X, A, fin, gin, fout, c, i, j, k);
+    flow_cell<D, false, 3>(g, X, A, fin, gin, fout, c, i, j, k);
 }
 
 template <int D>
@@ -114,7 +104,7 @@ __global__ void __launch_bounds__(128, 6) k_xthermal_in(Geo g, PhysX X, FixedArr
     long long c;
     int i, j, k;
     if (!fixed_interior_cell(g, c, i, j, k)) return;
-    thermal_cell<D, false, 1>(g, X, A, fin, gin, gout, c, i, j, k);
+    thermal_cell<D, false, 3>(g, X, A, fin, gin, gout, c, i, j, k);
 }
 
 template <int D>
@@ -376,15 +366,16 @@ void fixed_fused_pass(const Geo& g, const PhysX& X, const long long* fin, const 
 template <int D>
 static void steady_step(const Geo& g, const PhysX& X, const FixedArrays& A, const long long* fprev,
                         const long long* gprev, long long* fnext, long long* gnext, cudaStream_t s, bool fl, bool th) {
-    const dim3 bin(128), gin_grid((unsigned)((g.nx + 127) / 128), (unsigned)(g.ny - 2), D == 3 ? (unsigned)(g.nz - 2) : 1u);
-    const unsigned nf = xblocks(fixed_face_count(g), 128);
+    const unsigned bx = (unsigned)((g.nx + 127) / 128);
+    const dim3 bin(128), gin_grid(bx, (unsigned)(g.ny - 2), D == 3 ? (unsigned)(g.nz - 2) : 1u);
+    const dim3 gface(bx, (unsigned)fixed_face_rows(g), 1u);
     if (fl) {
         k_xflow_in<D><<<gin_grid, bin, 0, s>>>(g, X, A, fprev, gprev, fnext);
-        k_xflow_face<D><<<nf, 128, 0, s>>>(g, X, A, fprev, gprev, fnext);
+        k_xflow_face<D><<<gface, bin, 0, s>>>(g, X, A, fprev, gprev, fnext);
     }
     if (th) {
         k_xthermal_in<D><<<gin_grid, bin, 0, s>>>(g, X, A, fnext, gprev, gnext);
-        k_xthermal_face<D><<<nf, 128, 0, s>>>(g, X, A, fnext, gprev, gnext);
+        k_xthermal_face<D><<<gface, bin, 0, s>>>(g, X, A, fnext, gprev, gnext);
     }
 }
 

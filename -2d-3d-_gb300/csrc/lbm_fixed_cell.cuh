@@ -501,7 +501,8 @@ namespace fxa {
 // u of the macro step of f_{n-1} with the lag.  2D stores the force F_y,n in the lag.
 // g: geometry whose thermal wall terms are deviations (wall term - 2 wT Tref).
 // PATH: 0 = any cell (the boundary rule where a pull leaves the lattice), 1 = a cell known to
-// touch no face (fixed-offset pulls only), 2 = a face cell (boundary path only).
+// touch no face (fixed-offset pulls only), 2 = a face cell (boundary path only), 3 = a cell of
+// an interior row (only x can leave the lattice: pull_flow_xrow / pull_thermal_xrow).
 template <int D, bool FIRST, int PATH = 0>
 __device__ __forceinline__ void flow_cell(const Geo& g, const PhysX& X, const FixedArrays& A, const long long* fin,
                                           const long long* gin, long long* fout, long long c, int i, int j, int k) {
@@ -520,7 +521,14 @@ __device__ __forceinline__ void flow_cell(const Geo& g, const PhysX& X, const Fi
         tdev = q60(A.T[c]) - Qb(X.tref);
     } else {
         q60 ts = Qb(0);
-        if (PATH == 1 || (PATH == 0 && aa_inner(g, i, j, k))) {  // no pull needs a boundary rule
+        if (PATH == 3) {
+            auto lf = [&](int a, long long cc) { return ldq(fin, a * n + cc); };
+            auto lg = [&](int a, long long cc) { return ldq(gin, a * n + cc); };
+#pragma unroll
+            for (int a = 0; a < Q; ++a) d[a] = pull_flow_xrow<Q, q60>(g, a, i, c, lf);
+#pragma unroll
+            for (int a = 0; a < QT; ++a) ts = ts + pull_thermal_xrow<QT, q60>(g, a, i, c, lg);
+        } else if (PATH == 1 || (PATH == 0 && aa_inner(g, i, j, k))) {  // no pull needs a boundary rule
 #pragma unroll
             for (int a = 0; a < Q; ++a) {
                 LBM_CHECK_CELL(g, c - lat_off<Q>(g, a));
@@ -558,7 +566,10 @@ __device__ __forceinline__ void thermal_cell(const Geo& g, const PhysX& X, const
     q60 d[Q], e[QT], ep[QT], rho, P[3], U[3], B[3], tdev;
     const bool inner = PATH == 1 || (PATH == 0 && aa_inner(g, i, j, k));
     auto lf = [&](int a, long long cc) { return ldq(fin, a * n + cc); };
-    if (inner) {
+    if (PATH == 3) {
+#pragma unroll
+        for (int a = 0; a < Q; ++a) d[a] = pull_flow_xrow<Q, q60>(g, a, i, c, lf);
+    } else if (inner) {
 #pragma unroll
         for (int a = 0; a < Q; ++a) d[a] = ldq(fin, a * n + c - lat_off<Q>(g, a));
     } else {
@@ -574,7 +585,14 @@ __device__ __forceinline__ void thermal_cell(const Geo& g, const PhysX& X, const
         B[2] = D == 3 ? q60(A.Bz[c]) : Qb(0);
     } else {
         q60 ts = Qb(0);
-        if (inner) {
+        if (PATH == 3) {
+            auto lg = [&](int a, long long cc) { return ldq(gin, a * n + cc); };
+#pragma unroll
+            for (int a = 0; a < QT; ++a) {
+                e[a] = pull_thermal_xrow<QT, q60>(g, a, i, c, lg);
+                ts = ts + e[a];
+            }
+        } else if (inner) {
 #pragma unroll
             for (int a = 0; a < QT; ++a) {
                 e[a] = ldq(gin, a * n + c - lat_off<QT>(g, a));
