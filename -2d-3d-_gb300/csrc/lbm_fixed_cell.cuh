@@ -100,16 +100,22 @@ __device__ __forceinline__ q60 mul(q60 a, q60 b) {
     return Qb((long long)(((__int128)a.s() * (__int128)b.s()) >> kFrac));
 #endif
 }
-// Product with a constant k given as K = round(k * 2^(64-S)) (|k| < 2^(S-1)), rounded down.
+// Product with a non-negative constant k given as an even K = round(k * 2^(64-S)) (k < 2^(S-1)),
+// rounded down: floor(a k).  Constants are stored as magnitudes and their signs written into
+// the formulas, because an unsigned high multiply needs no sign correction: with
+// a' = a + 2^63 (the top bit flipped, a' >= 0), floor(a' K / 2^64) = floor(a K / 2^64) + K/2
+// for an even K, and for S = 1, floor(a' K / 2^63) = floor(a K / 2^63) + K.
 template <int S>
 __device__ __forceinline__ q60 mulk(q60 a, long long K) {
 #ifdef __CUDA_ARCH__
-    const unsigned long long hi = (unsigned long long)__mul64hi(a.s(), K);
+    const unsigned long long ab = a.u ^ 0x8000000000000000ULL;
+    const unsigned long long Ku = (unsigned long long)K;
+    const unsigned long long hi = __umul64hi(ab, Ku);
     if constexpr (S == 0) {
-        return Qb((long long)hi);
+        return Qb((long long)(hi - (Ku >> 1)));
     } else {
-        const unsigned long long lo = a.u * (unsigned long long)K;
-        return Qb((long long)((hi << S) | (lo >> (64 - S))));
+        const unsigned long long lo = ab * Ku;
+        return Qb((long long)(((hi << S) | (lo >> (64 - S))) - Ku));
     }
 #else
     return Qb((long long)(((__int128)a.s() * (__int128)K) >> (64 - S)));
@@ -155,8 +161,9 @@ __device__ __forceinline__ q60 ldq(const long long* p, long long idx) {
 
 }  // namespace fxa
 
-// Constants of the fixed arithmetic for one run, from the commondata constants.  Products
-// with constants use K = round(k 2^64) (|k| < 1/2) unless noted (2^63, |k| < 1).
+// Constants of the fixed arithmetic for one run, from the commondata constants.  Each is the
+// magnitude of a constant as an even K = round(|k| 2^64) (|k| < 1/2), or 2^63 where noted
+// (|k| < 1); the comments give the signed constant and the formulas apply its sign.
 struct PhysX {
     long long w[19];     // flow rest weights w_a (q60): D2Q9 in the first 9, or D3Q19
     long long wt[7];     // thermal rest populations wT_a Tref (q60)
@@ -164,10 +171,10 @@ struct PhysX {
     long long gb;        // gBeta
     // 3D flow: c_i = k_n n_i + k_s (source product), n_i the non-equilibrium moment
     long long e_n, e_s;        // -Se/2394, (1 - Se/2) 38/2394 (times u.F)
-    long long p_n, p_s;        // -Seps/252, (1 - Seps/2) (-11)/252
-    long long q_n, q_p, q_s;   // -Sq/40, -Sq/60 (the -2/3 rho u of meq_q), (1 - Sq/2)(-2/3)/40 (times F_y)
+    long long p_n, p_s;        // -Seps/252, -(1 - Seps/2) 11/252
+    long long q_n, q_p, q_s;   // -Sq/40, -Sq/60 (the -2/3 rho u of meq_q), -(1 - Sq/2)(2/3)/40 (times F_y)
     long long j_f;             // 1/10 (F_y on the j_y moment)
-    long long x9_n, x9_s;      // -Snu/36, (1 - Snu/2)(-2)/36
+    long long x9_n, x9_s;      // -Snu/36, -(1 - Snu/2) 2/36
     long long x10_n, x10_s;    // -Spi/72, (1 - Spi/2)/72
     long long x11_n, x11_s;    // -Snu/12, (1 - Snu/2) 2/12
     long long x12_n, x12_s;    // -Spi/24, -(1 - Spi/2)/24
@@ -182,17 +189,18 @@ struct PhysX {
     // thermal (3D: n4 row norm 42, n5 12, n6 4; 2D: n3 20, n4 4)
     long long qk2;             // -Qk/2, scale 2^63
     long long sg2;             // SG/2
-    long long t_n, t_a;        // -Qnu/norm and Qnu a_T/norm of the a_T T moment
+    long long t_n, t_a;        // -Qnu/norm; Qnu a_T/norm of the a_T T moment, of sign t_a_neg
     long long t5_n, t6_n;      // 3D: -Qnu/12, -Qnu/4; 2D: t5_n = -Qnu/4
     long long bc_lo[3], bc_hi[3];  // constant-T wall terms of deviations (q60), per axis
+    int t_a_neg;               // 1 when Qnu a_T < 0 (a_T = -3/4, -2/3; the legacy paraA may be either)
     int use_g;
 };
 
-// Constant k as round(k * 2^(64-S)); false when |k| >= 2^(S-1).
+// Magnitude k >= 0 as an even round(k * 2^(64-S)); false when k leaves [0, 2^(S-1)).
 inline bool fx_const(long double k, int S, long long& K) {
     const long double lim = S == 0 ? 0.5L : 1.0L;
-    if (!(k > -lim && k < lim)) return false;
-    K = (long long)std::llround(k * (S == 0 ? 0x1p64L : 0x1p63L));
+    if (!(k >= 0 && k < lim)) return false;
+    K = (long long)std::llround(k * (S == 0 ? 0x1p64L : 0x1p63L)) & ~1LL;
     return true;
 }
 
@@ -217,31 +225,33 @@ inline bool make_physx(const lbm_params& p, const lbm_constants& c, PhysX& X) {
     bool ok = fx_const(c.gBeta, 0, X.gb);
     const long double Se = c.Se, Seps = c.Seps, Sq = c.Sq, Snu = c.Snu, Spi = c.Spi, Sm = c.Sm;
     if (d3) {
-        ok = ok && fx_const(-Se / 2394, 0, X.e_n) && fx_const((1 - Se / 2) * 38 / 2394, 0, X.e_s);
-        ok = ok && fx_const(-Seps / 252, 0, X.p_n) && fx_const((1 - Seps / 2) * (-11) / 252, 0, X.p_s);
-        ok = ok && fx_const(-Sq / 40, 0, X.q_n) && fx_const(-Sq / 60, 0, X.q_p) &&
-             fx_const((1 - Sq / 2) * (-2.0L / 3) / 40, 0, X.q_s);
+        ok = ok && fx_const(Se / 2394, 0, X.e_n) && fx_const((1 - Se / 2) * 38 / 2394, 0, X.e_s);
+        ok = ok && fx_const(Seps / 252, 0, X.p_n) && fx_const((1 - Seps / 2) * 11 / 252, 0, X.p_s);
+        ok = ok && fx_const(Sq / 40, 0, X.q_n) && fx_const(Sq / 60, 0, X.q_p) &&
+             fx_const((1 - Sq / 2) * (2.0L / 3) / 40, 0, X.q_s);
         ok = ok && fx_const(1.0L / 10, 0, X.j_f);
-        ok = ok && fx_const(-Snu / 36, 0, X.x9_n) && fx_const((1 - Snu / 2) * (-2) / 36, 0, X.x9_s);
-        ok = ok && fx_const(-Spi / 72, 0, X.x10_n) && fx_const((1 - Spi / 2) / 72, 0, X.x10_s);
-        ok = ok && fx_const(-Snu / 12, 0, X.x11_n) && fx_const((1 - Snu / 2) * 2 / 12, 0, X.x11_s);
-        ok = ok && fx_const(-Spi / 24, 0, X.x12_n) && fx_const(-(1 - Spi / 2) / 24, 0, X.x12_s);
-        ok = ok && fx_const(-Snu / 4, 0, X.x13_n) && fx_const((1 - Snu / 2) / 4, 0, X.x13_s);
-        ok = ok && fx_const(-Sm / 8, 0, X.m_n);
+        ok = ok && fx_const(Snu / 36, 0, X.x9_n) && fx_const((1 - Snu / 2) * 2 / 36, 0, X.x9_s);
+        ok = ok && fx_const(Spi / 72, 0, X.x10_n) && fx_const((1 - Spi / 2) / 72, 0, X.x10_s);
+        ok = ok && fx_const(Snu / 12, 0, X.x11_n) && fx_const((1 - Snu / 2) * 2 / 12, 0, X.x11_s);
+        ok = ok && fx_const(Spi / 24, 0, X.x12_n) && fx_const((1 - Spi / 2) / 24, 0, X.x12_s);
+        ok = ok && fx_const(Snu / 4, 0, X.x13_n) && fx_const((1 - Snu / 2) / 4, 0, X.x13_s);
+        ok = ok && fx_const(Sm / 8, 0, X.m_n);
     } else {
-        ok = ok && fx_const(-Snu / 36, 0, X.e2_n) && fx_const((6 - 3 * Snu) / 36, 0, X.e2_s);
-        ok = ok && fx_const(-Sq / 12, 0, X.q2_n) && fx_const(-(1 - Sq / 2) / 12, 0, X.q2_s);
+        ok = ok && fx_const(Snu / 36, 0, X.e2_n) && fx_const((6 - 3 * Snu) / 36, 0, X.e2_s);
+        ok = ok && fx_const(Sq / 12, 0, X.q2_n) && fx_const((1 - Sq / 2) / 12, 0, X.q2_s);
         ok = ok && fx_const(1.0L / 6, 0, X.j2_f);
-        ok = ok && fx_const(-Snu / 4, 0, X.x7_n) && fx_const(-(2 - Snu) / 4, 0, X.x7_s);
+        ok = ok && fx_const(Snu / 4, 0, X.x7_n) && fx_const((2 - Snu) / 4, 0, X.x7_s);
         ok = ok && fx_const((1 - Snu / 2) / 4, 0, X.x8_s);
     }
     const long double Qk = c.Qk, Qnu = c.Qnu, SG = c.SG;
     // a_T of the thermal equilibrium moment: -3/4 (3D), -2/3 (2D), paraA in the legacy scheme
     const long double aT = p.legacy_thermal ? (long double)c.paraA : (d3 ? -0.75L : -2.0L / 3);
     const long double nrm = d3 ? 42 : 20;
-    ok = ok && fx_const(-Qk / 2, 1, X.qk2) && fx_const(SG / 2, 0, X.sg2);
-    ok = ok && fx_const(-Qnu / nrm, 0, X.t_n) && fx_const(Qnu * aT / nrm, 0, X.t_a);
-    ok = ok && fx_const(d3 ? -Qnu / 12 : -Qnu / 4, 0, X.t5_n) && fx_const(-Qnu / 4, 0, X.t6_n);
+    const long double ta = Qnu * aT / nrm;
+    X.t_a_neg = ta < 0 ? 1 : 0;
+    ok = ok && fx_const(Qk / 2, 1, X.qk2) && fx_const(SG / 2, 0, X.sg2);
+    ok = ok && fx_const(Qnu / nrm, 0, X.t_n) && fx_const(ta < 0 ? -ta : ta, 0, X.t_a);
+    ok = ok && fx_const(d3 ? Qnu / 12 : Qnu / 4, 0, X.t5_n) && fx_const(Qnu / 4, 0, X.t6_n);
     X.use_g = p.use_g ? 1 : 0;
     const Geo dg = deviation_geo(make_geo(p, c), c);
     for (int a = 0; a < 3; ++a) {
@@ -308,13 +318,14 @@ __device__ __forceinline__ q60 collide_2d(const q60* d, q60 rho, const q60* P, c
     const q60 n7 = m7 - (ruu - rvv);
     const q60 n8 = m8 - ruv;
     // c_i = (-s_i n_i + source_i) / D_i (sources 2DRB.F90:729-737 with F_x = 0)
-    const q60 c1 = mulk<0>(n1, X.e2_n) + mulk<0>(vF, X.e2_s);
-    const q60 c2 = mulk<0>(n2, X.e2_n) - mulk<0>(vF, X.e2_s);
-    const q60 c4 = mulk<0>(m4 + P[0], X.q2_n);
+    const q60 sv = mulk<0>(vF, X.e2_s);
+    const q60 c1 = -mulk<0>(n1, X.e2_n) + sv;
+    const q60 c2 = -mulk<0>(n2, X.e2_n) - sv;
+    const q60 c4 = -mulk<0>(m4 + P[0], X.q2_n);
     const q60 c5 = mulk<0>(Fy, X.j2_f);
-    const q60 c6 = mulk<0>(m6 + P[1], X.q2_n) + mulk<0>(Fy, X.q2_s);
-    const q60 c7 = mulk<0>(n7, X.x7_n) + mulk<0>(vF, X.x7_s);
-    const q60 c8 = mulk<0>(n8, X.x7_n) + mulk<0>(uF, X.x8_s);
+    const q60 c6 = -mulk<0>(m6 + P[1], X.q2_n) - mulk<0>(Fy, X.q2_s);
+    const q60 c7 = -mulk<0>(n7, X.x7_n) - mulk<0>(vF, X.x7_s);
+    const q60 c8 = -mulk<0>(n8, X.x7_n) + mulk<0>(uF, X.x8_s);
     // f_post - f = M^T c (columns of M: 2DRB.F90:743-759 times the row norms)
     const q60 ax = -c1 - 2 * c2, dg = 2 * c1 + c2;
     const q60 X4 = 2 * c4, Y6 = c5 - 2 * c6, Y = c5 + c6;
@@ -377,20 +388,20 @@ __device__ __forceinline__ void collide_3d(const q60* d, q60 rho, const q60* P, 
     const q60 n9 = m9 - e9, n10 = m10 + half(e9);
     const q60 n11 = m11 - e11, n12 = m12 + half(e11);
     // c_i = (-s_i n_i + source_i) / D_i (rates 3DRB.F90:803-821, sources :831-849)
-    const q60 c1 = mulk<0>(n1, X.e_n) + mulk<0>(vF, X.e_s);
-    const q60 c2 = mulk<0>(n2, X.p_n) + mulk<0>(vF, X.p_s);
-    const q60 c4 = mulk<0>(m4, X.q_n) + mulk<0>(P[0], X.q_p);
+    const q60 c1 = -mulk<0>(n1, X.e_n) + mulk<0>(vF, X.e_s);
+    const q60 c2 = -mulk<0>(n2, X.p_n) - mulk<0>(vF, X.p_s);
+    const q60 c4 = -mulk<0>(m4, X.q_n) - mulk<0>(P[0], X.q_p);
     const q60 c5 = mulk<0>(Fy, X.j_f);
-    const q60 c6 = mulk<0>(m6, X.q_n) + mulk<0>(P[1], X.q_p) + mulk<0>(Fy, X.q_s);
-    const q60 c8 = mulk<0>(m8, X.q_n) + mulk<0>(P[2], X.q_p);
-    const q60 c9 = mulk<0>(n9, X.x9_n) + mulk<0>(vF, X.x9_s);
-    const q60 c10 = mulk<0>(n10, X.x10_n) + mulk<0>(vF, X.x10_s);
-    const q60 c11 = mulk<0>(n11, X.x11_n) + mulk<0>(vF, X.x11_s);
-    const q60 c12 = mulk<0>(n12, X.x12_n) + mulk<0>(vF, X.x12_s);
-    const q60 c13 = mulk<0>(m13 - ruv, X.x13_n) + mulk<0>(uF, X.x13_s);
-    const q60 c14 = mulk<0>(m14 - rvw, X.x13_n) + mulk<0>(wF, X.x13_s);
-    const q60 c15 = mulk<0>(m15 - ruw, X.x13_n);
-    const q60 c16 = mulk<0>(m16, X.m_n), c17 = mulk<0>(m17, X.m_n), c18 = mulk<0>(m18, X.m_n);
+    const q60 c6 = -mulk<0>(m6, X.q_n) - mulk<0>(P[1], X.q_p) - mulk<0>(Fy, X.q_s);
+    const q60 c8 = -mulk<0>(m8, X.q_n) - mulk<0>(P[2], X.q_p);
+    const q60 c9 = -mulk<0>(n9, X.x9_n) - mulk<0>(vF, X.x9_s);
+    const q60 c10 = -mulk<0>(n10, X.x10_n) + mulk<0>(vF, X.x10_s);
+    const q60 c11 = -mulk<0>(n11, X.x11_n) + mulk<0>(vF, X.x11_s);
+    const q60 c12 = -mulk<0>(n12, X.x12_n) - mulk<0>(vF, X.x12_s);
+    const q60 c13 = -mulk<0>(m13 - ruv, X.x13_n) + mulk<0>(uF, X.x13_s);
+    const q60 c14 = -mulk<0>(m14 - rvw, X.x13_n) + mulk<0>(wF, X.x13_s);
+    const q60 c15 = -mulk<0>(m15 - ruw, X.x13_n);
+    const q60 c16 = -mulk<0>(m16, X.m_n), c17 = -mulk<0>(m17, X.m_n), c18 = -mulk<0>(m18, X.m_n);
     // f_post - f = M^T c (columns of M: 3DRB.F90:861-943 times the row norms)
     const q60 ba = -11 * c1 - 4 * c2, bd = 8 * c1 + c2;
     const q60 p9 = -c9 + 2 * c10, p11 = c11 - 2 * c12;
@@ -442,11 +453,12 @@ __device__ __forceinline__ void collideT_3d(const q60* e, const q60* U, q60 tdev
     const q60 n4 = -6 * e[0] + s16;
     const q60 n5 = 2 * (e[1] + e[2]) - (e[3] + e[4] + e[5] + e[6]);
     const q60 n6 = e[3] + e[4] - e[5] - e[6];
-    const q60 c1 = mulk<1>(n1 - bx, X.qk2) + mulk<0>(dbx, X.sg2);
-    const q60 c2 = mulk<1>(n2 - by, X.qk2) + mulk<0>(dby, X.sg2);
-    const q60 c3 = mulk<1>(n3 - bz, X.qk2) + mulk<0>(dbz, X.sg2);
-    const q60 c4 = mulk<0>(n4, X.t_n) + mulk<0>(tdev, X.t_a);
-    const q60 c5 = mulk<0>(n5, X.t5_n), c6 = mulk<0>(n6, X.t6_n);
+    const q60 c1 = -mulk<1>(n1 - bx, X.qk2) + mulk<0>(dbx, X.sg2);
+    const q60 c2 = -mulk<1>(n2 - by, X.qk2) + mulk<0>(dby, X.sg2);
+    const q60 c3 = -mulk<1>(n3 - bz, X.qk2) + mulk<0>(dbz, X.sg2);
+    const q60 ta = mulk<0>(tdev, X.t_a);
+    const q60 c4 = -mulk<0>(n4, X.t_n) + (X.t_a_neg ? -ta : ta);
+    const q60 c5 = -mulk<0>(n5, X.t5_n), c6 = -mulk<0>(n6, X.t6_n);
     const q60 h = c4 - c5;
     ep[0] = e[0] - 6 * c4;
     ep[1] = e[1] + c1 + c4 + 2 * c5;
@@ -470,10 +482,11 @@ __device__ __forceinline__ void collideT_2d(const q60* e, const q60* U, q60 tdev
     const q60 n1 = e[1] - e[3], n2 = e[2] - e[4];
     const q60 n3 = -4 * e[0] + e[1] + e[2] + e[3] + e[4];
     const q60 n4 = e[1] - e[2] + e[3] - e[4];
-    const q60 c1 = mulk<1>(n1 - bx, X.qk2) + mulk<0>(dbx, X.sg2);
-    const q60 c2 = mulk<1>(n2 - by, X.qk2) + mulk<0>(dby, X.sg2);
-    const q60 c3 = mulk<0>(n3, X.t_n) + mulk<0>(tdev, X.t_a);
-    const q60 c4 = mulk<0>(n4, X.t5_n);
+    const q60 c1 = -mulk<1>(n1 - bx, X.qk2) + mulk<0>(dbx, X.sg2);
+    const q60 c2 = -mulk<1>(n2 - by, X.qk2) + mulk<0>(dby, X.sg2);
+    const q60 ta = mulk<0>(tdev, X.t_a);
+    const q60 c3 = -mulk<0>(n3, X.t_n) + (X.t_a_neg ? -ta : ta);
+    const q60 c4 = -mulk<0>(n4, X.t5_n);
     ep[0] = e[0] - 4 * c3;
     ep[1] = e[1] + c1 + c3 + c4;
     ep[2] = e[2] + c2 + c3 - c4;
