@@ -106,6 +106,12 @@ struct lbm_handle {
     cudaEvent_t order_ev = nullptr;    // orders the handle's stream against the ensemble's
 
     int reload_form = -1;  // form used by the last lbm_reload (0 reference, 1 continuation)
+
+    // State transfer straight between the caller's host arrays and the device arrays: the
+    // layout kernels read and write pageable host memory coherently (Grace + NVLink-C2C:
+    // cudaDevAttrPageableMemoryAccess), instead of a staged copy through the driver.
+    bool host_access = false;   // the device can
+    bool host_direct = false;   // and the handle does (LBM_OPT_HOST_DIRECT)
 };
 
 // ------------------------------------------------------------------------------------
@@ -458,6 +464,11 @@ extern "C" int lbm_create(const lbm_params* p, int device, lbm_handle** out) {
         release(h);
         delete h;
         return st;
+    }
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess && pageable) {
+        h->host_access = true;
+        h->host_direct = true;
     }
     *out = h;
     return LBM_OK;
@@ -1449,13 +1460,20 @@ static int state_io(lbm_handle* h, int field, double* dst, const double* src, si
                            false, 0.0, 0.0, h->stream);
             CK_LAUNCH(h, "module view");
             CK(h, cudaMemcpyAsync(dst, h->d_stage, want * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        } else if (dst && h->host_direct) {
+            soa_to_aos(soa, dst, qq, n, h->stream);  // written straight into the caller's array
+            CK_LAUNCH(h, "soa_to_aos");
         } else if (dst) {
             soa_to_aos(soa, h->d_stage, qq, n, h->stream);
             CK_LAUNCH(h, "soa_to_aos");
             CK(h, cudaMemcpyAsync(dst, h->d_stage, want * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         } else {
-            CK(h, cudaMemcpyAsync(h->d_stage, src, want * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-            aos_to_soa(h->d_stage, soa, qq, n, h->stream);
+            if (h->host_direct) {
+                aos_to_soa(src, soa, qq, n, h->stream);  // read straight from the caller's array
+            } else {
+                CK(h, cudaMemcpyAsync(h->d_stage, src, want * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+                aos_to_soa(h->d_stage, soa, qq, n, h->stream);
+            }
             CK_LAUNCH(h, "aos_to_soa");
             if (th) {  // module data in the streamed layout
                 h->aa.gpar = 0;
@@ -1469,8 +1487,14 @@ static int state_io(lbm_handle* h, int field, double* dst, const double* src, si
     }
     double* d = scalar_ptr(h, field);
     if (!d) return fail(h, LBM_ERR_PARAM, "field not defined for this dimension");
-    if (dst) CK(h, cudaMemcpyAsync(dst, d, want * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    else CK(h, cudaMemcpyAsync(d, src, want * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (h->host_direct) {
+        copy_doubles(dst ? d : src, dst ? dst : d, (long long)want, h->stream);
+        CK_LAUNCH(h, "field copy");
+    } else if (dst) {
+        CK(h, cudaMemcpyAsync(dst, d, want * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    } else {
+        CK(h, cudaMemcpyAsync(d, src, want * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    }
     CK(h, cudaStreamSynchronize(h->stream));
     return LBM_OK;
 }
@@ -1984,6 +2008,11 @@ extern "C" int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, 
 extern "C" int lbm_set_option(lbm_handle* h, int option, int value) {
     if (!h) return LBM_ERR_PARAM;
     switch (option) {
+        case LBM_OPT_HOST_DIRECT:
+            if (value != 0 && !h->host_access)
+                return fail(h, LBM_ERR_STATE, "the device cannot access pageable host memory");
+            h->host_direct = value != 0;
+            break;
         case LBM_OPT_SINGLE_KERNEL:
             if (h->fixed) {  // fused passes of the fixed arithmetic (3D), or its two-kernel step
                 h->xfused = value != 0;

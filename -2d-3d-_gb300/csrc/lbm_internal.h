@@ -222,7 +222,9 @@ int psi_fine_search(int nx, int ny, double xLen, double yLen, int nFineX, int nF
                     int* best_l, cudaStream_t s);
 
 // ---- layout transforms (lbm_reduce.cu) -------------------------------------------------
-// Fortran AoS f(0:q-1, cells) <-> device SoA f[q][cells], FP64.
+// Fortran AoS f(0:q-1, cells) <-> device SoA f[q][cells], FP64.  Either side may be host
+// memory that the device reads and writes coherently (cudaDevAttrPageableMemoryAccess).
+void copy_doubles(const double* src, double* dst, long long n, cudaStream_t s);
 void aos_to_soa(const double* aos, double* soa, int q, long long ncell, cudaStream_t s);
 void soa_to_aos(const double* soa, double* aos, int q, long long ncell, cudaStream_t s);
 

@@ -384,6 +384,15 @@ __global__ void k_soa_to_aos(const double* __restrict__ soa, double* __restrict_
     aos[e] = soa[(long long)a * n + c];
 }
 
+__global__ void k_copy_doubles(const double* __restrict__ src, double* __restrict__ dst, long long n) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) dst[e] = src[e];
+}
+
+void copy_doubles(const double* src, double* dst, long long n, cudaStream_t s) {
+    k_copy_doubles<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, dst, n);
+}
+
 void aos_to_soa(const double* aos, double* soa, int q, long long ncell, cudaStream_t s) {
     const long long tot = (long long)q * ncell;
     k_aos_to_soa<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(aos, soa, q, ncell);

@@ -42,6 +42,7 @@ module lbm_gpu_mod
   integer(c_int), parameter :: LBM_FIELD_FX = 10, LBM_FIELD_FY = 11, LBM_FIELD_F_POST = 12, LBM_FIELD_G_POST = 13
   integer(c_int), parameter :: LBM_OPT_SINGLE_KERNEL = 1, LBM_OPT_KCHUNK = 2, LBM_OPT_PAIRS = 3, LBM_OPT_STAGED = 4
   integer(c_int), parameter :: LBM_OPT_FP16_ROUNDING = 5   ! 1 stochastic (default), 0 nearest
+  integer(c_int), parameter :: LBM_OPT_HOST_DIRECT = 6     ! state transfer on host arrays directly
 
   type, bind(C) :: lbm_params
     integer(c_int32_t) :: dim, nx, ny, nz

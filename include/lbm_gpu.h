@@ -273,6 +273,13 @@ int lbm_footprint(const lbm_params* p, size_t* bytes);
 #define LBM_OPT_PAIRS         3
 #define LBM_OPT_STAGED        4
 #define LBM_OPT_FP16_ROUNDING 5 /* FP16 storage: 1 stochastic rounding (default), 0 nearest */
+/* LBM_OPT_HOST_DIRECT: lbm_get_state / lbm_set_state of an FP64 handle move the caller's host
+ *   array straight to and from the device arrays with the layout kernels reading and writing
+ *   the host memory coherently (1; the default where the device reports
+ *   cudaDevAttrPageableMemoryAccess, as a GPU attached to a Grace CPU over NVLink-C2C does),
+ *   or stage them through a device buffer with a copy (0).  Same values either way; the host
+ *   array must stay valid until the call returns (the calls synchronise). */
+#define LBM_OPT_HOST_DIRECT   6
 int lbm_set_option(lbm_handle* h, int option, int value);
 
 /* ---- measurement hooks (no counterpart in the reference, which times its loop with
