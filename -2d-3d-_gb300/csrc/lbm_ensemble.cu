@@ -36,6 +36,32 @@ struct EnsMember {
 template <int D>
 constexpr bool kEnsInner = true;
 
+// Cell coordinates of a thread's cells in a tile, stepped instead of divided: one division
+// at the tile's first cell, then (i, j, k) advance by blockDim.x cells with carries (i by
+// less than a row; j may wrap several planes on narrow lattices).
+struct CellWalk {
+    long long c;
+    int i, j, k, di, dj;
+    __device__ __forceinline__ CellWalk(const Geo& g, long long c0) : c(c0) {
+        cell_coords(g, c0, i, j, k);
+        di = (int)(blockDim.x % (unsigned)g.nx);
+        dj = (int)(blockDim.x / (unsigned)g.nx);
+    }
+    __device__ __forceinline__ void next(const Geo& g) {
+        c += blockDim.x;
+        i += di;
+        j += dj;
+        if (i >= g.nx) {
+            i -= g.nx;
+            j += 1;
+        }
+        while (j >= g.ny) {
+            j -= g.ny;
+            k += 1;
+        }
+    }
+};
+
 template <int D, class S>
 __global__ void __launch_bounds__(256, 2) k_ens_flow(const EnsMember<S>* __restrict__ mem, const int2* __restrict__ tiles,
                                                   int ntiles, int tile_cells, int flip) {
@@ -51,11 +77,8 @@ __global__ void __launch_bounds__(256, 2) k_ens_flow(const EnsMember<S>* __restr
         A.tick = m.tick;
         const long long c0 = (long long)tt.y * tile_cells;
         const long long ce = min(c0 + tile_cells, g.ncell);
-        for (long long c = c0 + threadIdx.x; c < ce; c += blockDim.x) {
-            int i, j, k;
-            cell_coords(g, c, i, j, k);
-            flow_cell_2k<D, false, S, kEnsInner<D>>(g, P, A, m.f[cur], m.gp[cur], m.f[nxt], c, i, j, k);
-        }
+        for (CellWalk w(g, c0 + threadIdx.x); w.c < ce; w.next(g))
+            flow_cell_2k<D, false, S, kEnsInner<D>>(g, P, A, m.f[cur], m.gp[cur], m.f[nxt], w.c, w.i, w.j, w.k);
     }
 }
 
@@ -77,11 +100,8 @@ __global__ void __launch_bounds__(256, 2) k_ens_thermal(const EnsMember<S>* __re
         A.tick = m.tick;
         const long long c0 = (long long)tt.y * tile_cells;
         const long long ce = min(c0 + tile_cells, g.ncell);
-        for (long long c = c0 + threadIdx.x; c < ce; c += blockDim.x) {
-            int i, j, k;
-            cell_coords(g, c, i, j, k);
-            thermal_cell_2k<D, false, S, kEnsInner<D>>(g, P, A, m.f[nxt], m.gp[cur], m.gp[nxt], c, i, j, k);
-        }
+        for (CellWalk w(g, c0 + threadIdx.x); w.c < ce; w.next(g))
+            thermal_cell_2k<D, false, S, kEnsInner<D>>(g, P, A, m.f[nxt], m.gp[cur], m.gp[nxt], w.c, w.i, w.j, w.k);
     }
 }
 
