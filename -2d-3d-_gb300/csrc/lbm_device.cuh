@@ -179,8 +179,9 @@ __device__ __forceinline__ T pull_flow_xrow(const Geo& g, int a, int i, long lon
     const int si = i - Lat<Q>::ex(a);
     const bool out = si < 0 || si >= g.nx;
     if (g.bcf[0] == LBM_BC_NOSLIP) return out ? load(Lat<Q>::opp(a), c) : load(a, c - off);
-    // periodic: the same-row copy from the other end of the row
-    return load(a, c - off + (out ? (long long)Lat<Q>::ex(a) * g.nx : 0LL));
+    // periodic: the same-row copy from the other end of the row (j and k unchanged, also
+    // for the diagonal directions: the reference's x-periodic copy, 2DRB.F90:821-828)
+    return load(a, out ? c + (long long)Lat<Q>::ex(a) * (g.nx - 1) : c - off);
 }
 template <int QT, class T, class LOAD>
 __device__ __forceinline__ T pull_thermal_xrow(const Geo& g, int a, int i, long long c, LOAD load) {
@@ -189,7 +190,7 @@ __device__ __forceinline__ T pull_thermal_xrow(const Geo& g, int a, int i, long 
     const int si = i - Lat<QT>::ex(a);
     const bool out = si < 0 || si >= g.nx;
     const int bt = g.bct[0];
-    if (bt == LBM_BCT_PERIODIC) return load(a, c - off + (out ? (long long)Lat<QT>::ex(a) * g.nx : 0LL));
+    if (bt == LBM_BCT_PERIODIC) return load(a, out ? c + (long long)Lat<QT>::ex(a) * (g.nx - 1) : c - off);
     const T v = out ? load(Lat<QT>::opp(a), c) : load(a, c - off);
     if (bt == LBM_BCT_CONST && out) return -v + (T)(si < 0 ? g.bcT_lo[0] : g.bcT_hi[0]);
     return v;

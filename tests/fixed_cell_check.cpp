@@ -18,6 +18,14 @@ using namespace lbm::fxa;
 
 namespace {
 
+// A row of the steady-state step's interior-row kernels (0 < j < ny-1, and 0 < k < nz-1 in
+// 3D); the other rows go to the face-row kernels.  The stepper takes the same path per cell as
+// the GPU (PATH 3: select-based x rule; PATH 2: full boundary rule), and the first step the
+// any-cell path of the first-step kernels.
+static bool interior_row(const Geo& g, int j, int k) {
+    return j > 0 && j < g.ny - 1 && (g.nz == 1 || (k > 0 && k < g.nz - 1));
+}
+
 template <int D>
 void run(const Geo& g, const PhysX& X, FixedArrays& A, long long nsteps, std::vector<long long>* fb,
          std::vector<long long>* gb) {
@@ -28,12 +36,16 @@ void run(const Geo& g, const PhysX& X, FixedArrays& A, long long nsteps, std::ve
         for (long long c = 0; c < n; ++c) {
             const int i = (int)(c % g.nx), j = (int)((c / g.nx) % g.ny), k = (int)(c / ((long long)g.nx * g.ny));
             if (s == 0) flow_cell<D, true>(g, X, A, fb[cur].data(), gb[cur].data(), fb[nxt].data(), c, i, j, k);
-            else flow_cell<D, false>(g, X, A, fb[cur].data(), gb[cur].data(), fb[nxt].data(), c, i, j, k);
+            else if (interior_row(g, j, k))
+                flow_cell<D, false, 3>(g, X, A, fb[cur].data(), gb[cur].data(), fb[nxt].data(), c, i, j, k);
+            else flow_cell<D, false, 2>(g, X, A, fb[cur].data(), gb[cur].data(), fb[nxt].data(), c, i, j, k);
         }
         for (long long c = 0; c < n; ++c) {
             const int i = (int)(c % g.nx), j = (int)((c / g.nx) % g.ny), k = (int)(c / ((long long)g.nx * g.ny));
             if (s == 0) thermal_cell<D, true>(g, X, A, fb[nxt].data(), gb[cur].data(), gb[nxt].data(), c, i, j, k);
-            else thermal_cell<D, false>(g, X, A, fb[nxt].data(), gb[cur].data(), gb[nxt].data(), c, i, j, k);
+            else if (interior_row(g, j, k))
+                thermal_cell<D, false, 3>(g, X, A, fb[nxt].data(), gb[cur].data(), gb[nxt].data(), c, i, j, k);
+            else thermal_cell<D, false, 2>(g, X, A, fb[nxt].data(), gb[cur].data(), gb[nxt].data(), c, i, j, k);
         }
         cur = nxt;
     }
