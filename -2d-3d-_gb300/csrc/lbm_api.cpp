@@ -2271,13 +2271,36 @@ extern "C" int lbm_ensemble_sync(lbm_ensemble* e) {
     return LBM_OK;
 }
 
+extern "C" int lbm_ensemble_configure(lbm_ensemble* e, int block, int tile_cells, int grid_mul, int pairs) {
+    if (!e) return LBM_ERR_PARAM;
+    if ((block != 128 && block != 256) || tile_cells <= 0 || tile_cells % block != 0 || grid_mul < 1 ||
+        grid_mul > 64 || pairs < 0 || pairs > 3)
+        return efail(e, LBM_ERR_PARAM, "lbm_ensemble_configure: block 128 or 256, tile_cells a positive multiple "
+                                       "of block, grid_mul 1..64, pairs 0..3");
+    e->cfg = EnsLaunchCfg{block, tile_cells, grid_mul, pairs};
+    e->dirty = true;
+    return LBM_OK;
+}
+
+extern "C" int lbm_ensemble_get_launch(const lbm_ensemble* e, int* block, int* tile_cells, int* grid_mul,
+                                       int* pairs) {
+    if (!e) return LBM_ERR_PARAM;
+    if (block) *block = e->cfg.block;
+    if (tile_cells) *tile_cells = e->cfg.tile_cells;
+    if (grid_mul) *grid_mul = e->cfg.grid_mul;
+    if (pairs) *pairs = e->cfg.pairs;
+    return LBM_OK;
+}
+
 // Time `nsteps` batched steps per launch configuration and keep the fastest.  The steps
 // are real steps: every member advances by ncand * nsteps steps.
 extern "C" int lbm_ensemble_autotune(lbm_ensemble* e, int nsteps, int* best_block, int* best_tile, int* best_grid) {
     if (!e || nsteps <= 0) return LBM_ERR_PARAM;
     if (e->members.empty()) return LBM_OK;
-    const EnsLaunchCfg cands[] = {{128, 512, 8}, {128, 1024, 16}, {256, 1024, 4}, {256, 2048, 8},
-                                  {256, 4096, 8}, {128, 2048, 8}};
+    // pairs: bit 0 pairs the 2D members, bit 1 the 3D members
+    const EnsLaunchCfg cands[] = {{128, 1024, 16, 1}, {128, 1024, 32, 1}, {128, 1024, 64, 1}, {128, 512, 64, 1},
+                                  {128, 2048, 32, 1}, {256, 2048, 16, 1}, {256, 4096, 8, 1},  {128, 1024, 32, 3},
+                                  {128, 1024, 16, 0}, {128, 1024, 32, 0}, {128, 512, 64, 0},  {256, 2048, 8, 0}};
     ECK(e, cudaSetDevice(e->device));
     int st = lbm_ensemble_step(e, 1);  // first steps and ordering
     if (st != LBM_OK) return st;

@@ -5,15 +5,16 @@
 // (member m, first cell c0) and covers tile_cells consecutive cells of member m.  Each
 // block reads the member's descriptor (geometry, relaxation rates, buffer pointers and
 // parity), then runs the same per-cell bodies as the single-lattice two-kernel step
-// (lbm_fast_cells.cuh) on its cells.  Small lattices therefore fill the GPU together
-// instead of one launch each.
+// (lbm_fast_cells.cuh, or the paired bodies of lbm_fast_pairs.cuh for members with even
+// nx) on its cells.  Small lattices therefore fill the GPU together instead of one launch
+// each.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <vector>
 
 #include "lbm_ensemble.h"
-#include "lbm_fast_cells.cuh"
+#include "lbm_fast_pairs.cuh"
 
 namespace lbm {
 
@@ -29,26 +30,29 @@ struct EnsMember {
     int cur;    // buffer parity when the table was built
 };
 
-// Fixed-offset pulls for the cells off the faces (lbm_fast_cells.cuh), and two resident
-// blocks per SM (the 3D thermal kernel otherwise takes 242 registers, one block): measured
-// on GB300, 64 2D RB instances (8.4 M cells) 1.4x faster in FP32 and 2.8x in FP16, twelve
-// 3D instances of 64^3-192^3 (23.5 M cells) 2.1x in FP32.
+// Fixed-offset pulls for the cells off the faces (lbm_fast_cells.cuh).  Resident blocks of
+// 256 threads per SM: three, except two for the paired 3D bodies (about 115 registers).
+// With the member descriptor and buffer arguments staged in shared memory the one-cell
+// kernels take 66-80 registers, against 96-128 with register copies of the descriptor
+// (the 3D thermal kernel took 242 without a bound), and none spills.
 template <int D>
 constexpr bool kEnsInner = true;
+template <int D, bool PAIR>
+constexpr int kEnsBlocks = (D == 3 && PAIR) ? 2 : 3;
 
 // Cell coordinates of a thread's cells in a tile, stepped instead of divided: one division
-// at the tile's first cell, then (i, j, k) advance by blockDim.x cells with carries (i by
+// at the thread's first cell, then (i, j, k) advance by `stride` cells with carries (i by
 // less than a row; j may wrap several planes on narrow lattices).
 struct CellWalk {
     long long c;
-    int i, j, k, di, dj;
-    __device__ __forceinline__ CellWalk(const Geo& g, long long c0) : c(c0) {
+    int i, j, k, di, dj, stride;
+    __device__ __forceinline__ CellWalk(const Geo& g, long long c0, int stride_) : c(c0), stride(stride_) {
         cell_coords(g, c0, i, j, k);
-        di = (int)(blockDim.x % (unsigned)g.nx);
-        dj = (int)(blockDim.x / (unsigned)g.nx);
+        di = (int)((unsigned)stride % (unsigned)g.nx);
+        dj = (int)((unsigned)stride / (unsigned)g.nx);
     }
     __device__ __forceinline__ void next(const Geo& g) {
-        c += blockDim.x;
+        c += stride;
         i += di;
         j += dj;
         if (i >= g.nx) {
@@ -62,46 +66,96 @@ struct CellWalk {
     }
 };
 
-template <int D, class S>
-__global__ void __launch_bounds__(256, 2) k_ens_flow(const EnsMember<S>* __restrict__ mem, const int2* __restrict__ tiles,
-                                                  int ntiles, int tile_cells, int flip) {
+// The member descriptor of a block's current tile and the buffer arguments of this step,
+// staged in shared memory: the cell bodies read geometry, constants and buffer pointers
+// from there as the single-lattice kernels read them from the kernel parameters, instead of
+// holding register copies across the cell loop.  `args` (thread 0) fills the arguments from
+// the descriptor in global memory.
+template <class S>
+struct EnsStage {
+    EnsMember<S> m;
+    FastArgs<S> A;
+};
+
+template <class S, class ARGS>
+__device__ __forceinline__ const EnsStage<S>& stage_member(const EnsMember<S>* __restrict__ mem, int idx,
+                                                           unsigned* __restrict__ sh, ARGS args) {
+    static_assert(sizeof(EnsMember<S>) % 4 == 0, "descriptor copied in 32-bit words");
+    EnsStage<S>& st = *reinterpret_cast<EnsStage<S>*>(sh);
+    const unsigned* src = reinterpret_cast<const unsigned*>(mem + idx);
+    __syncthreads();  // the block's previous tile is done with the staged copy
+    for (int w = threadIdx.x; w < (int)(sizeof(EnsMember<S>) / 4); w += blockDim.x) sh[w] = __ldg(src + w);
+    if (threadIdx.x == 0) {
+        FastArgs<S> A{};
+        args(mem[idx], A);
+        st.A = A;
+    }
+    __syncthreads();
+    return st;
+}
+
+// PAIR: the thread's cells are c and c + 1 (same row: nx even, tiles start on even cells,
+// c even), walked with a stride of two cells per thread.
+template <int D, class S, bool PAIR>
+__global__ void __launch_bounds__(256, (kEnsBlocks<D, PAIR>)) k_ens_flow(const EnsMember<S>* __restrict__ mem,
+                                                                       const int2* __restrict__ tiles, int ntiles,
+                                                                       int tile_cells, int flip) {
+    constexpr int W = PAIR ? 2 : 1;
+    __shared__ __align__(16) unsigned sh[(sizeof(EnsStage<S>) + 3) / 4];
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tt = tiles[t];
-        const EnsMember<S>& m = mem[tt.x];
-        const Geo g = m.g;
-        const PhysF P = m.P;
+        const EnsStage<S>& st = stage_member<S>(mem, tt.x, sh, [flip](const EnsMember<S>& gm, FastArgs<S>& A) {
+            const int c = gm.cur ^ flip;
+            A.lag_in = gm.L[c];
+            A.lag_out = gm.L[c ^ 1];
+            A.tick = gm.tick;
+        });
+        const EnsMember<S>& m = st.m;
+        const FastArgs<S>& A = st.A;
+        const Geo& g = m.g;
+        const PhysF& P = m.P;
         const int cur = m.cur ^ flip, nxt = cur ^ 1;
-        FastArgs<S> A{};
-        A.lag_in = m.L[cur];
-        A.lag_out = m.L[nxt];
-        A.tick = m.tick;
         const long long c0 = (long long)tt.y * tile_cells;
         const long long ce = min(c0 + tile_cells, g.ncell);
-        for (CellWalk w(g, c0 + threadIdx.x); w.c < ce; w.next(g))
-            flow_cell_2k<D, false, S, kEnsInner<D>>(g, P, A, m.f[cur], m.gp[cur], m.f[nxt], w.c, w.i, w.j, w.k);
+        for (CellWalk w(g, c0 + W * (long long)threadIdx.x, W * (int)blockDim.x); w.c < ce; w.next(g)) {
+            if constexpr (PAIR)
+                flow_pair_2k<D, S>(g, P, A, m.f[cur], m.gp[cur], m.f[nxt], w.c, w.i, w.j, w.k);
+            else
+                flow_cell_2k<D, false, S, kEnsInner<D>>(g, P, A, m.f[cur], m.gp[cur], m.f[nxt], w.c, w.i, w.j, w.k);
+        }
     }
 }
 
-template <int D, class S>
-__global__ void __launch_bounds__(256, 2) k_ens_thermal(const EnsMember<S>* __restrict__ mem,
-                                                     const int2* __restrict__ tiles, int ntiles, int tile_cells,
-                                                     int flip) {
+template <int D, class S, bool PAIR>
+__global__ void __launch_bounds__(256, (kEnsBlocks<D, PAIR>)) k_ens_thermal(const EnsMember<S>* __restrict__ mem,
+                                                                          const int2* __restrict__ tiles, int ntiles,
+                                                                          int tile_cells, int flip) {
+    constexpr int W = PAIR ? 2 : 1;
+    __shared__ __align__(16) unsigned sh[(sizeof(EnsStage<S>) + 3) / 4];
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tt = tiles[t];
-        const EnsMember<S>& m = mem[tt.x];
-        const Geo g = m.g;
-        const PhysF P = m.P;
+        const EnsStage<S>& st = stage_member<S>(mem, tt.x, sh, [flip](const EnsMember<S>& gm, FastArgs<S>& A) {
+            const int c = gm.cur ^ flip, n = c ^ 1;
+            A.Bin0 = gm.B[c][0]; A.Bin1 = gm.B[c][1]; A.Bin2 = gm.B[c][2];
+            A.Bout0 = gm.B[n][0]; A.Bout1 = gm.B[n][1]; A.Bout2 = gm.B[n][2];
+            A.lag_in = gm.L[n];
+            A.lag_out = gm.L[n];
+            A.tick = gm.tick;
+        });
+        const EnsMember<S>& m = st.m;
+        const FastArgs<S>& A = st.A;
+        const Geo& g = m.g;
+        const PhysF& P = m.P;
         const int cur = m.cur ^ flip, nxt = cur ^ 1;
-        FastArgs<S> A{};
-        A.Bin0 = m.B[cur][0]; A.Bin1 = m.B[cur][1]; A.Bin2 = m.B[cur][2];
-        A.Bout0 = m.B[nxt][0]; A.Bout1 = m.B[nxt][1]; A.Bout2 = m.B[nxt][2];
-        A.lag_in = m.L[nxt];
-        A.lag_out = m.L[nxt];
-        A.tick = m.tick;
         const long long c0 = (long long)tt.y * tile_cells;
         const long long ce = min(c0 + tile_cells, g.ncell);
-        for (CellWalk w(g, c0 + threadIdx.x); w.c < ce; w.next(g))
-            thermal_cell_2k<D, false, S, kEnsInner<D>>(g, P, A, m.f[nxt], m.gp[cur], m.gp[nxt], w.c, w.i, w.j, w.k);
+        for (CellWalk w(g, c0 + W * (long long)threadIdx.x, W * (int)blockDim.x); w.c < ce; w.next(g)) {
+            if constexpr (PAIR)
+                thermal_pair_2k<D, S>(g, P, A, m.f[nxt], m.gp[cur], m.gp[nxt], w.c, w.i, w.j, w.k);
+            else
+                thermal_cell_2k<D, false, S, kEnsInner<D>>(g, P, A, m.f[nxt], m.gp[cur], m.gp[nxt], w.c, w.i, w.j,
+                                                           w.k);
+        }
     }
 }
 
@@ -114,12 +168,16 @@ __global__ void k_ens_tick(const EnsMember<S>* __restrict__ mem, int nmem) {
 
 template <class S>
 static cudaError_t build_typed(EnsPlan& plan, const std::vector<EnsMemberHost>& members) {
-    for (int di = 0; di < 2; ++di) {
-        const int dim = di == 0 ? 2 : 3;
+    // a member pairs when the configuration pairs, its rows hold whole pairs, and every tile
+    // starts on an even cell
+    for (int li = 0; li < kEnsLists; ++li) {
+        const int dim = (li & 1) ? 3 : 2;
+        const bool paired = (li & 2) != 0;
+        const bool pairing = (plan.cfg.pairs & (dim == 3 ? 2 : 1)) != 0 && plan.cfg.tile_cells % 2 == 0;
         std::vector<EnsMember<S>> hm;
         std::vector<int2> tiles;
         for (const EnsMemberHost& mh : members) {
-            if (mh.dim != dim) continue;
+            if (mh.dim != dim || (pairing && mh.geo.nx % 2 == 0) != paired) continue;
             EnsMember<S> m{};
             m.g = dev_geo(mh.geo, mh.phys);
             m.P = fast_physf(*mh.F, mh.phys);
@@ -137,28 +195,28 @@ static cudaError_t build_typed(EnsPlan& plan, const std::vector<EnsMemberHost>& 
             plan.cells += m.g.ncell;
             hm.push_back(m);
         }
-        plan.nmembers[di] = (int)hm.size();
-        plan.ntiles[di] = (int)tiles.size();
+        plan.nmembers[li] = (int)hm.size();
+        plan.ntiles[li] = (int)tiles.size();
         if (hm.empty()) continue;
-        cudaError_t e = cudaMalloc(&plan.d_members[di], hm.size() * sizeof(EnsMember<S>));
+        cudaError_t e = cudaMalloc(&plan.d_members[li], hm.size() * sizeof(EnsMember<S>));
         if (e != cudaSuccess) return e;
-        e = cudaMalloc((void**)&plan.d_tiles[di], tiles.size() * sizeof(int2));
+        e = cudaMalloc((void**)&plan.d_tiles[li], tiles.size() * sizeof(int2));
         if (e != cudaSuccess) return e;
-        e = cudaMemcpy(plan.d_members[di], hm.data(), hm.size() * sizeof(EnsMember<S>), cudaMemcpyHostToDevice);
+        e = cudaMemcpy(plan.d_members[li], hm.data(), hm.size() * sizeof(EnsMember<S>), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return e;
-        e = cudaMemcpy(plan.d_tiles[di], tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice);
+        e = cudaMemcpy(plan.d_tiles[li], tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
 void ens_free(EnsPlan& plan) {
-    for (int di = 0; di < 2; ++di) {
-        if (plan.d_members[di]) cudaFree(plan.d_members[di]);
-        if (plan.d_tiles[di]) cudaFree(plan.d_tiles[di]);
-        plan.d_members[di] = nullptr;
-        plan.d_tiles[di] = nullptr;
-        plan.nmembers[di] = plan.ntiles[di] = 0;
+    for (int li = 0; li < kEnsLists; ++li) {
+        if (plan.d_members[li]) cudaFree(plan.d_members[li]);
+        if (plan.d_tiles[li]) cudaFree(plan.d_tiles[li]);
+        plan.d_members[li] = nullptr;
+        plan.d_tiles[li] = nullptr;
+        plan.nmembers[li] = plan.ntiles[li] = 0;
     }
     plan.cells = 0;
 }
@@ -171,27 +229,35 @@ cudaError_t ens_build(EnsPlan& plan, const std::vector<EnsMemberHost>& members, 
     return plan.precision == LBM_FP16 ? build_typed<__half>(plan, members) : build_typed<float>(plan, members);
 }
 
+template <int D, class S, bool PAIR>
+static void launch_list(const EnsPlan& plan, int li, int stage, int flip, cudaStream_t s) {
+    const int grid = min(plan.ntiles[li], plan.sms * plan.cfg.grid_mul);
+    const EnsMember<S>* mem = (const EnsMember<S>*)plan.d_members[li];
+    if (stage == 0)
+        k_ens_flow<D, S, PAIR><<<grid, plan.cfg.block, 0, s>>>(mem, plan.d_tiles[li], plan.ntiles[li],
+                                                               plan.cfg.tile_cells, flip);
+    else
+        k_ens_thermal<D, S, PAIR><<<grid, plan.cfg.block, 0, s>>>(mem, plan.d_tiles[li], plan.ntiles[li],
+                                                                  plan.cfg.tile_cells, flip);
+}
+
 template <class S>
 static void step_typed(const EnsPlan& plan, int flip, cudaStream_t s) {
-    const int blk = plan.cfg.block, tc = plan.cfg.tile_cells;
     for (int stage = 0; stage < 2; ++stage) {
-        for (int di = 0; di < 2; ++di) {
-            if (plan.ntiles[di] == 0) continue;
-            const int grid = min(plan.ntiles[di], plan.sms * plan.cfg.grid_mul);
-            const EnsMember<S>* mem = (const EnsMember<S>*)plan.d_members[di];
-            if (stage == 0) {
-                if (di == 0) k_ens_flow<2, S><<<grid, blk, 0, s>>>(mem, plan.d_tiles[di], plan.ntiles[di], tc, flip);
-                else k_ens_flow<3, S><<<grid, blk, 0, s>>>(mem, plan.d_tiles[di], plan.ntiles[di], tc, flip);
-            } else {
-                if (di == 0) k_ens_thermal<2, S><<<grid, blk, 0, s>>>(mem, plan.d_tiles[di], plan.ntiles[di], tc, flip);
-                else k_ens_thermal<3, S><<<grid, blk, 0, s>>>(mem, plan.d_tiles[di], plan.ntiles[di], tc, flip);
+        for (int li = 0; li < kEnsLists; ++li) {
+            if (plan.ntiles[li] == 0) continue;
+            switch (li) {
+                case 0: launch_list<2, S, false>(plan, li, stage, flip, s); break;
+                case 1: launch_list<3, S, false>(plan, li, stage, flip, s); break;
+                case 2: launch_list<2, S, true>(plan, li, stage, flip, s); break;
+                default: launch_list<3, S, true>(plan, li, stage, flip, s); break;
             }
         }
     }
-    for (int di = 0; di < 2; ++di) {
-        if (plan.nmembers[di] == 0) continue;
-        k_ens_tick<S><<<(plan.nmembers[di] + 127) / 128, 128, 0, s>>>((const EnsMember<S>*)plan.d_members[di],
-                                                                      plan.nmembers[di]);
+    for (int li = 0; li < kEnsLists; ++li) {
+        if (plan.nmembers[li] == 0) continue;
+        k_ens_tick<S><<<(plan.nmembers[li] + 127) / 128, 128, 0, s>>>((const EnsMember<S>*)plan.d_members[li],
+                                                                      plan.nmembers[li]);
     }
 }
 

@@ -2,8 +2,10 @@
 //
 // Members keep their own buffers (each is an ordinary handle); the ensemble builds a
 // device table of member descriptors (geometry, constants, buffer pointers, buffer
-// parity) and a packed tile table (member, first cell) over all members of one
-// dimension, and advances every member with one flow and one thermal launch per step.
+// parity) and a packed tile table (member, first cell) per member list, and advances every
+// member with one flow and one thermal launch per list and step.  Lists: 2D and 3D members
+// taken one cell per thread, and 2D and 3D members with even nx taken two x-adjacent cells
+// per thread (2-element vector loads and stores) when the launch configuration pairs.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -24,15 +26,19 @@ struct EnsMemberHost {
 struct EnsLaunchCfg {
     int block = 128;        // threads per block
     int tile_cells = 1024;  // cells per tile (a multiple of `block`)
-    int grid_mul = 8;       // grid = min(tiles, SMs * grid_mul)
+    int grid_mul = 32;      // grid = min(tiles, SMs * grid_mul)
+    int pairs = 1;          // members with even nx two cells per thread: bit 0 2D, bit 1 3D
 };
+
+// Member lists of a plan: index (dim == 3) + 2 * paired.
+constexpr int kEnsLists = 4;
 
 struct EnsPlan {
     int precision = LBM_FP32;
-    int nmembers[2] = {0, 0};  // [0] = 2D, [1] = 3D
-    void* d_members[2] = {nullptr, nullptr};
-    int2* d_tiles[2] = {nullptr, nullptr};
-    int ntiles[2] = {0, 0};
+    int nmembers[kEnsLists] = {};
+    void* d_members[kEnsLists] = {};
+    int2* d_tiles[kEnsLists] = {};
+    int ntiles[kEnsLists] = {};
     long long cells = 0;
     EnsLaunchCfg cfg;
     int sms = 152;

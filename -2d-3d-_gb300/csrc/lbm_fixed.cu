@@ -13,10 +13,11 @@ namespace lbm {
 
 using namespace fxa;
 
-// Resident blocks per SM asked of the interior flow kernel: 4 (128 registers, no spill) ran
-// faster on GB300 than 5 (96 registers and a spill) or 6, at 128^3, 256^3 and 384^3.
+// Resident blocks per SM asked of the interior flow kernel: 5 (96 registers, no spill) ran
+// the kernel 8% faster on GB300 than 4 (124 registers) at 256^3 and 384^3, where the warps
+// wait on their loads (long-scoreboard stalls) at half the issue rate; 6 spills.
 #ifndef LBM_XFLOW_MIN_BLOCKS
-#define LBM_XFLOW_MIN_BLOCKS 4
+#define LBM_XFLOW_MIN_BLOCKS 5
 #endif
 
 __device__ __forceinline__ bool fixed_cell_of_thread(const Geo& g, long long& c, int& i, int& j, int& k) {

@@ -78,6 +78,8 @@ SIGNATURES = {
     "lbm_ensemble_get_stream": ([_vp, C.POINTER(_vp)], _i32),
     "lbm_ensemble_last_error": ([_vp], C.c_char_p),
     "lbm_ensemble_autotune": ([_vp, _i32, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32)], _i32),
+    "lbm_ensemble_configure": ([_vp, _i32, _i32, _i32, _i32], _i32),
+    "lbm_ensemble_get_launch": ([_vp, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32)], _i32),
     "lbm_SideHeatedcalc_Nu_global": ([_vp, _dp], _i32),
     "lbm_SideHeatedcalc_Nu_wall_avg": ([_vp, _vp], _i32),
     "lbm_SideHeatedcalc_umid_max": ([_vp, _vp], _i32),
@@ -419,7 +421,19 @@ class Ensemble:
         b, t, g = C.c_int(), C.c_int(), C.c_int()
         self._ck(self.lib.lbm_ensemble_autotune(self._h, int(nsteps), C.byref(b), C.byref(t), C.byref(g)),
                  "lbm_ensemble_autotune")
-        return {"block": b.value, "tile_cells": t.value, "grid_per_sm": g.value}
+        return self.launch()
+
+    def configure(self, block=128, tile_cells=1024, grid_per_sm=8, pairs=1):
+        """Set the launch configuration (pairs: bit 0 pairs 2D members with even nx, bit 1
+        3D members); the values do not depend on it."""
+        self._ck(self.lib.lbm_ensemble_configure(self._h, int(block), int(tile_cells), int(grid_per_sm), int(pairs)),
+                 "lbm_ensemble_configure")
+
+    def launch(self):
+        b, t, g, p = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self._ck(self.lib.lbm_ensemble_get_launch(self._h, C.byref(b), C.byref(t), C.byref(g), C.byref(p)),
+                 "lbm_ensemble_get_launch")
+        return {"block": b.value, "tile_cells": t.value, "grid_per_sm": g.value, "pairs": p.value}
 
     def close(self):
         if getattr(self, "_h", None):

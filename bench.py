@@ -433,7 +433,7 @@ def ensemble_run(args, local, steps_total=13000, every=500):
     return {"workload": "64 D2Q9/D2Q5 RB instances, aspect 2, ny in {64..512}, Ra log-uniform 1e4..1e8, "
                         "Pr in {0.71,7}, FP32 storage, %d cells" % cells,
             "aggregate_mlups": mlups, "ms_per_step": ms / k, "steps_timed": k, "autotuned": cfg,
-            "launches_per_step": 2,
+            "launches_per_step": 3,  # flow, thermal, step counters (one member list: all 2D, even nx)
             "dNu_vs_fp64": {
                 "compared": len(good), "median": good[len(good) // 2] if good else None,
                 "max": good[-1] if good else None, "within_1pct": sum(1 for x in good if x <= 0.01),

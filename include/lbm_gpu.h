@@ -239,6 +239,14 @@ const char* lbm_ensemble_last_error(const lbm_ensemble* e);
 /* Tile/block autotuner: times `nsteps` steps of each launch configuration and keeps the
  * fastest (members advance by those steps); outputs may be NULL. */
 int lbm_ensemble_autotune(lbm_ensemble* e, int nsteps, int* best_block, int* best_tile, int* best_grid);
+/* Launch configuration of the batched step: threads per block (128 or 256), cells per tile
+ * (a positive multiple of the block), grid = min(tiles, SMs x grid_mul) with grid_mul in
+ * 1..64, and pairs (bit 0: 2D members with even nx take two x-adjacent cells per thread with
+ * 2-element vector loads and stores; bit 1: the same for 3D members).  Every configuration
+ * gives the same values bit for bit; lbm_ensemble_autotune picks one by timing.
+ * LBM_ERR_PARAM for values out of range.  get_launch: outputs may be NULL. */
+int lbm_ensemble_configure(lbm_ensemble* e, int block, int tile_cells, int grid_mul, int pairs);
+int lbm_ensemble_get_launch(const lbm_ensemble* e, int* block, int* tile_cells, int* grid_mul, int* pairs);
 /* Device bytes lbm_create allocates for these parameters (for admission against an HBM
  * budget). */
 int lbm_footprint(const lbm_params* p, size_t* bytes);

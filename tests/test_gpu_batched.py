@@ -2,7 +2,8 @@
 
 * An ensemble of uneven 2D/3D lattices advanced together must give every member exactly
   the state it reaches when advanced alone (same per-cell arithmetic; only the tile table
-  differs).
+  differs), under launch configurations that take the members with even nx one cell or two
+  x-adjacent cells per thread.
 * The autotuner advances the members by real steps and keeps them consistent.
 * lbm_footprint matches what lbm_create takes from the device.
 * The server gives each solve the same result alone and in a mix of concurrent solves.
@@ -21,7 +22,14 @@ MEMBERS = [
     dict(dim=3, nx=16, ny=16, nz=16, Ra=1e6, Pr=0.71, seed=3),
     dict(dim=2, nx=128, ny=64, Ra=2e4, Pr=0.71, seed=4),
     dict(dim=3, nx=20, ny=12, nz=10, Ra=5e5, Pr=7.0, seed=5),
+    dict(dim=2, nx=75, ny=30, Ra=2e5, Pr=0.71, seed=6, periodic_x=False),  # odd nx: one cell per thread
+    dict(dim=3, nx=15, ny=12, nz=9, Ra=5e5, Pr=0.71, seed=7),
+    dict(dim=2, nx=70, ny=20, Ra=1e5, Pr=0.71, seed=8),  # rows not aligned with tiles
 ]
+
+# launch configurations: (block, tile_cells, grid_per_sm, pairs); pairs bit 0 pairs the 2D
+# members with even nx, bit 1 the 3D members
+LAUNCHES = [(128, 1024, 8, 0), (128, 1024, 8, 1), (256, 2048, 4, 3), (128, 512, 16, 2)]
 
 
 def make(m, precision="fp32"):
@@ -31,9 +39,13 @@ def make(m, precision="fp32"):
     return lat
 
 
+@pytest.mark.parametrize("launch", LAUNCHES)
 @pytest.mark.parametrize("precision", ["fp32", "fp16"])
-def test_ensemble_matches_individual(precision):
+def test_ensemble_matches_individual(precision, launch):
     ens = Ensemble()
+    block, tile, grid, pairs = launch
+    ens.configure(block=block, tile_cells=tile, grid_per_sm=grid, pairs=pairs)
+    assert ens.launch() == {"block": block, "tile_cells": tile, "grid_per_sm": grid, "pairs": pairs}
     batched = [make(m, precision) for m in MEMBERS]
     for lat in batched:
         ens.add(lat)
@@ -54,8 +66,9 @@ def test_ensemble_matches_individual(precision):
     ens.step(10)
     for lat in alone:
         lat.step(10)
-    for i in (0, 2, 3, 4):
-        assert np.array_equal(batched[i].get_state("T"), alone[i].get_state("T"))
+    for i in range(len(MEMBERS)):
+        if i != 1:
+            assert np.array_equal(batched[i].get_state("T"), alone[i].get_state("T"))
     ens.close()
 
 
@@ -65,7 +78,7 @@ def test_autotune_keeps_members_consistent():
     for lat in batched:
         ens.add(lat)
     cfg = ens.autotune(2)
-    assert cfg["block"] in (128, 256) and cfg["tile_cells"] % cfg["block"] == 0
+    assert cfg["block"] in (128, 256) and cfg["tile_cells"] % cfg["block"] == 0 and cfg["pairs"] in (0, 1, 2, 3)
     steps = batched[0].itc
     assert all(lat.itc == steps for lat in batched)
     alone = [make(m) for m in MEMBERS]
@@ -78,6 +91,9 @@ def test_autotune_keeps_members_consistent():
 
 def test_ensemble_rejects_fp64_and_duplicates():
     ens = Ensemble()
+    for bad in ((64, 1024, 8, 1), (128, 1000, 8, 1), (128, 1024, 0, 1), (256, 1024, 8, 4)):
+        with pytest.raises(LbmError):
+            ens.configure(*bad)
     p = rb_params(dim=2, nx=32, ny=16, Ra=1e5)
     lat = Lattice(p)
     lat.initial()
