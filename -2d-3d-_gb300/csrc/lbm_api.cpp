@@ -2033,6 +2033,10 @@ extern "C" int lbm_set_option(lbm_handle* h, int option, int value) {
             if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the plain FP64 method has no paired form");
             h->F.pairs = value != 0;
             break;
+        case LBM_OPT_ROWS:
+            if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the FP64 forms choose their own launches");
+            h->F.rows = value != 0;
+            break;
         case LBM_OPT_STAGED:
             if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the plain FP64 method has no staged form");
             h->F.tma = value != 0;

@@ -168,6 +168,46 @@ __device__ __forceinline__ T pull_thermal(const Geo& g, int a, int i, int j, int
     return pull_thermal_w<QT, T>(g, a, i, j, k, c, load, [&](int, int d, long long cc) { return load(d, cc); });
 }
 
+// Row launches.  Interior rows (0 < j < ny-1, and 0 < k < nz-1 in 3D): block (bx, j-1, k-1)
+// holds cells i = bx*blockDim.x + t of row (j, k), so warps start at row starts and every
+// access of a warp is one contiguous run; only x can take a pull source outside the lattice
+// there.  Face rows: the y faces (j = 0, ny-1; every k), then in 3D the z faces (k = 0,
+// nz-1; 0 < j < ny-1); block (bx, r) holds cells i = bx*blockDim.x + t of face row r.
+#if defined(__CUDACC__)
+__device__ __forceinline__ bool row_interior_cell(const Geo& g, long long& c, int& i, int& j, int& k) {
+    i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    j = (int)blockIdx.y + 1;
+    k = g.nz > 1 ? (int)blockIdx.z + 1 : 0;
+    if (i >= g.nx) return false;
+    c = (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
+    return true;
+}
+#endif
+__host__ __device__ __forceinline__ long long face_row_count(const Geo& g) {
+    return 2LL * g.nz + (g.nz > 1 ? 2LL * (g.ny - 2) : 0LL);
+}
+#if defined(__CUDACC__)
+__device__ __forceinline__ bool row_face_cell(const Geo& g, long long& c, int& i, int& j, int& k) {
+    i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= g.nx) return false;
+    const int r = (int)blockIdx.y;
+    if (r < 2 * g.nz) {
+        j = (r & 1) ? g.ny - 1 : 0;
+        k = r >> 1;
+    } else {
+        const int s = r - 2 * g.nz;
+        k = (s & 1) ? g.nz - 1 : 0;
+        j = 1 + (s >> 1);
+    }
+    c = (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
+    return true;
+}
+#endif
+// The row launches need interior rows: ny >= 3 and, in 3D, nz >= 3.
+__host__ __device__ __forceinline__ bool row_launch_supported(const Geo& g) {
+    return g.ny >= 3 && (g.nz == 1 || g.nz >= 3);
+}
+
 // Pulls of a cell whose row is interior (0 < j < ny-1 and, in 3D, 0 < k < nz-1): only the x
 // axis can take a source outside the lattice, at i = 0 or nx-1.  The rule is pull_flow's /
 // pull_thermal's for that case, written with selects so that every lane of a warp runs the

@@ -123,6 +123,66 @@ static void pair_launch(const Geo& g, dim3& grid, dim3& block) {
     grid = dim3((pairs + bx - 1) / bx, (g.ny + by - 1) / by, g.nz);
 }
 
+// Row form of the two kernels (option LBM_OPT_ROWS): interior rows with the select-based x
+// rule (flow_cell_row / thermal_cell_row), face rows with the full boundary rule; no
+// division of a cell index, and no per-cell choice between a fixed-offset and a boundary
+// path.  Same values as the one-cell kernels bit for bit.
+template <int D, class S>
+__global__ void __launch_bounds__(128, (OneCellBlocks<S, false>::value)) k_fast_flow_rows(Geo g, PhysF P, FastArgs<S> A,
+                                                                                         const S* __restrict__ fin,
+                                                                                         const S* __restrict__ gin,
+                                                                                         S* __restrict__ fout) {
+    long long c;
+    int i, j, k;
+    if (!row_interior_cell(g, c, i, j, k)) return;
+    flow_cell_row<D, S>(g, P, A, fin, gin, fout, c, i);
+}
+
+template <int D, class S>
+__global__ void __launch_bounds__(128, (OneCellBlocks<S, true>::value)) k_fast_thermal_rows(Geo g, PhysF P, FastArgs<S> A,
+                                                                                           const S* __restrict__ fin,
+                                                                                           const S* __restrict__ gin,
+                                                                                           S* __restrict__ gout) {
+    long long c;
+    int i, j, k;
+    if (!row_interior_cell(g, c, i, j, k)) return;
+    thermal_cell_row<D, S>(g, P, A, fin, gin, gout, c, i);
+}
+
+template <int D, class S>
+__global__ void __launch_bounds__(128) k_fast_flow_facerows(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
+                                                            const S* __restrict__ gin, S* __restrict__ fout) {
+    long long c;
+    int i, j, k;
+    if (!row_face_cell(g, c, i, j, k)) return;
+    flow_cell_2k<D, false, S, false>(g, P, A, fin, gin, fout, c, i, j, k);
+}
+
+template <int D, class S>
+__global__ void __launch_bounds__(128) k_fast_thermal_facerows(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
+                                                               const S* __restrict__ gin, S* __restrict__ gout) {
+    long long c;
+    int i, j, k;
+    if (!row_face_cell(g, c, i, j, k)) return;
+    thermal_cell_2k<D, false, S, false>(g, P, A, fin, gin, gout, c, i, j, k);
+}
+
+template <int D, class S>
+static void rows_step(const Geo& g, const PhysF& pf, const FastArgs<S>& Af, const FastArgs<S>& At, const S* fin,
+                      const S* gin, S* fout, S* gout, cudaStream_t s, bool fl, bool th) {
+    const unsigned bx = (unsigned)((g.nx + 127) / 128);
+    const dim3 gin_grid(bx, (unsigned)(g.ny - 2), D == 3 ? (unsigned)(g.nz - 2) : 1u);
+    const dim3 gface(bx, (unsigned)face_row_count(g), 1u);
+    if (fl) {
+        k_fast_flow_rows<D, S><<<gin_grid, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
+        k_fast_flow_facerows<D, S><<<gface, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
+    }
+    if (th) {
+        k_fast_thermal_rows<D, S><<<gin_grid, 128, 0, s>>>(g, pf, At, fout, gin, gout);
+        k_fast_thermal_facerows<D, S><<<gface, 128, 0, s>>>(g, pf, At, fout, gin, gout);
+    }
+}
+
 // Module arrays of step N from F[cur] = f_post_N, G[cur] = g_post_N, L[cur] (lag_in).
 template <int D, class S>
 __global__ void k_fast_materialize(Geo g, PhysF P, FastArgs<S> A, const S* __restrict__ fin,
@@ -327,6 +387,7 @@ void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first,
     }
     const unsigned blocks = nb(g.ncell, 128);
     const bool paired = F.pairs && g.nx % 2 == 0;
+    const bool rows = F.rows && !paired && row_launch_supported(g);
     dim3 pgrid, pblock;
     pair_launch(g, pgrid, pblock);
     F.ahead = false;
@@ -347,6 +408,8 @@ void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first,
             } else if (paired) {
                 if (fl) k_fast_flow_pair<2, S><<<pgrid, pblock, 0, s>>>(g, pf, Af, fin, gin, fout);
                 if (th) k_fast_thermal_pair<2, S><<<pgrid, pblock, 0, s>>>(g, pf, At, fout, gin, gout);
+            } else if (rows) {
+                rows_step<2, S>(g, pf, Af, At, fin, gin, fout, gout, s, fl, th);
             } else {
                 if (fl) k_fast_flow<2, false, S><<<blocks, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
                 if (th) k_fast_thermal<2, false, S><<<blocks, 128, 0, s>>>(g, pf, At, fout, gin, gout);
@@ -358,6 +421,8 @@ void fast_step(FastState& F, const Geo& g0, const PhysC& P, int dim, bool first,
             } else if (paired) {
                 if (fl) k_fast_flow_pair<3, S><<<pgrid, pblock, 0, s>>>(g, pf, Af, fin, gin, fout);
                 if (th) k_fast_thermal_pair<3, S><<<pgrid, pblock, 0, s>>>(g, pf, At, fout, gin, gout);
+            } else if (rows) {
+                rows_step<3, S>(g, pf, Af, At, fin, gin, fout, gout, s, fl, th);
             } else {
                 if (fl) k_fast_flow<3, false, S><<<blocks, 128, 0, s>>>(g, pf, Af, fin, gin, fout);
                 if (th) k_fast_thermal<3, false, S><<<blocks, 128, 0, s>>>(g, pf, At, fout, gin, gout);

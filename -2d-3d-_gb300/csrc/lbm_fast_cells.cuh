@@ -147,4 +147,87 @@ __device__ __forceinline__ void thermal_cell_2k(const Geo& g, const PhysF& P, co
     for (int a = 0; a < QT; ++a) gout[a * n + c] = hs[a];
 }
 
+// The steady-state bodies above for a cell of an interior row (0 < j < ny-1 and, in 3D,
+// 0 < k < nz-1): only the x axis can take a pull source outside the lattice, which the row
+// pulls resolve with selects (pull_flow_xrow / pull_thermal_xrow: the same sources and
+// rules), so a warp runs one instruction stream whatever its lanes' x positions.  The
+// arithmetic after the pulls is flow_cell_2k's / thermal_cell_2k's, statement for
+// statement.
+template <int D, class S>
+__device__ __forceinline__ void flow_cell_row(const Geo& g, const PhysF& P, const FastArgs<S>& A,
+                                              const S* __restrict__ fin, const S* __restrict__ gin,
+                                              S* __restrict__ fout, long long c, int i) {
+    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
+    const long long n = g.ncell;
+    auto lf = [&](int a, long long cc) { return ldS(fin, a * n + cc); };
+    auto lg = [&](int a, long long cc) { return ldS(gin, a * n + cc); };
+    float d[Q], dp[Q], dr, rho, u, v, w = 0.0f, T;
+    {
+        float ts = 0.0f;
+#pragma unroll
+        for (int a = 0; a < Q; ++a) d[a] = pull_flow_xrow<Q, float>(g, a, i, c, lf);
+#pragma unroll
+        for (int a = 0; a < QT; ++a) ts += pull_thermal_xrow<QT, float>(g, a, i, c, lg);
+        T = ts + P.Tref;
+        float Fy;
+        fmacro<D>(d, A.lag_in[c], P, dr, rho, u, v, w, Fy);
+    }
+    const float Fy = rho * P.gBeta * (T - P.Tref);
+    if (D == 2) {
+        A.lag_out[c] = Fy;
+        fcollide_2d(d, dr, rho, u, v, Fy, P, dp);
+    } else {
+        fcollide_3d(d, dr, rho, u, v, w, Fy, P, dp);
+    }
+    S hs[Q];
+    round_cell<Q>(dp, hs, P.sr != 0, sr_seed(*A.tick, c, 0));
+#pragma unroll
+    for (int a = 0; a < Q; ++a) fout[a * n + c] = hs[a];
+}
+
+template <int D, class S>
+__device__ __forceinline__ void thermal_cell_row(const Geo& g, const PhysF& P, const FastArgs<S>& A,
+                                                 const S* __restrict__ fin, const S* __restrict__ gin,
+                                                 S* __restrict__ gout, long long c, int i) {
+    constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
+    const long long n = g.ncell;
+    auto lf = [&](int a, long long cc) { return ldS(fin, a * n + cc); };
+    auto lg = [&](int a, long long cc) { return ldS(gin, a * n + cc); };
+    float d[Q], G[QT], GP[QT];
+#pragma unroll
+    for (int a = 0; a < Q; ++a) d[a] = pull_flow_xrow<Q, float>(g, a, i, c, lf);
+    float Tprev;
+    {
+        float ts = 0.0f;
+#pragma unroll
+        for (int a = 0; a < QT; ++a) {
+            G[a] = pull_thermal_xrow<QT, float>(g, a, i, c, lg) + wT<QT>(P, a) * P.Tref;
+            ts += G[a];
+        }
+        Tprev = ts;
+    }
+    float dr, rho, u, v, w, Fy;
+    fmacro<D>(d, D == 2 ? A.lag_in[c] : Tprev, P, dr, rho, u, v, w, Fy);
+    if (D == 2) {
+        float Bx = A.Bin0[c], By = A.Bin1[c];
+        fcollideT_2d(G, u, v, Tprev, Bx, By, P, GP);
+        A.Bout0[c] = Bx;
+        A.Bout1[c] = By;
+    } else {
+        float Bx = A.Bin0[c], By = A.Bin1[c], Bz = A.Bin2[c];
+        fcollideT_3d(G, u, v, w, Tprev, Bx, By, Bz, P, GP);
+        A.Bout0[c] = Bx;
+        A.Bout1[c] = By;
+        A.Bout2[c] = Bz;
+        A.lag_out[c] = Tprev;
+    }
+    float ev[QT];
+    S hs[QT];
+#pragma unroll
+    for (int a = 0; a < QT; ++a) ev[a] = GP[a] - wT<QT>(P, a) * P.Tref;
+    round_cell<QT>(ev, hs, P.sr != 0, sr_seed(*A.tick, c, 1));
+#pragma unroll
+    for (int a = 0; a < QT; ++a) gout[a * n + c] = hs[a];
+}
+
 }  // namespace lbm

@@ -45,47 +45,15 @@ __global__ void __launch_bounds__(128) k_xthermal(Geo g, PhysX X, FixedArrays A,
     thermal_cell<D, FIRST>(g, X, A, fin, gin, gout, c, i, j, k);
 }
 
-// Cells of interior rows (0 < j < ny-1, and 0 < k < nz-1 in 3D) in the steady-state step:
-// block (bx, j, k) holds cells i = bx*128 + t of the row, so warps start at row starts (rows
-// are 2 KB-aligned when nx is a multiple of 32) and every access of a warp is one contiguous
-// run.  Only x can take a pull source outside the lattice there, which the row pulls handle
-// with selects; the face kernels take the y- and z-face rows.
-__device__ __forceinline__ bool fixed_interior_cell(const Geo& g, long long& c, int& i, int& j, int& k) {
-    i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    j = (int)blockIdx.y + 1;
-    k = g.nz > 1 ? (int)blockIdx.z + 1 : 0;
-    if (i >= g.nx) return false;
-    c = (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
-    return true;
-}
-
-// Face rows: the y faces (j = 0, ny-1; every k), then in 3D the z faces (k = 0, nz-1;
-// 0 < j < ny-1); block (bx, r) holds cells i = bx*128 + t of face row r.
-__host__ __device__ __forceinline__ long long fixed_face_rows(const Geo& g) {
-    return 2LL * g.nz + (g.nz > 1 ? 2LL * (g.ny - 2) : 0LL);
-}
-__device__ __forceinline__ bool fixed_face_cell(const Geo& g, long long& c, int& i, int& j, int& k) {
-    i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (i >= g.nx) return false;
-    const int r = (int)blockIdx.y;
-    if (r < 2 * g.nz) {
-        j = (r & 1) ? g.ny - 1 : 0;
-        k = r >> 1;
-    } else {
-        const int s = r - 2 * g.nz;
-        k = (s & 1) ? g.nz - 1 : 0;
-        j = 1 + (s >> 1);
-    }
-    c = (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * (long long)k);
-    return true;
-}
-
+// Interior rows and face rows of the steady-state step: row_interior_cell and
+// row_face_cell (lbm_device.cuh).  Interior rows pull with selects for the x faces; the face
+// kernels take the y- and z-face rows with the full boundary rule.
 template <int D>
 __global__ void __launch_bounds__(128, LBM_XFLOW_MIN_BLOCKS) k_xflow_in(Geo g, PhysX X, FixedArrays A, const long long* __restrict__ fin,
                                                      const long long* __restrict__ gin, long long* __restrict__ fout) {
     long long c;
     int i, j, k;
-    if (!fixed_interior_cell(g, c, i, j, k)) return;
+    if (!row_interior_cell(g, c, i, j, k)) return;
     flow_cell<D, false, 3>(g, X, A, fin, gin, fout, c, i, j, k);
 }
 
@@ -94,7 +62,7 @@ __global__ void __launch_bounds__(128) k_xflow_face(Geo g, PhysX X, FixedArrays 
                                                     const long long* __restrict__ gin, long long* __restrict__ fout) {
     long long c;
     int i, j, k;
-    if (!fixed_face_cell(g, c, i, j, k)) return;
+    if (!row_face_cell(g, c, i, j, k)) return;
     flow_cell<D, false, 2>(g, X, A, fin, gin, fout, c, i, j, k);
 }
 
@@ -104,7 +72,7 @@ __global__ void __launch_bounds__(128, 6) k_xthermal_in(Geo g, PhysX X, FixedArr
                                                         const long long* __restrict__ gin, long long* __restrict__ gout) {
     long long c;
     int i, j, k;
-    if (!fixed_interior_cell(g, c, i, j, k)) return;
+    if (!row_interior_cell(g, c, i, j, k)) return;
     thermal_cell<D, false, 3>(g, X, A, fin, gin, gout, c, i, j, k);
 }
 
@@ -114,7 +82,7 @@ __global__ void __launch_bounds__(128) k_xthermal_face(Geo g, PhysX X, FixedArra
                                                        const long long* __restrict__ gin, long long* __restrict__ gout) {
     long long c;
     int i, j, k;
-    if (!fixed_face_cell(g, c, i, j, k)) return;
+    if (!row_face_cell(g, c, i, j, k)) return;
     thermal_cell<D, false, 2>(g, X, A, fin, gin, gout, c, i, j, k);
 }
 
@@ -369,13 +337,15 @@ static void steady_step(const Geo& g, const PhysX& X, const FixedArrays& A, cons
                         const long long* gprev, long long* fnext, long long* gnext, cudaStream_t s, bool fl, bool th) {
     const unsigned bx = (unsigned)((g.nx + 127) / 128);
     const dim3 bin(128), gin_grid(bx, (unsigned)(g.ny - 2), D == 3 ? (unsigned)(g.nz - 2) : 1u);
-    const dim3 gface(bx, (unsigned)fixed_face_rows(g), 1u);
+    const dim3 gface(bx, (unsigned)face_row_count(g), 1u);
+    // a 3D lattice of two planes has no interior rows: the face rows hold every cell
+    const bool interior = D == 2 || g.nz > 2;
     if (fl) {
-        k_xflow_in<D><<<gin_grid, bin, 0, s>>>(g, X, A, fprev, gprev, fnext);
+        if (interior) k_xflow_in<D><<<gin_grid, bin, 0, s>>>(g, X, A, fprev, gprev, fnext);
         k_xflow_face<D><<<gface, bin, 0, s>>>(g, X, A, fprev, gprev, fnext);
     }
     if (th) {
-        k_xthermal_in<D><<<gin_grid, bin, 0, s>>>(g, X, A, fnext, gprev, gnext);
+        if (interior) k_xthermal_in<D><<<gin_grid, bin, 0, s>>>(g, X, A, fnext, gprev, gnext);
         k_xthermal_face<D><<<gface, bin, 0, s>>>(g, X, A, fnext, gprev, gnext);
     }
 }

@@ -43,6 +43,7 @@ module lbm_gpu_mod
   integer(c_int), parameter :: LBM_OPT_SINGLE_KERNEL = 1, LBM_OPT_KCHUNK = 2, LBM_OPT_PAIRS = 3, LBM_OPT_STAGED = 4
   integer(c_int), parameter :: LBM_OPT_FP16_ROUNDING = 5   ! 1 stochastic (default), 0 nearest
   integer(c_int), parameter :: LBM_OPT_HOST_DIRECT = 6     ! state transfer on host arrays directly
+  integer(c_int), parameter :: LBM_OPT_ROWS = 7            ! FP32/FP16: interior-row and face-row launches
 
   type, bind(C) :: lbm_params
     integer(c_int32_t) :: dim, nx, ny, nz

@@ -288,6 +288,11 @@ int lbm_footprint(const lbm_params* p, size_t* bytes);
  *   or stage them through a device buffer with a copy (0).  Same values either way; the host
  *   array must stay valid until the call returns (the calls synchronise). */
 #define LBM_OPT_HOST_DIRECT   6
+/* LBM_OPT_ROWS: FP32/FP16 two-buffer steps launch interior rows (only x can leave the
+ *   lattice there: the x rule by selects, no cell-index division) and face rows (the full
+ *   boundary rule) as separate kernels (1), or one cell per thread in lattice order (0).  Two
+ *   cells per thread, where chosen, takes precedence.  Same values either way. */
+#define LBM_OPT_ROWS          7
 int lbm_set_option(lbm_handle* h, int option, int value);
 
 /* ---- measurement hooks (no counterpart in the reference, which times its loop with

@@ -74,6 +74,8 @@ def cases():
         "rb3d_noslip": rb_params(dim=3, nx=10, ny=9, nz=8, Ra=1e6, noise_amp=1e-3, seed=5),
         "rb3d_periodic_legacy": legacy,
         "side3d": side,
+        # two planes in z: no interior rows, the face-row kernels hold every cell
+        "rb3d_two_planes": rb_params(dim=3, nx=12, ny=8, nz=2, Ra=1e5, noise_amp=1e-3, seed=9),
     }
 
 

@@ -1,11 +1,12 @@
 """The paired two-kernel FP32/FP16 step (two x-adjacent cells per thread, 2-cell vector
-loads and stores) against the one-cell-per-thread step: the same values, bit for bit, on
-lattices with every boundary kind on the x faces (the faces where a pair is split into a
+loads and stores) and the row form (interior rows with select-based x pulls, face rows with
+the full boundary rule) against the one-cell-per-thread step: the same values, bit for bit,
+on lattices with every boundary kind on the x faces (the faces where a pair is split into a
 vector part and a scalar boundary part), and the fallback for odd nx."""
 import numpy as np
 import pytest
 
-from lbmgpu import LBM_OPT_PAIRS, Lattice
+from lbmgpu import LBM_OPT_PAIRS, LBM_OPT_ROWS, Lattice
 from lbmgpu.abi import LBM_BC_PERIODIC, LBM_BCT_CONST, LBM_BCT_PERIODIC, LBM_CELL_SIDE, rb_params
 
 pytestmark = pytest.mark.gpu
@@ -45,3 +46,21 @@ def test_paired_equals_one_cell(name, precision):
     for field in ("f", "g", "T", "u", "v", "Bx_prev", "By_prev"):
         x, y = a.get_state(field), b.get_state(field)
         assert np.array_equal(x, y), (name, precision, field, float(np.abs(x - y).max()))
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+@pytest.mark.parametrize("name", sorted(cases()))
+def test_rows_equal_one_cell(name, precision):
+    p = cases()[name].copy()
+    p.precision = {"fp32": 1, "fp16": 2}[precision]
+    a, b = Lattice(p), Lattice(p)
+    for lat, rows in ((a, 1), (b, 0)):
+        lat.set_option(LBM_OPT_PAIRS, 0)
+        lat.set_option(LBM_OPT_ROWS, rows)
+        lat.initial()
+        lat.step(70)  # first step, single steps and two graph chunks
+    for field in ("f", "g", "T", "u", "v", "Bx_prev", "By_prev"):
+        x, y = a.get_state(field), b.get_state(field)
+        assert np.array_equal(x, y), (name, precision, field, float(np.abs(x - y).max()))
+    a.close()
+    b.close()
