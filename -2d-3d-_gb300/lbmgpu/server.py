@@ -154,6 +154,7 @@ class SolveServer:
         self.results = []
         self.peak_active = 0
         self.peak_queue = 0
+        self.cell_steps = 0  # cell updates advanced by the ensemble, finished solves or not
 
     def _reject(self, req, now, why):
         self.results.append(Result(req.rid, float("nan"), float("nan"), 0, False, req.arrival, now, now, req.cells,
@@ -259,6 +260,7 @@ class SolveServer:
             if self.autotune and not tuned and len(self.active) > 1:
                 self.ens.autotune(2)
                 tuned = True
+            self.cell_steps += self.chunk * sum(a[0].cells for a in self.active.values())
             self.ens.step(self.chunk)
             self.ens.sync()
             self._check(clock() - t0)
@@ -272,7 +274,9 @@ class SolveServer:
         self.ens.close()
 
 
-def summarize(results, wall_seconds):
+def summarize(results, wall_seconds, cell_steps=None):
+    """cell_steps: every cell update the server advanced (SolveServer.cell_steps), including
+    solves still running at a time limit; without it the aggregate counts finished solves."""
     ran = [r for r in results if r.steps > 0]
     conv = [r for r in ran if r.converged]
     tts = sorted(r.time_to_solution for r in conv)
@@ -284,7 +288,7 @@ def summarize(results, wall_seconds):
         return xs[k]
 
     tts_all = sorted(r.time_to_solution for r in ran)
-    cells_steps = sum(r.cells * r.steps for r in ran)
+    cells_steps = cell_steps if cell_steps is not None else sum(r.cells * r.steps for r in ran)
     return {
         "completed": len(ran),
         "converged": len(conv),

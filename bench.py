@@ -468,7 +468,7 @@ def served_run(args, local):
     wall = time.perf_counter() - t0
     finished = {r.rid for r in results}
     unfinished = len(reqs) - len(finished)
-    summary = srv.summarize(results, wall)
+    summary = srv.summarize(results, wall, s.cell_steps)
     peak = (s.peak_active, s.peak_queue)
     s.close()
     by_id = {r.rid: r for r in reqs}

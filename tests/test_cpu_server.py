@@ -131,6 +131,18 @@ def test_cap_and_summary():
     assert s["completed_solves_per_hour"] == 2.0
 
 
+def test_cell_steps_count_unfinished_solves():
+    # a solve that never settles is cut off by the time limit: its steps still count
+    ticks = iter(range(1000))
+    srv, _ = make_server(budget=100, chunk_steps=500, window=1000, max_steps=50000, osc={0: 1.0})
+    results = srv.run([req(0, 10)], time_limit=5.5, clock=lambda: float(next(ticks)), sleep=lambda t: None)
+    assert results == [] and srv.cell_steps > 0
+    cells = req(0, 10).cells
+    assert srv.cell_steps % (500 * cells) == 0
+    s = summarize(results, 10.0, srv.cell_steps)
+    assert s["aggregate_mlups"] == srv.cell_steps / 10.0 / 1e6
+
+
 def test_oversized_and_foreign_precision_requests_are_rejected():
     srv, _ = make_server(budget=50, chunk_steps=500, window=1000, max_steps=2000)
     other = req(2, 10)
