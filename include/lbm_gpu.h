@@ -281,12 +281,13 @@ int lbm_footprint(const lbm_params* p, size_t* bytes);
 #define LBM_OPT_PAIRS         3
 #define LBM_OPT_STAGED        4
 #define LBM_OPT_FP16_ROUNDING 5 /* FP16 storage: 1 stochastic rounding (default), 0 nearest */
-/* LBM_OPT_HOST_DIRECT: lbm_get_state / lbm_set_state of an FP64 handle move the caller's host
- *   array straight to and from the device arrays with the layout kernels reading and writing
- *   the host memory coherently (1; the default where the device reports
- *   cudaDevAttrPageableMemoryAccess, as a GPU attached to a Grace CPU over NVLink-C2C does),
- *   or stage them through a device buffer with a copy (0).  Same values either way; the host
- *   array must stay valid until the call returns (the calls synchronise). */
+/* LBM_OPT_HOST_DIRECT: state transfer of an FP64 handle with the layout kernels reading
+ *   (bit 0: lbm_set_state) and writing (bit 1: lbm_get_state) the caller's host array
+ *   coherently, where the device reports cudaDevAttrPageableMemoryAccess (a GPU attached to a
+ *   Grace CPU over NVLink-C2C), instead of staging it through a device buffer with a copy.
+ *   Default 1 there (reads; 0 elsewhere): writes into host memory not yet touched fault its
+ *   pages in from the GPU side and run slower than a staged copy.  Same values either way;
+ *   the host array must stay valid until the call returns (the calls synchronise). */
 #define LBM_OPT_HOST_DIRECT   6
 /* LBM_OPT_ROWS: FP32/FP16 two-buffer steps launch interior rows (only x can leave the
  *   lattice there: the x rule by selects, no cell-index division) and face rows (the full

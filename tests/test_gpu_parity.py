@@ -260,7 +260,7 @@ def test_state_transfer_direct_and_staged_agree(dim):
     g.step(30)
     names = ["f", "g", "T", "u", "rho"]
     try:
-        g.set_option(LBM_OPT_HOST_DIRECT, 1)
+        g.set_option(LBM_OPT_HOST_DIRECT, 3)  # reads and writes
     except LbmError:
         pytest.skip("the device cannot access pageable host memory")
     direct = {k: g.get_state(k) for k in names}
@@ -276,4 +276,7 @@ def test_state_transfer_direct_and_staged_agree(dim):
         g.set_state(k, x)
         g.set_option(LBM_OPT_HOST_DIRECT, 0)
         assert np.array_equal(g.get_state(k), x), k
+        g.set_state(k, staged[k])
+        g.set_option(LBM_OPT_HOST_DIRECT, 2)  # writes direct, reads staged
+        assert np.array_equal(g.get_state(k), staged[k]), k
     g.close()
