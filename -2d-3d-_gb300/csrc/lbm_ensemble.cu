@@ -35,10 +35,13 @@ struct EnsMember {
 // With the member descriptor and buffer arguments staged in shared memory the one-cell
 // kernels take 66-80 registers, against 96-128 with register copies of the descriptor
 // (the 3D thermal kernel took 242 without a bound), and none spills.
+#ifndef LBM_ENS_PAIR2D_BLOCKS
+#define LBM_ENS_PAIR2D_BLOCKS 3
+#endif
 template <int D>
 constexpr bool kEnsInner = true;
 template <int D, bool PAIR>
-constexpr int kEnsBlocks = (D == 3 && PAIR) ? 2 : 3;
+constexpr int kEnsBlocks = (D == 3 && PAIR) ? 2 : (D == 2 && PAIR) ? LBM_ENS_PAIR2D_BLOCKS : 3;
 
 // Cell coordinates of a thread's cells in a tile, stepped instead of divided: one division
 // at the thread's first cell, then (i, j, k) advance by `stride` cells with carries (i by

@@ -36,7 +36,6 @@ struct FusedArgs {
     S* gout;         // g_post_n       (G[cur^1])
     float *Bout0, *Bout1, *Bout2;
     float* lag_out;  // 3D: T_{n-1} -> L[cur^1]; 2D: F_y,n+1 -> L[cur]
-    float bc_lo[3], bc_hi[3];  // anti-bounce-back terms for full g (2 wT Tw)
     const unsigned long long* tick;  // step counter n: g_post_n rounds with n, f_post_{n+1} with n+1
 };
 
@@ -45,8 +44,14 @@ struct Tile;
 template <> struct Tile<3> { static constexpr int TX = 32, TY = 8, MINB = 2; };
 template <> struct Tile<2> { static constexpr int TX = 32, TY = 4, MINB = 4; };
 
-// Thermal stage at one cell: pulls, macro, thermal collision.  Returns g_post_n (full g)
-// and, through the references, the flow state f_n (deviations), rho_n, u_n.
+// A stored population as a pull reads it back (ldS).
+__device__ __forceinline__ float stored_value(float h) { return h; }
+__device__ __forceinline__ float stored_value(__half h) { return __half2float(h); }
+
+// Thermal stage at one cell: pulls, macro, thermal collision.  Returns g_post_n as the
+// next pull reads it (the stored deviations, rounded to the storage type and back; halo
+// cells round with the owner's random bits, so they hold the owner's values) and, through
+// the references, the flow state f_n (deviations), rho_n, u_n.
 template <int D, class S>
 __device__ __forceinline__ void thermal_cell(const Geo& g, const PhysF& P, const FusedArgs<S>& A, int x, int y, int z,
                                              bool owner, float* d, float& dr, float& rho, float& u, float& v, float& w,
@@ -83,14 +88,15 @@ __device__ __forceinline__ void thermal_cell(const Geo& g, const PhysF& P, const
             A.lag_out[c] = Tprev;
         }
     }
-    if (owner) {
-        float ev[QT];
-        S hs[QT];
+    float ev[QT];
+    S hs[QT];
 #pragma unroll
-        for (int a = 0; a < QT; ++a) ev[a] = GP[a] - wT<QT>(P, a) * P.Tref;
-        round_cell<QT>(ev, hs, P.sr != 0, sr_seed(*A.tick, c, 1));
+    for (int a = 0; a < QT; ++a) ev[a] = GP[a] - wT<QT>(P, a) * P.Tref;
+    round_cell<QT>(ev, hs, P.sr != 0, sr_seed(*A.tick, c, 1));
 #pragma unroll
-        for (int a = 0; a < QT; ++a) A.gout[a * n + c] = hs[a];
+    for (int a = 0; a < QT; ++a) {
+        if (owner) A.gout[a * n + c] = hs[a];
+        GP[a] = stored_value(hs[a]);
     }
 }
 
@@ -137,8 +143,10 @@ __device__ __forceinline__ void thermal_plane(const Geo& g, const PhysF& P, cons
 }
 
 // Flow stage of the own cell on plane k: f_n pulled again (the thermal stage loaded the
-// same lines one plane earlier), T_n summed from the ring with the thermal wall rules,
-// then the MRT collision.  m = (dr, rho, u, v, w) of the cell from the thermal stage.
+// same lines one plane earlier), T_n summed from the ring's stored deviations with the
+// thermal wall rules in pull_thermal's order and form (so T_n equals the two-kernel
+// step's bit for bit), then the MRT collision.  m = (dr, rho, u, v, w) of the cell from the
+// thermal stage, whose macro step takes the same pulled f and the same lagged T.
 template <int D, class S, int HX, int HY>
 __device__ __forceinline__ void flow_cell(const Geo& g, const PhysF& P, const FusedArgs<S>& A, const Place& pl,
                                           const float* s_prev, const float* s_cur, const float* s_next, int k,
@@ -148,7 +156,7 @@ __device__ __forceinline__ void flow_cell(const Geo& g, const PhysF& P, const Fu
     const long long n = g.ncell;
     const int x = pl.x, y = pl.y, lx = pl.tx + 1, ly = pl.ty + 1;
     const long long c = cell_index(g, x, y, k);
-    float Tn = 0.0f;
+    float ts = 0.0f;
 #pragma unroll
     for (int a = 0; a < QT; ++a) {
         const int ex = Lat<QT>::ex(a), ey = Lat<QT>::ey(a), ez = Lat<QT>::ez(a);
@@ -157,15 +165,16 @@ __device__ __forceinline__ void flow_cell(const Geo& g, const PhysF& P, const Fu
         if (ex != 0 && !pl.perx && (x - ex < 0 || x - ex >= g.nx)) { axis = 0; low = x - ex < 0; }
         if (ey != 0 && !pl.pery && (y - ey < 0 || y - ey >= g.ny)) { axis = 1; low = y - ey < 0; }
         if (ez != 0 && !pl.perz && (k - ez < 0 || k - ez >= g.nz)) { axis = 2; low = k - ez < 0; }
-        if (axis < 0) {
+        if (a == 0 || axis < 0) {
             const float* sl = ez > 0 ? s_prev : (ez < 0 ? s_next : s_cur);
-            Tn += sl[(a * HY + ly - ey) * HX + lx - ex];
+            ts += sl[(a * HY + ly - ey) * HX + lx - ex];
         } else {
-            const float gopp = s_cur[(Lat<QT>::opp(a) * HY + ly) * HX + lx];
-            Tn += (pick3(g.bct, axis) == LBM_BCT_CONST) ? (-gopp + (low ? pick3(A.bc_lo, axis) : pick3(A.bc_hi, axis)))
-                                                         : gopp;
+            const float eopp = s_cur[(Lat<QT>::opp(a) * HY + ly) * HX + lx];
+            ts += (pick3(g.bct, axis) == LBM_BCT_CONST) ? (-eopp + (float)(low ? pick3(g.bcT_lo, axis) : pick3(g.bcT_hi, axis)))
+                                                         : eopp;
         }
     }
+    const float Tn = ts + P.Tref;  // sum of deviations + Tref * sum(wT)
     float d[Q], dp[Q];
     auto lf = [&](int a, long long cc) { return ldS(A.fin, a * n + cc); };
 #pragma unroll
@@ -270,10 +279,6 @@ void fast_fused_step(FastState& F, const Geo& g0, const PhysC& P, int dim, cudaS
         } else {
             A.lag_in = nullptr;
             A.lag_out = F.L[c ^ 1];
-        }
-        for (int a = 0; a < 3; ++a) {
-            A.bc_lo[a] = (float)g0.bcT_lo[a];
-            A.bc_hi[a] = (float)g0.bcT_hi[a];
         }
         if (dim == 3) {
             const int kc = F.kchunk > 0 ? F.kchunk : 16;
