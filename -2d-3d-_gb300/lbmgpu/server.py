@@ -2,7 +2,9 @@
 
 Requests (a Rayleigh-Benard solve each: 2D or 3D, size, Ra, Pr, seed) arrive over time.
 The server keeps every admitted lattice resident in HBM and advances all of them together
-with one flow and one thermal launch per step (lbm_ensemble_step).  Requests that arrive
+with one flow and one thermal launch per step (lbm_ensemble_step) in FP32/FP16 storage, or,
+for solves at FP64 accuracy (the fixed arithmetic, "fp64x", or the plain method, "fp64"),
+each with its own lbm_step on its own stream so that their launches overlap.  Requests that arrive
 while others run are admitted as soon as their device footprint (lbm_footprint) fits under
 the HBM budget, and join the running batch at the next chunk boundary.
 
@@ -111,10 +113,44 @@ def windowed_steady(history, window, rel_tol):
     return abs(m1 - m0) <= rel_tol * abs(m0)
 
 
+class StreamBatch:
+    """The ensemble interface for storage forms the batched kernels do not take (FP64: the
+    plain method and the fixed arithmetic): every member advances with its own lbm_step on
+    its own CUDA stream, so the members' launches overlap on the GPU.  A chunk is one
+    lbm_step(n) per member, enqueued without waiting; sync waits for all of them."""
+
+    def __init__(self):
+        self.members = []
+
+    def add(self, lat):
+        self.members.append(lat)
+
+    def remove(self, lat):
+        self.members.remove(lat)
+
+    def step(self, n):
+        for lat in self.members:
+            lat.step(n)
+
+    def sync(self):
+        for lat in self.members:
+            lat.sync()
+
+    def autotune(self, nsteps):
+        pass
+
+    def close(self):
+        self.members = []
+
+
+BATCHED_PRECISIONS = ("fp32", "fp16")
+
+
 class SolveServer:
     """lattice_factory(params) -> a Lattice-like object (initial, calNuRe, itc, close);
     ensemble: an Ensemble-like object (add, remove, step, sync, autotune, close);
-    footprint_fn(params) -> bytes.  The defaults are the library's own; tests pass fakes."""
+    footprint_fn(params) -> bytes.  The defaults are the library's own (the batched form for
+    FP32/FP16, a StreamBatch for the FP64 forms "fp64" and "fp64x"); tests pass fakes."""
 
     def __init__(self, device=0, hbm_budget_bytes=None, budget_fraction=0.8, chunk_steps=500, window=5000,
                  rel_tol=1e-3, max_steps=50000, autotune=False, max_bypass=8, precision="fp32",
@@ -129,7 +165,8 @@ class SolveServer:
         if lattice_factory is None or ensemble is None or footprint_fn is None:
             from . import Ensemble, Lattice, footprint
             lattice_factory = lattice_factory or (lambda p: Lattice(p, device=device))
-            ensemble = ensemble if ensemble is not None else Ensemble(device)
+            if ensemble is None:
+                ensemble = Ensemble(device) if precision in BATCHED_PRECISIONS else StreamBatch()
             footprint_fn = footprint_fn or footprint
         self.make_lattice = lattice_factory
         self.ens = ensemble

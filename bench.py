@@ -445,15 +445,18 @@ def ensemble_run(args, local, steps_total=13000, every=500):
                                                          "LBM_ERR_DIVERGED"}}
 
 
-def served_run(args, local):
+def served_run(args, local, precision="fp32"):
     """Served form (BASELINE config 4): Poisson arrivals at 2/s, half 2D (ny 64..512, aspect 2)
-    half 3D (n 64..192), Ra log-uniform 1e4..1e8, Pr in {0.71, 7}, FP32, admission by an 80%
-    HBM budget, each solve run until its windowed-mean Nu changes by < 0.1% between
-    consecutive windows, or a step cap.  The default run is scaled to fit a bench (20 s of
-    arrivals, 1000-step window, 4000-step cap); --served-full runs the configuration as stated
-    (600 s, 5000-step window).  A seeded random sample of the served requests is then run one
-    at a time with the plain FP64 method and with the FP64-accuracy fixed arithmetic for the
-    same steps: their measured solves/h, and |dNu| of the windowed means."""
+    half 3D (n 64..192), Ra log-uniform 1e4..1e8, Pr in {0.71, 7}, admission by an 80% HBM
+    budget, each solve run until its windowed-mean Nu changes by < 0.1% between consecutive
+    windows, or a step cap.  FP32 storage runs as the batched form; FP64 accuracy ("fp64x",
+    the fixed arithmetic) runs each solve with its own lbm_step on its own stream.  The default
+    run is scaled to fit a bench (20 s of arrivals, 1000-step window, 4000-step cap);
+    --served-full runs the configuration as stated (600 s, 5000-step window).  A seeded random
+    sample of the served requests is then run one at a time with the plain FP64 method and
+    with the fixed arithmetic for the same steps: their measured solves/h, and |dNu| of the
+    windowed means (FP32 streams against the fixed arithmetic, the FP64-accuracy stream
+    against the plain method)."""
     import random
     import lbmgpu
     from lbmgpu import server as srv
@@ -461,8 +464,10 @@ def served_run(args, local):
     window, cap = args.served_window, args.served_cap
     chunk = 500
     reqs = srv.poisson_requests(2.0, duration)
+    for q in reqs:
+        q.precision = precision
     s = srv.SolveServer(device=local, chunk_steps=chunk, window=window, rel_tol=1e-3, max_steps=cap,
-                        autotune=False)
+                        autotune=False, precision=precision)
     t0 = time.perf_counter()
     results = s.run(reqs, time_limit=duration + drain)
     wall = time.perf_counter() - t0
@@ -490,24 +495,29 @@ def served_run(args, local):
         rec = {"rid": r.rid, "dim": q.dim, "n": q.n, "Ra": q.Ra, "Pr": q.Pr, "steps": r.steps,
                "converged": r.converged}
         last = [nu for st, nu in r.nu_history if st > r.steps - window]
-        rec["Nu_fp32_served"] = sum(last) / len(last) if last else None
+        rec["Nu_served"] = sum(last) / len(last) if last else None
         for prec in ("fp64x", "fp64"):
             t, h, div = run_sampled(q.params(prec), local, r.steps, chunk)
             plain[prec][0] += t
             plain[prec][1] += 1
             rec["s_" + prec] = t
-            if prec == "fp64x" and not div:
+            # the reference of the comparison: FP64 accuracy for reduced-precision streams,
+            # the plain FP64 method for the FP64-accuracy stream
+            if prec == ("fp64" if precision == "fp64x" else "fp64x") and not div:
                 rec["Nu_fp64"] = tail_mean(h, r.steps - window)
-        if rec.get("Nu_fp64") and rec["Nu_fp32_served"] is not None:
-            rec["rel_dNu"] = abs(rec["Nu_fp32_served"] - rec["Nu_fp64"]) / abs(rec["Nu_fp64"])
+        if rec.get("Nu_fp64") and rec["Nu_served"] is not None:
+            rec["rel_dNu"] = abs(rec["Nu_served"] - rec["Nu_fp64"]) / abs(rec["Nu_fp64"])
         dnu.append(rec)
     rel = sorted(x["rel_dNu"] for x in dnu if "rel_dNu" in x and x["converged"])
     rel_cap = sorted(x["rel_dNu"] for x in dnu if "rel_dNu" in x and not x["converged"])
     summary.update({
         "workload": "Poisson arrivals 2/s for %.0f s, 50/50 2D (ny 64..512, aspect 2) / 3D (n 64..192), Ra "
-                    "log-uniform 1e4..1e8, Pr {0.71,7}, FP32, 80%% HBM budget, stop when the %d-step windowed mean "
-                    "of Nu changes < 0.1%% or at %d steps; drain limit %.0f s%s" % (duration, window, cap, drain,
-                    "" if args.served_full else " (scaled from 600 s / 5000-step window)"),
+                    "log-uniform 1e4..1e8, Pr {0.71,7}, %s, 80%% HBM budget, stop when the %d-step windowed mean "
+                    "of Nu changes < 0.1%% or at %d steps; drain limit %.0f s%s" % (
+                        duration, {"fp32": "FP32 (batched)", "fp16": "FP16 (batched)",
+                                   "fp64x": "FP64 accuracy (fixed arithmetic, one stream per solve)"}.get(
+                            precision, precision), window, cap, drain,
+                        "" if args.served_full else " (scaled from 600 s / 5000-step window)"),
         "arrived": len(reqs), "unfinished_at_limit": unfinished, "wall_s": wall,
         "peak_active": peak[0], "peak_queue": peak[1],
         "one_at_a_time_sample": {
@@ -523,9 +533,10 @@ def served_run(args, local):
                         "capped_compared": len(rel_cap),
                         "capped_median": rel_cap[len(rel_cap) // 2] if rel_cap else None,
                         "solves": dnu,
-                        "how": "windowed mean of Nu over the solve's last window: served FP32 vs the same request "
-                               "alone at FP64 accuracy (fixed arithmetic) for the same steps; capped solves stopped "
-                               "inside a transient and are listed apart"},
+                        "how": ("windowed mean of Nu over the solve's last window: served %s vs the same request "
+                                "alone %s for the same steps; capped solves stopped inside a transient and are "
+                                "listed apart" % (precision, "with the plain FP64 method" if precision == "fp64x"
+                                                  else "at FP64 accuracy (fixed arithmetic)"))},
     })
     # throughput of the same sampled work: served aggregate cell updates/s against one at a time
     if plain["fp64"][0] and dnu:
@@ -810,7 +821,8 @@ def run_gpu(args):
     if rank == 0 and not args.no_ensemble:
         line["batched"] = ensemble_run(args, local)
     if rank == 0 and not args.no_served:
-        line["served"] = served_run(args, local)
+        for prec in args.served_precisions.split(","):
+            line["served" if prec == "fp32" else "served_" + prec] = served_run(args, local, prec)
     if rank == 0 and not args.no_size:
         line["at_384"] = at_size_run(args, local, peak)
     if rank == 0 and not args.no_config0:
@@ -835,6 +847,8 @@ def main():
     ap.add_argument("--no-size", action="store_true", help="skip the 384^3 leg (in-place vs two-buffer pattern)")
     ap.add_argument("--no-config0", action="store_true", help="skip the 2D 256 x 128 FP64 leg (20,000 steps)")
     ap.add_argument("--served-full", action="store_true", help="served leg as configured: 600 s, 5000-step window")
+    ap.add_argument("--served-precisions", default="fp32,fp64x",
+                    help="served legs: fp32 (batched form), fp64x (FP64 accuracy, one stream per solve)")
     ap.add_argument("--served-seconds", type=float, default=20.0)
     ap.add_argument("--served-drain", type=float, default=40.0)
     ap.add_argument("--served-window", type=int, default=1000)

@@ -156,3 +156,31 @@ def test_oversized_and_foreign_precision_requests_are_rejected():
 def test_step_cap_must_be_a_whole_number_of_chunks():
     with pytest.raises(ValueError):
         make_server(chunk_steps=500, window=1000, max_steps=1234)
+
+
+def test_stream_batch_steps_every_member():
+    """The FP64 forms' batch: each member advances with its own step call per chunk."""
+    from lbmgpu.server import StreamBatch
+
+    class Steppable(FakeLattice):
+        def step(self, n):
+            self.itc += n
+
+        def sync(self):
+            pass
+
+    created = []
+
+    def factory(p):
+        lat = Steppable(p, tau=100.0)
+        created.append(lat)
+        return lat
+
+    srv = SolveServer(hbm_budget_bytes=100, lattice_factory=factory, ensemble=StreamBatch(),
+                      footprint_fn=lambda p: p.ny, chunk_steps=500, window=1000, max_steps=4000, precision="fp64x")
+    reqs = [req(0, 10), req(1, 20)]
+    for q in reqs:
+        q.precision = "fp64x"
+    results = {r.rid: r for r in srv.run(reqs)}
+    assert set(results) == {0, 1} and all(r.converged for r in results.values())
+    assert srv.cell_steps == sum(results[r].steps * reqs[r].cells for r in results)

@@ -123,18 +123,23 @@ def test_footprint_matches_allocation():
         lat.close()
 
 
-def test_server_result_same_alone_and_in_mix():
+@pytest.mark.parametrize("precision", ["fp32", "fp64x"])
+def test_server_result_same_alone_and_in_mix(precision):
+    """FP32: the batched form; fp64x: FP64 accuracy with one stream per solve."""
     from lbmgpu.server import Request, SolveServer
     reqs = [Request(0, 2, 32, 2e5, 0.71, 11, arrival=0.0), Request(1, 3, 16, 1e6, 7.0, 12, arrival=0.0),
             Request(2, 2, 48, 5e4, 0.71, 13, arrival=0.05), Request(3, 3, 12, 3e5, 0.71, 14, arrival=0.1)]
-    kw = dict(chunk_steps=200, check_every=1000, rel_tol=1e-3, max_steps=6000)
+    for q in reqs:
+        q.precision = precision
+    kw = dict(chunk_steps=200, check_every=1000, rel_tol=1e-3, max_steps=6000, precision=precision)
     srv = SolveServer(**kw)
     mixed = {r.rid: r for r in srv.run(reqs)}
     srv.close()
     assert len(mixed) == 4
     for req in reqs:
         solo = SolveServer(**kw)
-        r = solo.run([Request(req.rid, req.dim, req.n, req.Ra, req.Pr, req.seed, arrival=0.0)])[0]
+        r = solo.run([Request(req.rid, req.dim, req.n, req.Ra, req.Pr, req.seed, arrival=0.0,
+                              precision=precision)])[0]
         solo.close()
         m = mixed[req.rid]
         assert r.steps == m.steps and r.converged == m.converged
