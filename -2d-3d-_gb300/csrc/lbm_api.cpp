@@ -113,6 +113,7 @@ struct lbm_handle {
     bool host_access = false;   // the device can
     bool host_direct = false;   // and lbm_set_state reads the caller's array so (LBM_OPT_HOST_DIRECT bit 0)
     bool host_direct_wr = false;  // and lbm_get_state writes it so (bit 1)
+    bool wide_index = false;      // fixed arithmetic: 64-bit cell indices everywhere (LBM_OPT_WIDE_INDEX)
 };
 
 // ------------------------------------------------------------------------------------
@@ -718,7 +719,7 @@ static void enqueue_one(lbm_handle* h, bool first) {
     } else if (h->p.precision == LBM_FP64 && h->fixed) {
         fixed_fused_step(h->xgeo, h->px, fixed_arrays(h), h->dim, first, (const long long*)h->fbuf[h->cur],
                          (const long long*)h->gbuf[h->cur], (long long*)h->fbuf[nxt], (long long*)h->gbuf[nxt],
-                         h->stream);
+                         h->stream, 2, h->wide_index);
         h->cur = nxt;
     } else if (h->p.precision == LBM_FP64) {
         exact_fused_step(h->geo, h->phys, h->A, h->dim, first, h->fbuf[h->cur], h->gbuf[h->cur], h->fbuf[nxt],
@@ -775,7 +776,8 @@ static bool use_xfused(const lbm_handle* h) {
 static void x_enter(lbm_handle* h) {
     const int nxt = h->cur ^ 1;
     fixed_fused_step(h->xgeo, h->px, fixed_arrays(h), h->dim, false, (const long long*)h->fbuf[h->cur],
-                     (const long long*)h->gbuf[h->cur], (long long*)h->fbuf[nxt], nullptr, h->stream, 0);
+                     (const long long*)h->gbuf[h->cur], (long long*)h->fbuf[nxt], nullptr, h->stream, 0,
+                     h->wide_index);
     h->cur = nxt;  // f is one step ahead: fbuf[cur] = f_post_{N+1}, gbuf[cur ^ 1] = g_post_N
 }
 
@@ -794,7 +796,7 @@ static void x_pass(lbm_handle* h) {
 static void x_exit(lbm_handle* h) {
     const int c = h->cur;
     fixed_fused_step(h->xgeo, h->px, fixed_arrays(h), h->dim, false, nullptr, (const long long*)h->gbuf[c ^ 1],
-                     (long long*)h->fbuf[c], (long long*)h->gbuf[c], h->stream, 1);
+                     (long long*)h->fbuf[c], (long long*)h->gbuf[c], h->stream, 1, h->wide_index);
 }
 
 // Capture key of a chunk of fused passes: the buffer parity and which B_prev set is current.
@@ -1964,9 +1966,9 @@ extern "C" int lbm_time_kernels(lbm_handle* h, int64_t nsteps, double* ms_flow, 
             const FixedArrays X = fixed_arrays(h);
             const long long *fc = (const long long*)h->fbuf[h->cur], *gc = (const long long*)h->gbuf[h->cur];
             long long *fn = (long long*)h->fbuf[nxt], *gn = (long long*)h->gbuf[nxt];
-            fixed_fused_step(h->xgeo, h->px, X, h->dim, false, fc, gc, fn, gn, h->stream, 0);
+            fixed_fused_step(h->xgeo, h->px, X, h->dim, false, fc, gc, fn, gn, h->stream, 0, h->wide_index);
             CK(h, cudaEventRecord(ev[2 * k + 1], h->stream));
-            fixed_fused_step(h->xgeo, h->px, X, h->dim, false, fc, gc, fn, gn, h->stream, 1);
+            fixed_fused_step(h->xgeo, h->px, X, h->dim, false, fc, gc, fn, gn, h->stream, 1, h->wide_index);
             h->cur = nxt;
         } else if (h->p.precision == LBM_FP64) {
             const int nxt = h->cur ^ 1;
@@ -2038,6 +2040,10 @@ extern "C" int lbm_set_option(lbm_handle* h, int option, int value) {
         case LBM_OPT_PAIRS:
             if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the plain FP64 method has no paired form");
             h->F.pairs = value != 0;
+            break;
+        case LBM_OPT_WIDE_INDEX:
+            if (!h->fixed) return fail(h, LBM_ERR_STATE, "the index width option is for the fixed arithmetic");
+            h->wide_index = value != 0;  // the captured chunk is dropped below
             break;
         case LBM_OPT_ROWS:
             if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the FP64 forms choose their own launches");

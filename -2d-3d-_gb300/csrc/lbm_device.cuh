@@ -212,25 +212,27 @@ __host__ __device__ __forceinline__ bool row_launch_supported(const Geo& g) {
 // axis can take a source outside the lattice, at i = 0 or nx-1.  The rule is pull_flow's /
 // pull_thermal's for that case, written with selects so that every lane of a warp runs the
 // same instructions (x-face lanes share warps with interior ones).
-template <int Q, class T, class LOAD>
-__device__ __forceinline__ T pull_flow_xrow(const Geo& g, int a, int i, long long c, LOAD load) {
-    const long long off = (long long)Lat<Q>::ex(a) + (long long)g.nx * ((long long)Lat<Q>::ey(a) + (long long)g.ny * (long long)Lat<Q>::ez(a));
+// I: the cell-index type (long long; int where every index of the arrays fits in 32 bits,
+// which halves the address arithmetic).
+template <int Q, class T, class LOAD, class I = long long>
+__device__ __forceinline__ T pull_flow_xrow(const Geo& g, int a, int i, I c, LOAD load) {
+    const I off = (I)Lat<Q>::ex(a) + (I)g.nx * ((I)Lat<Q>::ey(a) + (I)g.ny * (I)Lat<Q>::ez(a));
     if (Lat<Q>::ex(a) == 0) return load(a, c - off);
     const int si = i - Lat<Q>::ex(a);
     const bool out = si < 0 || si >= g.nx;
     if (g.bcf[0] == LBM_BC_NOSLIP) return out ? load(Lat<Q>::opp(a), c) : load(a, c - off);
     // periodic: the same-row copy from the other end of the row (j and k unchanged, also
     // for the diagonal directions: the reference's x-periodic copy, 2DRB.F90:821-828)
-    return load(a, out ? c + (long long)Lat<Q>::ex(a) * (g.nx - 1) : c - off);
+    return load(a, out ? c + (I)Lat<Q>::ex(a) * (I)(g.nx - 1) : c - off);
 }
-template <int QT, class T, class LOAD>
-__device__ __forceinline__ T pull_thermal_xrow(const Geo& g, int a, int i, long long c, LOAD load) {
-    const long long off = (long long)Lat<QT>::ex(a) + (long long)g.nx * ((long long)Lat<QT>::ey(a) + (long long)g.ny * (long long)Lat<QT>::ez(a));
+template <int QT, class T, class LOAD, class I = long long>
+__device__ __forceinline__ T pull_thermal_xrow(const Geo& g, int a, int i, I c, LOAD load) {
+    const I off = (I)Lat<QT>::ex(a) + (I)g.nx * ((I)Lat<QT>::ey(a) + (I)g.ny * (I)Lat<QT>::ez(a));
     if (Lat<QT>::ex(a) == 0) return load(a, c - off);
     const int si = i - Lat<QT>::ex(a);
     const bool out = si < 0 || si >= g.nx;
     const int bt = g.bct[0];
-    if (bt == LBM_BCT_PERIODIC) return load(a, out ? c + (long long)Lat<QT>::ex(a) * (g.nx - 1) : c - off);
+    if (bt == LBM_BCT_PERIODIC) return load(a, out ? c + (I)Lat<QT>::ex(a) * (I)(g.nx - 1) : c - off);
     const T v = out ? load(Lat<QT>::opp(a), c) : load(a, c - off);
     if (bt == LBM_BCT_CONST && out) return -v + (T)(si < 0 ? g.bcT_lo[0] : g.bcT_hi[0]);
     return v;

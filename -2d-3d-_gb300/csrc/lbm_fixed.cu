@@ -48,13 +48,14 @@ __global__ void __launch_bounds__(128) k_xthermal(Geo g, PhysX X, FixedArrays A,
 // Interior rows and face rows of the steady-state step: row_interior_cell and
 // row_face_cell (lbm_device.cuh).  Interior rows pull with selects for the x faces; the face
 // kernels take the y- and z-face rows with the full boundary rule.
-template <int D>
+// I: int when q * ncell < 2^31 (every array index fits in 32 bits), else long long.
+template <int D, class I>
 __global__ void __launch_bounds__(128, LBM_XFLOW_MIN_BLOCKS) k_xflow_in(Geo g, PhysX X, FixedArrays A, const long long* __restrict__ fin,
                                                      const long long* __restrict__ gin, long long* __restrict__ fout) {
     long long c;
     int i, j, k;
     if (!row_interior_cell(g, c, i, j, k)) return;
-    flow_cell<D, false, 3>(g, X, A, fin, gin, fout, c, i, j, k);
+    flow_cell<D, false, 3, I>(g, X, A, fin, gin, fout, c, i, j, k);
 }
 
 template <int D>
@@ -66,14 +67,14 @@ __global__ void __launch_bounds__(128) k_xflow_face(Geo g, PhysX X, FixedArrays 
     flow_cell<D, false, 2>(g, X, A, fin, gin, fout, c, i, j, k);
 }
 
-template <int D>
+template <int D, class I>
 __global__ void __launch_bounds__(128, 6) k_xthermal_in(Geo g, PhysX X, FixedArrays A,
                                                         const long long* __restrict__ fin,
                                                         const long long* __restrict__ gin, long long* __restrict__ gout) {
     long long c;
     int i, j, k;
     if (!row_interior_cell(g, c, i, j, k)) return;
-    thermal_cell<D, false, 3>(g, X, A, fin, gin, gout, c, i, j, k);
+    thermal_cell<D, false, 3, I>(g, X, A, fin, gin, gout, c, i, j, k);
 }
 
 template <int D>
@@ -334,24 +335,29 @@ void fixed_fused_pass(const Geo& g, const PhysX& X, const long long* fin, const 
 // Steady-state step of one dimension: interior kernel and face kernel for each half.
 template <int D>
 static void steady_step(const Geo& g, const PhysX& X, const FixedArrays& A, const long long* fprev,
-                        const long long* gprev, long long* fnext, long long* gnext, cudaStream_t s, bool fl, bool th) {
+                        const long long* gprev, long long* fnext, long long* gnext, cudaStream_t s, bool fl, bool th,
+                        bool wide) {
     const unsigned bx = (unsigned)((g.nx + 127) / 128);
     const dim3 bin(128), gin_grid(bx, (unsigned)(g.ny - 2), D == 3 ? (unsigned)(g.nz - 2) : 1u);
     const dim3 gface(bx, (unsigned)face_row_count(g), 1u);
     // a 3D lattice of two planes has no interior rows: the face rows hold every cell
     const bool interior = D == 2 || g.nz > 2;
+    constexpr int Q = D == 3 ? 19 : 9;
+    const bool idx32 = !wide && (long long)Q * g.ncell < (1LL << 31);
     if (fl) {
-        if (interior) k_xflow_in<D><<<gin_grid, bin, 0, s>>>(g, X, A, fprev, gprev, fnext);
+        if (interior && idx32) k_xflow_in<D, int><<<gin_grid, bin, 0, s>>>(g, X, A, fprev, gprev, fnext);
+        else if (interior) k_xflow_in<D, long long><<<gin_grid, bin, 0, s>>>(g, X, A, fprev, gprev, fnext);
         k_xflow_face<D><<<gface, bin, 0, s>>>(g, X, A, fprev, gprev, fnext);
     }
     if (th) {
-        if (interior) k_xthermal_in<D><<<gin_grid, bin, 0, s>>>(g, X, A, fnext, gprev, gnext);
+        if (interior && idx32) k_xthermal_in<D, int><<<gin_grid, bin, 0, s>>>(g, X, A, fnext, gprev, gnext);
+        else if (interior) k_xthermal_in<D, long long><<<gin_grid, bin, 0, s>>>(g, X, A, fnext, gprev, gnext);
         k_xthermal_face<D><<<gface, bin, 0, s>>>(g, X, A, fnext, gprev, gnext);
     }
 }
 
 void fixed_fused_step(const Geo& g, const PhysX& X, const FixedArrays& A, int dim, bool first, const long long* fprev,
-                      const long long* gprev, long long* fnext, long long* gnext, cudaStream_t s, int part) {
+                      const long long* gprev, long long* fnext, long long* gnext, cudaStream_t s, int part, bool wide) {
     const int bs = 128;
     const unsigned nb = xblocks(g.ncell, bs);
     const bool fl = part != 1, th = part != 0;
@@ -360,14 +366,14 @@ void fixed_fused_step(const Geo& g, const PhysX& X, const FixedArrays& A, int di
             if (fl) k_xflow<2, true><<<nb, bs, 0, s>>>(g, X, A, fprev, gprev, fnext);
             if (th) k_xthermal<2, true><<<nb, bs, 0, s>>>(g, X, A, fnext, gprev, gnext);
         } else {
-            steady_step<2>(g, X, A, fprev, gprev, fnext, gnext, s, fl, th);
+            steady_step<2>(g, X, A, fprev, gprev, fnext, gnext, s, fl, th, wide);
         }
     } else {
         if (first) {
             if (fl) k_xflow<3, true><<<nb, bs, 0, s>>>(g, X, A, fprev, gprev, fnext);
             if (th) k_xthermal<3, true><<<nb, bs, 0, s>>>(g, X, A, fnext, gprev, gnext);
         } else {
-            steady_step<3>(g, X, A, fprev, gprev, fnext, gnext, s, fl, th);
+            steady_step<3>(g, X, A, fprev, gprev, fnext, gnext, s, fl, th, wide);
         }
     }
 }

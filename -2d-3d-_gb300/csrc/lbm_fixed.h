@@ -9,8 +9,10 @@ namespace lbm {
 
 // One fused step (part 0: flow kernel, 1: thermal kernel, 2: both) on q60 fused buffers.
 // first: the inputs are the FP64 module arrays.  g: deviation geometry (deviation_geo).
+// wide: 64-bit cell indices in the interior-row kernels even where 32-bit ones fit.
 void fixed_fused_step(const Geo& g, const PhysX& X, const FixedArrays& A, int dim, bool first, const long long* fprev,
-                      const long long* gprev, long long* fnext, long long* gnext, cudaStream_t s, int part = 2);
+                      const long long* gprev, long long* fnext, long long* gnext, cudaStream_t s, int part = 2,
+                      bool wide = false);
 // The FP64 module arrays of the current step from the q60 fused buffers and the lag.
 void fixed_materialize(const Geo& g, const PhysX& X, const FixedArrays& A, int dim, const long long* fcur,
                        const long long* gcur, cudaStream_t s);

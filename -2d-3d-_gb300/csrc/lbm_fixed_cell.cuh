@@ -516,11 +516,14 @@ namespace fxa {
 // PATH: 0 = any cell (the boundary rule where a pull leaves the lattice), 1 = a cell known to
 // touch no face (fixed-offset pulls only), 2 = a face cell (boundary path only), 3 = a cell of
 // an interior row (only x can leave the lattice: pull_flow_xrow / pull_thermal_xrow).
-template <int D, bool FIRST, int PATH = 0>
+// I: index type of the cell's own accesses and of PATH 3's pulls (int when every array
+// index fits in 32 bits: half the address arithmetic; the values do not depend on it).
+template <int D, bool FIRST, int PATH = 0, class I = long long>
 __device__ __forceinline__ void flow_cell(const Geo& g, const PhysX& X, const FixedArrays& A, const long long* fin,
                                           const long long* gin, long long* fout, long long c, int i, int j, int k) {
     constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
     const long long n = g.ncell;
+    const I ni = (I)g.ncell, ci = (I)c;
     q60 d[Q], dp[Q], rho, P[3], U[3], tdev;
     if (FIRST) {
 #pragma unroll
@@ -535,12 +538,12 @@ __device__ __forceinline__ void flow_cell(const Geo& g, const PhysX& X, const Fi
     } else {
         q60 ts = Qb(0);
         if (PATH == 3) {
-            auto lf = [&](int a, long long cc) { return ldq(fin, a * n + cc); };
-            auto lg = [&](int a, long long cc) { return ldq(gin, a * n + cc); };
+            auto lf = [&](int a, I cc) { return ldq(fin, a * ni + cc); };
+            auto lg = [&](int a, I cc) { return ldq(gin, a * ni + cc); };
 #pragma unroll
-            for (int a = 0; a < Q; ++a) d[a] = pull_flow_xrow<Q, q60>(g, a, i, c, lf);
+            for (int a = 0; a < Q; ++a) d[a] = pull_flow_xrow<Q, q60>(g, a, i, ci, lf);
 #pragma unroll
-            for (int a = 0; a < QT; ++a) ts = ts + pull_thermal_xrow<QT, q60>(g, a, i, c, lg);
+            for (int a = 0; a < QT; ++a) ts = ts + pull_thermal_xrow<QT, q60>(g, a, i, ci, lg);
         } else if (PATH == 1 || (PATH == 0 && aa_inner(g, i, j, k))) {  // no pull needs a boundary rule
 #pragma unroll
             for (int a = 0; a < Q; ++a) {
@@ -558,30 +561,32 @@ __device__ __forceinline__ void flow_cell(const Geo& g, const PhysX& X, const Fi
             for (int a = 0; a < QT; ++a) ts = ts + pull_thermal<QT, q60>(g, a, i, j, k, c, lg);
         }
         tdev = ts;
-        macro<D>(d, Qb(A.xlag[c]), X, rho, P, U);
+        macro<D>(d, Qb(A.xlag[ci]), X, rho, P, U);
     }
     if (D == 2) {
         const q60 Fy = collide_2d(d, rho, P, U, tdev, X, dp);
-        A.xlag[c] = Fy.s();
+        A.xlag[ci] = Fy.s();
     } else {
         collide_3d(d, rho, P, U, tdev, X, dp);
     }
 #pragma unroll
-    for (int a = 0; a < Q; ++a) fout[a * n + c] = dp[a].s();
+    for (int a = 0; a < Q; ++a) fout[a * ni + ci] = dp[a].s();
 }
 
 // Streaming, boundary and macro of the flow, and thermal collision of step n (k_thermal).
-template <int D, bool FIRST, int PATH = 0>
+template <int D, bool FIRST, int PATH = 0, class I = long long>
 __device__ __forceinline__ void thermal_cell(const Geo& g, const PhysX& X, const FixedArrays& A, const long long* fin,
                                              const long long* gin, long long* gout, long long c, int i, int j, int k) {
     constexpr int Q = (D == 2) ? 9 : 19, QT = (D == 2) ? 5 : 7;
     const long long n = g.ncell;
+    const I ni = (I)g.ncell, ci = (I)c;
     q60 d[Q], e[QT], ep[QT], rho, P[3], U[3], B[3], tdev;
     const bool inner = PATH == 1 || (PATH == 0 && aa_inner(g, i, j, k));
     auto lf = [&](int a, long long cc) { return ldq(fin, a * n + cc); };
     if (PATH == 3) {
+        auto lfi = [&](int a, I cc) { return ldq(fin, a * ni + cc); };
 #pragma unroll
-        for (int a = 0; a < Q; ++a) d[a] = pull_flow_xrow<Q, q60>(g, a, i, c, lf);
+        for (int a = 0; a < Q; ++a) d[a] = pull_flow_xrow<Q, q60>(g, a, i, ci, lfi);
     } else if (inner) {
 #pragma unroll
         for (int a = 0; a < Q; ++a) d[a] = ldq(fin, a * n + c - lat_off<Q>(g, a));
@@ -599,10 +604,10 @@ __device__ __forceinline__ void thermal_cell(const Geo& g, const PhysX& X, const
     } else {
         q60 ts = Qb(0);
         if (PATH == 3) {
-            auto lg = [&](int a, long long cc) { return ldq(gin, a * n + cc); };
+            auto lg = [&](int a, I cc) { return ldq(gin, a * ni + cc); };
 #pragma unroll
             for (int a = 0; a < QT; ++a) {
-                e[a] = pull_thermal_xrow<QT, q60>(g, a, i, c, lg);
+                e[a] = pull_thermal_xrow<QT, q60>(g, a, i, ci, lg);
                 ts = ts + e[a];
             }
         } else if (inner) {
@@ -620,24 +625,24 @@ __device__ __forceinline__ void thermal_cell(const Geo& g, const PhysX& X, const
             }
         }
         tdev = ts;
-        B[0] = Qb(A.xb0[c]);
-        B[1] = Qb(A.xb1[c]);
-        B[2] = D == 3 ? Qb(A.xb2[c]) : Qb(0);
+        B[0] = Qb(A.xb0[ci]);
+        B[1] = Qb(A.xb1[ci]);
+        B[2] = D == 3 ? Qb(A.xb2[ci]) : Qb(0);
     }
-    macro<D>(d, D == 2 ? Qb(A.xlag[c]) : tdev, X, rho, P, U);
+    macro<D>(d, D == 2 ? Qb(A.xlag[ci]) : tdev, X, rho, P, U);
     if (D == 2) {
         collideT_2d(e, U, tdev, B, X, ep);
     } else {
         collideT_3d(e, U, tdev, B, X, ep);
-        A.xlag[c] = tdev.s();
+        A.xlag[ci] = tdev.s();
     }
     if (FIRST || X.use_g) {
-        A.xb0[c] = B[0].s();
-        A.xb1[c] = B[1].s();
-        if (D == 3) A.xb2[c] = B[2].s();
+        A.xb0[ci] = B[0].s();
+        A.xb1[ci] = B[1].s();
+        if (D == 3) A.xb2[ci] = B[2].s();
     }
 #pragma unroll
-    for (int a = 0; a < QT; ++a) gout[a * n + c] = ep[a].s();
+    for (int a = 0; a < QT; ++a) gout[a * ni + ci] = ep[a].s();
 }
 
 // The module arrays of step N (FP64) from the fused buffers f_post_N, g_post_N and the lag:

@@ -44,6 +44,7 @@ module lbm_gpu_mod
   integer(c_int), parameter :: LBM_OPT_FP16_ROUNDING = 5   ! 1 stochastic (default), 0 nearest
   integer(c_int), parameter :: LBM_OPT_HOST_DIRECT = 6     ! state transfer on host arrays directly
   integer(c_int), parameter :: LBM_OPT_ROWS = 7            ! FP32/FP16: interior-row and face-row launches
+  integer(c_int), parameter :: LBM_OPT_WIDE_INDEX = 8      ! fixed arithmetic: 64-bit indices in every kernel
 
   type, bind(C) :: lbm_params
     integer(c_int32_t) :: dim, nx, ny, nz

@@ -115,6 +115,7 @@ LBM_OPT_KCHUNK = 2
 LBM_OPT_PAIRS = 3
 LBM_OPT_STAGED = 4
 LBM_OPT_FP16_ROUNDING = 5  # FP16 storage: 1 stochastic rounding (default), 0 nearest
+LBM_OPT_WIDE_INDEX = 8     # fixed arithmetic: 64-bit indices in every kernel (1) or 32-bit ones where they fit (0)
 LBM_OPT_ROWS = 7           # FP32/FP16 two-buffer steps: interior-row and face-row launches (1) or one cell per thread
 LBM_OPT_HOST_DIRECT = 6    # state transfer on the caller's host arrays: bit 0 set_state reads, bit 1 get_state writes
 

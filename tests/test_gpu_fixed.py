@@ -151,3 +151,21 @@ def test_fixed_fused_pass_equals_two_kernel_step(gpu_lib, shape, periodic):
         assert np.array_equal(a.get_state(k), b.get_state(k)), k
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("name", ["rb2d_periodic", "rb3d_noslip", "rb3d_periodic_legacy"])
+def test_wide_and_narrow_indices_agree(gpu_lib, name):
+    """The interior-row kernels with 32-bit cell indices (the default where every index
+    fits) and with 64-bit ones (the form of lattices with q * ncell >= 2^31) give the same
+    bits, across a captured chunk and single steps."""
+    from lbmgpu import LBM_OPT_WIDE_INDEX
+    p = fixed(cases()[name])
+    a, b = Lattice(p), Lattice(p)
+    b.set_option(LBM_OPT_WIDE_INDEX, 1)
+    for lat in (a, b):
+        lat.initial()
+        lat.step(45)
+    for k in module_fields(p):
+        assert np.array_equal(a.get_state(k), b.get_state(k)), k
+    a.close()
+    b.close()
