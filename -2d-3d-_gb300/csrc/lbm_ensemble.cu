@@ -31,7 +31,8 @@ struct EnsMember {
 };
 
 // Fixed-offset pulls for the cells off the faces (lbm_fast_cells.cuh).  Resident blocks of
-// 256 threads per SM: three, except two for the paired 3D bodies (about 115 registers).
+// 256 threads per SM: three, except two for the paired 3D bodies (about 115 registers);
+// four for the paired 2D bodies spills 48-60 bytes and measured no faster on GB300.
 // With the member descriptor and buffer arguments staged in shared memory the one-cell
 // kernels take 66-80 registers, against 96-128 with register copies of the descriptor
 // (the 3D thermal kernel took 242 without a bound), and none spills.
