@@ -413,6 +413,21 @@ def ensemble_run(args, local, steps_total=13000, every=500):
     ens.close()
     for lat in lats:
         lat.close()
+    # the same members at FP64 accuracy (the fixed arithmetic), one stream per member
+    from lbmgpu.server import StreamBatch
+    xl = [lbmgpu.Lattice(rb_params(precision="fp64x", **sp), device=local) for sp in specs]
+    sb = StreamBatch()
+    for lat in xl:
+        lat.initial()
+        sb.add(lat)
+    sb.step(64)
+    sb.sync()
+    t0 = time.perf_counter()
+    sb.step(k)
+    sb.sync()
+    fp64x_mlups = cells * k / (time.perf_counter() - t0) / 1e6
+    for lat in xl:
+        lat.close()
     half = steps_total // 2
     members = []
     for m, sp in enumerate(specs):
@@ -433,6 +448,9 @@ def ensemble_run(args, local, steps_total=13000, every=500):
     return {"workload": "64 D2Q9/D2Q5 RB instances, aspect 2, ny in {64..512}, Ra log-uniform 1e4..1e8, "
                         "Pr in {0.71,7}, FP32 storage, %d cells" % cells,
             "aggregate_mlups": mlups, "ms_per_step": ms / k, "steps_timed": k, "autotuned": cfg,
+            "fp64_accuracy_streams_mlups": fp64x_mlups,
+            "fp64_accuracy_note": "the same members at FP64 accuracy (fixed arithmetic), one lbm_step per member "
+                                  "on its own stream, %d steps, wall clock" % k,
             "launches_per_step": 3,  # flow, thermal, step counters (one member list: all 2D, even nx)
             "dNu_vs_fp64": {
                 "compared": len(good), "median": good[len(good) // 2] if good else None,
