@@ -2042,8 +2042,10 @@ extern "C" int lbm_set_option(lbm_handle* h, int option, int value) {
             h->F.pairs = value != 0;
             break;
         case LBM_OPT_WIDE_INDEX:
-            if (!h->fixed) return fail(h, LBM_ERR_STATE, "the index width option is for the fixed arithmetic");
+            if (h->p.precision == LBM_FP64 && !h->fixed)
+                return fail(h, LBM_ERR_STATE, "the plain FP64 method indexes with 64-bit integers only");
             h->wide_index = value != 0;  // the captured chunk is dropped below
+            h->F.wide = value != 0;
             break;
         case LBM_OPT_ROWS:
             if (h->p.precision == LBM_FP64) return fail(h, LBM_ERR_STATE, "the FP64 forms choose their own launches");

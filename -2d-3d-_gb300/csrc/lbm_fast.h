@@ -47,6 +47,7 @@ struct FastState {
     bool pairs = false;
     bool tma = false;
     bool rows = false;          // interior-row and face-row launches (LBM_OPT_ROWS)
+    bool wide = false;          // 64-bit cell indices where 32-bit ones fit (LBM_OPT_WIDE_INDEX)
     int* err = nullptr;         // device flag: a bounded wait of a staged kernel gave up
     // In-place (AA) pattern: fbuf[0] / gbuf[0] are the only population arrays and also the
     // module arrays (fref, gref alias them); B and L have one buffer each.

@@ -384,6 +384,19 @@ __device__ __forceinline__ bool fcell(const Geo& g, long long& c, int& i, int& j
     cell_coords(g, c, i, j, k);
     return true;
 }
+// The same with the cell index and its divisions in the index type I (int where every
+// array index fits in 32 bits).
+template <class I>
+__device__ __forceinline__ bool fcell_i(const Geo& g, I& c, int& i, int& j, int& k) {
+    c = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
+    if (c >= (I)g.ncell) return false;
+    const I plane = (I)g.nx * (I)g.ny;
+    k = (int)(c / plane);
+    const I r = c - (I)k * plane;
+    j = (int)(r / (I)g.nx);
+    i = (int)(r - (I)j * (I)g.nx);
+    return true;
+}
 
 // Cell of a thread, x-face cells apart: threads [0, rows*(nx-2)) take the cells with
 // 0 < i < nx-1 row by row, the last 2*rows threads the x-face cells (i = 0, nx-1 of each

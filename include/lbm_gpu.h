@@ -296,10 +296,12 @@ int lbm_footprint(const lbm_params* p, size_t* bytes);
  *   boundary rule) as separate kernels (1), or one cell per thread in lattice order (0).  Two
  *   cells per thread, where chosen, takes precedence.  Same values either way. */
 #define LBM_OPT_ROWS          7
-/* LBM_OPT_WIDE_INDEX: fixed-arithmetic handles index their arrays with 64-bit integers in
- *   every kernel (1), the form lattices of q * ncell >= 2^31 take, or with 32-bit indices in
- *   the interior-row kernels where every index fits (0, default: half the address
- *   arithmetic).  Same values either way. */
+/* LBM_OPT_WIDE_INDEX: fixed-arithmetic and FP32/FP16 handles index their arrays with 64-bit
+ *   integers in every kernel (1), the form lattices of q * ncell >= 2^31 take, or with 32-bit
+ *   indices in the main step kernels (the fixed arithmetic's interior rows, the FP16
+ *   one-cell kernels and the FP32 thermal kernel, where they measured faster on GB300) where
+ *   every index fits (0, default: half the address arithmetic and 32-bit divisions of the
+ *   cell index).  Same values either way. */
 #define LBM_OPT_WIDE_INDEX    8
 int lbm_set_option(lbm_handle* h, int option, int value);
 

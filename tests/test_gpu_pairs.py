@@ -64,3 +64,24 @@ def test_rows_equal_one_cell(name, precision):
         assert np.array_equal(x, y), (name, precision, field, float(np.abs(x - y).max()))
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+@pytest.mark.parametrize("name", sorted(cases()))
+def test_wide_index_equals_narrow(name, precision):
+    """The one-cell kernels with 32-bit cell indices (the default where every index fits) and
+    with 64-bit ones give the same bits."""
+    from lbmgpu import LBM_OPT_WIDE_INDEX
+    p = cases()[name].copy()
+    p.precision = {"fp32": 1, "fp16": 2}[precision]
+    a, b = Lattice(p), Lattice(p)
+    for lat, wide in ((a, 0), (b, 1)):
+        lat.set_option(LBM_OPT_PAIRS, 0)
+        lat.set_option(LBM_OPT_WIDE_INDEX, wide)
+        lat.initial()
+        lat.step(70)
+    for field in ("f", "g", "T", "u", "v", "Bx_prev", "By_prev"):
+        x, y = a.get_state(field), b.get_state(field)
+        assert np.array_equal(x, y), (name, precision, field, float(np.abs(x - y).max()))
+    a.close()
+    b.close()
