@@ -279,8 +279,10 @@ def time_precision(prec, args, pg, local, size=None):
             "ms_flow": ms_flow, "ms_thermal": ms_thermal, "Nu": nu, "Re": re}
 
 
-def e2e_run(prec, args, local):
-    """State in from host arrays (Fortran layout), K steps, T field and Nu/Re out, via the C ABI."""
+def e2e_run(prec, args, local, jobs=3):
+    """State in from host arrays (Fortran layout), K steps, T field and Nu/Re out, via the C ABI.
+    The whole job runs `jobs` times back to back (each with every transfer); the median job
+    gives the value, and every job's time is listed."""
     import numpy as np
     import lbmgpu
     p = workload_params(prec, args.size)
@@ -290,21 +292,25 @@ def e2e_run(prec, args, local):
     host = {k: np.ascontiguousarray(lat.get_state(k)) for k in names}
     lat.step(args.warmup)
     lat.sync()
-    t0 = time.perf_counter()
-    for k in names:
-        lat.set_state(k, host[k])
-    lat.step(args.steps)
-    T = lat.get_state("T")
-    nu, re = lat.calNuRe()
-    dt = time.perf_counter() - t0
+    times = []
+    for _ in range(jobs):
+        t0 = time.perf_counter()
+        for k in names:
+            lat.set_state(k, host[k])
+        lat.step(args.steps)
+        T = lat.get_state("T")
+        nu, re = lat.calNuRe()
+        times.append(time.perf_counter() - t0)
     lat.close()
+    dt = sorted(times)[len(times) // 2]
     h2d = sum(a.nbytes for a in host.values())
     d2h = T.nbytes + 16
     cells = p.nx * p.ny * p.nz
     return {"value": cells * args.steps / dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
             "d2h_bytes_per_step": d2h / args.steps,
             "job": "lbm_set_state x%d (Fortran-layout host arrays) + lbm_step(%d) + lbm_get_state(T) + lbm_calNuRe"
-                   % (len(names), args.steps)}
+                   % (len(names), args.steps),
+            "jobs_ms": [round(t * 1e3, 1) for t in times], "statistic": "median of %d jobs" % jobs}
 
 
 def plain_rate_2d(local, ny=128):
