@@ -15,7 +15,7 @@ storage forms.  `e2e` is the headline metric through the C ABI with host buffers
 reference's Fortran layout (state in, steps, T field and Nu/Re out).  `cpu_baseline` is the
 C++ restatement of the reference's OpenMP CPU path timed on this host's cores; the GPU then
 runs the same steps with the reference's arithmetic and the two temperature fields are
-compared bit for bit.  The 128^3 configuration is a secondary leg (`config1_128`).
+compared bit for bit.  The 128^3 cube is a secondary leg (`cube128`).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
@@ -364,7 +364,7 @@ def tail_mean(hist, from_step):
 
 
 def ensemble_run(args, local, steps_total=13000, every=500):
-    """Batched form (BASELINE config 3): 64 D2Q9/D2Q5 RB instances, aspect 2, ny drawn from
+    """Batched form (the many-instance 2D workload): 64 D2Q9/D2Q5 RB instances, aspect 2, ny drawn from
     {64,...,512}, Ra log-uniform in [1e4, 1e8], Pr in {0.71, 7}, U = 0.1, FP32 storage, one
     launch per stage over a packed tile table, graph replay, autotuned tiles.  Every member's
     Nu is sampled every `every` steps; each member is then run alone at FP64 accuracy (the
@@ -470,7 +470,7 @@ def ensemble_run(args, local, steps_total=13000, every=500):
 
 
 def served_run(args, local, precision="fp32"):
-    """Served form (BASELINE config 4): Poisson arrivals at 2/s, half 2D (ny 64..512, aspect 2)
+    """Served form (the Poisson solve stream): Poisson arrivals at 2/s, half 2D (ny 64..512, aspect 2)
     half 3D (n 64..192), Ra log-uniform 1e4..1e8, Pr in {0.71, 7}, admission by an 80% HBM
     budget, each solve run until its windowed-mean Nu changes by < 0.1% between consecutive
     windows, or a step cap.  FP32 storage runs as the batched form; FP64 accuracy ("fp64x",
@@ -672,14 +672,14 @@ def time_series_run(p, local, steps, every, tail_frac):
 def accuracy_run(args, local):
     """Time-averaged Nu and Re of the storage forms against FP64 on one configuration.
 
-    config1: the 128^3 cube at Ra 1e7 (U 0.1); config2: the 384^3 cube at Ra 1e9 (U 0.07,
+    cube128: the 128^3 cube at Ra 1e7 (U 0.1); cube384: the 384^3 cube at Ra 1e9 (U 0.07,
     in-place pattern).  Each run samples calNuRe every `every` steps and averages the last
     `tail` fraction; the standard error comes from batch means.  Two seeds per storage form
     give the spread of the time average that the chaotic flow itself produces, against which
     |dNu| between storage forms is read."""
     from lbmgpu.abi import rb_params
     cfg = args.accuracy
-    if cfg == "config1":
+    if cfg == "cube128":
         base = dict(dim=3, n=128, Ra=1e7, Pr=0.71, U=0.1, noise_amp=1e-3, pattern="AB")
         default_steps, tail = 150000, 0.5
     else:
@@ -724,7 +724,7 @@ def accuracy_run(args, local):
     return 0
 
 
-def config0_run(args, local, steps=20000, cpu_steps=20000):
+def rb2d_run(args, local, steps=20000, cpu_steps=20000):
     """The 2D reference case (256 x 128, x-periodic, Ra 1e5, Pr 0.71, U 0.1, plain FP64): its
     full 20,000 steps on the GPU through lbm_step, the wall-averaged Nu and volume Re at the
     end, and the same 20,000 steps of the CPU oracle (about 2.5 s on 16 host threads), with
@@ -839,7 +839,7 @@ def run_gpu(args):
                          "ms_thermal": r["ms_thermal"], "Nu": r["Nu"], "Re": r["Re"],
                          "hbm_frac": BYTES_PER_CELL[prec] * 128 ** 3 / ((r["ms_flow"] + r["ms_thermal"]) / 1e3) / 1e9
                          / peak}
-        line["config1_128"] = {"workload": workload_config(128)["workload"], "forms": leg,
+        line["cube128"] = {"workload": workload_config(128)["workload"], "forms": leg,
                                "note": "hbm_frac: algorithmic bytes over the flow + thermal kernel time per step, "
                                        "of the measured HBM peak"}
     if rank == 0 and not args.no_ensemble:
@@ -849,8 +849,8 @@ def run_gpu(args):
             line["served" if prec == "fp32" else "served_" + prec] = served_run(args, local, prec)
     if rank == 0 and not args.no_size:
         line["at_384"] = at_size_run(args, local, peak)
-    if rank == 0 and not args.no_config0:
-        line["config0_2d"] = config0_run(args, local)
+    if rank == 0 and not args.no_rb2d:
+        line["rb2d_256x128"] = rb2d_run(args, local)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n=args.size, device=local)
     if rank == 0:
@@ -869,7 +869,7 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-form leg (64 2D instances)")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream leg")
     ap.add_argument("--no-size", action="store_true", help="skip the 384^3 leg (in-place vs two-buffer pattern)")
-    ap.add_argument("--no-config0", action="store_true", help="skip the 2D 256 x 128 FP64 leg (20,000 steps)")
+    ap.add_argument("--no-rb2d", action="store_true", help="skip the 2D 256 x 128 FP64 leg (20,000 steps)")
     ap.add_argument("--served-full", action="store_true", help="served leg as configured: 600 s, 5000-step window")
     ap.add_argument("--served-precisions", default="fp32,fp64x",
                     help="served legs: fp32 (batched form), fp64x (FP64 accuracy, one stream per solve)")
@@ -884,7 +884,7 @@ def main():
     ap.add_argument("--precisions", default="fp64x,fp64,fp32,fp16",
                     help="comma list; the first is the headline form (fp64x: FP64 handle, fixed arithmetic)")
     ap.add_argument("--no-128", action="store_true", help="skip the 128^3 secondary leg")
-    ap.add_argument("--accuracy", choices=["config1", "config2"], default=None,
+    ap.add_argument("--accuracy", choices=["cube128", "cube384"], default=None,
                     help="instead of the benchmark: time-averaged Nu/Re of the storage forms against FP64")
     ap.add_argument("--accuracy-forms", default="fp64,fp64:1,fp32,fp32:1,fp16,fp16:1",
                     help="comma list of precision[:seed offset] runs of the accuracy leg")

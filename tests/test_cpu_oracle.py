@@ -114,8 +114,8 @@ def test_equilibrium_is_fixed_point_of_collision(oracle_mod):
         assert np.abs(fpost - feq).max() < tol
 
 
-def test_constants_config0(oracle_mod):
-    """BASELINE config 0 (2D, 256x128, Ra 1e5, Pr 0.71, U 0.1): nu = U H sqrt(Pr/Ra)."""
+def test_constants_rb2d_256x128(oracle_mod):
+    """The 2D reference case (256x128, Ra 1e5, Pr 0.71, U 0.1): nu = U H sqrt(Pr/Ra)."""
     p = rb_params(dim=2, ny=128, Ra=1e5, Pr=0.71, U=0.1)
     o = oracle_mod.Oracle(p)
     c = o.constants(LbmConstants)
