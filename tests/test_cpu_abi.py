@@ -118,3 +118,35 @@ def test_in_place_pattern_accepted_and_smaller(gpu_lib):
             lag = 0 if prec == "fp64" else 4 * n * (4 if dim == 3 else 3)
             faces = es * (19 + 7 if dim == 3 else 9 + 5) * ab.ny if dim == 2 else 0  # 2D cells are x-periodic
             assert saved == 2 * es * q * n + lag - faces, (dim, prec)
+
+
+def header_constants():
+    """#define LBM_* integer constants of the C header."""
+    out = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        for m in re.finditer(r"^#define\s+(LBM_[A-Z0-9_]+)\s+(-?\d+)\b", open(h).read(), re.M):
+            out[m.group(1)] = int(m.group(2))
+    return out
+
+
+def test_python_and_fortran_constants_match_the_header():
+    """Every LBM_* constant the Python package or the Fortran module defines has the header's
+    value (the three copies are written by hand)."""
+    import lbmgpu
+    import lbmgpu.abi as abi
+    hdr = header_constants()
+    assert "LBM_OPT_WIDE_INDEX" in hdr and "LBM_OPT_ROWS" in hdr
+    py = {k: getattr(mod, k) for mod in (lbmgpu, abi) for k in dir(mod) if k.startswith("LBM_")
+          and isinstance(getattr(mod, k), int)}
+    wrong = {k: (v, hdr[k]) for k, v in py.items() if k in hdr and v != hdr[k]}
+    assert not wrong, wrong
+    for k in [k for k in hdr if k.startswith("LBM_OPT_")]:
+        assert k in py, "lbmgpu lacks %s" % k
+    fortran = glob.glob(os.path.join(ROOT, "-2d-3d-_gb300", "fortran", "*.F90"))
+    assert fortran
+    text = open(fortran[0]).read()
+    fvals = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(LBM_[A-Z0-9_]+)\s*=\s*(-?\d+)", text)}
+    wrong = {k: (v, hdr[k]) for k, v in fvals.items() if k in hdr and v != hdr[k]}
+    assert not wrong, wrong
+    for k in [k for k in hdr if k.startswith("LBM_OPT_")]:
+        assert k in fvals, "the Fortran module lacks %s" % k
